@@ -1,0 +1,96 @@
+"""ctypes binding of libgfgpu.so (C ABI declared in include/gfgpu.h).
+
+The library is built in-tree by galaxy_formation_gb300/build.py. Loading fails loudly when
+it is missing or when no GPU is usable: there is no CPU fallback.
+"""
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_dbl = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_f32 = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_u8 = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+_i32 = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_i64 = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+_ci, _cd, _cf, _vp = ctypes.c_int, ctypes.c_double, ctypes.c_float, ctypes.c_void_p
+
+# Every exported symbol with (argtypes, restype); include/gfgpu.h is the source of truth
+# and tests/test_capi.py checks that the two agree.
+SIGNATURES = {
+    "nbody_num_threads": ([], _ci),
+    "nbody_accel_active": ([_ci, _dbl, _dbl, _dbl, _cd, _cd, _u8, _ci], None),
+    "nbody_accel_direct": ([_ci, _dbl, _dbl, _dbl, _cd], None),
+    "nbody_render": ([_ci, _dbl, _u8, _ci, _dbl, _dbl, _cd, _ci, _ci, _f32], None),
+    "nbody_tonemap": ([_ci, _ci, _ci, _f32, _f32, _ci, _ci, _f32, _cf, _cf, _cf, _u8], None),
+    "gf_last_status": ([], _ci),
+    "gf_last_error": ([], ctypes.c_char_p),
+    "gf_tree_size": ([ctypes.POINTER(_ci), ctypes.POINTER(_ci)], _ci),
+    "gf_tree_export": ([_i32, _f32, _i32, _i32], _ci),
+    "gf_accel_active_dev": ([_ci, _vp, _vp, _vp, _cd, _cd, _vp, _ci, _vp], _ci),
+    "gf_accel_direct_dev": ([_ci, _vp, _vp, _vp, _cd, _vp], _ci),
+    "gf_accel_direct_targets": ([_ci, _dbl, _dbl, _ci, _i64, _dbl, _cd], _ci),
+    "gf_sph_kernel": ([_ci, _dbl, _dbl, _vp, _vp], _ci),
+    "gf_sph_forces": ([_ci, _ci, _dbl, _dbl, _dbl, _i64, _dbl, _dbl, _cd, _cd, _cd,
+                       _dbl, _dbl, _dbl, _dbl], _ci),
+    "gf_sph_forces_dev": ([_ci, _ci, _vp, _vp, _vp, _vp, _vp, _vp, _cd, _cd, _cd,
+                           _vp, _vp, _vp, _vp, _vp], _ci),
+    "gf_knn_from_candidates": ([_ci, _ci, _dbl, _i64, _ci, _i64, _dbl], _ci),
+    "gf_knn": ([_ci, _dbl, _ci, _dbl, _i64], _ci),
+    "gf_knn_iterations": ([], ctypes.c_longlong),
+    "gf_accelerations_dev": ([_ci, _vp, _vp, _vp, _vp, _vp, _cd, _cd, _cd, _cd, _cd, _vp, _ci, _ci,
+                              _ci, _vp, _vp, _vp], _ci),
+    "gf_accelerations": ([_ci, _dbl, _dbl, _dbl, np.ctypeslib.ndpointer(np.int8, flags="C_CONTIGUOUS"),
+                          _dbl, _cd, _cd, _cd, _cd, _cd, _vp, _ci, _ci, _ci, _dbl, _dbl], _ci),
+    "gf_force_info": ([ctypes.POINTER(_ci), ctypes.POINTER(_cd), ctypes.POINTER(_cd),
+                       ctypes.POINTER(ctypes.c_longlong)], _ci),
+    "gf_profile": ([_ci], _ci),
+    "gf_profile_stage": ([_ci, ctypes.POINTER(_cd), ctypes.POINTER(_ci)], _ci),
+    "gf_launch_count": ([], ctypes.c_longlong),
+    "gf_walk_pairs": ([], ctypes.c_longlong),
+    "gf_fp32_peak": ([ctypes.POINTER(_cd)], _ci),
+}
+
+STAGES = ["tree_build", "tree_refit", "walk", "group_prep", "knn", "knn_tree", "sph_density",
+          "sph_force", "verlet", "force"]
+
+LIB_PATH = _build.LIB
+_lib = None
+
+
+class GpuError(RuntimeError):
+    """A libgfgpu call reported a non-zero status (GF_ERR_* bits in .status)."""
+
+    def __init__(self, status, msg):
+        super().__init__(f"libgfgpu status {status}: {msg}")
+        self.status = status
+
+
+def load(path=None):
+    """Loads (once) and returns the library with argtypes set."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"{path} is missing: run galaxy_formation_gb300.build.build()")
+    lib = ctypes.CDLL(path)
+    for name, (args, res) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    if path == LIB_PATH:
+        _lib = lib
+    return lib
+
+
+def check(status=None):
+    """Raises GpuError when the last call failed."""
+    lib = load()
+    st = lib.gf_last_status() if status is None else status
+    if st:
+        raise GpuError(st, (lib.gf_last_error() or b"").decode())
+    return st

@@ -1,0 +1,460 @@
+// gf_capi.cu — extern "C" entry points of libgfgpu.so (declared in include/gfgpu.h).
+//
+// Host-pointer entry points keep the reference's calling convention (cpp/nbody.cpp:415-505
+// via galaxy_formation/engine.py; galaxy_formation/sph.py): they copy inputs to the GPU,
+// run the kernels on the library stream, copy results back and synchronise. `_dev` entry
+// points take device pointers and only enqueue work.
+#include <cstring>
+#include <vector>
+
+#include "gf_hydro.cuh"
+
+namespace gf {
+namespace {
+
+struct Staging {
+    DevBuf pos, mass, acc, active, vel, h, u, nb, rho, dudt, dt, dist, cand, r, w, dw;
+    DevBuf img, glow, colors, rot, center, group, out, targets, flags, kind, dt_ind;
+};
+Staging g_st;
+SphScratch g_sph;
+Octree g_knn_tree;
+unsigned long long g_knn_iters = 0;
+
+template <class F>
+int guarded(F&& f) {
+    Context& c = ctx();
+    c.last_status = 0;
+    c.last_error.clear();
+    try {
+        ensure_ready();
+        f();
+    } catch (const Error& e) {
+        c.last_status |= e.code;
+        c.last_error = e.what();
+    } catch (const std::exception& e) {
+        c.last_status |= GF_ERR_CUDA;
+        c.last_error = e.what();
+    }
+    return c.last_status;
+}
+
+inline cudaStream_t pick(void* stream) {
+    return stream ? static_cast<cudaStream_t>(stream) : ctx().stream;
+}
+
+template <class T>
+T* upload(DevBuf& b, const T* host, size_t count, cudaStream_t s) {
+    T* d = b.get<T>(count);
+    if (count) GF_CUDA(cudaMemcpyAsync(d, host, sizeof(T) * count, cudaMemcpyHostToDevice, s));
+    return d;
+}
+
+template <class T>
+void download(T* host, const T* dev, size_t count, cudaStream_t s) {
+    if (count) GF_CUDA(cudaMemcpyAsync(host, dev, sizeof(T) * count, cudaMemcpyDeviceToHost, s));
+}
+
+void require(bool ok, const char* what) {
+    if (!ok) throw Error(GF_ERR_ARG, what);
+}
+
+void accel_active_device(int n, const double* pos, const double* mass, double* acc, double theta,
+                         double eps, const uint8_t* active, int rebuild, cudaStream_t s) {
+    Octree& T = gravity_tree();
+    if (rebuild || !T.valid || T.n != n)
+        T.build(n, pos, mass, theta, s);
+    else
+        T.refit(pos, mass, s);
+    T.prepare_walk(active, s);
+    T.walk(eps, acc, s);
+}
+
+}  // namespace
+}  // namespace gf
+
+using namespace gf;
+
+extern "C" {
+
+int nbody_num_threads(void) {
+    try {
+        ensure_ready();
+        return ctx().sms;
+    } catch (...) {
+        return 0;
+    }
+}
+
+void nbody_accel_active(int n, const double* pos, const double* mass, double* acc, double theta,
+                        double eps, const uint8_t* active, int rebuild) {
+    guarded([&] {
+        require(n >= 0, "n < 0");
+        if (n == 0) return;
+        require(pos && mass && acc, "null array");
+        require(n < (1 << 27), "n too large");
+        cudaStream_t s = ctx().stream;
+        double* d_pos = upload(g_st.pos, pos, 3 * size_t(n), s);
+        double* d_mass = upload(g_st.mass, mass, size_t(n), s);
+        double* d_acc = upload(g_st.acc, acc, 3 * size_t(n), s);
+        const uint8_t* d_act = active ? upload(g_st.active, active, size_t(n), s) : nullptr;
+        accel_active_device(n, d_pos, d_mass, d_acc, theta, eps, d_act, rebuild, s);
+        download(acc, d_acc, 3 * size_t(n), s);
+        collect_status(s);
+    });
+}
+
+void nbody_accel_direct(int n, const double* pos, const double* mass, double* acc, double eps) {
+    guarded([&] {
+        require(n >= 0, "n < 0");
+        if (n == 0) return;
+        require(pos && mass && acc, "null array");
+        cudaStream_t s = ctx().stream;
+        double* d_pos = upload(g_st.pos, pos, 3 * size_t(n), s);
+        double* d_mass = upload(g_st.mass, mass, size_t(n), s);
+        double* d_acc = g_st.acc.get<double>(3 * size_t(n));
+        direct_sum(n, d_pos, d_mass, n, nullptr, d_acc, eps, s);
+        download(acc, d_acc, 3 * size_t(n), s);
+        collect_status(s);
+    });
+}
+
+void nbody_render(int n, const double* pos, const uint8_t* group, int ngroups, const double* rot,
+                  const double* center, double scale, int W, int H, float* img) {
+    guarded([&] {
+        require(n >= 0 && ngroups >= 0 && W >= 0 && H >= 0, "negative size");
+        require(img && rot && center && (n == 0 || (pos && group)), "null array");
+        cudaStream_t s = ctx().stream;
+        const double* d_pos = upload(g_st.pos, pos, 3 * size_t(n), s);
+        const uint8_t* d_grp = upload(g_st.group, group, size_t(n), s);
+        const double* d_rot = upload(g_st.rot, rot, 9, s);
+        const double* d_cen = upload(g_st.center, center, 3, s);
+        const size_t npx = size_t(ngroups) * W * H;
+        float* d_img = g_st.img.get<float>(npx);
+        render_splat(n, d_pos, d_grp, ngroups, d_rot, d_cen, scale, W, H, d_img, s);
+        download(img, d_img, npx, s);
+        collect_status(s);
+    });
+}
+
+void nbody_tonemap(int W, int H, int ngroups, const float* img, const float* glow, int gw, int gh,
+                   const float* colors, float inv_ref, float K, float exposure, uint8_t* out) {
+    guarded([&] {
+        require(W >= 0 && H >= 0 && ngroups >= 0 && gw >= 2 && gh >= 2, "bad size");
+        require(img && glow && colors && out, "null array");
+        cudaStream_t s = ctx().stream;
+        const float* d_img = upload(g_st.img, img, size_t(ngroups) * W * H, s);
+        const float* d_glow = upload(g_st.glow, glow, size_t(ngroups) * gw * gh, s);
+        const float* d_col = upload(g_st.colors, colors, 3 * size_t(ngroups), s);
+        uint8_t* d_out = g_st.out.get<uint8_t>(3 * size_t(W) * H);
+        render_tonemap(W, H, ngroups, d_img, d_glow, gw, gh, d_col, inv_ref, K, exposure, d_out, s);
+        download(out, d_out, 3 * size_t(W) * H, s);
+        collect_status(s);
+    });
+}
+
+int gf_last_status(void) {
+    Context& c = ctx();
+    if (c.ready) {
+        try {
+            GF_CUDA(cudaDeviceSynchronize());
+            collect_status(c.stream);
+        } catch (const Error& e) {
+            c.last_status |= e.code;
+            c.last_error = e.what();
+        }
+    }
+    return c.last_status;
+}
+
+const char* gf_last_error(void) { return ctx().last_error.c_str(); }
+
+int gf_tree_size(int* num_nodes, int* num_groups) {
+    return guarded([&] {
+        Octree& T = gravity_tree();
+        int nn = 0, ng = 0;
+        if (T.valid) {
+            TreeCounts h;
+            GF_CUDA(cudaMemcpy(&h, T.counts.as<TreeCounts>(), sizeof h, cudaMemcpyDeviceToHost));
+            nn = T.nn;
+            ng = h.num_groups;
+        }
+        if (num_nodes) *num_nodes = nn;
+        if (num_groups) *num_groups = ng;
+    });
+}
+
+int gf_tree_export(int32_t* ints, float* floats, int32_t* order, int32_t* groups) {
+    return guarded([&] {
+        Octree& T = gravity_tree();
+        require(T.valid, "no tree");
+        GF_CUDA(cudaDeviceSynchronize());
+        const int nn = T.nn, n = T.n;
+        TreeCounts h;
+        GF_CUDA(cudaMemcpy(&h, T.counts.as<TreeCounts>(), sizeof h, cudaMemcpyDeviceToHost));
+        std::vector<int4> i4(nn);
+        std::vector<float4> mom(nn), geo(nn);
+        std::vector<float> open(nn);
+        GF_CUDA(cudaMemcpy(i4.data(), T.n_i4.p, sizeof(int4) * nn, cudaMemcpyDeviceToHost));
+        GF_CUDA(cudaMemcpy(mom.data(), T.n_mom.p, sizeof(float4) * nn, cudaMemcpyDeviceToHost));
+        GF_CUDA(cudaMemcpy(geo.data(), T.n_geo.p, sizeof(float4) * nn, cudaMemcpyDeviceToHost));
+        GF_CUDA(cudaMemcpy(open.data(), T.n_open.p, sizeof(float) * nn, cudaMemcpyDeviceToHost));
+        for (int k = 0; k < nn; ++k) {
+            ints[4 * k] = i4[k].x;
+            ints[4 * k + 1] = i4[k].y;
+            ints[4 * k + 2] = i4[k].z;
+            ints[4 * k + 3] = i4[k].w & 1;
+            const float f[9] = {mom[k].x, mom[k].y, mom[k].z, mom[k].w, open[k],
+                                geo[k].x, geo[k].y, geo[k].z, geo[k].w};
+            std::memcpy(floats + 9 * size_t(k), f, sizeof f);
+        }
+        GF_CUDA(cudaMemcpy(order, T.perm.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+        GF_CUDA(cudaMemcpy(groups, T.groups.p, sizeof(int32_t) * h.num_groups, cudaMemcpyDeviceToHost));
+    });
+}
+
+int gf_accel_active_dev(int n, const double* pos, const double* mass, double* acc, double theta,
+                        double eps, const uint8_t* active, int rebuild, void* stream) {
+    return guarded([&] {
+        require(n >= 0, "n < 0");
+        if (n == 0) return;
+        require(pos && mass && acc, "null array");
+        require(n < (1 << 27), "n too large");
+        accel_active_device(n, pos, mass, acc, theta, eps, active, rebuild, pick(stream));
+    });
+}
+
+int gf_accel_direct_dev(int n, const double* pos, const double* mass, double* acc, double eps,
+                        void* stream) {
+    return guarded([&] {
+        require(n >= 0, "n < 0");
+        if (n == 0) return;
+        require(pos && mass && acc, "null array");
+        direct_sum(n, pos, mass, n, nullptr, acc, eps, pick(stream));
+    });
+}
+
+int gf_accel_direct_targets(int n, const double* pos, const double* mass, int nt,
+                            const int64_t* targets, double* acc, double eps) {
+    return guarded([&] {
+        require(n >= 0 && nt >= 0, "negative size");
+        if (n == 0 || nt == 0) return;
+        require(pos && mass && targets && acc, "null array");
+        for (int t = 0; t < nt; ++t) require(targets[t] >= 0 && targets[t] < n, "target out of range");
+        cudaStream_t s = ctx().stream;
+        const double* d_pos = upload(g_st.pos, pos, 3 * size_t(n), s);
+        const double* d_mass = upload(g_st.mass, mass, size_t(n), s);
+        const int64_t* d_t = upload(g_st.targets, targets, size_t(nt), s);
+        double* d_acc = g_st.acc.get<double>(3 * size_t(nt));
+        direct_sum(n, d_pos, d_mass, nt, d_t, d_acc, eps, s);
+        download(acc, d_acc, 3 * size_t(nt), s);
+        collect_status(s);
+    });
+}
+
+int gf_sph_kernel(int n, const double* r, const double* h, double* w, double* dw) {
+    return guarded([&] {
+        require(n >= 0, "n < 0");
+        if (n == 0) return;
+        require(r && h && (w || dw), "null array");
+        cudaStream_t s = ctx().stream;
+        const double* d_r = upload(g_st.r, r, size_t(n), s);
+        const double* d_h = upload(g_st.h, h, size_t(n), s);
+        double* d_w = w ? g_st.w.get<double>(n) : nullptr;
+        double* d_dw = dw ? g_st.dw.get<double>(n) : nullptr;
+        sph_kernel_values(n, d_r, d_h, d_w, d_dw, s);
+        if (w) download(w, d_w, size_t(n), s);
+        if (dw) download(dw, d_dw, size_t(n), s);
+        collect_status(s);
+    });
+}
+
+int gf_sph_forces(int n, int k, const double* pos, const double* vel, const double* mass,
+                  const int64_t* nb, const double* h, const double* u, double gamma, double alpha,
+                  double beta, double* rho, double* acc, double* dudt, double* dt_i) {
+    return guarded([&] {
+        require(n >= 0 && k >= 0, "negative size");
+        if (n == 0) return;
+        require(pos && vel && mass && nb && h && u && rho && acc && dudt && dt_i, "null array");
+        for (size_t t = 0; t < size_t(n) * k; ++t) require(nb[t] >= 0 && nb[t] < n, "neighbour out of range");
+        cudaStream_t s = ctx().stream;
+        const double* d_pos = upload(g_st.pos, pos, 3 * size_t(n), s);
+        const double* d_vel = upload(g_st.vel, vel, 3 * size_t(n), s);
+        const double* d_mass = upload(g_st.mass, mass, size_t(n), s);
+        const int64_t* d_nb = upload(g_st.nb, nb, size_t(n) * k, s);
+        const double* d_h = upload(g_st.h, h, size_t(n), s);
+        const double* d_u = upload(g_st.u, u, size_t(n), s);
+        double* d_rho = g_st.rho.get<double>(n);
+        double* d_acc = g_st.acc.get<double>(3 * size_t(n));
+        double* d_dudt = g_st.dudt.get<double>(n);
+        double* d_dt = g_st.dt.get<double>(n);
+        sph_forces<int64_t>(g_sph, n, k, k, d_pos, d_vel, d_mass, d_nb, d_h, d_u, gamma, alpha, beta,
+                            d_rho, d_acc, d_dudt, d_dt, s);
+        download(rho, d_rho, size_t(n), s);
+        download(acc, d_acc, 3 * size_t(n), s);
+        download(dudt, d_dudt, size_t(n), s);
+        download(dt_i, d_dt, size_t(n), s);
+        collect_status(s);
+    });
+}
+
+int gf_sph_forces_dev(int n, int k, const double* pos, const double* vel, const double* mass,
+                      const int64_t* nb, const double* h, const double* u, double gamma, double alpha,
+                      double beta, double* rho, double* acc, double* dudt, double* dt_i, void* stream) {
+    return guarded([&] {
+        require(n >= 0 && k >= 0, "negative size");
+        if (n == 0) return;
+        require(pos && vel && mass && nb && h && u && rho && acc && dudt && dt_i, "null array");
+        sph_forces<int64_t>(g_sph, n, k, k, pos, vel, mass, nb, h, u, gamma, alpha, beta, rho, acc, dudt,
+                            dt_i, pick(stream));
+    });
+}
+
+int gf_knn_from_candidates(int n, int m, const double* pos, const int64_t* cand, int k, int64_t* nb,
+                           double* dist) {
+    int ok = 1;
+    const int st = guarded([&] {
+        require(n >= 0 && m >= 0 && k >= 1, "bad size");
+        require(m <= 64 && k <= m, "need k <= m <= 64");
+        if (n == 0) return;
+        require(pos && cand && nb && dist, "null array");
+        for (size_t t = 0; t < size_t(n) * m; ++t) require(cand[t] >= -1 && cand[t] < n, "candidate out of range");
+        cudaStream_t s = ctx().stream;
+        const double* d_pos = upload(g_st.pos, pos, 3 * size_t(n), s);
+        const int64_t* d_cand = upload(g_st.cand, cand, size_t(n) * m, s);
+        int64_t* d_nb = upload(g_st.nb, nb, size_t(n) * k, s);
+        double* d_dist = upload(g_st.dist, dist, size_t(n) * k, s);
+        int* d_ok = g_st.flags.get<int>(1);
+        GF_CUDA(cudaMemcpyAsync(d_ok, &ok, sizeof(int), cudaMemcpyHostToDevice, s));
+        knn_from_candidates(n, m, d_pos, d_cand, k, d_nb, d_dist, d_ok, s);
+        download(nb, d_nb, size_t(n) * k, s);
+        download(dist, d_dist, size_t(n) * k, s);
+        download(&ok, d_ok, 1, s);
+        collect_status(s);
+    });
+    return st ? -st : ok;
+}
+
+int gf_knn(int n, const double* pos, int k, double* dist, int64_t* nb) {
+    return guarded([&] {
+        require(n >= 1 && k >= 1 && k <= 64 && k <= n, "need 1 <= k <= min(64, n)");
+        require(pos && dist && nb, "null array");
+        require(n < (1 << 27), "n too large");
+        cudaStream_t s = ctx().stream;
+        const double* d_pos = upload(g_st.pos, pos, 3 * size_t(n), s);
+        int64_t* d_nb = g_st.nb.get<int64_t>(size_t(n) * k);
+        double* d_dist = g_st.dist.get<double>(size_t(n) * k);
+        unsigned long long* d_it = g_st.flags.get<unsigned long long>(1);
+        GF_CUDA(cudaMemsetAsync(d_it, 0, sizeof(unsigned long long), s));
+        knn_exact(g_knn_tree, n, d_pos, k, nullptr, d_nb, d_dist, d_it, s);
+        download(nb, d_nb, size_t(n) * k, s);
+        download(dist, d_dist, size_t(n) * k, s);
+        download(&g_knn_iters, d_it, 1, s);
+        collect_status(s);
+    });
+}
+
+long long gf_knn_iterations(void) { return (long long)g_knn_iters; }
+
+static void force_args_check(int n, const void* pos, const void* vel, const void* mass, const void* kind,
+                             const void* u, const void* acc, const void* dt_ind) {
+    require(n >= 0, "n < 0");
+    require(n < (1 << 27), "n too large");
+    require(n == 0 || (pos && vel && mass && kind && u && acc && dt_ind), "null array");
+}
+
+int gf_accelerations_dev(int n, const double* pos, const double* vel, const double* mass,
+                         const int8_t* kind, const double* u, double theta, double eps, double gamma,
+                         double alpha, double beta, const uint8_t* active, int rebuild, int sph,
+                         int fresh_nb, double* acc, double* dt_ind, void* stream) {
+    return guarded([&] {
+        force_args_check(n, pos, vel, mass, kind, u, acc, dt_ind);
+        if (n == 0) return;
+        ForceArgs a{n, pos, vel, mass, kind, u, theta, eps, gamma, alpha, beta, active, rebuild, sph,
+                    fresh_nb, acc, dt_ind};
+        force_engine().evaluate(a, pick(stream));
+    });
+}
+
+int gf_accelerations(int n, const double* pos, const double* vel, const double* mass, const int8_t* kind,
+                     const double* u, double theta, double eps, double gamma, double alpha, double beta,
+                     const uint8_t* active, int rebuild, int sph, int fresh_nb, double* acc,
+                     double* dt_ind) {
+    return guarded([&] {
+        force_args_check(n, pos, vel, mass, kind, u, acc, dt_ind);
+        if (n == 0) return;
+        cudaStream_t s = ctx().stream;
+        ForceArgs a{n,
+                    upload(g_st.pos, pos, 3 * size_t(n), s),
+                    upload(g_st.vel, vel, 3 * size_t(n), s),
+                    upload(g_st.mass, mass, size_t(n), s),
+                    upload(g_st.kind, kind, size_t(n), s),
+                    upload(g_st.u, u, size_t(n), s),
+                    theta, eps, gamma, alpha, beta,
+                    active ? upload(g_st.active, active, size_t(n), s) : nullptr,
+                    rebuild, sph, fresh_nb,
+                    g_st.acc.get<double>(3 * size_t(n)),
+                    g_st.dt_ind.get<double>(size_t(n))};
+        force_engine().evaluate(a, s);
+        download(acc, a.acc, 3 * size_t(n), s);
+        download(dt_ind, a.dt_ind, size_t(n), s);
+        collect_status(s);
+    });
+}
+
+int gf_profile(int on) {
+    return guarded([&] {
+        GF_CUDA(cudaDeviceSynchronize());
+        ctx().prof.clear();
+        ctx().prof.on = on != 0;
+    });
+}
+
+int gf_profile_stage(int stage, double* total_ms, int* launches) {
+    return guarded([&] {
+        require(stage >= 0 && stage < kStCount, "bad stage");
+        GF_CUDA(cudaDeviceSynchronize());
+        double t = 0;
+        for (auto& pr : ctx().prof.recs[stage]) {
+            float ms = 0;
+            GF_CUDA(cudaEventElapsedTime(&ms, pr.first, pr.second));
+            t += ms;
+        }
+        if (total_ms) *total_ms = t;
+        if (launches) *launches = int(ctx().prof.recs[stage].size());
+    });
+}
+
+long long gf_launch_count(void) { return ctx().launches; }
+
+int gf_fp32_peak(double* tflops) {
+    return guarded([&] {
+        require(tflops != nullptr, "null pointer");
+        *tflops = fp32_peak_tflops();
+    });
+}
+
+long long gf_walk_pairs(void) {
+    unsigned long long p = 0;
+    guarded([&] {
+        Octree& T = gravity_tree();
+        if (!T.valid) return;
+        GF_CUDA(cudaDeviceSynchronize());
+        GF_CUDA(cudaMemcpy(&p, &T.counts.as<TreeCounts>()->pairs, sizeof p, cudaMemcpyDeviceToHost));
+    });
+    return (long long)p;
+}
+
+int gf_force_info(int* n_gas, double* dt_grav, double* dt_gas, long long* knn_iters) {
+    return guarded([&] {
+        ForceEngine& F = force_engine();
+        GF_CUDA(cudaDeviceSynchronize());
+        const HydroScalars* h = F.scalars_h;
+        if (n_gas) *n_gas = h ? F.ng : 0;
+        if (dt_grav) *dt_grav = h ? h->dt_grav : 0.0;
+        if (dt_gas) *dt_gas = h ? h->dt_gas : 0.0;
+        if (knn_iters) *knn_iters = h ? (long long)h->knn_iters : 0;
+    });
+}
+
+}  // extern "C"

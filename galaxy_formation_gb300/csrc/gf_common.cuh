@@ -1,0 +1,167 @@
+// gf_common.cuh — shared definitions of the GB300 force library (libgfgpu.so).
+//
+// Error model: internal host code throws gf::Error; every extern "C" entry point catches it
+// and turns it into a status word readable through gf_last_status()/gf_last_error().
+// Kernels never trap: they OR a bit into a device status word (ctx.d_status) and return.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/gfgpu.h"
+
+namespace gf {
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+[[noreturn]] void cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+
+#define GF_CUDA(call)                                                  \
+    do {                                                               \
+        cudaError_t gf_e_ = (call);                                    \
+        if (gf_e_ != cudaSuccess) gf::cuda_fail(gf_e_, #call, __FILE__, __LINE__); \
+    } while (0)
+
+#define GF_CHECK_LAUNCH()               \
+    do {                                \
+        GF_CUDA(cudaGetLastError());    \
+        ++gf::ctx().launches;           \
+    } while (0)
+
+// A grow-only device allocation.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    template <class T>
+    T* get(size_t count) {
+        const size_t need = count * sizeof(T) + 256;
+        if (need > bytes) {
+            if (p) GF_CUDA(cudaFree(p));
+            p = nullptr;
+            bytes = 0;
+            GF_CUDA(cudaMalloc(&p, need));
+            bytes = need;
+        }
+        return static_cast<T*>(p);
+    }
+    template <class T>
+    T* as() const { return static_cast<T*>(p); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
+constexpr int kWarp = 32;
+
+__host__ __device__ inline int div_up(long long a, long long b) { return int((a + b - 1) / b); }
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+__device__ __forceinline__ int warp_incl_scan(int v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_min(float v) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ int warp_sum(int v) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ void raise_status(uint32_t* st, uint32_t bit) {
+    if (st) atomicOr(st, bit);
+}
+
+// Device-wide exclusive scan of int32 (n may be 0). `total` (device) receives the sum.
+void exclusive_scan(const int* in, int* out, int n, int* total, cudaStream_t s);
+
+// Stable LSD radix sort of (key, value) pairs on bits [bit_lo, bit_hi) of the keys.
+// Results end in keys/vals (the alternate buffers are scratch of the same size).
+void radix_sort_pairs(uint64_t* keys, int* vals, uint64_t* keys_alt, int* vals_alt, int n,
+                      int bit_lo, int bit_hi, cudaStream_t s);
+
+// Timed stages (CUDA events recorded on the launching stream while profiling is on).
+enum Stage {
+    kStTreeBuild = 0,  // whole gravity tree build (bbox .. walk layout)
+    kStTreeRefit,      // refit
+    kStWalk,           // the walk kernel (k_walk_mono) alone
+    kStGroupPrep,      // work list of active groups
+    kStKnn,            // neighbour-search kernel (k_knn) alone
+    kStKnnTree,        // octree of the gas for the neighbour search
+    kStSphDensity,     // density kernel alone
+    kStSphForce,       // force kernel alone
+    kStVerlet,         // Verlet reselection
+    kStForce,          // one whole force evaluation
+    kStCount
+};
+
+struct Profiler {
+    bool on = false;
+    std::vector<cudaEvent_t> pool;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> recs[kStCount];
+    cudaEvent_t take();
+    void clear();
+};
+
+// Records the start/stop events of a stage around a scope (no-op when profiling is off).
+struct ProfScope {
+    int stage;
+    cudaStream_t s;
+    bool on;
+    ProfScope(int st, cudaStream_t st_s);
+    ~ProfScope();
+};
+
+// Per-process state shared by every entry point.
+struct Context {
+    bool ready = false;
+    int device = -1;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    uint32_t* d_status = nullptr;   // device status word (kernels OR bits into it)
+    uint32_t* h_status = nullptr;   // pinned host mirror
+    int last_status = 0;
+    std::string last_error;
+    DevBuf scan_tmp, sort_tmp;      // scratch of the scan / radix sort
+    long long launches = 0;         // kernels launched since load
+    Profiler prof;
+};
+
+Context& ctx();
+void ensure_ready();
+// Measured float32 FFMA throughput of this GPU (TFLOP/s, FMA = 2 flops), best of 5.
+double fp32_peak_tflops();
+// Adds the device status word to the host status and clears it (synchronises `s`).
+int collect_status(cudaStream_t s);
+
+}  // namespace gf

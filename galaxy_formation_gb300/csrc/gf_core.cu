@@ -1,0 +1,349 @@
+// gf_core.cu — library context, status handling, device-wide scan and radix sort.
+//
+// Radix sort: stable LSD sort of (uint64 key, int32 value) pairs, 8-bit digits. Per digit:
+//   upsweep   per-tile digit histograms (warp-aggregated shared-memory atomics),
+//   scan      one exclusive scan over the digit-major histogram table [256][tiles],
+//   downsweep stable in-tile ranks (__match_any_sync per warp, warp-ordered tiles) and
+//             scatter to the scanned offsets.
+// Tiles are 4096 keys (256 threads x 16). Traffic per pass: 8 B read (upsweep) + 12 B read
+// + 12 B write (downsweep) per pair.
+#include <cstdarg>
+#include <algorithm>
+#include <cstring>
+
+#include "gf_common.cuh"
+
+namespace gf {
+
+static Context g_ctx;
+
+Context& ctx() { return g_ctx; }
+
+void cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
+    char buf[512];
+    snprintf(buf, sizeof buf, "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+    throw Error(GF_ERR_CUDA, buf);
+}
+
+void ensure_ready() {
+    Context& c = g_ctx;
+    if (c.ready) return;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        throw Error(GF_ERR_NO_DEVICE, "no CUDA device");
+    }
+    GF_CUDA(cudaGetDevice(&c.device));
+    GF_CUDA(cudaDeviceGetAttribute(&c.sms, cudaDevAttrMultiProcessorCount, c.device));
+    GF_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    GF_CUDA(cudaMalloc(&c.d_status, sizeof(uint32_t)));
+    GF_CUDA(cudaMemset(c.d_status, 0, sizeof(uint32_t)));
+    GF_CUDA(cudaMallocHost(&c.h_status, sizeof(uint32_t)));
+    *c.h_status = 0;
+    c.ready = true;
+}
+
+cudaEvent_t Profiler::take() {
+    if (!pool.empty()) {
+        cudaEvent_t e = pool.back();
+        pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    GF_CUDA(cudaEventCreate(&e));
+    return e;
+}
+
+void Profiler::clear() {
+    for (auto& v : recs) {
+        for (auto& pr : v) {
+            pool.push_back(pr.first);
+            pool.push_back(pr.second);
+        }
+        v.clear();
+    }
+}
+
+ProfScope::ProfScope(int st, cudaStream_t st_s) : stage(st), s(st_s), on(g_ctx.prof.on) {
+    if (!on) return;
+    Profiler& P = g_ctx.prof;
+    cudaEvent_t a = P.take(), b = P.take();
+    P.recs[stage].push_back({a, b});
+    GF_CUDA(cudaEventRecord(a, s));
+}
+
+ProfScope::~ProfScope() {
+    if (!on) return;
+    cudaEventRecord(g_ctx.prof.recs[stage].back().second, s);
+}
+
+int collect_status(cudaStream_t s) {
+    Context& c = g_ctx;
+    GF_CUDA(cudaMemcpyAsync(c.h_status, c.d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    GF_CUDA(cudaMemsetAsync(c.d_status, 0, sizeof(uint32_t), s));
+    GF_CUDA(cudaStreamSynchronize(s));
+    const int st = int(*c.h_status);
+    if (st) {
+        c.last_status |= st;
+        if (c.last_error.empty()) {
+            char buf[128];
+            snprintf(buf, sizeof buf, "device status 0x%x", st);
+            c.last_error = buf;
+        }
+    }
+    return st;
+}
+
+// ---------------------------------------------------------------------------------------
+// exclusive scan (int32): tile sums -> scan of tile sums -> per-tile scan + offset
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ int block_excl_scan(int v, int* s_warp, int* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
+    int incl = warp_incl_scan(v);
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < nw ? s_warp[lane] : 0;
+        int wi = warp_incl_scan(w);
+        if (lane < nw) s_warp[lane] = wi - w;
+        if (lane == nw - 1) s_warp[32] = wi;
+    }
+    __syncthreads();
+    const int r = incl - v + s_warp[warp];
+    if (total) *total = s_warp[32];
+    __syncthreads();
+    return r;
+}
+
+__global__ void k_scan_tile_sums(const int* __restrict__ in, int n, int* __restrict__ sums) {
+    __shared__ int s_warp[33];
+    const int base = blockIdx.x * kScanTile;
+    int acc = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const int i = base + k * kScanThreads + threadIdx.x;
+        if (i < n) acc += in[i];
+    }
+    int tot;
+    block_excl_scan(acc, s_warp, &tot);
+    if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+// single block: exclusive scan of `cnt` tile sums in place, total to *total
+__global__ void k_scan_sums(int* sums, int cnt, int* total) {
+    __shared__ int s_warp[33];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < cnt; base += blockDim.x * kScanItems) {
+        int v[kScanItems];
+        int acc = 0;
+        const int b0 = base + threadIdx.x * kScanItems;
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            v[k] = (b0 + k < cnt) ? sums[b0 + k] : 0;
+            acc += v[k];
+        }
+        int tot;
+        int ex = block_excl_scan(acc, s_warp, &tot) + carry;
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            if (b0 + k < cnt) sums[b0 + k] = ex;
+            ex += v[k];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && total) *total = carry;
+}
+
+__global__ void k_scan_tiles(const int* __restrict__ in, int* __restrict__ out, int n,
+                             const int* __restrict__ offs) {
+    __shared__ int s_warp[33];
+    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    int v[kScanItems];
+    int acc = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        v[k] = (base + k < n) ? in[base + k] : 0;
+        acc += v[k];
+    }
+    int ex = block_excl_scan(acc, s_warp, nullptr) + offs[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        if (base + k < n) out[base + k] = ex;
+        ex += v[k];
+    }
+}
+
+void exclusive_scan(const int* in, int* out, int n, int* total, cudaStream_t s) {
+    Context& c = g_ctx;
+    if (n <= 0) {
+        if (total) GF_CUDA(cudaMemsetAsync(total, 0, sizeof(int), s));
+        return;
+    }
+    const int tiles = div_up(n, kScanTile);
+    int* sums = c.scan_tmp.get<int>(size_t(tiles) + 1);
+    k_scan_tile_sums<<<tiles, kScanThreads, 0, s>>>(in, n, sums);
+    GF_CHECK_LAUNCH();
+    k_scan_sums<<<1, 1024, 0, s>>>(sums, tiles, total);
+    GF_CHECK_LAUNCH();
+    k_scan_tiles<<<tiles, kScanThreads, 0, s>>>(in, out, n, sums);
+    GF_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------------------
+// radix sort
+
+constexpr int kRsThreads = 256;
+constexpr int kRsWarps = kRsThreads / 32;
+constexpr int kRsItems = 16;                  // per thread
+constexpr int kRsWarpItems = 32 * kRsItems;   // 512 consecutive keys per warp
+constexpr int kRsTile = kRsThreads * kRsItems;
+
+__global__ void __launch_bounds__(kRsThreads) k_rs_upsweep(const uint64_t* __restrict__ keys, int n,
+                                                           int shift, int* __restrict__ hist,
+                                                           int tiles) {
+    __shared__ int h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int base = blockIdx.x * kRsTile + warp * kRsWarpItems;
+#pragma unroll 4
+    for (int s = 0; s < kRsItems; ++s) {
+        const int i = base + s * 32 + lane;
+        const bool ok = i < n;
+        const unsigned d = ok ? unsigned((keys[i] >> shift) & 255u) : 256u;
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        if (ok && lane == __ffs(peers) - 1) atomicAdd(&h[d], __popc(peers));
+    }
+    __syncthreads();
+    hist[threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(kRsThreads) k_rs_downsweep(
+    const uint64_t* __restrict__ kin, const int* __restrict__ vin, uint64_t* __restrict__ kout,
+    int* __restrict__ vout, int n, int shift, const int* __restrict__ offs, int tiles) {
+    __shared__ int s_cnt[kRsWarps][256];
+    __shared__ int s_off[256];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int w = 0; w < kRsWarps; ++w) s_cnt[w][threadIdx.x] = 0;
+    s_off[threadIdx.x] = offs[threadIdx.x * tiles + blockIdx.x];
+    __syncthreads();
+    const int base = blockIdx.x * kRsTile + warp * kRsWarpItems;
+    uint64_t k[kRsItems];
+    int v[kRsItems];
+    int rank[kRsItems];
+    const unsigned lt = lanemask_lt();
+#pragma unroll
+    for (int s = 0; s < kRsItems; ++s) {
+        const int i = base + s * 32 + lane;
+        const bool ok = i < n;
+        k[s] = ok ? kin[i] : 0ull;
+        v[s] = ok ? vin[i] : 0;
+        const unsigned d = ok ? unsigned((k[s] >> shift) & 255u) : 256u;
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const int before = ok ? s_cnt[warp][d] : 0;
+        rank[s] = before + __popc(peers & lt);
+        __syncwarp();
+        if (ok && lane == __ffs(peers) - 1) s_cnt[warp][d] = before + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    {   // exclusive prefix over warps, per digit (thread t owns digit t)
+        int run = 0;
+        for (int w = 0; w < kRsWarps; ++w) {
+            const int c = s_cnt[w][threadIdx.x];
+            s_cnt[w][threadIdx.x] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < kRsItems; ++s) {
+        const int i = base + s * 32 + lane;
+        if (i < n) {
+            const unsigned d = unsigned((k[s] >> shift) & 255u);
+            const int pos = s_off[d] + s_cnt[warp][d] + rank[s];
+            kout[pos] = k[s];
+            vout[pos] = v[s];
+        }
+    }
+}
+
+void radix_sort_pairs(uint64_t* keys, int* vals, uint64_t* keys_alt, int* vals_alt, int n,
+                      int bit_lo, int bit_hi, cudaStream_t s) {
+    if (n <= 1) return;
+    Context& c = g_ctx;
+    const int tiles = div_up(n, kRsTile);
+    int* hist = c.sort_tmp.get<int>(size_t(256) * tiles * 2);
+    int* offs = hist + size_t(256) * tiles;
+    uint64_t *ka = keys, *kb = keys_alt;
+    int *va = vals, *vb = vals_alt;
+    int passes = 0;
+    for (int shift = bit_lo; shift < bit_hi; shift += 8) {
+        k_rs_upsweep<<<tiles, kRsThreads, 0, s>>>(ka, n, shift, hist, tiles);
+        GF_CHECK_LAUNCH();
+        exclusive_scan(hist, offs, 256 * tiles, nullptr, s);
+        k_rs_downsweep<<<tiles, kRsThreads, 0, s>>>(ka, va, kb, vb, n, shift, offs, tiles);
+        GF_CHECK_LAUNCH();
+        std::swap(ka, kb);
+        std::swap(va, vb);
+        ++passes;
+    }
+    if (passes & 1) {
+        GF_CUDA(cudaMemcpyAsync(keys, ka, sizeof(uint64_t) * n, cudaMemcpyDeviceToDevice, s));
+        GF_CUDA(cudaMemcpyAsync(vals, va, sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// FP32 CUDA-core calibration: 8 independent FFMA chains per thread, all SMs busy.
+
+__global__ void k_ffma_peak(float* out, int iters, float a, float b) {
+    float x[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = threadIdx.x * 1e-3f + k;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) x[k] = fmaf(x[k], a, b);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += x[k];
+    if (s == 12345.678f) out[0] = s;  // keeps the chains alive
+}
+
+double fp32_peak_tflops() {
+    Context& c = g_ctx;
+    float* out = c.scan_tmp.get<float>(1);
+    const int blocks = c.sms * 8, threads = 256, iters = 4096;
+    cudaEvent_t e0, e1;
+    GF_CUDA(cudaEventCreate(&e0));
+    GF_CUDA(cudaEventCreate(&e1));
+    k_ffma_peak<<<blocks, threads, 0, c.stream>>>(out, iters, 0.9999f, 1e-4f);  // warm-up
+    GF_CHECK_LAUNCH();
+    double best = 0;
+    for (int rep = 0; rep < 5; ++rep) {
+        GF_CUDA(cudaEventRecord(e0, c.stream));
+        k_ffma_peak<<<blocks, threads, 0, c.stream>>>(out, iters, 0.9999f, 1e-4f);
+        GF_CHECK_LAUNCH();
+        GF_CUDA(cudaEventRecord(e1, c.stream));
+        GF_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        GF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        const double flops = 2.0 * 8 * double(iters) * blocks * threads;
+        best = std::max(best, flops / (ms * 1e-3) / 1e12);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return best;
+}
+
+}  // namespace gf

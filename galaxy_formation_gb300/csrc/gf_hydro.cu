@@ -1,0 +1,330 @@
+// gf_hydro.cu — one device-resident force evaluation: GalaxyFormation.accelerations() and
+// _hydro() of galaxy_formation/simulation.py:61-95, with the SPH neighbour cache of
+// NeighbourFinder (galaxy_formation/sph.py:138-170), all on the GPU.
+//
+//   gravity ........ Barnes-Hut of the active particles into the persistent acc_grav
+//                    (inactive rows keep their previous value, as self.acc_grav does);
+//   _hydro ......... (when sph) gas = flatnonzero(kind == GAS); returns early at <= 40 gas;
+//                    neighbours: on a sub-step (fresh_nb = 0) the 32 nearest are re-selected
+//                    among the 48 cached candidates that are still gas; a full search runs
+//                    when fresh_nb, when some gas particle is not in the cache, or when a
+//                    particle has fewer than 32 candidates left; h = max(d_32 / 2, eps / 2);
+//                    sph_forces; acc_sph and dt_courant scattered to global rows (zero / inf
+//                    elsewhere); dt_gas = min dt_i;
+//   combination .... acc = acc_grav + acc_sph, dt_ind = min(0.3 sqrt(eps / |a|), dt_courant),
+//                    dt_grav = 0.3 sqrt(eps / max |a|)  (|a| floored at 1e-30).
+// When sph = 0, acc_sph and dt_courant keep the values of the last hydro call, as in the
+// reference.
+#include <algorithm>
+#include <cfloat>
+
+#include "gf_hydro.cuh"
+
+namespace gf {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kCand = 48;   // sph.py:27 N_CANDIDATES
+constexpr int kNgb = 32;    // sph.py:26 N_NEIGHBOURS
+
+__global__ void k_gas_flag(int n, const int8_t* __restrict__ kind, int* __restrict__ flag) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) flag[i] = kind[i] == 0 ? 1 : 0;
+}
+
+__global__ void k_gas_gather(int n, const int* __restrict__ flag, const int* __restrict__ scan,
+                             const double* __restrict__ pos, const double* __restrict__ vel,
+                             const double* __restrict__ mass, const double* __restrict__ u,
+                             int* __restrict__ gidx, double* __restrict__ gpos, double* __restrict__ gvel,
+                             double* __restrict__ gmass, double* __restrict__ gu) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !flag[i]) return;
+    const int g = scan[i];
+    gidx[g] = i;
+    for (int a = 0; a < 3; ++a) {
+        gpos[3 * size_t(g) + a] = pos[3 * size_t(i) + a];
+        gvel[3 * size_t(g) + a] = vel[3 * size_t(i) + a];
+    }
+    gmass[g] = mass[i];
+    gu[g] = u[i];
+}
+
+// loc[global] = local gas index (loc preset to -1); fails when a gas particle has no cache row
+__global__ void k_verlet_prep(int ng, const int* __restrict__ gidx, const int* __restrict__ row,
+                              int* __restrict__ loc, int* __restrict__ fail) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ng) return;
+    const int g = gidx[i];
+    loc[g] = i;
+    if (row[g] < 0) *fail = 1;
+}
+
+// sph.py:155-164 + knn_from_candidates (sph.py:109-135): one warp per gas particle.
+constexpr int kSelWarps = 8;
+__global__ void __launch_bounds__(kSelWarps * 32) k_verlet_select(
+    int ng, const int* __restrict__ gidx, const int* __restrict__ row, const int* __restrict__ cache,
+    const int* __restrict__ loc, const double* __restrict__ gpos, int* __restrict__ nb, double* __restrict__ d31,
+    int* __restrict__ fail) {
+    __shared__ double s_key[kSelWarps][64];
+    __shared__ int s_tag[kSelWarps][64];
+    __shared__ int s_loc[kSelWarps][64];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int i = blockIdx.x * kSelWarps + w; i < ng; i += gridDim.x * kSelWarps) {
+        const int r = row[gidx[i]];
+        if (r < 0) continue;  // handled by k_verlet_prep's flag
+        const double xi = gpos[3 * size_t(i)], yi = gpos[3 * size_t(i) + 1], zi = gpos[3 * size_t(i) + 2];
+        int valid = 0;
+        for (int jj = lane; jj < 64; jj += 32) {
+            double d2 = INFINITY;
+            int j = -1;
+            if (jj < kCand) {
+                const int c = cache[size_t(r) * kCand + jj];
+                j = c >= 0 ? loc[c] : -1;
+                if (j >= 0) {
+                    const double dx = xi - gpos[3 * size_t(j)], dy = yi - gpos[3 * size_t(j) + 1],
+                                 dz = zi - gpos[3 * size_t(j) + 2];
+                    d2 = dx * dx + dy * dy + dz * dz;
+                    ++valid;
+                }
+            }
+            s_key[w][jj] = d2;
+            s_tag[w][jj] = jj;
+            s_loc[w][jj] = j;
+        }
+        valid = warp_sum(valid);
+        __syncwarp();
+        if (valid < kNgb) {
+            if (lane == 0) *fail = 1;
+            continue;
+        }
+        // bitonic sort of 64 (key, slot) pairs
+        for (int size = 2; size <= 64; size <<= 1) {
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                const int t = lane;
+                const int a = 2 * stride * (t / stride) + (t % stride);
+                const int b = a + stride;
+                const bool up = (a & size) == 0;
+                const double ka = s_key[w][a], kb = s_key[w][b];
+                const int ta = s_tag[w][a], tb = s_tag[w][b];
+                const bool gt = ka > kb || (ka == kb && ta > tb);
+                if (gt == up) {
+                    s_key[w][a] = kb;
+                    s_key[w][b] = ka;
+                    s_tag[w][a] = tb;
+                    s_tag[w][b] = ta;
+                }
+                __syncwarp();
+            }
+        }
+        nb[size_t(i) * kCand + lane] = s_loc[w][s_tag[w][lane]];
+        if (lane == kNgb - 1) d31[i] = sqrt(s_key[w][lane]);
+        __syncwarp();
+    }
+}
+
+__global__ void k_cache_store(int ng, int kq, const int* __restrict__ gidx, const int* __restrict__ nb,
+                              int* __restrict__ row, int* __restrict__ cache) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ng) return;
+    row[gidx[i]] = i;
+    for (int jj = 0; jj < kCand; ++jj)
+        cache[size_t(i) * kCand + jj] = jj < kq ? gidx[nb[size_t(i) * kCand + jj]] : -1;
+}
+
+__global__ void k_guess(int ng, const int* __restrict__ gidx, const double* __restrict__ hprev, float* __restrict__ rg) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ng) return;
+    // the 48th neighbour lies near 2 h (48/32)^(1/3) = 2.29 h; start slightly outside
+    rg[i] = float(2.4 * hprev[gidx[i]]);
+}
+
+__global__ void k_smoothing(int ng, const double* __restrict__ d31, double eps, const int* __restrict__ gidx,
+                            double* __restrict__ h, double* __restrict__ hprev) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ng) return;
+    const double v = fmax(0.5 * d31[i], 0.5 * eps);  // simulation.py:84
+    h[i] = v;
+    hprev[gidx[i]] = 0.5 * d31[i] > 0 ? 0.5 * d31[i] : v;
+}
+
+__global__ void k_fill(int n, double* __restrict__ a, double v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = v;
+}
+
+__global__ void k_scatter_sph(int ng, const int* __restrict__ gidx, const double* __restrict__ a,
+                              const double* __restrict__ dti, double* __restrict__ acc_sph,
+                              double* __restrict__ dt_courant, unsigned long long* __restrict__ dtmin_bits) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v = INFINITY;
+    if (i < ng) {
+        const int g = gidx[i];
+        for (int c = 0; c < 3; ++c) acc_sph[3 * size_t(g) + c] = a[3 * size_t(i) + c];
+        dt_courant[g] = dti[i];
+        v = dti[i];
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0 && v >= 0) atomicMin(dtmin_bits, __double_as_longlong(v));
+}
+
+__global__ void k_combine(int n, const double* __restrict__ ag, const double* __restrict__ as,
+                          const double* __restrict__ dtc, double eps, double* __restrict__ acc,
+                          double* __restrict__ dt_ind, unsigned long long* __restrict__ amax_bits) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double m = 0;
+    if (i < n) {
+        double a2 = 0;
+        for (int c = 0; c < 3; ++c) {
+            const double v = ag[3 * size_t(i) + c] + as[3 * size_t(i) + c];
+            acc[3 * size_t(i) + c] = v;
+            a2 += v * v;
+        }
+        m = sqrt(a2);
+        dt_ind[i] = fmin(0.3 * sqrt(eps / fmax(m, 1e-30)), dtc[i]);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(amax_bits, __double_as_longlong(m));
+}
+
+__global__ void k_finish(HydroScalars* sc, double eps) {
+    const double amax = __longlong_as_double(sc->amax_bits);
+    sc->dt_grav = 0.3 * sqrt(eps / fmax(amax, 1e-30));
+    sc->dt_gas = sc->ng > 40 ? __longlong_as_double(sc->dtmin_bits) : INFINITY;
+}
+
+}  // namespace
+
+static ForceEngine g_force;
+ForceEngine& force_engine() { return g_force; }
+
+void ForceEngine::evaluate(const ForceArgs& a, cudaStream_t s) {
+    Context& C = ctx();
+    ProfScope ps(kStForce, s);
+    const int n = a.n;
+    if (n_total != n) {  // new particle set: reset persistent state (np.zeros / np.full)
+        n_total = n;
+        double* ag = acc_grav.get<double>(3 * size_t(n));
+        GF_CUDA(cudaMemsetAsync(ag, 0, sizeof(double) * 3 * size_t(n), s));
+        GF_CUDA(cudaMemsetAsync(acc_sph.get<double>(3 * size_t(n)), 0, sizeof(double) * 3 * size_t(n), s));
+        k_fill<<<div_up(n, kThreads), kThreads, 0, s>>>(n, dt_courant.get<double>(n), INFINITY);
+        GF_CHECK_LAUNCH();
+        GF_CUDA(cudaMemsetAsync(h_prev.get<double>(n), 0, sizeof(double) * size_t(n), s));
+        cache_valid = false;
+        have_hprev = false;
+        row.get<int>(n);
+        loc.get<int>(n);
+    }
+    if (!scalars_h) GF_CUDA(cudaMallocHost(&scalars_h, sizeof(HydroScalars)));
+    HydroScalars* sc = scalars.get<HydroScalars>(1);
+
+    // gravity (simulation.py:64)
+    Octree& T = gravity_tree();
+    if (a.rebuild || !T.valid || T.n != n)
+        T.build(n, a.pos, a.mass, a.theta, s);
+    else
+        T.refit(a.pos, a.mass, s);
+    T.prepare_walk(a.active, s);
+    T.walk(a.eps, acc_grav.as<double>(), s);
+
+    if (a.sph) hydro(a, s);
+
+    // combination (simulation.py:68-71)
+    GF_CUDA(cudaMemsetAsync(&sc->amax_bits, 0, sizeof(unsigned long long), s));
+    k_combine<<<div_up(n, kThreads), kThreads, 0, s>>>(n, acc_grav.as<double>(), acc_sph.as<double>(),
+                                                       dt_courant.as<double>(), a.eps, a.acc, a.dt_ind,
+                                                       &sc->amax_bits);
+    GF_CHECK_LAUNCH();
+    k_finish<<<1, 1, 0, s>>>(sc, a.eps);
+    GF_CHECK_LAUNCH();
+    GF_CUDA(cudaMemcpyAsync(scalars_h, sc, sizeof(HydroScalars), cudaMemcpyDeviceToHost, s));
+    (void)C;
+}
+
+void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
+    const int n = a.n;
+    const int grid = div_up(n, kThreads);
+    HydroScalars* sc = scalars.as<HydroScalars>();
+    double* as = acc_sph.as<double>();
+    double* dtc = dt_courant.as<double>();
+    GF_CUDA(cudaMemsetAsync(as, 0, sizeof(double) * 3 * size_t(n), s));  // simulation.py:75-76
+    k_fill<<<grid, kThreads, 0, s>>>(n, dtc, INFINITY);
+    GF_CHECK_LAUNCH();
+
+    int* fl = flag.get<int>(n);
+    int* sc_ = scan.get<int>(n);
+    k_gas_flag<<<grid, kThreads, 0, s>>>(n, a.kind, fl);
+    GF_CHECK_LAUNCH();
+    GF_CUDA(cudaMemsetAsync(sc, 0, sizeof(HydroScalars), s));
+    GF_CUDA(cudaMemsetAsync(&sc->dtmin_bits, 0x7f, sizeof(unsigned long long), s));
+    exclusive_scan(fl, sc_, n, &sc->ng, s);
+    GF_CUDA(cudaMemcpyAsync(&scalars_h->ng, &sc->ng, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GF_CUDA(cudaStreamSynchronize(s));
+    ng = scalars_h->ng;
+    if (ng <= 40) {  // simulation.py:80
+        ng_valid = 0;
+        return;
+    }
+    ng_valid = ng;
+    int* gi = gidx.get<int>(ng);
+    double* gp = gpos.get<double>(3 * size_t(ng));
+    double* gv = gvel.get<double>(3 * size_t(ng));
+    double* gm = gmass.get<double>(ng);
+    double* gu = gu_.get<double>(ng);
+    k_gas_gather<<<grid, kThreads, 0, s>>>(n, fl, sc_, a.pos, a.vel, a.mass, a.u, gi, gp, gv, gm, gu);
+    GF_CHECK_LAUNCH();
+
+    const int ggrid = div_up(ng, kThreads);
+    int* nb = nb48.get<int>(size_t(ng) * kCand);
+    double* d31 = dsel.get<double>(ng);
+    bool have_nb = false;
+    if (!a.fresh_nb && cache_valid) {
+        int* lc = loc.as<int>();
+        GF_CUDA(cudaMemsetAsync(lc, 0xff, sizeof(int) * size_t(n), s));
+        GF_CUDA(cudaMemsetAsync(&sc->fail, 0, sizeof(int), s));
+        k_verlet_prep<<<ggrid, kThreads, 0, s>>>(ng, gi, row.as<int>(), lc, &sc->fail);
+        GF_CHECK_LAUNCH();
+        const int blocks = std::min(div_up(ng, kSelWarps), 16 * ctx().sms);
+        ProfScope pv(kStVerlet, s);
+        k_verlet_select<<<blocks, kSelWarps * 32, 0, s>>>(ng, gi, row.as<int>(), cache.as<int>(), lc, gp, nb,
+                                                          d31, &sc->fail);
+        GF_CHECK_LAUNCH();
+        GF_CUDA(cudaMemcpyAsync(&scalars_h->fail, &sc->fail, sizeof(int), cudaMemcpyDeviceToHost, s));
+        GF_CUDA(cudaStreamSynchronize(s));
+        have_nb = scalars_h->fail == 0;
+        verlet_hits += have_nb ? 1 : 0;
+    }
+    if (!have_nb) {  // full search, 48 candidates (sph.py:165-169)
+        const int kq = std::min(kCand, ng);
+        float* rg = nullptr;
+        if (have_hprev) {
+            rg = rguess.get<float>(ng);
+            k_guess<<<ggrid, kThreads, 0, s>>>(ng, gi, h_prev.as<double>(), rg);
+            GF_CHECK_LAUNCH();
+        }
+        knn_exact(knn_tree, ng, gp, kq, rg, nullptr, nullptr, &sc->knn_iters, s, nb, kCand, d31, kNgb - 1);
+        int* ca = cache.get<int>(size_t(ng) * kCand);
+        int* rw = row.as<int>();
+        GF_CUDA(cudaMemsetAsync(rw, 0xff, sizeof(int) * size_t(n), s));
+        k_cache_store<<<ggrid, kThreads, 0, s>>>(ng, kq, gi, nb, rw, ca);
+        GF_CHECK_LAUNCH();
+        cache_valid = true;
+        full_searches += 1;
+    }
+    double* hh = h.get<double>(ng);
+    k_smoothing<<<ggrid, kThreads, 0, s>>>(ng, d31, a.eps, gi, hh, h_prev.as<double>());
+    GF_CHECK_LAUNCH();
+    have_hprev = true;
+
+    double* r = rho.get<double>(ng);
+    double* ga = gacc.get<double>(3 * size_t(ng));
+    double* du = dudt.get<double>(ng);
+    double* dti = dt_i.get<double>(ng);
+    sph_forces<int>(sph, ng, kNgb, kCand, gp, gv, gm, nb, hh, gu, a.gamma, a.alpha, a.beta, r, ga, du, dti, s);
+    k_scatter_sph<<<ggrid, kThreads, 0, s>>>(ng, gi, ga, dti, as, dtc, &sc->dtmin_bits);
+    GF_CHECK_LAUNCH();
+}
+
+}  // namespace gf

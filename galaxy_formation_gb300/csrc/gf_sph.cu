@@ -1,0 +1,512 @@
+// gf_sph.cu — SPH on the GPU (galaxy_formation/sph.py).
+//
+//   kernel / kernel_grad ..... sph.py:31-54, float64
+//   sph_forces ............... sph.py:57-106: density pass, then an equation-of-state pass
+//                              (P/rho^2 and sound speed per particle), then the force pass
+//                              (pressure, Monaghan-Gingold viscosity on approaching pairs,
+//                              du/dt, Courant step); one thread per particle, float64.
+//   knn_from_candidates ...... sph.py:109-135: one warp per particle, float64 distances,
+//                              bitonic sort of the (<= 64) candidates in registers.
+//   exact k nearest .......... replaces cKDTree(p).query(p, k) (sph.py:165-166):
+//                              octree of the points (same builder as gravity); one warp per
+//                              query walks it with a radius R, collecting points within R
+//                              (float32 distances from hi/lo split coordinates) until the
+//                              count lies in [k, 128] — the radius iteration, Newton steps
+//                              on count ~ R^3 from a guess (previous h, or the leaf's cell
+//                              density). The collected points are sorted, the k nearest plus
+//                              near-ties at the boundary are re-measured in float64 and
+//                              sorted again, so the result is the exact float64 kNN.
+#include <algorithm>
+#include <cmath>
+
+#include "gf_sph.cuh"
+#include "gf_tree.cuh"
+
+namespace gf {
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr int kThreads = 256;
+
+// sph.py:31-40
+__device__ __forceinline__ double w_m4(double r, double h) {
+    const double q = r / h;
+    const double s = 1.0 / (kPi * h * h * h);
+    if (q < 1.0) return s * (1 - 1.5 * q * q + 0.75 * q * q * q);
+    if (q < 2.0) {
+        const double t = 2 - q;
+        return s * 0.25 * t * t * t;
+    }
+    return 0.0;
+}
+
+// sph.py:43-54
+__device__ __forceinline__ double dw_m4(double r, double h) {
+    const double q = r / h;
+    const double s = 1.0 / (kPi * h * h * h * h);
+    double g;
+    if (q < 1.0) {
+        g = s * (-3 * q + 2.25 * q * q);
+    } else if (q < 2.0) {
+        const double t = 2 - q;
+        g = -s * 0.75 * t * t;
+    } else {
+        return 0.0;
+    }
+    return g / fmax(r, 1e-30);
+}
+
+__global__ void k_sph_kernel(int n, const double* __restrict__ r, const double* __restrict__ h,
+                             double* __restrict__ w, double* __restrict__ dw) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (w) w[i] = w_m4(r[i], h[i]);
+    if (dw) dw[i] = dw_m4(r[i], h[i]);
+}
+
+// pass 1 (sph.py:63-71): rho_i = sum_j m_j W(r_ij, h_i), the particle itself included
+template <class Idx>
+__global__ void k_sph_density(int n, int k, int ld, const double* __restrict__ pos, const double* __restrict__ mass,
+                              const Idx* __restrict__ nb, const double* __restrict__ h,
+                              double* __restrict__ rho) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double xi = pos[3 * size_t(i)], yi = pos[3 * size_t(i) + 1], zi = pos[3 * size_t(i) + 2];
+    const double hi = h[i];
+    double s = 0.0;
+    for (int jj = 0; jj < k; ++jj) {
+        const int64_t j = nb[size_t(i) * ld + jj];
+        const double dx = xi - pos[3 * j], dy = yi - pos[3 * j + 1], dz = zi - pos[3 * j + 2];
+        s += mass[j] * w_m4(sqrt(dx * dx + dy * dy + dz * dz), hi);
+    }
+    rho[i] = s;
+}
+
+// P / rho^2 and the sound speed of every particle (the per-j factors of sph.py:88-89)
+__global__ void k_sph_eos(int n, const double* __restrict__ rho, const double* __restrict__ u,
+                          double gamma, double* __restrict__ pr2, double* __restrict__ cs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double P = (gamma - 1) * rho[i] * u[i];
+    pr2[i] = P / (rho[i] * rho[i]);
+    cs[i] = sqrt(gamma * (gamma - 1) * u[i]);
+}
+
+// pass 2 (sph.py:72-106)
+template <class Idx>
+__global__ void k_sph_force(int n, int k, int ld, const double* __restrict__ pos, const double* __restrict__ vel,
+                            const double* __restrict__ mass, const Idx* __restrict__ nb,
+                            const double* __restrict__ h, const double* __restrict__ rho,
+                            const double* __restrict__ pr2, const double* __restrict__ cs, double alpha,
+                            double beta, double* __restrict__ acc, double* __restrict__ dudt,
+                            double* __restrict__ dt_i) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double xi = pos[3 * size_t(i)], yi = pos[3 * size_t(i) + 1], zi = pos[3 * size_t(i) + 2];
+    const double vxi = vel[3 * size_t(i)], vyi = vel[3 * size_t(i) + 1], vzi = vel[3 * size_t(i) + 2];
+    const double hi = h[i], rhoi = rho[i], pri = pr2[i], ci = cs[i];
+    double ax = 0, ay = 0, az = 0, du = 0, mu_max = 0;
+    for (int jj = 0; jj < k; ++jj) {
+        const int64_t j = nb[size_t(i) * ld + jj];
+        if (j == i) continue;
+        const double dx = xi - pos[3 * j], dy = yi - pos[3 * j + 1], dz = zi - pos[3 * j + 2];
+        const double r = sqrt(dx * dx + dy * dy + dz * dz);
+        const double hj = h[j];
+        const double gi = dw_m4(r, hi);
+        const double gj = dw_m4(r, hj);
+        const double vr = (vxi - vel[3 * j]) * dx + (vyi - vel[3 * j + 1]) * dy + (vzi - vel[3 * j + 2]) * dz;
+        double visc = 0.0;
+        if (vr < 0) {
+            const double hb = 0.5 * (hi + hj);
+            const double mu = hb * vr / (r * r + 0.01 * hb * hb);
+            mu_max = fmax(mu_max, -mu);
+            visc = (-alpha * 0.5 * (ci + cs[j]) * mu + beta * mu * mu) / (0.5 * (rhoi + rho[j]));
+        }
+        const double gb = 0.5 * (gi + gj);
+        const double f = pri * gi + pr2[j] * gj + visc * gb;
+        const double mj = mass[j];
+        ax -= mj * f * dx;
+        ay -= mj * f * dy;
+        az -= mj * f * dz;
+        du += mj * (pri * gi + 0.5 * visc * gb) * vr;
+    }
+    acc[3 * size_t(i)] = ax;
+    acc[3 * size_t(i) + 1] = ay;
+    acc[3 * size_t(i) + 2] = az;
+    dudt[i] = du;
+    dt_i[i] = 0.3 * hi / (ci + 1.2 * (alpha * ci + beta * mu_max) + 1e-30);
+}
+
+// ------------------------------------------------------------------- warp bitonic sorts
+
+// In-place ascending bitonic sort of P (power of two <= 128) keys in shared memory by the
+// calling warp; ties broken by the integer tag.
+template <class K>
+__device__ void warp_bitonic(K* key, int* tag, int P) {
+    const int lane = threadIdx.x & 31;
+    for (int size = 2; size <= P; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int t = lane; t < P / 2; t += 32) {
+                const int a = 2 * stride * (t / stride) + (t % stride);
+                const int b = a + stride;
+                const bool up = (a & size) == 0;
+                const K ka = key[a], kb = key[b];
+                const int ta = tag[a], tb = tag[b];
+                const bool gt = ka > kb || (ka == kb && ta > tb);
+                if (gt == up) {
+                    key[a] = kb;
+                    key[b] = ka;
+                    tag[a] = tb;
+                    tag[b] = ta;
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// --------------------------------------------------------------- knn_from_candidates
+
+constexpr int kCandWarps = 8;
+
+__global__ void __launch_bounds__(kCandWarps * 32) k_knn_cand(
+    int n, int m, const double* __restrict__ pos, const int64_t* __restrict__ cand, int k,
+    int64_t* __restrict__ nb, double* __restrict__ dist, int* __restrict__ all_ok) {
+    __shared__ double s_key[kCandWarps][64];
+    __shared__ int s_tag[kCandWarps][64];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double* key = s_key[w];
+    int* tag = s_tag[w];
+    const int nwarps = gridDim.x * kCandWarps;
+    for (int i = blockIdx.x * kCandWarps + w; i < n; i += nwarps) {
+        const double xi = pos[3 * size_t(i)], yi = pos[3 * size_t(i) + 1], zi = pos[3 * size_t(i) + 2];
+        int valid = 0;
+        for (int jj = lane; jj < 64; jj += 32) {
+            double d2 = INFINITY;
+            if (jj < m) {
+                const int64_t j = cand[size_t(i) * m + jj];
+                if (j >= 0) {
+                    const double dx = xi - pos[3 * j], dy = yi - pos[3 * j + 1], dz = zi - pos[3 * j + 2];
+                    d2 = dx * dx + dy * dy + dz * dz;
+                    ++valid;
+                }
+            }
+            key[jj] = d2;
+            tag[jj] = jj;
+        }
+        valid = warp_sum(valid);
+        __syncwarp();
+        if (valid < k) {  // sph.py:128-130: not enough candidates, row untouched
+            if (lane == 0) *all_ok = 0;
+            continue;
+        }
+        warp_bitonic(key, tag, 64);
+        for (int t = lane; t < k; t += 32) {
+            nb[size_t(i) * k + t] = cand[size_t(i) * m + tag[t]];
+            dist[size_t(i) * k + t] = sqrt(key[t]);
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------------ exact kNN
+
+constexpr int kKnnWarps = 8;
+constexpr int kKnnStack = 512;
+constexpr int kKnnCap = 128;
+
+struct KnnSmem {
+    int stack[kKnnStack];
+    float d2[kKnnCap];
+    int idx[kKnnCap];
+    double dd[64];
+    int di[64];
+    int lanemap[32];
+};
+
+struct KnnArgs {
+    int n, k, nn;
+    const float4* wb;
+    const float4* wgeo;
+    const float4* p4;
+    const float4* plo;
+    const int* perm;
+    const int* leaf_of;
+    const double* pos;      // caller order
+    const float* r_guess;   // caller order, optional
+    int64_t* nb;            // (n, k) caller order, or null
+    double* dist;           // (n, k), or null
+    int* nb32;              // (n, ld32) caller order, or null
+    int ld32;
+    double* dsel;           // distance of neighbour `dsel_col` (n,), or null
+    int dsel_col;
+    uint32_t* status;
+    unsigned long long* iters;
+};
+
+// Collects the points within sqrt(R2) of the query into S (first kKnnCap of them);
+// returns their number, or -1 on stack overflow.
+__device__ int knn_collect(const KnnArgs& A, KnnSmem& S, float4 xh, float4 xl, float R2) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = lanemask_lt();
+    int cnt = 0;
+    int sp = 1;
+    if (lane == 0) S.stack[0] = (0 << 4) | 1;
+    __syncwarp();
+    for (int rounds = 0; sp > 0; ++rounds) {
+        if (rounds > A.nn) return -1;  // each node is popped at most once
+        const int kk = min(sp, 32);
+        int e = 0, c = 0;
+        if (lane < kk) {
+            e = S.stack[sp - 1 - lane];
+            c = e & 15;
+        }
+        const int incl = warp_incl_scan(c);
+        const int excl = incl - c;
+        const unsigned fullm = __ballot_sync(0xffffffffu, lane < kk && incl <= 32);
+        const int nfull = __popc(fullm);
+        int nnodes = __shfl_sync(0xffffffffu, incl, kk - 1);
+        int take = c;
+        if (nfull < kk) {
+            nnodes = 32;
+            if (lane == nfull) {
+                take = 32 - excl;
+                S.stack[sp - 1 - lane] = (((e >> 4) + take) << 4) | (c - take);
+            }
+        }
+        __syncwarp();
+        if (lane < kk && lane <= nfull) {
+            const int first = e >> 4;
+            for (int t = 0; t < take && excl + t < 32; ++t) S.lanemap[excl + t] = first + t;
+        }
+        sp -= nfull;
+        __syncwarp();
+        const bool valid = lane < nnodes;
+        const int node = valid ? S.lanemap[lane] : 0;
+        __syncwarp();
+        bool open = false;
+        int first = 0, code = 0;
+        if (valid) {
+            const float4 g = A.wgeo[node];
+            const float4 B = A.wb[node];
+            first = __float_as_int(B.y);
+            code = __float_as_int(B.z);
+            // distance from the query to the cell cube, padded for float32 rounding
+            const float pad = 2e-6f * (fabsf(g.x) + fabsf(g.y) + fabsf(g.z) + g.w) + 1e-30f;
+            const float ex = fmaxf(fabsf((g.x - xh.x) - xl.x) - g.w - pad, 0.f);
+            const float ey = fmaxf(fabsf((g.y - xh.y) - xl.y) - g.w - pad, 0.f);
+            const float ez = fmaxf(fabsf((g.z - xh.z) - xl.z) - g.w - pad, 0.f);
+            open = ex * ex + ey * ey + ez * ez <= R2;
+        }
+        const bool inner = open && code > 0;
+        const bool leaf = open && code < 0;
+        const unsigned om = __ballot_sync(0xffffffffu, inner);
+        const int npush = __popc(om);
+        if (sp + npush > kKnnStack) return -1;
+        if (inner) S.stack[sp + __popc(om & lt)] = (first << 4) | code;
+        sp += npush;
+        int lc = leaf ? -code : 0;
+        int maxc = lc;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) maxc = max(maxc, __shfl_xor_sync(0xffffffffu, maxc, o));
+        for (int t = 0; t < maxc; ++t) {
+            bool hit = false;
+            float d2 = 0.f;
+            int j = 0;
+            if (t < lc) {
+                j = first + t;
+                const float4 ph = A.p4[j], pl = A.plo[j];
+                const float dx = (ph.x - xh.x) + (pl.x - xl.x);
+                const float dy = (ph.y - xh.y) + (pl.y - xl.y);
+                const float dz = (ph.z - xh.z) + (pl.z - xl.z);
+                d2 = dx * dx + dy * dy + dz * dz;
+                hit = d2 <= R2;
+            }
+            const unsigned hm = __ballot_sync(0xffffffffu, hit);
+            if (hit) {
+                const int slot = cnt + __popc(hm & lt);
+                if (slot < kKnnCap) {
+                    S.d2[slot] = d2;
+                    S.idx[slot] = j;
+                }
+            }
+            cnt += __popc(hm);
+        }
+        __syncwarp();
+    }
+    return cnt;
+}
+
+__global__ void __launch_bounds__(kKnnWarps * 32) k_knn(KnnArgs A) {
+    __shared__ KnnSmem smem_all[kKnnWarps];
+    KnnSmem& S = smem_all[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const int k = A.k;
+    const int nwarps = gridDim.x * kKnnWarps;
+    for (int q = blockIdx.x * kKnnWarps + (threadIdx.x >> 5); q < A.n; q += nwarps) {
+        const float4 xh = A.p4[q], xl = A.plo[q];
+        const int oq = A.perm[q];
+        float R;
+        if (A.r_guess) {
+            R = A.r_guess[oq];
+        } else {  // from the density of the particle's leaf cell
+            const int lf = A.leaf_of[q];
+            const float half = A.wgeo[lf].w;
+            const int c = max(1, -__float_as_int(A.wb[lf].z));
+            R = 2.0f * half * cbrtf(float(k) / float(c));
+        }
+        if (!(R > 0.f) || !isfinite(R)) R = 1e-3f;
+        // Newton steps on count ~ R^3 until the count is bracketed, then bisection: the
+        // count lands in [k, kKnnCap] unless > kKnnCap - k points share one distance.
+        int cnt = 0, it = 0;
+        bool ok = false;
+        float lo = 0.f, hi = INFINITY;
+        for (; it < 48; ++it) {
+            cnt = knn_collect(A, S, xh, xl, R * R);
+            if (cnt < 0) break;
+            if (cnt >= k && cnt <= kKnnCap) {
+                ok = true;
+                break;
+            }
+            float next;
+            if (cnt < k) {
+                lo = R;
+                next = R * (cnt >= 4 ? cbrtf(1.3f * float(k) / float(cnt)) : 2.0f);
+            } else {
+                hi = R;
+                next = R * cbrtf(0.75f * float(kKnnCap) / float(cnt));
+            }
+            if (lo > 0.f && hi < INFINITY) next = 0.5f * (lo + hi);
+            R = next;
+        }
+        if (lane == 0 && A.iters) atomicAdd(A.iters, (unsigned long long)(it + 1));
+        if (!ok) {
+            if (lane == 0) raise_status(A.status, cnt < 0 ? GF_ERR_WALK_STACK : GF_ERR_KNN);
+            for (int t = lane; t < k; t += 32) {
+                if (A.nb) A.nb[size_t(oq) * k + t] = -1;
+                if (A.dist) A.dist[size_t(oq) * k + t] = INFINITY;
+                if (A.nb32) A.nb32[size_t(oq) * A.ld32 + t] = -1;
+            }
+            if (A.dsel && lane == 0) A.dsel[oq] = INFINITY;
+            continue;
+        }
+        // float32 sort of the collected points
+        int P = 64;
+        while (P < cnt) P <<= 1;
+        for (int t = cnt + lane; t < P; t += 32) {
+            S.d2[t] = INFINITY;
+            S.idx[t] = 0x7fffffff;
+        }
+        __syncwarp();
+        warp_bitonic(S.d2, S.idx, P);
+        // the k nearest and everything within float32 rounding of the k-th distance
+        const float thr = S.d2[k - 1] * (1.0f + 2e-5f);
+        int m = 0;
+        for (int t = lane; t < cnt; t += 32) m += S.d2[t] <= thr;
+        m = min(64, warp_sum(m));
+        const int pi = A.perm[q];
+        const double xi = A.pos[3 * size_t(pi)], yi = A.pos[3 * size_t(pi) + 1], zi = A.pos[3 * size_t(pi) + 2];
+        for (int t = lane; t < 64; t += 32) {
+            double dd = INFINITY;
+            int tag = 0x7fffffff;
+            if (t < m) {
+                const int pj = A.perm[S.idx[t]];
+                const double dx = xi - A.pos[3 * size_t(pj)], dy = yi - A.pos[3 * size_t(pj) + 1],
+                             dz = zi - A.pos[3 * size_t(pj) + 2];
+                dd = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+                tag = pj;
+            }
+            S.dd[t] = dd;
+            S.di[t] = tag;
+        }
+        __syncwarp();
+        warp_bitonic(S.dd, S.di, 64);
+        for (int t = lane; t < k; t += 32) {
+            if (A.nb) A.nb[size_t(oq) * k + t] = S.di[t];
+            if (A.dist) A.dist[size_t(oq) * k + t] = __dsqrt_rn(S.dd[t]);
+            if (A.nb32) A.nb32[size_t(oq) * A.ld32 + t] = S.di[t];
+            if (A.dsel && t == A.dsel_col) A.dsel[oq] = __dsqrt_rn(S.dd[t]);
+        }
+        __syncwarp();
+    }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------- host
+
+void sph_kernel_values(int n, const double* r, const double* h, double* w, double* dw, cudaStream_t s) {
+    if (n <= 0) return;
+    k_sph_kernel<<<div_up(n, kThreads), kThreads, 0, s>>>(n, r, h, w, dw);
+    GF_CHECK_LAUNCH();
+}
+
+template <class Idx>
+void sph_forces(SphScratch& S, int n, int k, int ld, const double* pos, const double* vel, const double* mass,
+                const Idx* nb, const double* h, const double* u, double gamma, double alpha,
+                double beta, double* rho, double* acc, double* dudt, double* dt_i, cudaStream_t s) {
+    if (n <= 0) return;
+    const int grid = div_up(n, kThreads);
+    {
+        ProfScope ps(kStSphDensity, s);
+        k_sph_density<Idx><<<grid, kThreads, 0, s>>>(n, k, ld, pos, mass, nb, h, rho);
+        GF_CHECK_LAUNCH();
+    }
+    double* pr2 = S.pr2.get<double>(n);
+    double* cs = S.cs.get<double>(n);
+    k_sph_eos<<<grid, kThreads, 0, s>>>(n, rho, u, gamma, pr2, cs);
+    GF_CHECK_LAUNCH();
+    ProfScope ps(kStSphForce, s);
+    k_sph_force<Idx><<<grid, kThreads, 0, s>>>(n, k, ld, pos, vel, mass, nb, h, rho, pr2, cs, alpha, beta,
+                                               acc, dudt, dt_i);
+    GF_CHECK_LAUNCH();
+}
+template void sph_forces<int64_t>(SphScratch&, int, int, int, const double*, const double*, const double*,
+                                  const int64_t*, const double*, const double*, double, double, double,
+                                  double*, double*, double*, double*, cudaStream_t);
+template void sph_forces<int>(SphScratch&, int, int, int, const double*, const double*, const double*,
+                              const int*, const double*, const double*, double, double, double,
+                              double*, double*, double*, double*, cudaStream_t);
+
+void knn_from_candidates(int n, int m, const double* pos, const int64_t* cand, int k, int64_t* nb,
+                         double* dist, int* d_ok, cudaStream_t s) {
+    if (n <= 0) return;
+    const int blocks = std::min(div_up(n, kCandWarps), 8 * ctx().sms);
+    k_knn_cand<<<blocks, kCandWarps * 32, 0, s>>>(n, m, pos, cand, k, nb, dist, d_ok);
+    GF_CHECK_LAUNCH();
+}
+
+void knn_exact(Octree& T, int n, const double* pos, int k, const float* r_guess, int64_t* nb,
+               double* dist, unsigned long long* d_iters, cudaStream_t s, int* nb32, int ld32,
+               double* dsel, int dsel_col) {
+    if (n <= 0) return;
+    T.want_knn = true;
+    T.build(n, pos, nullptr, 0.7, s);
+    KnnArgs A{};
+    A.n = n;
+    A.k = k;
+    A.nn = T.nn;
+    A.wb = T.w_b.as<float4>();
+    A.wgeo = T.w_geo.as<float4>();
+    A.p4 = T.p4.as<float4>();
+    A.plo = T.plo.as<float4>();
+    A.perm = T.perm.as<int>();
+    A.leaf_of = T.leaf_of.as<int>();
+    A.pos = pos;
+    A.r_guess = r_guess;
+    A.nb = nb;
+    A.dist = dist;
+    A.nb32 = nb32;
+    A.ld32 = ld32;
+    A.dsel = dsel;
+    A.dsel_col = dsel_col;
+    A.status = ctx().d_status;
+    A.iters = d_iters;
+    const int blocks = std::min(div_up(n, kKnnWarps), 16 * ctx().sms);
+    ProfScope ps(kStKnn, s);
+    k_knn<<<blocks, kKnnWarps * 32, 0, s>>>(A);
+    GF_CHECK_LAUNCH();
+}
+
+}  // namespace gf

@@ -1,0 +1,40 @@
+// gf_sph.cuh — internal entry points shared by the C ABI (gf_capi.cu).
+#pragma once
+
+#include "gf_tree.cuh"
+
+namespace gf {
+
+struct SphScratch {
+    DevBuf pr2, cs;
+};
+
+void sph_kernel_values(int n, const double* r, const double* h, double* w, double* dw, cudaStream_t s);
+
+// nb: (n, ld) neighbour indices, the first k of each row used.
+template <class Idx>
+void sph_forces(SphScratch& S, int n, int k, int ld, const double* pos, const double* vel, const double* mass,
+                const Idx* nb, const double* h, const double* u, double gamma, double alpha,
+                double beta, double* rho, double* acc, double* dudt, double* dt_i, cudaStream_t s);
+
+void knn_from_candidates(int n, int m, const double* pos, const int64_t* cand, int k, int64_t* nb,
+                         double* dist, int* d_ok, cudaStream_t s);
+
+// Exact float64 k nearest neighbours of every point (itself included), ascending; builds
+// the point octree in T. r_guess (caller order, optional): starting search radius.
+// Outputs either nb/dist (n,k) int64/float64, or nb32 (n, ld32) int32 plus the distance of
+// neighbour `dsel_col` in dsel (n,).
+void knn_exact(Octree& T, int n, const double* pos, int k, const float* r_guess, int64_t* nb,
+               double* dist, unsigned long long* d_iters, cudaStream_t s, int* nb32 = nullptr,
+               int ld32 = 0, double* dsel = nullptr, int dsel_col = -1);
+
+void direct_sum(int n, const double* pos, const double* mass, int nt, const int64_t* targets,
+                double* acc, double eps, cudaStream_t s);
+
+void render_splat(int n, const double* pos, const uint8_t* group, int ngroups, const double* rot,
+                  const double* center, double scale, int W, int H, float* img, cudaStream_t s);
+void render_tonemap(int W, int H, int ngroups, const float* img, const float* glow, int gw, int gh,
+                    const float* colors, float inv_ref, float K, float exposure, uint8_t* out,
+                    cudaStream_t s);
+
+}  // namespace gf

@@ -1,0 +1,794 @@
+// gf_tree.cu — GPU octree that reproduces the reference's Barnes-Hut tree
+// (cpp/nbody.cpp:76-256) and its refit (cpp/nbody.cpp:262-305).
+//
+// The reference partitions index ranges recursively: a particle goes to octant bit k of a
+// cell when coordinate k is strictly greater than the cell centre, centres being computed
+// in float64 by repeated halving (child = parent +- half/2). Partitions are stable, so
+// inside every cell particles keep increasing index order; a cell is a leaf when it holds
+// at most 8 particles or sits at depth 48; nodes are stored depth-first with `next` links.
+//
+// Here the same tree comes out of a sort:
+//   1. float64 bbox -> root cube, same formula as cpp/nbody.cpp:218-219.
+//   2. 63-bit Morton key per particle holding its octant at levels 1..21. Fast path: a
+//      fixed-point grid position; when a coordinate lies within a rounding margin of a
+//      cell wall the key is recomputed with the exact float64 centre chain, so every
+//      octant decision equals the reference's `pos > c` test.
+//   3. stable radix sort of (key, index): tree order = (octant path, index).
+//   4. cells: 9 consecutive sorted keys sharing a level-d prefix <=> that cell holds > 8
+//      particles, so each particle's leaf depth and the nodes that start at it follow from
+//      common-prefix lengths of neighbouring keys; an exclusive scan numbers the nodes in
+//      depth-first order, and `next` is the id of the first node starting after the cell.
+//      Cells that still hold > 8 particles at level 21 get extension keys (levels 22..48,
+//      exact chain) and are re-sorted in shared memory.
+//   5. leaves re-sorted by index (the reference never partitions a leaf).
+//   6. moments bottom-up in one launch (the last child to arrive computes its parent,
+//      children summed in octant order), float64 sums of the same terms as the reference,
+//      rounded to the same float32 node record.
+#include <algorithm>
+#include <cfloat>
+
+#include "gf_tree.cuh"
+
+namespace gf {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+// ---------------------------------------------------------------------------- bbox
+
+__global__ void k_bbox_partial(const double* __restrict__ pos, int n, double* __restrict__ part) {
+    double lo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, hi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+    double bad = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const double v = pos[3 * size_t(i) + a];
+            if (!isfinite(v)) bad = 1.0;
+            lo[a] = fmin(lo[a], v);
+            hi[a] = fmax(hi[a], v);
+        }
+    }
+    __shared__ double s[7][kThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = fmin(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+            hi[a] = fmax(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+        }
+        bad = fmax(bad, __shfl_xor_sync(0xffffffffu, bad, o));
+    }
+    if (lane == 0) {
+        for (int a = 0; a < 3; ++a) {
+            s[a][warp] = lo[a];
+            s[3 + a][warp] = hi[a];
+        }
+        s[6][warp] = bad;
+    }
+    __syncthreads();
+    if (threadIdx.x < 7) {
+        double v = s[threadIdx.x][0];
+        for (int w = 1; w < kThreads / 32; ++w)
+            v = threadIdx.x < 3 ? fmin(v, s[threadIdx.x][w]) : fmax(v, s[threadIdx.x][w]);
+        part[7 * blockIdx.x + threadIdx.x] = v;
+    }
+}
+
+__global__ void k_bbox_final(const double* __restrict__ part, int nparts, RootBox* __restrict__ root,
+                             uint32_t* status) {
+    if (threadIdx.x != 0) return;
+    double lo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, hi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+    double bad = 0;
+    for (int b = 0; b < nparts; ++b) {
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = fmin(lo[a], part[7 * b + a]);
+            hi[a] = fmax(hi[a], part[7 * b + 3 + a]);
+        }
+        bad = fmax(bad, part[7 * b + 6]);
+    }
+    if (bad > 0) raise_status(status, GF_ERR_NONFINITE);
+    RootBox R;
+    double ext = 0;
+    for (int a = 0; a < 3; ++a) {
+        R.c[a] = __dmul_rn(0.5, __dadd_rn(lo[a], hi[a]));
+        ext = fmax(ext, __dsub_rn(hi[a], lo[a]));
+    }
+    // 0.5 * max extent * 1.0001 + 1e-12 (cpp/nbody.cpp:219), unfused
+    R.half = __dadd_rn(__dmul_rn(__dmul_rn(0.5, ext), 1.0001), 1e-12);
+    double cmax = 0;
+    for (int a = 0; a < 3; ++a) {
+        R.lo[a] = __dsub_rn(R.c[a], R.half);
+        cmax = fmax(cmax, fabs(R.c[a]));
+    }
+    R.inv_w = __ddiv_rn(2097152.0, __dmul_rn(2.0, R.half));
+    // Rounding of the float64 centre chain (<= 21 roundings of <= 1/2 ulp(|c| + half)) plus
+    // that of the fixed-point position stays below 2^-27 (|c|/half + 2) grid units; the
+    // margin keeps a factor 8 on top.
+    R.margin = ldexp(1.0, -24) * (cmax / R.half + 2.0);
+    *root = R;
+}
+
+// ---------------------------------------------------------------------------- keys
+
+__device__ __forceinline__ uint64_t part1by2(uint32_t v) {
+    uint64_t x = v & 0x1fffffu;
+    x = (x | (x << 32)) & 0x1f00000000ffffull;
+    x = (x | (x << 16)) & 0x1f0000ff0000ffull;
+    x = (x | (x << 8)) & 0x100f00f00f00f00full;
+    x = (x | (x << 4)) & 0x10c30c30c30c30c3ull;
+    x = (x | (x << 2)) & 0x1249249249249249ull;
+    return x;
+}
+
+// Exact octant digits from the float64 centre chain (cpp/nbody.cpp:80, :92-96, :135-139).
+// Levels 1..21 -> k0, 22..42 -> k1, 43..48 -> k2 (each left-aligned in its word).
+__device__ void exact_keys(double x, double y, double z, const RootBox& R, int levels,
+                           uint64_t& k0, uint64_t& k1, uint64_t& k2) {
+    double cx = R.c[0], cy = R.c[1], cz = R.c[2], h = R.half;
+    k0 = k1 = k2 = 0;
+    for (int l = 1; l <= levels; ++l) {
+        h = 0.5 * h;
+        const unsigned o = unsigned(x > cx) | (unsigned(y > cy) << 1) | (unsigned(z > cz) << 2);
+        cx = __dadd_rn(cx, (o & 1) ? h : -h);
+        cy = __dadd_rn(cy, (o & 2) ? h : -h);
+        cz = __dadd_rn(cz, (o & 4) ? h : -h);
+        if (l <= 21)
+            k0 = (k0 << 3) | o;
+        else if (l <= 42)
+            k1 = (k1 << 3) | o;
+        else
+            k2 = (k2 << 3) | o;
+    }
+    if (levels < 21) k0 <<= 3 * (21 - levels);
+}
+
+__device__ __forceinline__ bool grid_coord(double x, int a, const RootBox& R, uint32_t& ic) {
+    const double u = __dmul_rn(__dsub_rn(x, R.lo[a]), R.inv_w);
+    const double f = floor(u);
+    const double fr = u - f;
+    if (!(f >= 0.0 && f < 2097152.0 && fr >= R.margin && fr <= 1.0 - R.margin)) return false;
+    ic = uint32_t(f);
+    return true;
+}
+
+__global__ void k_keys(const double* __restrict__ pos, int n, const RootBox* __restrict__ rootp,
+                       uint64_t* __restrict__ key, int* __restrict__ perm) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const RootBox R = *rootp;
+    const double x = pos[3 * size_t(i)], y = pos[3 * size_t(i) + 1], z = pos[3 * size_t(i) + 2];
+    uint32_t ix, iy, iz;
+    uint64_t k;
+    if (grid_coord(x, 0, R, ix) && grid_coord(y, 1, R, iy) && grid_coord(z, 2, R, iz)) {
+        k = part1by2(ix) | (part1by2(iy) << 1) | (part1by2(iz) << 2);
+    } else {
+        uint64_t k1, k2;
+        exact_keys(x, y, z, R, 21, k, k1, k2);
+    }
+    key[i] = k;
+    perm[i] = i;
+}
+
+// ---------------------------------------------------------------------------- prefixes
+
+struct KeyView {
+    const uint64_t* k0;
+    const uint64_t* k1;  // null unless some level-21 cell holds > 8 particles
+    const uint64_t* k2;
+};
+
+// Number of leading octree levels shared by sorted positions i and j (0..48).
+__device__ __forceinline__ int cpl(const KeyView& K, int i, int j) {
+    uint64_t a = K.k0[i], b = K.k0[j];
+    if (a != b) return (__clzll(a ^ b) - 1) / 3;
+    if (!K.k1) return 21;
+    a = K.k1[i];
+    b = K.k1[j];
+    if (a != b) return 21 + (__clzll(a ^ b) - 1) / 3;
+    a = K.k2[i];
+    b = K.k2[j];
+    if (a != b) return 42 + (__clzll(a ^ b) - 46) / 3;
+    return 48;
+}
+
+__device__ __forceinline__ int digit(const KeyView& K, int i, int l) {
+    if (l <= 21) return int((K.k0[i] >> (3 * (21 - l))) & 7);
+    if (l <= 42) return int((K.k1[i] >> (3 * (42 - l))) & 7);
+    return int((K.k2[i] >> (3 * (48 - l))) & 7);
+}
+
+__global__ void k_cpl9(KeyView K, int n, int8_t* __restrict__ cpl9, TreeCounts* cnt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int c = -1;
+    if (i + kLeafMax < n) c = cpl(K, i, i + kLeafMax);
+    if (c == 21 && !K.k1) cnt->deep = 1;
+    cpl9[i] = int8_t(c);
+}
+
+__global__ void k_nstart(KeyView K, int n, const int8_t* __restrict__ cpl9, int8_t* __restrict__ ldepth,
+                         int8_t* __restrict__ dsplit, int* __restrict__ nstart) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int m = -1;
+    for (int j = max(0, i - kLeafMax); j <= i; ++j) m = max(m, int(cpl9[j]));
+    const int ld = min(kDepthMax, m + 1);
+    const int ds = i == 0 ? 0 : cpl(K, i - 1, i) + 1;
+    ldepth[i] = int8_t(ld);
+    dsplit[i] = int8_t(min(ds, 127));
+    nstart[i] = max(0, ld - ds + 1);
+}
+
+// first j > i with j == n or cpl(i, j) < d
+__device__ int run_end(const KeyView& K, int n, int i, int d) {
+    if (d == 0) return n;
+    int j = i + 1;
+    for (int t = 0; t < 9 && j < n; ++t, ++j)
+        if (cpl(K, i, j) < d) return j;
+    if (j >= n) return n;
+    int lo = j, step = 16, hi;
+    for (;;) {
+        hi = lo + step;
+        if (hi >= n) {
+            hi = n;
+            break;
+        }
+        if (cpl(K, i, hi) < d) break;
+        lo = hi + 1;
+        step *= 2;
+    }
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (cpl(K, i, mid) < d)
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    return lo;
+}
+
+// first j <= i with cpl(j, i) >= lev
+__device__ int run_begin(const KeyView& K, int i, int lev) {
+    int hi = i, step = 1, lo;
+    for (;;) {
+        lo = hi - step;
+        if (lo < 0) {
+            lo = -1;
+            break;
+        }
+        if (cpl(K, lo, i) < lev) break;
+        hi = lo;
+        step *= 2;
+    }
+    int a = lo + 1, b = hi;
+    while (a < b) {
+        const int mid = (a + b) >> 1;
+        if (cpl(K, mid, i) >= lev)
+            b = mid;
+        else
+            a = mid + 1;
+    }
+    return b;
+}
+
+// ---------------------------------------------------------------------------- emit
+
+__global__ void k_emit(KeyView K, int n, const RootBox* __restrict__ rootp,
+                       const int8_t* __restrict__ ldepth, const int8_t* __restrict__ dsplit,
+                       const int* __restrict__ nstart, const int* __restrict__ nbase,
+                       const TreeCounts* __restrict__ cnt, int4* __restrict__ n_i4,
+                       double4* __restrict__ n_cd, float4* __restrict__ n_geo,
+                       int* __restrict__ n_parent) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || nstart[i] == 0) return;
+    const RootBox R = *rootp;
+    const int total = cnt->total_nodes;
+    const int ds = dsplit[i], ld = ldepth[i], base = nbase[i];
+    double c[3] = {R.c[0], R.c[1], R.c[2]};
+    double h = R.half;
+    for (int l = 1; l <= ds; ++l) {
+        h = 0.5 * h;
+        const int o = digit(K, i, l);
+        c[0] = __dadd_rn(c[0], (o & 1) ? h : -h);
+        c[1] = __dadd_rn(c[1], (o & 2) ? h : -h);
+        c[2] = __dadd_rn(c[2], (o & 4) ? h : -h);
+    }
+    for (int d = ds; d <= ld; ++d) {
+        if (d > ds) {
+            h = 0.5 * h;
+            const int o = digit(K, i, d);
+            c[0] = __dadd_rn(c[0], (o & 1) ? h : -h);
+            c[1] = __dadd_rn(c[1], (o & 2) ? h : -h);
+            c[2] = __dadd_rn(c[2], (o & 4) ? h : -h);
+        }
+        const int id = base + (d - ds);
+        const int end = run_end(K, n, i, d);
+        const int next = end < n ? nbase[end] : total;
+        int parent;
+        if (d == 0) {
+            parent = -1;
+        } else if (d > ds) {
+            parent = id - 1;
+        } else {
+            const int s = run_begin(K, i, d - 1);
+            parent = nbase[s] + (d - 1 - dsplit[s]);
+        }
+        n_i4[id] = make_int4(i, end - i, next, (d == ld ? 1 : 0) | (d << 8));
+        n_cd[id] = make_double4(c[0], c[1], c[2], h);
+        n_geo[id] = make_float4(float(c[0]), float(c[1]), float(c[2]), float(h));
+        n_parent[id] = parent;
+    }
+}
+
+__global__ void k_nchild(int nn, const int4* __restrict__ n_i4, int* __restrict__ nchild,
+                         int* __restrict__ counter) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nn) return;
+    const int4 q = n_i4[k];
+    int c = 0;
+    if (!(q.w & 1)) {
+        for (int ch = k + 1; ch < q.z && c <= 8; ch = n_i4[ch].z) ++c;  // <= 8 children
+    }
+    nchild[k] = c;
+    counter[k] = 0;
+}
+
+// Inside a leaf the reference keeps increasing particle index (stable partitions).
+__global__ void k_leaf_sort(int nn, const int4* __restrict__ n_i4, int* __restrict__ perm) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nn) return;
+    const int4 q = n_i4[k];
+    if (!(q.w & 1) || q.y > 64) return;  // larger leaves hold identical keys: already sorted
+    int* p = perm + q.x;
+    for (int a = 1; a < q.y; ++a) {
+        const int v = p[a];
+        int b = a - 1;
+        while (b >= 0 && p[b] > v) {
+            p[b + 1] = p[b];
+            --b;
+        }
+        p[b + 1] = v;
+    }
+}
+
+__global__ void k_gather(int n, const int* __restrict__ perm, const double* __restrict__ pos,
+                         const double* __restrict__ mass, const double* __restrict__ xbuild,
+                         float4* __restrict__ p4, float* __restrict__ pdisp, float4* __restrict__ plo) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int j = perm[i];
+    const double x = pos[3 * size_t(j)], y = pos[3 * size_t(j) + 1], z = pos[3 * size_t(j) + 2];
+    const double m = mass ? mass[j] : 1.0;
+    const float fx = float(x), fy = float(y), fz = float(z);
+    p4[i] = make_float4(fx, fy, fz, float(m));
+    if (plo) plo[i] = make_float4(float(x - double(fx)), float(y - double(fy)), float(z - double(fz)), 0.f);
+    if (pdisp) {  // refit: displacement since the build (cpp/nbody.cpp:273-275)
+        const double dx = __dsub_rn(x, xbuild[3 * size_t(j)]);
+        const double dy = __dsub_rn(y, xbuild[3 * size_t(j) + 1]);
+        const double dz = __dsub_rn(z, xbuild[3 * size_t(j) + 2]);
+        pdisp[i] = m > 0 ? float(__dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
+                                                      __dmul_rn(dz, dz))))
+                         : 0.0f;
+    }
+}
+
+// ---------------------------------------------------------------------------- moments
+
+struct MomentArgs {
+    int nn;
+    bool refit;
+    float theta;
+    const int4* n_i4;
+    const int* parent;
+    const int* nchild;
+    int* counter;
+    const double4* n_cd;  // build: float64 centre + half
+    const float4* n_geo;  // refit: float32 centre + half
+    float4* mom;
+    float* open_r;
+    float* ndisp;
+    // leaf inputs
+    const int* perm;
+    const double* pos;
+    const double* mass;
+    const float4* p4;
+    const float* pdisp;
+};
+
+__device__ __forceinline__ void finalize(const MomentArgs& A, int k, double M, double sx, double sy,
+                                         double sz, float dm) {
+    const double inv = M > 0 ? __ddiv_rn(1.0, M) : 0.0;
+    const double mx = __dmul_rn(sx, inv), my = __dmul_rn(sy, inv), mz = __dmul_rn(sz, inv);
+    A.mom[k] = make_float4(float(mx), float(my), float(mz), float(M));
+    double ox, oy, oz, first;
+    if (!A.refit) {  // cpp/nbody.cpp:104-106
+        const double4 c = A.n_cd[k];
+        ox = __dsub_rn(mx, c.x);
+        oy = __dsub_rn(my, c.y);
+        oz = __dsub_rn(mz, c.z);
+        first = __ddiv_rn(__dmul_rn(2.0, c.w), double(A.theta));
+    } else {  // cpp/nbody.cpp:301-303: the first term is evaluated in float32
+        const float4 g = A.n_geo[k];
+        ox = __dsub_rn(mx, double(g.x));
+        oy = __dsub_rn(my, double(g.y));
+        oz = __dsub_rn(mz, double(g.z));
+        first = double(__fdiv_rn(__fmul_rn(2.0f, __fadd_rn(g.w, dm)), A.theta));
+        A.ndisp[k] = dm;
+    }
+    const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(ox, ox), __dmul_rn(oy, oy)), __dmul_rn(oz, oz)));
+    A.open_r[k] = float(__dadd_rn(first, r));
+}
+
+__global__ void k_moments(MomentArgs A) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= A.nn) return;
+    const int4 q = A.n_i4[k];
+    if (!(q.w & 1)) return;
+    double M = 0, sx = 0, sy = 0, sz = 0;
+    float dm = 0.f;
+    for (int i = q.x; i < q.x + q.y; ++i) {
+        if (!A.refit) {  // cpp/nbody.cpp:124-131
+            const int j = A.perm[i];
+            const double m = A.mass ? A.mass[j] : 1.0;
+            M = __dadd_rn(M, m);
+            sx = __dadd_rn(sx, __dmul_rn(m, A.pos[3 * size_t(j)]));
+            sy = __dadd_rn(sy, __dmul_rn(m, A.pos[3 * size_t(j) + 1]));
+            sz = __dadd_rn(sz, __dmul_rn(m, A.pos[3 * size_t(j) + 2]));
+        } else {  // cpp/nbody.cpp:285-289 (float x float products are exact in float64)
+            const float4 p = A.p4[i];
+            const double m = double(p.w);
+            M = __dadd_rn(M, m);
+            sx = __dadd_rn(sx, m * double(p.x));
+            sy = __dadd_rn(sy, m * double(p.y));
+            sz = __dadd_rn(sz, m * double(p.z));
+            dm = fmaxf(dm, A.pdisp[i]);
+        }
+    }
+    finalize(A, k, M, sx, sy, sz, dm);
+    __threadfence();
+    int p = A.parent[k];
+    while (p >= 0) {
+        const int arrived = atomicAdd(&A.counter[p], 1);
+        if (arrived != A.nchild[p] - 1) return;
+        __threadfence();
+        double PM = 0, px = 0, py = 0, pz = 0;
+        float pd = 0.f;
+        const int end = A.n_i4[p].z;
+        int seen = 0;
+        for (int c = p + 1; c < end && seen < 8; c = A.n_i4[c].z, ++seen) {  // octant order
+            const float4 cm = __ldcg(&A.mom[c]);
+            const double m = double(cm.w);
+            PM = __dadd_rn(PM, m);
+            px = __dadd_rn(px, m * double(cm.x));
+            py = __dadd_rn(py, m * double(cm.y));
+            pz = __dadd_rn(pz, m * double(cm.z));
+            if (A.refit) pd = fmaxf(pd, __ldcg(&A.ndisp[c]));
+        }
+        finalize(A, p, PM, px, py, pz, pd);
+        __threadfence();
+        p = A.parent[p];
+    }
+}
+
+// ---------------------------------------------------------------------------- groups + layout
+
+__global__ void k_group_flag(int nn, const int4* __restrict__ n_i4, const int* __restrict__ parent,
+                             int* __restrict__ flag) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nn) return;
+    const int4 q = n_i4[k];
+    const bool candidate = q.y <= kGroupMax || (q.w & 1);
+    const int p = parent[k];
+    flag[k] = candidate && (p < 0 || n_i4[p].y > kGroupMax) ? 1 : 0;
+}
+
+__global__ void k_group_write(int nn, const int* __restrict__ flag, const int* __restrict__ scan,
+                              int* __restrict__ groups) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nn) return;
+    if (flag[k]) groups[scan[k]] = k;
+}
+
+__global__ void k_bfs_keys(int nn, const int4* __restrict__ n_i4, uint64_t* __restrict__ key,
+                           int* __restrict__ val) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nn) return;
+    key[k] = uint64_t(n_i4[k].w >> 8);
+    val[k] = k;
+}
+
+__global__ void k_bfs_index(int nn, const int* __restrict__ val, int* __restrict__ bfs) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nn) return;
+    bfs[val[b]] = b;
+}
+
+__global__ void k_walk_fill(int nn, const int4* __restrict__ n_i4, const int* __restrict__ nchild,
+                            const int* __restrict__ bfs, const float4* __restrict__ mom,
+                            const float* __restrict__ open_r, const float4* __restrict__ geo,
+                            float4* __restrict__ wa, float4* __restrict__ wb,
+                            float4* __restrict__ wgeo, int* __restrict__ leaf_of) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nn) return;
+    const int4 q = n_i4[k];
+    const int b = bfs[k];
+    int first, code;
+    if (q.w & 1) {
+        first = q.x;
+        code = -q.y;
+        if (leaf_of)
+            for (int i = q.x; i < q.x + q.y; ++i) leaf_of[i] = b;
+    } else {
+        first = bfs[k + 1];
+        code = nchild[k];
+    }
+    wa[b] = mom[k];
+    wb[b] = make_float4(open_r[k], __int_as_float(first), __int_as_float(code), 0.f);
+    if (wgeo) wgeo[b] = geo[k];
+}
+
+// ---------------------------------------------------------------------------- deep cells
+
+// Positions of cells that still hold > 8 particles at level 21 get extension keys.
+__global__ void k_deep_keys(int n, const uint64_t* __restrict__ k0, const int* __restrict__ perm,
+                            const double* __restrict__ pos, const RootBox* __restrict__ rootp,
+                            uint64_t* __restrict__ k1, uint64_t* __restrict__ k2,
+                            int* __restrict__ starts, int* __restrict__ nstarts) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    bool deep = false;
+    for (int j = max(0, i - kLeafMax); j <= i && !deep; ++j)
+        deep = j + kLeafMax < n && k0[j] == k0[j + kLeafMax];
+    uint64_t a = 0, b = 0;
+    if (deep) {
+        const RootBox R = *rootp;
+        const int p = perm[i];
+        uint64_t c0;
+        exact_keys(pos[3 * size_t(p)], pos[3 * size_t(p) + 1], pos[3 * size_t(p) + 2], R, kDepthMax, c0, a, b);
+        if (i == 0 || k0[i - 1] != k0[i]) starts[atomicAdd(nstarts, 1)] = i;
+    }
+    k1[i] = a;
+    k2[i] = b;
+}
+
+// One block per deep run: stable sort of (k1, k2) inside the run (ties keep index order).
+__global__ void k_deep_sort(int n, const uint64_t* __restrict__ k0, uint64_t* __restrict__ k1,
+                            uint64_t* __restrict__ k2, int* __restrict__ perm,
+                            const int* __restrict__ starts, const int* __restrict__ nstarts,
+                            uint32_t* status) {
+    extern __shared__ unsigned char smem[];
+    uint64_t* s1 = reinterpret_cast<uint64_t*>(smem);
+    uint64_t* s2 = s1 + kDeepRunMax;
+    int* sp = reinterpret_cast<int*>(s2 + kDeepRunMax);
+    for (int r = blockIdx.x; r < *nstarts; r += gridDim.x) {
+        const int b = starts[r];
+        __shared__ int s_len;
+        if (threadIdx.x == 0) {
+            int e = b + 1;
+            while (e < n && k0[e] == k0[b]) ++e;
+            s_len = e - b;
+        }
+        __syncthreads();
+        const int len = s_len;
+        if (len > kDeepRunMax) {
+            // sorted already when every extension key is equal (coincident particles)
+            bool sorted = true;
+            for (int i = b + 1 + threadIdx.x; i < b + len; i += blockDim.x)
+                if (k1[i] < k1[i - 1] || (k1[i] == k1[i - 1] && k2[i] < k2[i - 1])) sorted = false;
+            if (__syncthreads_or(!sorted) && threadIdx.x == 0) raise_status(status, GF_ERR_DEEP_CELL);
+            __syncthreads();
+            continue;
+        }
+        int P = 1;
+        while (P < len) P <<= 1;
+        for (int t = threadIdx.x; t < P; t += blockDim.x) {
+            if (t < len) {
+                s1[t] = k1[b + t];
+                s2[t] = k2[b + t];
+                sp[t] = perm[b + t];
+            } else {
+                s1[t] = ~0ull;
+                s2[t] = ~0ull;
+                sp[t] = 0x7fffffff;
+            }
+        }
+        __syncthreads();
+        for (int size = 2; size <= P; size <<= 1) {
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                for (int t = threadIdx.x; t < P; t += blockDim.x) {
+                    const int u = t ^ stride;
+                    if (u > t) {
+                        const bool up = (t & size) == 0;
+                        const bool gt = s1[t] > s1[u] || (s1[t] == s1[u] && (s2[t] > s2[u] ||
+                                                          (s2[t] == s2[u] && sp[t] > sp[u])));
+                        if (gt == up) {
+                            uint64_t x = s1[t]; s1[t] = s1[u]; s1[u] = x;
+                            x = s2[t]; s2[t] = s2[u]; s2[u] = x;
+                            const int y = sp[t]; sp[t] = sp[u]; sp[u] = y;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (int t = threadIdx.x; t < len; t += blockDim.x) {
+            k1[b + t] = s1[t];
+            k2[b + t] = s2[t];
+            perm[b + t] = sp[t];
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------- host side
+
+static Octree g_tree;
+Octree& gravity_tree() { return g_tree; }
+
+void Octree::build(int n_, const double* pos, const double* mass, double theta, cudaStream_t s) {
+    Context& C = ctx();
+    ProfScope ps(want_knn ? kStKnnTree : kStTreeBuild, s);
+    n = n_;
+    theta_f = float(theta);
+    valid = false;
+    if (!h_counts) GF_CUDA(cudaMallocHost(&h_counts, sizeof(TreeCounts)));
+    TreeCounts* cnt = counts.get<TreeCounts>(1);
+    RootBox* R = root.get<RootBox>(1);
+    GF_CUDA(cudaMemsetAsync(cnt, 0, sizeof(TreeCounts), s));
+
+    const int grid = div_up(n, kThreads);
+    const int nparts = std::min(4 * C.sms, std::max(1, grid));
+    int* nb = nbase.get<int>(std::max(size_t(n) + 1, size_t(nparts) * 14 + 16));
+    double* part = reinterpret_cast<double*>(nb);  // bbox partials, consumed before the scan
+    k_bbox_partial<<<nparts, kThreads, 0, s>>>(pos, n, part);
+    GF_CHECK_LAUNCH();
+    k_bbox_final<<<1, 32, 0, s>>>(part, nparts, R, C.d_status);
+    GF_CHECK_LAUNCH();
+
+    uint64_t* k0 = key.get<uint64_t>(n);
+    int* pm = perm.get<int>(n);
+    k_keys<<<grid, kThreads, 0, s>>>(pos, n, R, k0, pm);
+    GF_CHECK_LAUNCH();
+    radix_sort_pairs(k0, pm, key_alt.get<uint64_t>(n), perm_alt.get<int>(n), n, 0, 63, s);
+
+    int8_t* c9 = cpl9.get<int8_t>(n);
+    int8_t* ld = ldepth.get<int8_t>(n);
+    int8_t* ds = dsplit.get<int8_t>(n);
+    int* ns = nstart.get<int>(n);
+    KeyView K{k0, nullptr, nullptr};
+    k_cpl9<<<grid, kThreads, 0, s>>>(K, n, c9, cnt);
+    GF_CHECK_LAUNCH();
+    k_nstart<<<grid, kThreads, 0, s>>>(K, n, c9, ld, ds, ns);
+    GF_CHECK_LAUNCH();
+    exclusive_scan(ns, nb, n, &cnt->total_nodes, s);
+    GF_CUDA(cudaMemcpyAsync(h_counts, cnt, sizeof(TreeCounts), cudaMemcpyDeviceToHost, s));
+    GF_CUDA(cudaStreamSynchronize(s));
+
+    if (h_counts->deep) {
+        uint64_t* e1 = key1.get<uint64_t>(n);
+        uint64_t* e2 = key2.get<uint64_t>(n);
+        int* starts = reinterpret_cast<int*>(key_alt.get<uint64_t>(n));  // scratch
+        int* nst = &cnt->pad[0];
+        k_deep_keys<<<grid, kThreads, 0, s>>>(n, k0, pm, pos, R, e1, e2, starts, nst);
+        GF_CHECK_LAUNCH();
+        const size_t sm = size_t(kDeepRunMax) * (2 * sizeof(uint64_t) + sizeof(int));
+        static bool attr = false;
+        if (!attr) {
+            GF_CUDA(cudaFuncSetAttribute(k_deep_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)));
+            attr = true;
+        }
+        k_deep_sort<<<2 * C.sms, 512, sm, s>>>(n, k0, e1, e2, pm, starts, nst, C.d_status);
+        GF_CHECK_LAUNCH();
+        K = KeyView{k0, e1, e2};
+        k_cpl9<<<grid, kThreads, 0, s>>>(K, n, c9, cnt);
+        GF_CHECK_LAUNCH();
+        k_nstart<<<grid, kThreads, 0, s>>>(K, n, c9, ld, ds, ns);
+        GF_CHECK_LAUNCH();
+        exclusive_scan(ns, nb, n, &cnt->total_nodes, s);
+        GF_CUDA(cudaMemcpyAsync(h_counts, cnt, sizeof(TreeCounts), cudaMemcpyDeviceToHost, s));
+        GF_CUDA(cudaStreamSynchronize(s));
+    }
+    nn = h_counts->total_nodes;
+
+    int4* i4 = n_i4.get<int4>(nn);
+    double4* cd = n_cd.get<double4>(nn);
+    float4* geo = n_geo.get<float4>(nn);
+    int* par = n_parent.get<int>(nn);
+    k_emit<<<grid, kThreads, 0, s>>>(K, n, R, ld, ds, ns, nb, cnt, i4, cd, geo, par);
+    GF_CHECK_LAUNCH();
+    const int ngrid = div_up(nn, kThreads);
+    int* nch = n_nchild.get<int>(nn);
+    int* ctr = n_counter.get<int>(nn);
+    k_nchild<<<ngrid, kThreads, 0, s>>>(nn, i4, nch, ctr);
+    GF_CHECK_LAUNCH();
+    k_leaf_sort<<<ngrid, kThreads, 0, s>>>(nn, i4, pm);
+    GF_CHECK_LAUNCH();
+
+    float4* pp = p4.get<float4>(n);
+    k_gather<<<grid, kThreads, 0, s>>>(n, pm, pos, mass, nullptr, pp, nullptr,
+                                       want_knn ? plo.get<float4>(n) : nullptr);
+    GF_CHECK_LAUNCH();
+    double* xb = xbuild.get<double>(3 * size_t(n));
+    GF_CUDA(cudaMemcpyAsync(xb, pos, sizeof(double) * 3 * size_t(n), cudaMemcpyDeviceToDevice, s));
+
+    MomentArgs A{};
+    A.nn = nn;
+    A.refit = false;
+    A.theta = theta_f;
+    A.n_i4 = i4;
+    A.parent = par;
+    A.nchild = nch;
+    A.counter = ctr;
+    A.n_cd = cd;
+    A.n_geo = geo;
+    A.mom = n_mom.get<float4>(nn);
+    A.open_r = n_open.get<float>(nn);
+    A.ndisp = n_disp.get<float>(nn);
+    A.perm = pm;
+    A.pos = pos;
+    A.mass = mass;
+    k_moments<<<ngrid, kThreads, 0, s>>>(A);
+    GF_CHECK_LAUNCH();
+
+    int* gf_ = gflag.get<int>(nn);
+    int* gs = gscan.get<int>(nn);
+    k_group_flag<<<ngrid, kThreads, 0, s>>>(nn, i4, par, gf_);
+    GF_CHECK_LAUNCH();
+    exclusive_scan(gf_, gs, nn, &cnt->num_groups, s);
+    k_group_write<<<ngrid, kThreads, 0, s>>>(nn, gf_, gs, groups.get<int>(nn));
+    GF_CHECK_LAUNCH();
+
+    uint64_t* bk = bfs_key.get<uint64_t>(nn);
+    int* bv = bfs_val.get<int>(nn);
+    k_bfs_keys<<<ngrid, kThreads, 0, s>>>(nn, i4, bk, bv);
+    GF_CHECK_LAUNCH();
+    radix_sort_pairs(bk, bv, bfs_key_alt.get<uint64_t>(nn), bfs_val_alt.get<int>(nn), nn, 0, 8, s);
+    int* bfs = n_bfs.get<int>(nn);
+    k_bfs_index<<<ngrid, kThreads, 0, s>>>(nn, bv, bfs);
+    GF_CHECK_LAUNCH();
+    k_walk_fill<<<ngrid, kThreads, 0, s>>>(nn, i4, nch, bfs, A.mom, A.open_r, geo, w_a.get<float4>(nn),
+                                           w_b.get<float4>(nn), want_knn ? w_geo.get<float4>(nn) : nullptr,
+                                           want_knn ? leaf_of.get<int>(n) : nullptr);
+    GF_CHECK_LAUNCH();
+    valid = true;
+}
+
+void Octree::refit(const double* pos, const double* mass, cudaStream_t s) {
+    ProfScope ps(kStTreeRefit, s);
+    const int grid = div_up(n, kThreads);
+    const int ngrid = div_up(nn, kThreads);
+    float4* pp = p4.as<float4>();
+    float* pd = pdisp.get<float>(n);
+    k_gather<<<grid, kThreads, 0, s>>>(n, perm.as<int>(), pos, mass, xbuild.as<double>(), pp, pd,
+                                       want_knn ? plo.get<float4>(n) : nullptr);
+    GF_CHECK_LAUNCH();
+    GF_CUDA(cudaMemsetAsync(n_counter.as<int>(), 0, sizeof(int) * size_t(nn), s));
+    MomentArgs A{};
+    A.nn = nn;
+    A.refit = true;
+    A.theta = theta_f;
+    A.n_i4 = n_i4.as<int4>();
+    A.parent = n_parent.as<int>();
+    A.nchild = n_nchild.as<int>();
+    A.counter = n_counter.as<int>();
+    A.n_cd = n_cd.as<double4>();
+    A.n_geo = n_geo.as<float4>();
+    A.mom = n_mom.as<float4>();
+    A.open_r = n_open.as<float>();
+    A.ndisp = n_disp.as<float>();
+    A.p4 = pp;
+    A.pdisp = pd;
+    k_moments<<<ngrid, kThreads, 0, s>>>(A);
+    GF_CHECK_LAUNCH();
+    k_walk_fill<<<ngrid, kThreads, 0, s>>>(nn, A.n_i4, A.nchild, n_bfs.as<int>(), A.mom, A.open_r,
+                                           A.n_geo, w_a.as<float4>(), w_b.as<float4>(),
+                                           want_knn ? w_geo.as<float4>() : nullptr,
+                                           want_knn ? leaf_of.as<int>() : nullptr);
+    GF_CHECK_LAUNCH();
+}
+
+}  // namespace gf

@@ -1,0 +1,79 @@
+// gf_tree.cuh — device octree: Morton-key build that reproduces the reference's tree,
+// refit, walk groups and the walk layout.
+#pragma once
+
+#include "gf_common.cuh"
+
+namespace gf {
+
+constexpr int kLeafMax = 8;      // cpp/nbody.cpp:33
+constexpr int kGroupMax = 64;    // cpp/nbody.cpp:34
+constexpr int kDepthMax = 48;    // cpp/nbody.cpp:35
+constexpr int kKeyLevels = 21;   // levels held by one 63-bit Morton key word
+constexpr int kDeepRunMax = 4096;
+
+// Root cube and the fixed-point grid used by the fast key path.
+struct RootBox {
+    double c[3];
+    double half;
+    double lo[3];     // c - half
+    double inv_w;     // 2^21 / (2 half): grid units per unit length
+    double margin;    // grid units: closer than this to a cell wall -> exact path
+};
+
+// Small device-side counters read back once per build.
+struct TreeCounts {
+    int total_nodes;
+    int deep;         // some level-21 cell holds more than kLeafMax particles
+    int num_groups;
+    int num_work;
+    int walk_next;    // dynamic scheduler of the walk
+    int pad[3];
+    unsigned long long pairs;  // particle-list interactions evaluated by the last walk
+};
+
+struct Octree {
+    int n = 0;        // particles
+    int nn = 0;       // nodes
+    int ng = 0;       // groups
+    int max_depth = 0;
+    float theta_f = 0.7f;
+    bool valid = false;
+    const uint8_t* active_ptr = nullptr;  // active flags of the current walk (device)
+
+    // particles (tree order unless noted)
+    DevBuf key, key_alt, perm, perm_alt, key1, key2, p4, xbuild, pdisp;
+    DevBuf cpl9, ldepth, dsplit, nstart, nbase;
+    // nodes, depth-first (preorder) order
+    DevBuf n_i4;      // int4 {start, count, next, leaf | depth << 8}
+    DevBuf n_mom;     // float4 {cx, cy, cz, m}
+    DevBuf n_open;    // float open_r
+    DevBuf n_geo;     // float4 {gx, gy, gz, half}
+    DevBuf n_cd;      // double4 {centre, half} (build only)
+    DevBuf n_parent, n_nchild, n_counter, n_disp, n_bfs;
+    // walk layout, breadth-first order: children of a node are contiguous
+    DevBuf w_a;       // float4 {cx, cy, cz, m}
+    DevBuf w_b;       // float4 {open_r, first (int bits), code (int bits), 0};
+                      //   code > 0: internal, `code` children from BFS index `first`;
+                      //   code < 0: leaf, -code particles from tree position `first`
+    DevBuf w_geo;     // float4 {gx, gy, gz, half} of the cell, breadth-first order
+    DevBuf bfs_key, bfs_key_alt, bfs_val, bfs_val_alt;
+    // neighbour search extras (tree order): float32 remainders x - float(x) and the
+    // breadth-first index of each particle's leaf
+    DevBuf plo, leaf_of;
+    bool want_knn = false;
+    // groups and walk work list
+    DevBuf gflag, gscan, groups, work, sphere;
+    DevBuf root, counts;
+    TreeCounts* h_counts = nullptr;  // pinned
+
+    void build(int n, const double* pos, const double* mass, double theta, cudaStream_t s);
+    void refit(const double* pos, const double* mass, cudaStream_t s);
+    // Work list of groups with at least one active particle (active may be null).
+    void prepare_walk(const uint8_t* active, cudaStream_t s);
+    void walk(double eps, double* acc, cudaStream_t s);
+};
+
+Octree& gravity_tree();
+
+}  // namespace gf

@@ -1,0 +1,320 @@
+// gf_walk.cu — group tree walk + interaction-list evaluation (cpp/nbody.cpp:323-411).
+//
+// One warp per walk group (the reference's groups: shallowest nodes with <= 64 particles),
+// persistent blocks pulling groups from an atomic counter (the reference's dynamic
+// schedule). Per group:
+//   * bounding sphere of its massive particles (float32, cpp/nbody.cpp:350-366) — computed
+//     once per call in k_group_prep together with the active count;
+//   * walk: the reference tests nodes one at a time along depth-first `next` links; here
+//     the warp tests up to 32 nodes at once, taken from a shared-memory stack of child
+//     ranges (children are contiguous in the breadth-first walk layout). A node is visited
+//     iff all its ancestors were opened, so the set of accepted nodes and opened leaves —
+//     the interaction list — is exactly the reference's; only the summation order differs;
+//   * accepted monopoles and opened-leaf particles are appended to a shared-memory tile of
+//     256 float4 entries, evaluated by the warp whenever it fills: each active particle of
+//     the group owns 1..32 lanes (lanes split the tile when the group is small, two
+//     particles per lane when it has more than 32 active particles);
+//   * pair term as cpp/nbody.cpp:398-402 in float32: a += m d / (|d|^2 + eps^2)^(3/2).
+// Accelerations are written as float64 into acc[3*k] for original index k (active only).
+#include <algorithm>
+
+#include "gf_tree.cuh"
+
+namespace gf {
+
+namespace {
+
+constexpr int kWalkWarps = 4;
+constexpr int kStackCap = 1024;   // child ranges per warp
+constexpr int kTileCap = 256;     // interaction entries per warp
+
+// Work list: groups with at least one active particle and a massive member.
+__global__ void k_group_prep(const int* __restrict__ groups, const int4* __restrict__ n_i4,
+                             const float4* __restrict__ p4, const int* __restrict__ perm,
+                             const uint8_t* __restrict__ active, TreeCounts* cnt,
+                             int4* __restrict__ work, float4* __restrict__ sphere) {
+    const int lane = threadIdx.x & 31;
+    const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const int ng = cnt->num_groups;
+    for (int g = wid; g < ng; g += nw) {
+        const int node = groups[g];
+        const int4 q = n_i4[node];
+        const int b = q.x, e = q.x + q.y;
+        int nact = 0;
+        float x0 = 1e30f, y0 = 1e30f, z0 = 1e30f, x1 = -1e30f, y1 = -1e30f, z1 = -1e30f;
+        for (int i = b + lane; i < e; i += 32) {
+            const bool a = active ? active[perm[i]] != 0 : true;
+            nact += __popc(__ballot_sync(__activemask(), a));
+            const float4 p = p4[i];
+            if (p.w > 0) {
+                x0 = fminf(x0, p.x); x1 = fmaxf(x1, p.x);
+                y0 = fminf(y0, p.y); y1 = fmaxf(y1, p.y);
+                z0 = fminf(z0, p.z); z1 = fmaxf(z1, p.z);
+            }
+        }
+        nact = __shfl_sync(0xffffffffu, nact, 0);
+        if (nact == 0) continue;
+        x0 = warp_min(x0); y0 = warp_min(y0); z0 = warp_min(z0);
+        x1 = warp_max(x1); y1 = warp_max(y1); z1 = warp_max(z1);
+        if (x0 > x1) continue;  // massless group
+        const float bx = 0.5f * (x0 + x1), by = 0.5f * (y0 + y1), bz = 0.5f * (z0 + z1);
+        float br2 = 0.f;
+        for (int i = b + lane; i < e; i += 32) {
+            const float4 p = p4[i];
+            if (p.w > 0) {
+                const float dx = p.x - bx, dy = p.y - by, dz = p.z - bz;
+                br2 = fmaxf(br2, dx * dx + dy * dy + dz * dz);
+            }
+        }
+        br2 = warp_max(br2);
+        int slot = 0;
+        if (lane == 0) slot = atomicAdd(&cnt->num_work, 1);
+        slot = __shfl_sync(0xffffffffu, slot, 0);
+        if (lane == 0) {
+            work[slot] = make_int4(b, q.y, nact, node);
+            sphere[slot] = make_float4(bx, by, bz, sqrtf(br2));
+        }
+    }
+}
+
+struct WarpSmem {
+    int stack[kStackCap];
+    float4 tile[kTileCap];
+    int lanemap[32];
+    int slot_pos[64];
+};
+
+__device__ __forceinline__ void pair_acc(const float4 e, float x, float y, float z, float eps2,
+                                         float& ax, float& ay, float& az) {
+    const float ex = e.x - x, ey = e.y - y, ez = e.z - z;
+    const float r2 = ex * ex + ey * ey + ez * ez + eps2;
+    const float inv = rsqrtf(r2);
+    const float f = e.w * inv * inv * inv;
+    ax += f * ex;
+    ay += f * ey;
+    az += f * ez;
+}
+
+__global__ void __launch_bounds__(kWalkWarps * 32) k_walk_mono(
+    const float4* __restrict__ wa, const float4* __restrict__ wb, const float4* __restrict__ p4,
+    const int* __restrict__ perm, const uint8_t* __restrict__ active, const int4* __restrict__ work,
+    const float4* __restrict__ sphere, TreeCounts* cnt, int nn, float eps2, double* __restrict__ acc,
+    uint32_t* status) {
+    __shared__ WarpSmem smem_all[kWalkWarps];
+    WarpSmem& S = smem_all[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = lanemask_lt();
+    const int nwork = cnt->num_work;
+
+    for (;;) {
+        int g = 0;
+        if (lane == 0) g = atomicAdd(&cnt->walk_next, 1);
+        g = __shfl_sync(0xffffffffu, g, 0);
+        if (g >= nwork) break;
+        const int4 w = work[g];
+        const float4 sph = sphere[g];
+        const int b = w.x, count = w.y, Pall = w.z;
+        // Groups hold <= 64 particles except depth-48 leaves of coincident points; those are
+        // evaluated in batches of 64 active particles, each batch walking the tree again.
+        for (int pb = 0; pb < Pall; pb += 64) {
+        const int P = min(64, Pall - pb);
+
+        // compact the active particles of this batch into slots
+        int nslot = 0;
+        for (int i0 = 0; i0 < count; i0 += 32) {
+            const int i = b + i0 + lane;
+            const bool a = i0 + lane < count && (active ? active[perm[i]] != 0 : true);
+            const unsigned m = __ballot_sync(0xffffffffu, a);
+            const int rank = nslot + __popc(m & lt);
+            if (a && rank >= pb && rank < pb + P) S.slot_pos[rank - pb] = i;
+            nslot += __popc(m);
+        }
+        __syncwarp();
+
+        // lane mapping: r lanes per particle (r = 1 and two slots per lane when P > 32)
+        int r = 1;
+        if (P <= 16) r = P <= 1 ? 32 : P <= 2 ? 16 : P <= 4 ? 8 : P <= 8 ? 4 : 2;
+        const int slot0 = lane / r, sub = lane % r;
+        const int slot1 = slot0 + 32;
+        const bool has0 = slot0 < P, has1 = P > 32 && slot1 < P;
+        float x0 = 0.f, y0 = 0.f, z0 = 0.f, x1 = 0.f, y1 = 0.f, z1 = 0.f;
+        if (has0) {
+            const float4 p = p4[S.slot_pos[slot0]];
+            x0 = p.x; y0 = p.y; z0 = p.z;
+        }
+        if (has1) {
+            const float4 p = p4[S.slot_pos[slot1]];
+            x1 = p.x; y1 = p.y; z1 = p.z;
+        }
+        float ax0 = 0.f, ay0 = 0.f, az0 = 0.f, ax1 = 0.f, ay1 = 0.f, az1 = 0.f;
+        const bool two = P > 32;
+
+        int fill = 0;
+        unsigned long long listlen = 0;
+        auto flush = [&]() {
+            listlen += fill;
+            __syncwarp();
+            if (two) {
+                for (int j = 0; j < fill; ++j) {
+                    const float4 e = S.tile[j];
+                    pair_acc(e, x0, y0, z0, eps2, ax0, ay0, az0);
+                    pair_acc(e, x1, y1, z1, eps2, ax1, ay1, az1);
+                }
+            } else {
+                for (int j = sub; j < fill; j += r) pair_acc(S.tile[j], x0, y0, z0, eps2, ax0, ay0, az0);
+            }
+            __syncwarp();
+            fill = 0;
+        };
+
+        int sp = 1;
+        if (lane == 0) S.stack[0] = (0 << 4) | 1;  // root: range (first 0, count 1)
+        bool overflow = false;
+        __syncwarp();
+        // every node is popped at most once per walk: more rounds than nodes is a bug
+        for (int rounds = 0; sp > 0; ++rounds) {
+            if (rounds > nn) {
+                overflow = true;
+                break;
+            }
+            // pop up to 32 nodes from the top ranges
+            const int k = min(sp, 32);
+            int e = 0, c = 0;
+            if (lane < k) {
+                e = S.stack[sp - 1 - lane];
+                c = e & 15;
+            }
+            const int incl = warp_incl_scan(c);
+            const int excl = incl - c;
+            const unsigned fullm = __ballot_sync(0xffffffffu, lane < k && incl <= 32);
+            const int nfull = __popc(fullm);
+            int nnodes = __shfl_sync(0xffffffffu, incl, k - 1);
+            int take = c;
+            if (nfull < k) {  // range `nfull` is split: the rest stays on the stack
+                nnodes = 32;
+                if (lane == nfull) {
+                    take = 32 - excl;
+                    S.stack[sp - 1 - lane] = (((e >> 4) + take) << 4) | (c - take);
+                }
+            }
+            __syncwarp();
+            if (lane < k && lane <= nfull) {
+                const int first = e >> 4;
+                for (int t = 0; t < take && excl + t < 32; ++t) S.lanemap[excl + t] = first + t;
+            }
+            sp -= nfull;
+            __syncwarp();
+            const bool valid = lane < nnodes;
+            const int node = valid ? S.lanemap[lane] : 0;
+            __syncwarp();
+
+            float4 A = make_float4(0.f, 0.f, 0.f, 0.f), B = A;
+            if (valid) {
+                A = wa[node];
+                B = wb[node];
+            }
+            const float dx = A.x - sph.x, dy = A.y - sph.y, dz = A.z - sph.z;
+            const float t = B.x + sph.w;
+            const bool accept = valid && (dx * dx + dy * dy + dz * dz > t * t);
+            const int first = __float_as_int(B.y), code = __float_as_int(B.z);
+            const bool leaf = valid && !accept && code < 0;
+            const bool open = valid && !accept && code > 0;
+
+            // opened internal nodes: push their child ranges
+            const unsigned om = __ballot_sync(0xffffffffu, open);
+            const int npush = __popc(om);
+            if (sp + npush > kStackCap) {
+                overflow = true;
+                break;
+            }
+            if (open) S.stack[sp + __popc(om & lt)] = (first << 4) | code;
+            sp += npush;
+
+            // accepted nodes: monopole entries
+            const unsigned am = __ballot_sync(0xffffffffu, accept);
+            const int na = __popc(am);
+            if (fill + na > kTileCap) flush();
+            if (accept) S.tile[fill + __popc(am & lt)] = A;
+            fill += na;
+
+            // opened leaves: their particles
+            const int lc = leaf ? -code : 0;
+            const int lincl = warp_incl_scan(lc);
+            const int lexcl = lincl - lc;
+            const int ltot = __shfl_sync(0xffffffffu, lincl, 31);
+            for (int done = 0; done < ltot;) {
+                if (fill == kTileCap) flush();
+                const int chunk = min(kTileCap - fill, ltot - done);
+                if (leaf) {
+                    const int a0 = max(lexcl, done), a1 = min(lexcl + lc, done + chunk);
+                    for (int q = a0; q < a1; ++q) S.tile[fill + q - done] = p4[first + q - lexcl];
+                }
+                fill += chunk;
+                done += chunk;
+            }
+            __syncwarp();
+        }
+        if (overflow) {
+            if (lane == 0) raise_status(status, GF_ERR_WALK_STACK);
+            break;
+        }
+        flush();
+
+        // combine the partial sums of the lanes that share a particle
+        for (int o = r >> 1; o > 0; o >>= 1) {
+            ax0 += __shfl_xor_sync(0xffffffffu, ax0, o);
+            ay0 += __shfl_xor_sync(0xffffffffu, ay0, o);
+            az0 += __shfl_xor_sync(0xffffffffu, az0, o);
+        }
+        if (lane == 0) atomicAdd(&cnt->pairs, listlen * (unsigned long long)P);
+        if (has0 && sub == 0) {
+            const int k = perm[S.slot_pos[slot0]];
+            acc[3 * size_t(k)] = ax0;
+            acc[3 * size_t(k) + 1] = ay0;
+            acc[3 * size_t(k) + 2] = az0;
+        }
+        if (has1) {
+            const int k = perm[S.slot_pos[slot1]];
+            acc[3 * size_t(k)] = ax1;
+            acc[3 * size_t(k) + 1] = ay1;
+            acc[3 * size_t(k) + 2] = az1;
+        }
+        __syncwarp();
+        }  // batches
+    }
+}
+
+}  // namespace
+
+void Octree::prepare_walk(const uint8_t* active, cudaStream_t s) {
+    Context& C = ctx();
+    TreeCounts* cnt = counts.as<TreeCounts>();
+    GF_CUDA(cudaMemsetAsync(&cnt->num_work, 0, 2 * sizeof(int), s));  // num_work, walk_next
+    GF_CUDA(cudaMemsetAsync(&cnt->pairs, 0, sizeof(unsigned long long), s));
+    ProfScope ps(kStGroupPrep, s);
+    const int cap = std::max(1, nn);
+    active_ptr = active;
+    k_group_prep<<<4 * C.sms, 256, 0, s>>>(groups.as<int>(), n_i4.as<int4>(), p4.as<float4>(),
+                                          perm.as<int>(), active, cnt, work.get<int4>(cap),
+                                          sphere.get<float4>(cap));
+    GF_CHECK_LAUNCH();
+}
+
+void Octree::walk(double eps, double* acc, cudaStream_t s) {
+    Context& C = ctx();
+    const float eps2 = float(eps * eps);
+    static int blocks_per_sm = 0;
+    if (!blocks_per_sm) {
+        GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_walk_mono,
+                                                              kWalkWarps * 32, 0));
+        blocks_per_sm = std::max(1, blocks_per_sm);
+    }
+    ProfScope ps(kStWalk, s);
+    k_walk_mono<<<blocks_per_sm * C.sms, kWalkWarps * 32, 0, s>>>(
+        w_a.as<float4>(), w_b.as<float4>(), p4.as<float4>(), perm.as<int>(), active_ptr,
+        work.as<int4>(), sphere.as<float4>(), counts.as<TreeCounts>(), nn, eps2, acc, C.d_status);
+    GF_CHECK_LAUNCH();
+}
+
+}  // namespace gf

@@ -1,0 +1,188 @@
+/* gfgpu.h — C ABI of libgfgpu.so, the GB300 (sm_103a) gravity + SPH force library.
+ *
+ * Drop-in for the force path of HugoGW/Galaxy_formation:
+ *   - the five extern "C" exports of cpp/nbody.cpp (bound with ctypes in
+ *     galaxy_formation/engine.py:30-35), with identical names and signatures;
+ *   - the SPH entry points of galaxy_formation/sph.py (sph_forces, knn_from_candidates and
+ *     the k-d tree query inside NeighbourFinder.find), as plain-pointer C functions.
+ *
+ * Conventions. Pointers of the reference-compatible functions are HOST pointers (the
+ * library copies to and from the GPU). Functions with the `_dev` suffix take DEVICE
+ * pointers and a CUDA stream (cudaStream_t passed as void*, NULL = the library's stream);
+ * they enqueue work and return without synchronising unless stated. Arrays are
+ * C-contiguous: positions (n,3) float64 row-major, etc.
+ *
+ * Errors. The reference's functions return void and have no error channel
+ * (cpp/nbody.cpp:415-441). Every entry point here records a status: the int-returning
+ * ones return it, and gf_last_status() returns the status of the last call (0 = ok,
+ * otherwise a bitwise OR of GF_ERR_*); gf_last_error() gives a message. Kernels never
+ * trap on bad input; they set a status bit and skip the offending work.
+ */
+#ifndef GFGPU_H
+#define GFGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status bits */
+#define GF_OK 0
+#define GF_ERR_CUDA 1         /* a CUDA runtime call failed (message in gf_last_error) */
+#define GF_ERR_ARG 2          /* invalid argument (negative size, null pointer, ...)  */
+#define GF_ERR_NONFINITE 4    /* a position was NaN or infinite                        */
+#define GF_ERR_WALK_STACK 8   /* tree-walk stack overflow: some accelerations skipped  */
+#define GF_ERR_DEEP_CELL 16   /* more than 4096 particles share one cell below level 21 */
+#define GF_ERR_KNN 32         /* neighbour search did not converge for some particles  */
+#define GF_ERR_NO_DEVICE 64   /* no CUDA device                                        */
+#define GF_ERR_CAPACITY 128   /* a fixed-capacity buffer was too small                 */
+
+/* ---- drop-ins for cpp/nbody.cpp (signatures identical to the reference) ---------------- */
+
+/* Replaces nbody_num_threads (cpp/nbody.cpp:417): returns the number of SMs of the GPU
+ * (the library's unit of parallelism), 0 when no GPU is usable. */
+int nbody_num_threads(void);
+
+/* Replaces nbody_accel_active (cpp/nbody.cpp:422-425). Barnes-Hut accelerations (G = 1,
+ * Plummer softening eps, opening angle theta) of the active particles (active[i] != 0, or
+ * all when active is NULL), written into acc (n,3); other rows of acc are left untouched.
+ * The octree always holds every particle and is kept on the GPU between calls:
+ * rebuild = 0 refits the previous tree (same cells, new moments, opening radii enlarged
+ * by the largest displacement since the build), unless n changed. Same tree, groups,
+ * interaction lists and float32 arithmetic as the reference. */
+void nbody_accel_active(int n, const double* pos, const double* mass, double* acc,
+                        double theta, double eps, const uint8_t* active, int rebuild);
+
+/* Replaces nbody_accel_direct (cpp/nbody.cpp:428-441): exact O(N^2) float64 sum. */
+void nbody_accel_direct(int n, const double* pos, const double* mass, double* acc,
+                        double eps);
+
+/* Replaces nbody_render (cpp/nbody.cpp:445-469): orthographic bilinear deposit of the
+ * first n particles into img (ngroups, H, W), float32. */
+void nbody_render(int n, const double* pos, const uint8_t* group, int ngroups,
+                  const double* rot, const double* center, double scale, int W, int H,
+                  float* img);
+
+/* Replaces nbody_tonemap (cpp/nbody.cpp:474-503): log tone map + glow + soft saturation
+ * of the per-group images to 8-bit RGB out (H, W, 3). */
+void nbody_tonemap(int W, int H, int ngroups, const float* img, const float* glow, int gw,
+                   int gh, const float* colors, float inv_ref, float K, float exposure,
+                   uint8_t* out);
+
+/* ---- status ------------------------------------------------------------------------- */
+
+/* Status of the last call (GF_OK or GF_ERR_* bits); synchronises the library stream. No
+ * reference counterpart: the reference has no error channel (cpp/nbody.cpp:415-441). */
+int gf_last_status(void);
+/* Message of the last failure ("" when none). No reference counterpart. */
+const char* gf_last_error(void);
+/* Number of octree nodes and walk groups of the current gravity tree (for tests). */
+int gf_tree_size(int* num_nodes, int* num_groups);
+/* Copies the current gravity tree out in the reference's depth-first node order
+ * (cpp/nbody.cpp:38-45 layout, split): ints (nn,4) = start, count, next, leaf;
+ * floats (nn,9) = cx, cy, cz, m, open_r, gx, gy, gz, half; order (n,) tree position ->
+ * particle index (cpp/nbody.cpp:62 idx); groups (ng,) node ids (cpp/nbody.cpp:235-243).
+ * Host pointers. No reference counterpart (test hook). */
+int gf_tree_export(int32_t* ints, float* floats, int32_t* order, int32_t* groups);
+
+/* ---- device-resident gravity -------------------------------------------------------- */
+
+/* nbody_accel_active on device pointers (same semantics). */
+int gf_accel_active_dev(int n, const double* pos, const double* mass, double* acc,
+                        double theta, double eps, const uint8_t* active, int rebuild,
+                        void* stream);
+/* nbody_accel_direct on device pointers. */
+int gf_accel_direct_dev(int n, const double* pos, const double* mass, double* acc,
+                        double eps, void* stream);
+/* Direct float64 sum for nt target particles (indices into pos) against all n sources;
+ * acc is (nt,3). Host pointers. Same arithmetic as nbody_accel_direct
+ * (cpp/nbody.cpp:428-441), for error reports at sizes where O(N^2) is too slow. */
+int gf_accel_direct_targets(int n, const double* pos, const double* mass, int nt,
+                            const int64_t* targets, double* acc, double eps);
+
+/* ---- SPH (galaxy_formation/sph.py) --------------------------------------------------- */
+
+/* Vectorised kernel(r, h) and kernel_grad(r, h) of sph.py:31-54 (either output may be
+ * NULL). Host pointers. */
+int gf_sph_kernel(int n, const double* r, const double* h, double* w, double* dw);
+
+/* Replaces sph_forces (sph.py:57-106): density, pressure + artificial-viscosity
+ * acceleration, du/dt and Courant time step of n gas particles with k neighbours each
+ * (nb (n,k) local indices, the particle itself included). Host pointers; outputs rho (n),
+ * acc (n,3), dudt (n), dt_i (n). float64 arithmetic as in the reference. */
+int gf_sph_forces(int n, int k, const double* pos, const double* vel, const double* mass,
+                  const int64_t* nb, const double* h, const double* u, double gamma,
+                  double alpha, double beta, double* rho, double* acc, double* dudt,
+                  double* dt_i);
+/* sph_forces on device pointers. */
+int gf_sph_forces_dev(int n, int k, const double* pos, const double* vel, const double* mass,
+                      const int64_t* nb, const double* h, const double* u, double gamma,
+                      double alpha, double beta, double* rho, double* acc, double* dudt,
+                      double* dt_i, void* stream);
+
+/* Replaces knn_from_candidates (sph.py:109-135): the k nearest of each particle among its
+ * m candidates (cand (n,m) local indices, -1 = none), ascending, into nb (n,k) and dist
+ * (n,k). Returns 1 when every particle had at least k candidates, 0 otherwise (rows of
+ * such particles are left untouched), or -GF_ERR_* on failure. Host pointers. */
+int gf_knn_from_candidates(int n, int m, const double* pos, const int64_t* cand, int k,
+                           int64_t* nb, double* dist);
+
+/* Replaces cKDTree(pos).query(pos, k) inside NeighbourFinder.find (sph.py:165-166): the
+ * exact k nearest points of every point (itself included), ascending distance, into dist
+ * (n,k) and nb (n,k). 1 <= k <= 64, k <= n. Host pointers. */
+int gf_knn(int n, const double* pos, int k, double* dist, int64_t* nb);
+/* Total search-radius iterations of the last gf_knn call, summed over particles (the
+ * neighbour-count iteration). No reference counterpart. */
+long long gf_knn_iterations(void);
+
+/* ---- fused force evaluation (galaxy_formation/simulation.py:61-95) ------------------- */
+
+/* One GalaxyFormation.accelerations(active, rebuild, sph, fresh_nb) call on device
+ * pointers: Barnes-Hut gravity of the active particles (into a persistent internal
+ * acc_grav), then, when sph != 0, the hydro step of simulation.py:74-95 for every particle
+ * with kind == 0 (gas): neighbour search (fresh_nb != 0: full 48-candidate search; else
+ * Verlet reselection among the cached candidates, falling back to a full search as
+ * sph.py:155-166 does), h = max(d_32 / 2, eps / 2), sph_forces, scatter. Outputs acc (n,3)
+ * = acc_grav + acc_sph and dt_ind (n,) = min(0.3 sqrt(eps / |a|), dt_courant). kind is
+ * (n,) int8 (0 gas, 1 star, 2 dark matter), u (n,) specific internal energy. State (tree,
+ * neighbour cache, acc_grav, acc_sph, dt_courant) persists between calls and is reset when
+ * n changes. */
+int gf_accelerations_dev(int n, const double* pos, const double* vel, const double* mass,
+                         const int8_t* kind, const double* u, double theta, double eps,
+                         double gamma, double alpha, double beta, const uint8_t* active,
+                         int rebuild, int sph, int fresh_nb, double* acc, double* dt_ind,
+                         void* stream);
+/* gf_accelerations_dev on host pointers (copies in and out, synchronises). */
+int gf_accelerations(int n, const double* pos, const double* vel, const double* mass,
+                     const int8_t* kind, const double* u, double theta, double eps, double gamma,
+                     double alpha, double beta, const uint8_t* active, int rebuild, int sph,
+                     int fresh_nb, double* acc, double* dt_ind);
+/* Scalars of the last force evaluation: gas count, dt_grav = 0.3 sqrt(eps / max |a|),
+ * dt_gas = min Courant step (inf without hydro), search-radius iterations of the last full
+ * neighbour search. Any pointer may be NULL. Synchronises the device. */
+int gf_force_info(int* n_gas, double* dt_grav, double* dt_gas, long long* knn_iters);
+
+/* ---- measurement hooks (no reference counterpart) ----------------------------------- */
+
+/* Starts (on != 0) or stops a profiling session; starting clears previous records. While
+ * on, every stage below is bracketed by CUDA events recorded on its launching stream. */
+int gf_profile(int on);
+/* Stage ids: 0 gravity tree build, 1 refit, 2 walk kernel, 3 walk work list, 4 neighbour
+ * search kernel, 5 gas octree build, 6 SPH density kernel, 7 SPH force kernel, 8 Verlet
+ * reselection, 9 whole force evaluation. Total milliseconds and number of launches
+ * recorded in the session; synchronises the device. */
+int gf_profile_stage(int stage, double* total_ms, int* launches);
+/* Kernels launched by the library since it was loaded. */
+long long gf_launch_count(void);
+/* Particle-list pair interactions evaluated by the last gravity walk (synchronises). */
+long long gf_walk_pairs(void);
+/* Measures the float32 FFMA throughput of the GPU (TFLOP/s, an FMA counting 2 flops): the
+ * roofline peak of the float32 walk. */
+int gf_fp32_peak(double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GFGPU_H */

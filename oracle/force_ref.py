@@ -1,0 +1,86 @@
+"""CPU restatement of one force evaluation (TEST INFRASTRUCTURE ONLY).
+
+Follows GalaxyFormation.accelerations / _hydro (galaxy_formation/simulation.py:61-95) and
+NeighbourFinder.find (galaxy_formation/sph.py:151-170) line by line, with:
+  * gravity ............ oracle.accel_active (restatement of cpp/nbody.cpp, OpenMP);
+  * full neighbour search scipy.spatial.cKDTree(p).query(p, k=48, workers=-1) — the
+                         reference's own call (sph.py:166);
+  * Verlet reselection . oracle.knn_from_candidates (restatement of sph.py:109-135);
+  * SPH forces ......... oracle.sph_forces (restatement of sph.py:57-106, OpenMP; the
+                         reference runs it through numba, absent here).
+Used as the checker of the fused GPU force evaluation and as the timed CPU baseline.
+"""
+
+import numpy as np
+from scipy.spatial import cKDTree
+
+import oracle
+
+GAS = 0
+N_NEIGHBOURS, N_CANDIDATES = 32, 48
+
+
+class ForceOracle:
+    def __init__(self, n, theta, eps, gamma=5.0 / 3.0, alpha=1.0, beta=2.0, use_ckdtree=True):
+        self.n, self.theta, self.eps = n, theta, eps
+        self.gamma, self.alpha, self.beta = gamma, alpha, beta
+        self.acc_grav = np.zeros((n, 3))
+        self.acc_sph = np.zeros((n, 3))
+        self.dt_courant = np.full(n, np.inf)
+        self.cache = None
+        self.use_ckdtree = use_ckdtree
+        self.full_searches = 0
+
+    def _find(self, g, p, fresh):
+        k = N_NEIGHBOURS
+        if not fresh and self.cache is not None:
+            row = self.cache["row"][g]
+            if (row >= 0).all():
+                loc = np.full(self.n, -1, np.int64)
+                loc[g] = np.arange(g.size)
+                cand = loc[self.cache["cand"][row]]
+                nb = np.empty((g.size, k), np.int64)
+                d = np.empty((g.size, k))
+                if oracle.knn_from_candidates(p, cand, k, nb, d):
+                    return d, nb
+        kq = min(N_CANDIDATES, g.size)
+        if self.use_ckdtree:
+            d, nb = cKDTree(p).query(p, k=kq, workers=-1)
+        else:
+            d, nb = oracle.knn_brute(p, kq)
+        self.full_searches += 1
+        row = np.full(self.n, -1, np.int64)
+        row[g] = np.arange(g.size)
+        self.cache = {"row": row, "cand": g[nb]}
+        return d[:, :k], np.ascontiguousarray(nb[:, :k])
+
+    def _hydro(self, pos, vel, mass, kind, u, fresh):
+        self.acc_sph[:] = 0.0
+        self.dt_courant[:] = np.inf
+        self.dt_gas = np.inf
+        g = np.flatnonzero(kind == GAS)
+        self.n_gas = g.size
+        if g.size <= 40:
+            return
+        p = np.ascontiguousarray(pos[g])
+        d, nb = self._find(g, p, fresh)
+        h = np.maximum(0.5 * d[:, -1], 0.5 * self.eps)
+        rho, a, dudt, dt_i = oracle.sph_forces(p, np.ascontiguousarray(vel[g]),
+                                               np.ascontiguousarray(mass[g]), nb, h,
+                                               np.ascontiguousarray(u[g]), self.gamma,
+                                               self.alpha, self.beta)
+        self.acc_sph[g] = a
+        self.dt_courant[g] = dt_i
+        self.dt_gas = dt_i.min()
+        self.h, self.rho, self.dudt, self.nb = h, rho, dudt, nb
+
+    def accelerations(self, pos, vel, mass, kind, u, active=None, rebuild=True, sph=True,
+                      fresh_nb=True):
+        oracle.accel_active(pos, mass, self.acc_grav, self.theta, self.eps, active, rebuild)
+        if sph:
+            self._hydro(pos, vel, mass, kind, u, fresh_nb)
+        acc = self.acc_grav + self.acc_sph
+        a_mag = np.sqrt(np.einsum("ij,ij->i", acc, acc))
+        self.dt_ind = np.minimum(0.3 * np.sqrt(self.eps / np.maximum(a_mag, 1e-30)), self.dt_courant)
+        self.dt_grav = 0.3 * np.sqrt(self.eps / max(a_mag.max(), 1e-30))
+        return acc

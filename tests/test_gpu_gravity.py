@@ -1,0 +1,206 @@
+"""GPU Barnes-Hut against the oracle and the reference's fixtures (through the C ABI).
+
+Parity bar: the same octree (node for node: start, count, next, leaf, groups, particle
+order) and per-particle relative acceleration error p99 <= 1e-4 against the reference's
+Barnes-Hut at the same theta and eps. The remaining difference is float32 summation order
+(and rsqrt rounding), ~1e-6.
+"""
+
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+P99_TOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def engine(gpulib):
+    from galaxy_formation_gb300.engine import Engine
+
+    return Engine()
+
+
+def compare_trees(a, b):
+    for f in ("start", "count", "next", "leaf", "order", "groups"):
+        assert np.array_equal(a[f], b[f]), f
+    for f in ("gx", "gy", "gz", "half", "m", "cx", "cy", "cz", "open_r"):
+        x, y = a[f].astype(np.float64), b[f].astype(np.float64)
+        # float32 records from float64 sums: equal up to the last bit
+        assert np.all(np.abs(x - y) <= 2 * np.spacing(np.abs(y).astype(np.float32)).astype(np.float64)), f
+
+
+def cases():
+    from galaxy_formation_gb300 import synthetic
+
+    rng = np.random.default_rng(0)
+    gauss = np.ascontiguousarray(rng.normal(size=(20000, 3)))
+    yield "gauss20k", gauss, np.full(20000, 1 / 20000), 0.7, 0.01
+    c = synthetic.rotating_cloud()
+    yield "cloud10k", c["pos"], c["mass"], 0.7, 0.4 / 3.5
+    d = synthetic.make_config(1, scale=0.25)
+    yield "disk50k", d["pos"], d["mass"], 0.7, 0.4 / 3.5
+    d = synthetic.make_config(3, scale=0.05)
+    yield "clumps50k", d["pos"], d["mass"], 0.5, 0.4 / 3.5
+
+
+@pytest.mark.parametrize("case", list(range(4)))
+def test_tree_identical_to_oracle(engine, oracle, case):
+    name, pos, mass, theta, eps = list(cases())[case]
+    t_gpu = engine.build_tree(pos, mass, theta)
+    t_orc = oracle.build_tree(pos, mass, theta)
+    compare_trees(t_gpu, t_orc)
+
+
+@pytest.mark.parametrize("case", list(range(4)))
+def test_accel_matches_oracle(engine, oracle, case):
+    name, pos, mass, theta, eps = list(cases())[case]
+    acc = np.zeros_like(pos)
+    engine.gravity(pos, mass, acc, theta, eps)
+    ref = np.zeros_like(pos)
+    oracle.accel_active(pos, mass, ref, theta, eps)
+    err = rel_err(acc, ref)
+    assert np.percentile(err, 99) <= P99_TOL, (name, np.percentile(err, 99))
+    assert err.max() < 1e-3, (name, err.max())
+
+
+def test_accel_matches_reference_fixture(engine, golden):
+    """Against the reference's own cpp/nbody.cpp outputs (tests/golden)."""
+    for fx in ("bh_gauss20k.npz", "cloud10k.npz"):
+        g = golden(fx)
+        acc = np.zeros_like(g["pos"])
+        engine.gravity(g["pos"], g["mass"], acc, float(g["theta"]), float(g["eps"]))
+        err = rel_err(acc, g["acc_bh"].astype(np.float64))
+        assert np.percentile(err, 99) <= P99_TOL, (fx, np.percentile(err, 99))
+
+
+def test_refit_with_active_subset_matches_reference(engine, golden):
+    c = golden("cloud10k.npz")
+    theta, eps = float(c["theta"]), float(c["eps"])
+    acc = np.zeros_like(c["pos"])
+    engine.gravity(c["pos"], c["mass"], acc, theta, eps)
+    before = acc.copy()
+    engine.gravity(c["pos1"], c["mass"], acc, theta, eps, active=c["active1"], rebuild=False)
+    act = c["active1"] != 0
+    err = rel_err(acc[act], c["acc_refit"].astype(np.float64)[act])
+    assert np.percentile(err, 99) <= P99_TOL
+    assert np.array_equal(acc[~act], before[~act])  # inactive rows untouched
+
+
+def test_refit_tree_matches_oracle(engine, oracle):
+    from galaxy_formation_gb300 import synthetic
+
+    d = synthetic.make_config(1, scale=0.1)
+    pos, mass = d["pos"], d["mass"]
+    engine.build_tree(pos, mass, 0.7)
+    oracle.build_tree(pos, mass, 0.7)
+    pos1 = np.ascontiguousarray(pos + 0.01 * d["vel"])
+    act = np.zeros(len(mass), np.uint8)
+    a = np.zeros_like(pos)
+    engine.gravity(pos1, mass, a, 0.7, 0.1, act, False)
+    oracle.accel_active(pos1, mass, a.copy(), 0.7, 0.1, act, False)
+    compare_trees(engine.tree(), oracle.tree_export())
+
+
+def test_barnes_hut_matches_direct_sum(engine):
+    """The reference's own acceptance test (tests/test_physics.py:20-30) on the GPU."""
+    rng = np.random.default_rng(0)
+    pos = np.ascontiguousarray(rng.normal(size=(20000, 3)))
+    mass = np.full(len(pos), 1.0 / len(pos))
+    acc = np.zeros_like(pos)
+    engine.gravity(pos, mass, acc, theta=0.7, eps=0.01)
+    exact = engine.gravity_direct(pos, mass, eps=0.01)
+    err = np.linalg.norm(acc - exact, axis=1) / np.linalg.norm(exact, axis=1)
+    assert np.median(err) < 1e-2
+
+
+def test_direct_matches_reference_fixture(engine, golden):
+    g = golden("bh_gauss20k.npz")
+    exact = engine.gravity_direct(g["pos"], g["mass"], float(g["eps"]))
+    ref = g["acc_direct"]
+    assert np.abs(exact[g["targets"]] - ref).max() <= 1e-12 * np.abs(ref).max()
+    sub = engine.gravity_direct_targets(g["pos"], g["mass"], g["targets"], float(g["eps"]))
+    assert np.abs(sub - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("n", [1, 2, 8, 9, 64, 65, 513])
+def test_small_sizes(engine, oracle, n):
+    rng = np.random.default_rng(n)
+    pos = np.ascontiguousarray(rng.uniform(-1, 1, size=(n, 3)))
+    mass = rng.uniform(0.5, 1.5, n)
+    acc = np.zeros_like(pos)
+    engine.gravity(pos, mass, acc, 0.7, 0.05)
+    ref = np.zeros_like(pos)
+    oracle.accel_active(pos, mass, ref, 0.7, 0.05)
+    assert np.allclose(acc, ref, rtol=1e-5, atol=1e-6 * np.abs(ref).max() + 1e-30)
+    compare_trees(engine.build_tree(pos, mass, 0.7), oracle.build_tree(pos, mass, 0.7))
+
+
+def test_coincident_and_deep_cells(engine, oracle):
+    """Particles sharing a level-21 cell: 20 coincident points (a depth-48 leaf) and a
+    tight cluster that separates below level 21."""
+    rng = np.random.default_rng(4)
+    base = rng.normal(size=(3000, 3))
+    dup = np.repeat(base[:1], 20, axis=0)
+    tight = base[1] + 1e-9 * rng.normal(size=(30, 3))
+    pos = np.ascontiguousarray(np.concatenate([base, dup, tight]))
+    mass = np.full(len(pos), 1.0 / len(pos))
+    compare_trees(engine.build_tree(pos, mass, 0.7), oracle.build_tree(pos, mass, 0.7))
+    acc = np.zeros_like(pos)
+    engine.gravity(pos, mass, acc, 0.7, 0.01)
+    ref = np.zeros_like(pos)
+    oracle.accel_active(pos, mass, ref, 0.7, 0.01)
+    assert np.percentile(rel_err(acc, ref), 99) <= P99_TOL
+
+
+def test_massless_and_inactive_groups(engine, oracle):
+    rng = np.random.default_rng(5)
+    pos = np.ascontiguousarray(rng.normal(size=(5000, 3)))
+    mass = np.where(rng.uniform(size=5000) < 0.3, 0.0, 1.0 / 5000)
+    act = (rng.uniform(size=5000) < 0.1).astype(np.uint8)
+    acc = np.full_like(pos, 7.0)
+    engine.gravity(pos, mass, acc, 0.7, 0.01, act)
+    ref = np.full_like(pos, 7.0)
+    oracle.accel_active(pos, mass, ref, 0.7, 0.01, act)
+    assert np.array_equal(acc[act == 0], ref[act == 0])
+    err = rel_err(acc[act != 0], ref[act != 0])
+    assert np.percentile(err, 99) <= P99_TOL
+
+
+def test_nonfinite_position_reported(engine):
+    from galaxy_formation_gb300 import _lib
+
+    pos = np.ascontiguousarray(np.random.default_rng(6).normal(size=(100, 3)))
+    pos[3, 1] = np.nan
+    acc = np.zeros_like(pos)
+    with pytest.raises(_lib.GpuError) as e:
+        engine.gravity(pos, np.ones(100), acc, 0.7, 0.01)
+    assert e.value.status & 4
+
+
+def test_deterministic(engine):
+    from galaxy_formation_gb300 import synthetic
+
+    d = synthetic.make_config(1, scale=0.1)
+    a = np.zeros_like(d["pos"])
+    b = np.zeros_like(d["pos"])
+    engine.gravity(d["pos"], d["mass"], a, 0.7, 0.1)
+    engine.gravity(d["pos"], d["mass"], b, 0.7, 0.1)
+    assert np.array_equal(a, b)
+
+
+def test_torch_device_path(engine):
+    torch = pytest.importorskip("torch")
+    from galaxy_formation_gb300 import synthetic
+
+    d = synthetic.make_config(1, scale=0.05)
+    acc = np.zeros_like(d["pos"])
+    engine.gravity(d["pos"], d["mass"], acc, 0.7, 0.1)
+    tp = torch.from_numpy(d["pos"]).cuda()
+    tm = torch.from_numpy(d["mass"]).cuda()
+    ta = torch.zeros_like(tp)
+    engine.gravity(tp, tm, ta, 0.7, 0.1)
+    torch.cuda.synchronize()
+    assert np.array_equal(ta.cpu().numpy(), acc)

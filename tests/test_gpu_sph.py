@@ -1,0 +1,136 @@
+"""GPU SPH against the reference's fixtures and the oracle (through the C ABI).
+
+Parity bars: neighbour sets identical (exact float64 kNN, ascending distance), smoothing
+lengths identical, densities / accelerations / du/dt / time steps within 1e-5 relative
+(float64 arithmetic here: observed ~1e-15).
+"""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def sph(gpulib):
+    from galaxy_formation_gb300 import sph as gsph
+
+    return gsph
+
+
+def test_kernel_values_match_reference(sph, golden):
+    s = golden("sph2k.npz")
+    w = sph.kernel(s["kernel_r"], 0.7)
+    g = sph.kernel_grad(s["kernel_r"], 0.7)
+    assert np.allclose(w, s["kernel_w"], rtol=1e-13, atol=0)
+    assert np.allclose(g, s["kernel_g"], rtol=1e-13, atol=0)
+    assert isinstance(sph.kernel(0.3, 0.7), float)
+
+
+def test_kernel_is_normalised(sph):
+    """tests/test_physics.py:33-38 of the reference, on the GPU kernel."""
+    h = 0.7
+    r = np.linspace(0, 2 * h, 20001)
+    w = sph.kernel(r, h)
+    assert abs(np.trapezoid(4 * np.pi * r ** 2 * w, r) - 1) < 1e-4
+
+
+def test_sph_forces_match_reference(sph, golden):
+    s = golden("sph2k.npz")
+    n = len(s["pos"])
+    rho, acc, dudt, dt = np.empty(n), np.empty((n, 3)), np.empty(n), np.empty(n)
+    sph.sph_forces(s["pos"], s["vel"], s["mass"], s["nb"].astype(np.int64), s["h"], s["u"],
+                   float(s["gamma"]), sph.ALPHA, sph.BETA, rho, acc, dudt, dt)
+    for x, y in ((rho, s["rho"]), (dudt, s["dudt"]), (dt, s["dt_i"])):
+        assert np.max(np.abs(x - y) / np.abs(y)) < TOL
+    an = np.linalg.norm(acc - s["acc"], axis=1) / np.linalg.norm(s["acc"], axis=1)
+    assert np.max(an) < TOL
+
+
+def test_knn_matches_ckdtree(sph, golden):
+    s = golden("sph2k.npz")
+    d, nb = sph.knn(s["pos"], 48)
+    assert np.array_equal(nb, s["cand"])
+    assert np.array_equal(nb[:, :32], s["nb"])
+    assert np.max(np.abs(d[:, :32] - s["dist"]) / np.maximum(s["dist"], 1e-300)) < 1e-14
+    h = np.maximum(0.5 * d[:, 31], 0.5 * float(s["eps"]))
+    assert np.max(np.abs(h - s["h"]) / s["h"]) < 1e-14
+
+
+def test_knn_matches_brute_force_on_clumps(sph, oracle):
+    from galaxy_formation_gb300 import synthetic
+
+    d = synthetic.disk_halo(n_gas=20000, n_dm=0, n_clumps=20, clump_frac=2e-3)
+    p = d["pos"]
+    dist, nb = sph.knn(p, 48)
+    rd, rnb = oracle.knn_brute(p, 48)
+    assert np.array_equal(nb, rnb)
+    assert np.max(np.abs(dist - rd)) <= 1e-15 * np.abs(rd).max()
+
+
+@pytest.mark.parametrize("n,k", [(1, 1), (5, 5), (48, 48), (49, 48), (300, 32)])
+def test_knn_small(sph, oracle, n, k):
+    p = np.ascontiguousarray(np.random.default_rng(n).uniform(size=(n, 3)))
+    d, nb = sph.knn(p, k)
+    rd, rnb = oracle.knn_brute(p, k)
+    assert np.array_equal(nb, rnb)
+    assert np.allclose(d, rd, rtol=1e-15, atol=0)
+
+
+def test_verlet_reselection_matches_reference(sph, golden):
+    s = golden("sph2k.npz")
+    n = len(s["pos"])
+    nb = np.zeros((n, 32), np.int64)
+    d = np.zeros((n, 32))
+    assert sph.knn_from_candidates(s["pos1"], s["cand"].astype(np.int64), 32, nb, d)
+    assert np.array_equal(nb, s["nb1"])
+    assert np.max(np.abs(d - s["dist1"])) < 1e-14
+
+
+def test_verlet_missing_candidates(sph, oracle):
+    rng = np.random.default_rng(9)
+    p = np.ascontiguousarray(rng.uniform(size=(200, 3)))
+    cand = oracle.knn_brute(p, 48)[1]
+    cand[7, :20] = -1   # only 28 candidates left for particle 7
+    nb = np.full((200, 32), -5, np.int64)
+    d = np.zeros((200, 32))
+    assert not sph.knn_from_candidates(p, cand, 32, nb, d)
+    assert np.all(nb[7] == -5)          # row left untouched, as in the reference
+    rnb = np.zeros((200, 32), np.int64)
+    oracle.knn_from_candidates(p, cand, 32, rnb, np.zeros((200, 32)))
+    ok_rows = np.arange(200) != 7
+    assert np.array_equal(nb[ok_rows], rnb[ok_rows])
+
+
+def test_neighbour_finder_flow(sph, golden):
+    """NeighbourFinder.find on the reference's 2k-gas cloud: full search, then a Verlet
+    sub-step, both against the reference's outputs."""
+    s = golden("sph2k.npz")
+    n_gas = len(s["pos"])
+    g = np.arange(n_gas)
+    f = sph.NeighbourFinder(2 * n_gas)
+    d, nb = f.find(g, s["pos"], True)
+    assert np.array_equal(nb, s["nb"])
+    d1, nb1 = f.find(g, s["pos1"], False)
+    assert np.array_equal(nb1, s["nb1"])
+
+
+def test_sph_forces_match_oracle_disk(sph, oracle):
+    from galaxy_formation_gb300 import params, synthetic
+
+    d = synthetic.make_config(1, scale=0.05)
+    gas = d["kind"] == params.GAS
+    p, v, m, u = (np.ascontiguousarray(d[k][gas]) for k in ("pos", "vel", "mass", "u"))
+    dist, nb = sph.knn(p, 32)
+    h = np.maximum(0.5 * dist[:, -1], 0.5 * params.EPS)
+    n = len(p)
+    rho, acc, dudt, dt = np.empty(n), np.empty((n, 3)), np.empty(n), np.empty(n)
+    sph.sph_forces(p, v, m, nb, h, u, params.GAMMA, 1.0, 2.0, rho, acc, dudt, dt)
+    r_rho, r_acc, r_dudt, r_dt = oracle.sph_forces(p, v, m, nb, h, u, params.GAMMA, 1.0, 2.0)
+    assert np.max(np.abs(rho - r_rho) / r_rho) < TOL
+    assert np.max(np.abs(dt - r_dt) / r_dt) < TOL
+    an = np.linalg.norm(acc - r_acc, axis=1) / np.linalg.norm(r_acc, axis=1)
+    assert np.max(an) < TOL
+    assert np.max(np.abs(dudt - r_dudt)) <= TOL * np.abs(r_dudt).max()
