@@ -38,6 +38,8 @@ SIGNATURES = {
                        _dbl, _dbl, _dbl, _dbl], _ci),
     "gf_sph_forces_dev": ([_ci, _ci, _vp, _vp, _vp, _vp, _vp, _vp, _cd, _cd, _cd,
                            _vp, _vp, _vp, _vp, _vp], _ci),
+    "gf_sph_forces_noalloc_dev": ([_ci, _ci, _vp, _vp, _vp, _vp, _vp, _vp, _cd, _cd, _cd,
+                                   _vp, _vp, _vp, _vp, _vp], _ci),
     "gf_knn_from_candidates": ([_ci, _ci, _dbl, _i64, _ci, _i64, _dbl], _ci),
     "gf_knn": ([_ci, _dbl, _ci, _dbl, _i64], _ci),
     "gf_knn_iterations": ([], ctypes.c_longlong),

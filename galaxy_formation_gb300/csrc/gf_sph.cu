@@ -18,6 +18,9 @@
 //                              sorted again, so the result is the exact float64 kNN.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <mutex>
+#include <string>
 
 #include "gf_sph.cuh"
 #include "gf_tree.cuh"
@@ -510,3 +513,97 @@ void knn_exact(Octree& T, int n, const double* pos, int k, const float* r_guess,
 }
 
 }  // namespace gf
+
+// ---------------------------------------------------------------------------------------
+// sph_forces without any device allocation.
+//
+// Some callers cannot call cudaMalloc: hosts whose own memory pool owns the whole GPU (an
+// extra allocation fails or fragments their pool), and step loops that must not allocate
+// because cudaMalloc / cudaFree synchronise the device. gf_sph_forces_noalloc_dev serves
+// them: the caller passes inputs and outputs in device memory as for gf_sph_forces_dev, and
+// the per-particle scratch (P / rho^2 and the sound speed, 16 bytes per particle) lives in
+// the fixed array below instead of a growing allocation. The array holds
+// GF_SPH_NOALLOC_MAX_N particles (4 MiB); every GPU that loads the library keeps it until
+// the process exits.
+//
+// In host code `g_sph_noalloc_scratch` names a host-side stand-in, not device memory: the
+// device address is fetched with cudaGetSymbolAddress once per device (with that device
+// current) by the first call on that device, and passed to the kernels.
+
+namespace gf {
+namespace {
+
+constexpr int kNoallocMaxN = GF_SPH_NOALLOC_MAX_N;
+constexpr int kNoallocMaxDevices = 64;
+
+static __device__ __align__(256) double g_sph_noalloc_scratch[2 * size_t(kNoallocMaxN)];
+
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[kNoallocMaxDevices] = {};
+
+// Device address of g_sph_noalloc_scratch on the current device (set up on first use).
+cudaError_t noalloc_scratch(double** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kNoallocMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_sph_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_noalloc_ptr[dev] = static_cast<double*>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return cudaSuccess;
+}
+
+int noalloc_fail(int code, const std::string& msg) {
+    Context& c = ctx();
+    c.last_status = code;
+    c.last_error = msg;
+    return code;
+}
+
+}  // namespace
+
+}  // namespace gf
+
+extern "C" int gf_sph_forces_noalloc_dev(int n, int k, const double* pos, const double* vel,
+                                         const double* mass, const int64_t* nb, const double* h,
+                                         const double* u, double gamma, double alpha, double beta,
+                                         double* rho, double* acc, double* dudt, double* dt_i,
+                                         void* stream) {
+    using namespace gf;
+    Context& c = ctx();
+    c.last_status = 0;
+    c.last_error.clear();
+    if (n < 0 || k < 0) return noalloc_fail(GF_ERR_ARG, "gf_sph_forces_noalloc_dev: negative size");
+    if (n > kNoallocMaxN) {
+        char buf[160];
+        snprintf(buf, sizeof buf, "gf_sph_forces_noalloc_dev: n = %d exceeds the fixed scratch of %d particles",
+                 n, kNoallocMaxN);
+        return noalloc_fail(GF_ERR_CAPACITY, buf);
+    }
+    if (n == 0) return GF_OK;
+    if (!(pos && vel && mass && nb && h && u && rho && acc && dudt && dt_i))
+        return noalloc_fail(GF_ERR_ARG, "gf_sph_forces_noalloc_dev: null array");
+    double* scratch = nullptr;
+    cudaError_t e = noalloc_scratch(&scratch);
+    if (e != cudaSuccess)
+        return noalloc_fail(GF_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    // P / rho^2 and the sound speed are written for every particle before they are read,
+    // so nothing left by an earlier call needs clearing.
+    double* pr2 = scratch;
+    double* cs = scratch + kNoallocMaxN;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int grid = div_up(n, kThreads);
+    k_sph_density<int64_t><<<grid, kThreads, 0, s>>>(n, k, k, pos, mass, nb, h, rho);
+    k_sph_eos<<<grid, kThreads, 0, s>>>(n, rho, u, gamma, pr2, cs);
+    k_sph_force<int64_t><<<grid, kThreads, 0, s>>>(n, k, k, pos, vel, mass, nb, h, rho, pr2, cs, alpha,
+                                                   beta, acc, dudt, dt_i);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return noalloc_fail(GF_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
+    c.launches += 3;
+    return GF_OK;
+}

@@ -115,11 +115,30 @@ int gf_sph_forces(int n, int k, const double* pos, const double* vel, const doub
                   const int64_t* nb, const double* h, const double* u, double gamma,
                   double alpha, double beta, double* rho, double* acc, double* dudt,
                   double* dt_i);
+/* Particles accepted by gf_sph_forces_noalloc_dev (its fixed scratch: 16 bytes each). */
+#define GF_SPH_NOALLOC_MAX_N 262144
+
 /* sph_forces on device pointers. */
 int gf_sph_forces_dev(int n, int k, const double* pos, const double* vel, const double* mass,
                       const int64_t* nb, const double* h, const double* u, double gamma,
                       double alpha, double beta, double* rho, double* acc, double* dudt,
                       double* dt_i, void* stream);
+
+/* gf_sph_forces_dev without any device allocation (no reference counterpart: the reference
+ * runs on the CPU and never faces this). For callers that cannot call cudaMalloc — a host
+ * whose memory pool owns the GPU, or a step loop that must not allocate because
+ * cudaMalloc/cudaFree synchronise the device. Inputs and outputs are the caller's device
+ * buffers; the per-particle scratch is a fixed array inside the library, so n is limited to
+ * GF_SPH_NOALLOC_MAX_N (larger n returns GF_ERR_CAPACITY without launching anything). The
+ * first call on a device looks up that array's device address (cudaGetSymbolAddress); make
+ * that first call before any stream capture. All calls share the one array: calls that
+ * overlap on the GPU (different streams, or different host threads) race and must be
+ * serialised by the caller. stream: cudaStream_t as void*, NULL = the legacy default
+ * stream. Returns GF_OK or GF_ERR_* bits; enqueues work without synchronising. */
+int gf_sph_forces_noalloc_dev(int n, int k, const double* pos, const double* vel,
+                              const double* mass, const int64_t* nb, const double* h,
+                              const double* u, double gamma, double alpha, double beta,
+                              double* rho, double* acc, double* dudt, double* dt_i, void* stream);
 
 /* Replaces knn_from_candidates (sph.py:109-135): the k nearest of each particle among its
  * m candidates (cand (n,m) local indices, -1 = none), ascending, into nb (n,k) and dist
