@@ -42,8 +42,8 @@ PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--scale", type=float, default=1.0, help="shrink the workload (testing only)")
     ap.add_argument("--no-e2e", action="store_true")
@@ -356,6 +356,9 @@ def run_gpu(args, world, rank, local):
         "accuracy": {"grav_p99_rel_err_vs_f64_direct": float(np.percentile(err, 99)),
                      "grav_median": float(np.median(err)), "targets": 2000},
         "knn_iterations_per_gas": info[3].value / max(1, info[0].value),
+        "walk": {"pair_interactions": pairs,
+                 "tflops": 20.0 * pairs / (stages["walk"]["ms_per_launch"] * 1e-3) / 1e12
+                 if "walk" in stages else None, "fp32_peak_tflops": fp32.value},
     }
     print(json.dumps(line), flush=True)
 

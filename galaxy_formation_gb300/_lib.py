@@ -36,6 +36,8 @@ SIGNATURES = {
     "gf_sph_kernel": ([_ci, _dbl, _dbl, _vp, _vp], _ci),
     "gf_sph_forces": ([_ci, _ci, _dbl, _dbl, _dbl, _i64, _dbl, _dbl, _cd, _cd, _cd,
                        _dbl, _dbl, _dbl, _dbl], _ci),
+    "gf_sph_forces_mixed": ([_ci, _ci, _dbl, _dbl, _dbl, _i64, _dbl, _dbl, _cd, _cd, _cd,
+                             _dbl, _dbl, _dbl, _dbl], _ci),
     "gf_sph_forces_dev": ([_ci, _ci, _vp, _vp, _vp, _vp, _vp, _vp, _cd, _cd, _cd,
                            _vp, _vp, _vp, _vp, _vp], _ci),
     "gf_sph_forces_noalloc_dev": ([_ci, _ci, _vp, _vp, _vp, _vp, _vp, _vp, _cd, _cd, _cd,
@@ -49,12 +51,33 @@ SIGNATURES = {
                           _dbl, _cd, _cd, _cd, _cd, _cd, _vp, _ci, _ci, _ci, _dbl, _dbl], _ci),
     "gf_force_info": ([ctypes.POINTER(_ci), ctypes.POINTER(_cd), ctypes.POINTER(_cd),
                        ctypes.POINTER(ctypes.c_longlong)], _ci),
+    "gf_sim_init": ([_ci, _dbl, _dbl, _dbl, np.ctypeslib.ndpointer(np.int8, flags="C_CONTIGUOUS"), _dbl,
+                     _cd, _cd, _cd, _cd, _cd], _ci),
+    "gf_sim_step": ([_cd, ctypes.POINTER(_cd), ctypes.POINTER(_ci)], _ci),
+    "gf_sim_read": ([_vp, _vp, _vp, _vp, ctypes.POINTER(_cd)], _ci),
+    "gf_set_option": ([_ci, _cd], _ci),
+    "gf_get_option": ([_ci], _cd),
+    "gf_force_stats": ([_dbl, _ci], _ci),
+    "gf_mlp_init": ([_ci], _ci),
+    "gf_mlp_set_params": ([_f32], _ci),
+    "gf_mlp_get_params": ([_f32], _ci),
+    "gf_mlp_set_norm": ([_f32, _f32, _cd, _cd], _ci),
+    "gf_mlp_predict": ([_ci, _f32, _f32], _ci),
+    "gf_mlp_gradient": ([_ci, _f32, _f32, _f32], _ci),
+    "gf_mlp_collected": ([_vp, _vp, ctypes.c_longlong], ctypes.c_longlong),
+    "gf_mlp_train": ([_ci, _ci, _cd, ctypes.POINTER(_cd)], _ci),
     "gf_profile": ([_ci], _ci),
     "gf_profile_stage": ([_ci, ctypes.POINTER(_cd), ctypes.POINTER(_ci)], _ci),
     "gf_launch_count": ([], ctypes.c_longlong),
     "gf_walk_pairs": ([], ctypes.c_longlong),
     "gf_fp32_peak": ([ctypes.POINTER(_cd)], _ci),
 }
+
+OPT_SPH_FLOAT32 = 0
+OPT_GRAVITY_QUAD = 1
+OPT_HGUESS = 2
+OPT_COLLECT = 3
+MLP_PARAMS = 4545
 
 STAGES = ["tree_build", "tree_refit", "walk", "group_prep", "knn", "knn_tree", "sph_density",
           "sph_force", "verlet", "force"]

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "gf_hydro.cuh"
+#include "gf_mlp.cuh"
 
 namespace gf {
 namespace {
@@ -15,9 +16,11 @@ namespace {
 struct Staging {
     DevBuf pos, mass, acc, active, vel, h, u, nb, rho, dudt, dt, dist, cand, r, w, dw;
     DevBuf img, glow, colors, rot, center, group, out, targets, flags, kind, dt_ind;
+    DevBuf mlpX, mlpY, mlpT, mlpG;
 };
 Staging g_st;
 SphScratch g_sph;
+Sph32Scratch g_sph32;
 Octree g_knn_tree;
 unsigned long long g_knn_iters = 0;
 
@@ -298,6 +301,35 @@ int gf_sph_forces(int n, int k, const double* pos, const double* vel, const doub
     });
 }
 
+int gf_sph_forces_mixed(int n, int k, const double* pos, const double* vel, const double* mass,
+                        const int64_t* nb, const double* h, const double* u, double gamma, double alpha,
+                        double beta, double* rho, double* acc, double* dudt, double* dt_i) {
+    return guarded([&] {
+        require(n >= 0 && k >= 0, "negative size");
+        if (n == 0) return;
+        require(pos && vel && mass && nb && h && u && rho && acc && dudt && dt_i, "null array");
+        for (size_t t = 0; t < size_t(n) * k; ++t) require(nb[t] >= 0 && nb[t] < n, "neighbour out of range");
+        cudaStream_t s = ctx().stream;
+        const double* d_pos = upload(g_st.pos, pos, 3 * size_t(n), s);
+        const double* d_vel = upload(g_st.vel, vel, 3 * size_t(n), s);
+        const double* d_mass = upload(g_st.mass, mass, size_t(n), s);
+        const int64_t* d_nb = upload(g_st.nb, nb, size_t(n) * k, s);
+        const double* d_h = upload(g_st.h, h, size_t(n), s);
+        const double* d_u = upload(g_st.u, u, size_t(n), s);
+        double* d_rho = g_st.rho.get<double>(n);
+        double* d_acc = g_st.acc.get<double>(3 * size_t(n));
+        double* d_dudt = g_st.dudt.get<double>(n);
+        double* d_dt = g_st.dt.get<double>(n);
+        sph_forces32<int64_t>(g_sph32, n, k, k, nullptr, d_pos, d_vel, d_mass, d_nb, d_h, d_u, gamma, alpha, beta,
+                              d_rho, d_acc, d_dudt, d_dt, s);
+        download(rho, d_rho, size_t(n), s);
+        download(acc, d_acc, 3 * size_t(n), s);
+        download(dudt, d_dudt, size_t(n), s);
+        download(dt_i, d_dt, size_t(n), s);
+        collect_status(s);
+    });
+}
+
 int gf_sph_forces_dev(int n, int k, const double* pos, const double* vel, const double* mass,
                       const int64_t* nb, const double* h, const double* u, double gamma, double alpha,
                       double beta, double* rho, double* acc, double* dudt, double* dt_i, void* stream) {
@@ -437,12 +469,173 @@ int gf_fp32_peak(double* tflops) {
 long long gf_walk_pairs(void) {
     unsigned long long p = 0;
     guarded([&] {
-        Octree& T = gravity_tree();
-        if (!T.valid) return;
+        Octree* T = last_walked();
+        if (!T || !T->valid) return;
         GF_CUDA(cudaDeviceSynchronize());
-        GF_CUDA(cudaMemcpy(&p, &T.counts.as<TreeCounts>()->pairs, sizeof p, cudaMemcpyDeviceToHost));
+        GF_CUDA(cudaMemcpy(&p, &T->counts.as<TreeCounts>()->pairs, sizeof p, cudaMemcpyDeviceToHost));
     });
     return (long long)p;
+}
+
+int gf_set_option(int key, double value) {
+    return guarded([&] {
+        ForceEngine& F = force_engine();
+        switch (key) {
+            case GF_OPT_SPH_FLOAT32: F.sph_float32 = value != 0; break;
+            case GF_OPT_GRAVITY_QUAD: F.gravity_quad = value != 0; break;
+            case GF_OPT_HGUESS:
+                require(value == 0 || value == 1 || value == 2, "h guess mode is 0, 1 or 2");
+                F.hguess = int(value);
+                break;
+            case GF_OPT_COLLECT: {
+                require(value >= 0 && value <= 2e8, "collect capacity out of range");
+                F.collect_cap = (long long)value;
+                F.collect_n = 0;
+                if (F.collect_cap > 0) {
+                    F.colX.get<float>(4 * size_t(F.collect_cap));
+                    F.colT.get<float>(size_t(F.collect_cap));
+                }
+                break;
+            }
+            default: throw Error(GF_ERR_ARG, "unknown option");
+        }
+    });
+}
+
+double gf_get_option(int key) {
+    ForceEngine& F = force_engine();
+    switch (key) {
+        case GF_OPT_SPH_FLOAT32: return F.sph_float32;
+        case GF_OPT_GRAVITY_QUAD: return F.gravity_quad;
+        case GF_OPT_HGUESS: return F.hguess;
+        case GF_OPT_COLLECT: return double(F.collect_n);
+        default: return -1.0;
+    }
+}
+
+int gf_sim_init(int n, const double* pos, const double* vel, const double* mass, const int8_t* kind,
+                const double* u, double theta, double eps, double gamma, double alpha, double beta) {
+    return guarded([&] {
+        require(n > 0 && n < (1 << 27), "bad n");
+        require(pos && vel && mass && kind && u, "null array");
+        sim_init(n, pos, vel, mass, kind, u, theta, eps, gamma, alpha, beta);
+        collect_status(ctx().stream);
+    });
+}
+
+int gf_sim_step(double dt_max, double* taken, int* substeps) {
+    return guarded([&] {
+        require(dt_max > 0, "dt_max <= 0");
+        const double D = sim_step(dt_max, substeps);
+        if (taken) *taken = D;
+        collect_status(ctx().stream);
+    });
+}
+
+int gf_sim_read(double* pos, double* vel, double* acc, double* dt_ind, double* t) {
+    return guarded([&] { sim_read(pos, vel, acc, dt_ind, t); });
+}
+
+int gf_mlp_init(int seed) {
+    return guarded([&] { mlp().init(unsigned(seed), ctx().stream); });
+}
+
+int gf_mlp_set_params(const float* p) {
+    return guarded([&] {
+        require(p != nullptr, "null params");
+        mlp().set_params(p, ctx().stream);
+        GF_CUDA(cudaStreamSynchronize(ctx().stream));
+    });
+}
+
+int gf_mlp_get_params(float* p) {
+    return guarded([&] {
+        require(p != nullptr && mlp().ready, "no model");
+        mlp().get_params(p, ctx().stream);
+    });
+}
+
+int gf_mlp_set_norm(const float* mean4, const float* std4, double t_mean, double t_std) {
+    return guarded([&] {
+        require(mean4 && std4 && t_std > 0, "bad normalisation");
+        MlpNorm& nm = mlp().norm;
+        for (int i = 0; i < 4; ++i) {
+            require(std4[i] > 0, "std <= 0");
+            nm.mean[i] = mean4[i];
+            nm.inv_std[i] = 1.f / std4[i];
+        }
+        nm.t_mean = float(t_mean);
+        nm.t_std = float(t_std);
+    });
+}
+
+int gf_mlp_predict(int n, const float* X, float* Y) {
+    return guarded([&] {
+        require(n >= 0 && (n == 0 || (X && Y)) && mlp().ready, "bad arguments or no model");
+        if (n == 0) return;
+        cudaStream_t s = ctx().stream;
+        const float* dX = upload(g_st.mlpX, X, 4 * size_t(n), s);
+        float* dY = g_st.mlpY.get<float>(n);
+        mlp().predict(n, dX, dY, s);
+        download(Y, dY, size_t(n), s);
+        collect_status(s);
+    });
+}
+
+int gf_mlp_gradient(int n, const float* X, const float* T, float* grad) {
+    return guarded([&] {
+        require(n > 0 && X && T && grad && mlp().ready, "bad arguments or no model");
+        cudaStream_t s = ctx().stream;
+        const float* dX = upload(g_st.mlpX, X, 4 * size_t(n), s);
+        const float* dT = upload(g_st.mlpT, T, size_t(n), s);
+        float* dG = g_st.mlpG.get<float>(kMlpParams);
+        mlp().gradient(n, nullptr, dX, dT, dG, s);
+        download(grad, dG, size_t(kMlpParams), s);
+        collect_status(s);
+    });
+}
+
+long long gf_mlp_collected(float* X, float* T, long long max_rows) {
+    long long got = 0;
+    guarded([&] {
+        ForceEngine& F = force_engine();
+        got = std::min<long long>(F.collect_n, std::max<long long>(0, max_rows));
+        if (got > 0 && X) GF_CUDA(cudaMemcpy(X, F.colX.p, sizeof(float) * 4 * size_t(got), cudaMemcpyDeviceToHost));
+        if (got > 0 && T) GF_CUDA(cudaMemcpy(T, F.colT.p, sizeof(float) * size_t(got), cudaMemcpyDeviceToHost));
+        if (!X && !T) got = F.collect_n;
+    });
+    return got;
+}
+
+int gf_mlp_train(int steps, int batch, double lr, double* loss) {
+    return guarded([&] {
+        ForceEngine& F = force_engine();
+        Mlp& M = mlp();
+        require(M.ready && F.collect_n > 0, "no model or no collected data");
+        require(steps >= 0 && batch > 0 && lr > 0, "bad training arguments");
+        M.X.p = nullptr;  // the training set is the collected one (not owned)
+        M.n_data = int(F.collect_n);
+        cudaStream_t s = ctx().stream;
+        const double l = train_on(M, F.colX.as<float>(), F.colT.as<float>(), steps, batch, lr, s);
+        if (loss) *loss = l;
+        collect_status(s);
+    });
+}
+
+int gf_force_stats(double* out, int nout) {
+    return guarded([&] {
+        require(out && nout >= 0, "bad output");
+        ForceEngine& F = force_engine();
+        GF_CUDA(cudaDeviceSynchronize());
+        const HydroScalars* h = F.scalars_h;
+        TreeCounts kc{};
+        if (F.knn_tree.valid)
+            GF_CUDA(cudaMemcpy(&kc, F.knn_tree.counts.p, sizeof kc, cudaMemcpyDeviceToHost));
+        const double v[8] = {h ? double(F.ng) : 0.0, h ? h->dt_grav : 0.0, h ? h->dt_gas : 0.0,
+                             h ? double(h->knn_iters) : 0.0, double(kc.pad[1]), double(F.full_searches),
+                             double(F.verlet_hits), double(F.knn_tree.nn)};
+        for (int i = 0; i < nout && i < 8; ++i) out[i] = v[i];
+    });
 }
 
 int gf_force_info(int* n_gas, double* dt_grav, double* dt_gas, long long* knn_iters) {

@@ -98,6 +98,17 @@ __device__ __forceinline__ int warp_sum(int v) {
     return v;
 }
 
+// Kahan-compensated float32 sum.
+struct KahanF {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float v) {
+        const float y = v - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+};
+
 __device__ __forceinline__ void raise_status(uint32_t* st, uint32_t bit) {
     if (st) atomicOr(st, bit);
 }

@@ -19,6 +19,7 @@
 #include <cfloat>
 
 #include "gf_hydro.cuh"
+#include "gf_mlp.cuh"
 
 namespace gf {
 
@@ -123,13 +124,14 @@ __global__ void __launch_bounds__(kSelWarps * 32) k_verlet_select(
     }
 }
 
+// one thread per cache entry (coalesced rows of 48 global indices)
 __global__ void k_cache_store(int ng, int kq, const int* __restrict__ gidx, const int* __restrict__ nb,
                               int* __restrict__ row, int* __restrict__ cache) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ng) return;
-    row[gidx[i]] = i;
-    for (int jj = 0; jj < kCand; ++jj)
-        cache[size_t(i) * kCand + jj] = jj < kq ? gidx[nb[size_t(i) * kCand + jj]] : -1;
+    const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= size_t(ng) * kCand) return;
+    const int i = int(t / kCand), jj = int(t % kCand);
+    if (jj == 0) row[gidx[i]] = i;
+    cache[t] = jj < kq ? gidx[nb[t]] : -1;
 }
 
 __global__ void k_guess(int ng, const int* __restrict__ gidx, const double* __restrict__ hprev, float* __restrict__ rg) {
@@ -146,6 +148,21 @@ __global__ void k_smoothing(int ng, const double* __restrict__ d31, double eps, 
     const double v = fmax(0.5 * d31[i], 0.5 * eps);  // simulation.py:84
     h[i] = v;
     hprev[gidx[i]] = 0.5 * d31[i] > 0 ? 0.5 * d31[i] : v;
+}
+
+// appends (features, log of the unfloored h = d_32 / 2) rows to the training set
+__global__ void k_collect(int ng, long long base, const float* __restrict__ X, const double* __restrict__ d31,
+                          float* __restrict__ colX, float* __restrict__ colT) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ng) return;
+    const size_t r = size_t(base) + i;
+    for (int c = 0; c < 4; ++c) colX[4 * r + c] = X[4 * size_t(i) + c];
+    colT[r] = float(log(0.5 * d31[i]));
+}
+
+__global__ void k_scatter_f(int ng, const int* __restrict__ gidx, const float* __restrict__ v, float* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ng) out[gidx[i]] = v[i];
 }
 
 __global__ void k_fill(int n, double* __restrict__ a, double v) {
@@ -214,6 +231,8 @@ void ForceEngine::evaluate(const ForceArgs& a, cudaStream_t s) {
         GF_CUDA(cudaMemsetAsync(h_prev.get<double>(n), 0, sizeof(double) * size_t(n), s));
         cache_valid = false;
         have_hprev = false;
+        have_divv = false;
+        GF_CUDA(cudaMemsetAsync(divv_prev.get<float>(n), 0, sizeof(float) * size_t(n), s));
         row.get<int>(n);
         loc.get<int>(n);
     }
@@ -221,9 +240,11 @@ void ForceEngine::evaluate(const ForceArgs& a, cudaStream_t s) {
     HydroScalars* sc = scalars.get<HydroScalars>(1);
 
     // gravity (simulation.py:64)
-    Octree& T = gravity_tree();
-    if (a.rebuild || !T.valid || T.n != n)
+    Octree& T = grav;
+    if (a.rebuild || !T.valid || T.n != n || T.quad != (gravity_quad != 0)) {
+        T.quad = gravity_quad != 0;
         T.build(n, a.pos, a.mass, a.theta, s);
+    }
     else
         T.refit(a.pos, a.mass, s);
     T.prepare_walk(a.active, s);
@@ -299,19 +320,34 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
     if (!have_nb) {  // full search, 48 candidates (sph.py:165-169)
         const int kq = std::min(kCand, ng);
         float* rg = nullptr;
-        if (have_hprev) {
+        if (have_hprev && hguess == 0) {  // previous h
             rg = rguess.get<float>(ng);
             k_guess<<<ggrid, kThreads, 0, s>>>(ng, gi, h_prev.as<double>(), rg);
             GF_CHECK_LAUNCH();
         }
-        knn_exact(knn_tree, ng, gp, kq, rg, nullptr, nullptr, &sc->knn_iters, s, nb, kCand, d31, kNgb - 1);
+        const bool collect = collect_cap > collect_n && have_hprev;
+        HGuess hg{gi, have_hprev ? h_prev.as<double>() : nullptr, have_divv ? divv_prev.as<float>() : nullptr,
+                  hX.get<float>(4 * size_t(ng)), hY.get<float>(ng), hrg.get<float>(ng),
+                  hguess == 2 && have_hprev && mlp().ready};
+        const bool features = collect || hg.use_mlp;
+        GF_CUDA(cudaMemsetAsync(&sc->knn_iters, 0, sizeof(unsigned long long), s));
+        knn_exact(knn_tree, ng, gp, kq, rg, nullptr, nullptr, &sc->knn_iters, s, nb, kCand, d31, kNgb - 1,
+                  features ? &hg : nullptr);
+        if (collect) {
+            const long long take = std::min<long long>(ng, collect_cap - collect_n);
+            k_collect<<<div_up(take, kThreads), kThreads, 0, s>>>(int(take), collect_n, hg.X, d31,
+                                                                  colX.as<float>(), colT.as<float>());
+            GF_CHECK_LAUNCH();
+            collect_n += take;
+        }
         int* ca = cache.get<int>(size_t(ng) * kCand);
         int* rw = row.as<int>();
         GF_CUDA(cudaMemsetAsync(rw, 0xff, sizeof(int) * size_t(n), s));
-        k_cache_store<<<ggrid, kThreads, 0, s>>>(ng, kq, gi, nb, rw, ca);
+        k_cache_store<<<div_up(size_t(ng) * kCand, kThreads), kThreads, 0, s>>>(ng, kq, gi, nb, rw, ca);
         GF_CHECK_LAUNCH();
         cache_valid = true;
         full_searches += 1;
+        order_ng = ng;
     }
     double* hh = h.get<double>(ng);
     k_smoothing<<<ggrid, kThreads, 0, s>>>(ng, d31, a.eps, gi, hh, h_prev.as<double>());
@@ -322,7 +358,19 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
     double* ga = gacc.get<double>(3 * size_t(ng));
     double* du = dudt.get<double>(ng);
     double* dti = dt_i.get<double>(ng);
-    sph_forces<int>(sph, ng, kNgb, kCand, gp, gv, gm, nb, hh, gu, a.gamma, a.alpha, a.beta, r, ga, du, dti, s);
+    float* dv = gdivv.get<float>(ng);
+    if (sph_float32) {
+        // visit the gas in the Morton order of the last neighbour-search tree (same gas set)
+        const int* order = order_ng == ng ? knn_tree.perm.as<int>() : nullptr;
+        sph_forces32<int>(sph32, ng, kNgb, kCand, order, gp, gv, gm, nb, hh, gu, a.gamma, a.alpha, a.beta, r, ga,
+                          du, dti, s, dv);
+    } else {
+        sph_forces<int>(sph, ng, kNgb, kCand, gp, gv, gm, nb, hh, gu, a.gamma, a.alpha, a.beta, r, ga, du, dti, s,
+                        dv);
+    }
+    k_scatter_f<<<ggrid, kThreads, 0, s>>>(ng, gi, dv, divv_prev.as<float>());
+    GF_CHECK_LAUNCH();
+    have_divv = true;
     k_scatter_sph<<<ggrid, kThreads, 0, s>>>(ng, gi, ga, dti, as, dtc, &sc->dtmin_bits);
     GF_CHECK_LAUNCH();
 }

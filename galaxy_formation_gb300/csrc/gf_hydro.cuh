@@ -29,15 +29,26 @@ struct ForceArgs {
 };
 
 struct ForceEngine {
+    // options (gf_set_option)
+    int sph_float32 = 0;     // 1: mixed-precision SPH (float32 + Kahan), 0: float64
+    int gravity_quad = 0;    // 1: quadrupole moments + Kahan tile sums, 0: the reference's monopole
+    int hguess = 0;          // start of the neighbour-count iteration: 0 previous h, 1 cell
+                             // density only, 2 the learned guess (MLP)
+    long long collect_cap = 0, collect_n = 0;  // (features, log h) training pairs kept
+    bool have_divv = false;
     int n_total = -1;
+    int order_ng = -1;       // gas count of the last full neighbour search
     int ng = 0, ng_valid = 0;
     bool cache_valid = false, have_hprev = false;
     long long full_searches = 0, verlet_hits = 0;
+    Octree grav;             // gravity tree of the fused path
     Octree knn_tree;
     SphScratch sph;
+    Sph32Scratch sph32;
     DevBuf acc_grav, acc_sph, dt_courant, h_prev, row, loc, cache;
     DevBuf flag, scan, gidx, gpos, gvel, gmass, gu_, nb48, dsel, rguess, h, rho, gacc, dudt, dt_i;
     DevBuf scalars;
+    DevBuf divv_prev, gdivv, hX, hY, hrg, colX, colT;
     HydroScalars* scalars_h = nullptr;  // pinned copy, valid after the stream synchronises
 
     void evaluate(const ForceArgs& a, cudaStream_t s);
@@ -45,5 +56,11 @@ struct ForceEngine {
 };
 
 ForceEngine& force_engine();
+
+// Device-resident step loop (gf_sim.cu).
+void sim_init(int n, const double* pos, const double* vel, const double* mass, const int8_t* kind, const double* u,
+              double theta, double eps, double gamma, double alpha, double beta);
+double sim_step(double dt_max, int* substeps);
+void sim_read(double* pos, double* vel, double* acc, double* dt_ind, double* t);
 
 }  // namespace gf

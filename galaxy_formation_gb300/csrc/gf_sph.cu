@@ -22,6 +22,7 @@
 #include <mutex>
 #include <string>
 
+#include "gf_mlp.cuh"
 #include "gf_sph.cuh"
 #include "gf_tree.cuh"
 
@@ -96,6 +97,22 @@ __global__ void k_sph_eos(int n, const double* __restrict__ rho, const double* _
     cs[i] = sqrt(gamma * (gamma - 1) * u[i]);
 }
 
+// (1/r) dW/dr of sph.py:43-54 with the per-particle factors 1/h and 1/(pi h^4) precomputed
+// and 1/r shared by both smoothing lengths of a pair (one float64 division per pair).
+__device__ __forceinline__ double dw_m4_pre(double r, double inv_r, double inv_h, double s4) {
+    const double q = r * inv_h;
+    double g;
+    if (q < 1.0) {
+        g = s4 * (-3 * q + 2.25 * q * q);
+    } else if (q < 2.0) {
+        const double t = 2 - q;
+        g = -s4 * 0.75 * t * t;
+    } else {
+        return 0.0;
+    }
+    return g * inv_r;
+}
+
 // pass 2 (sph.py:72-106)
 template <class Idx>
 __global__ void k_sph_force(int n, int k, int ld, const double* __restrict__ pos, const double* __restrict__ vel,
@@ -103,21 +120,24 @@ __global__ void k_sph_force(int n, int k, int ld, const double* __restrict__ pos
                             const double* __restrict__ h, const double* __restrict__ rho,
                             const double* __restrict__ pr2, const double* __restrict__ cs, double alpha,
                             double beta, double* __restrict__ acc, double* __restrict__ dudt,
-                            double* __restrict__ dt_i) {
+                            double* __restrict__ dt_i, float* __restrict__ divv) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double xi = pos[3 * size_t(i)], yi = pos[3 * size_t(i) + 1], zi = pos[3 * size_t(i) + 2];
     const double vxi = vel[3 * size_t(i)], vyi = vel[3 * size_t(i) + 1], vzi = vel[3 * size_t(i) + 2];
     const double hi = h[i], rhoi = rho[i], pri = pr2[i], ci = cs[i];
-    double ax = 0, ay = 0, az = 0, du = 0, mu_max = 0;
+    const double inv_hi = 1.0 / hi, s4i = 1.0 / (kPi * hi * hi * hi * hi);
+    double ax = 0, ay = 0, az = 0, du = 0, mu_max = 0, dv = 0;
     for (int jj = 0; jj < k; ++jj) {
         const int64_t j = nb[size_t(i) * ld + jj];
         if (j == i) continue;
         const double dx = xi - pos[3 * j], dy = yi - pos[3 * j + 1], dz = zi - pos[3 * j + 2];
         const double r = sqrt(dx * dx + dy * dy + dz * dz);
         const double hj = h[j];
-        const double gi = dw_m4(r, hi);
-        const double gj = dw_m4(r, hj);
+        const double inv_r = 1.0 / fmax(r, 1e-30);
+        const double gi = dw_m4_pre(r, inv_r, inv_hi, s4i);
+        const double inv_hj = 1.0 / hj, ih2 = inv_hj * inv_hj;
+        const double gj = dw_m4_pre(r, inv_r, inv_hj, ih2 * ih2 * (1.0 / kPi));
         const double vr = (vxi - vel[3 * j]) * dx + (vyi - vel[3 * j + 1]) * dy + (vzi - vel[3 * j + 2]) * dz;
         double visc = 0.0;
         if (vr < 0) {
@@ -133,12 +153,14 @@ __global__ void k_sph_force(int n, int k, int ld, const double* __restrict__ pos
         ay -= mj * f * dy;
         az -= mj * f * dz;
         du += mj * (pri * gi + 0.5 * visc * gb) * vr;
+        dv += mj * vr * gi;
     }
     acc[3 * size_t(i)] = ax;
     acc[3 * size_t(i) + 1] = ay;
     acc[3 * size_t(i) + 2] = az;
     dudt[i] = du;
     dt_i[i] = 0.3 * hi / (ci + 1.2 * (alpha * ci + beta * mu_max) + 1e-30);
+    if (divv) divv[i] = float(-dv / rhoi);  // SPH velocity divergence (a feature of the h guess)
 }
 
 // ------------------------------------------------------------------- warp bitonic sorts
@@ -246,16 +268,32 @@ struct KnnArgs {
     int dsel_col;
     uint32_t* status;
     unsigned long long* iters;
+    const int* wparent;     // breadth-first parent of each node (-1 for the root)
+    int exact_order;        // 1: float64 re-sort of the k nearest; 0: float32 order, float64
+                            //    only to settle the neighbour at dsel_col (the h boundary)
 };
 
 // Collects the points within sqrt(R2) of the query into S (first kKnnCap of them);
 // returns their number, or -1 on stack overflow.
-__device__ int knn_collect(const KnnArgs& A, KnnSmem& S, float4 xh, float4 xl, float R2) {
+__device__ int knn_collect(const KnnArgs& A, KnnSmem& S, float4 xh, float4 xl, float R2, int leaf, float R) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = lanemask_lt();
+    // start at the smallest ancestor of the query's leaf whose cube contains the sphere
+    // (every point within R then lies in that subtree)
+    int start = leaf;
+    for (int up = 0; start > 0 && up < 64; ++up) {
+        const float4 g = A.wgeo[start];
+        const float pad = 2e-6f * (fabsf(g.x) + fabsf(g.y) + fabsf(g.z) + g.w) + 1e-30f;
+        const float lim = g.w - R - pad;
+        if (fabsf((xh.x - g.x) + xl.x) <= lim && fabsf((xh.y - g.y) + xl.y) <= lim &&
+            fabsf((xh.z - g.z) + xl.z) <= lim)
+            break;
+        start = A.wparent[start];
+    }
+    if (start < 0) start = 0;
     int cnt = 0;
     int sp = 1;
-    if (lane == 0) S.stack[0] = (0 << 4) | 1;
+    if (lane == 0) S.stack[0] = (start << 4) | 1;
     __syncwarp();
     for (int rounds = 0; sp > 0; ++rounds) {
         if (rounds > A.nn) return -1;  // each node is popped at most once
@@ -341,6 +379,116 @@ __device__ int knn_collect(const KnnArgs& A, KnnSmem& S, float4 xh, float4 xl, f
     return cnt;
 }
 
+// Sorts the cnt (<= kKnnCap) collected points of query q (tree position) held in d2/idx,
+// re-measures the k nearest and the float32 near-ties in float64, sorts those and writes the
+// k nearest (ascending, ties by index) in the caller's order.
+__device__ void knn_finish(const KnnArgs& A, float* d2, int* idx, double* dd, int* di, int cnt, int q) {
+    const int lane = threadIdx.x & 31;
+    const int k = A.k;
+    const int oq = A.perm[q];
+    int P = 64;
+    while (P < cnt) P <<= 1;
+    for (int t = cnt + lane; t < P; t += 32) {
+        d2[t] = INFINITY;
+        idx[t] = 0x7fffffff;
+    }
+    __syncwarp();
+    warp_bitonic(d2, idx, P);
+    const int pi = oq;
+    if (!A.exact_order) {
+        // Float32 order: the k nearest as a set (only pairs tied to float32 rounding can
+        // swap). The neighbour at dsel_col fixes h: the entries within float32 rounding of
+        // it are re-measured in float64 and the dsel_col-th smallest is taken.
+        const int c = A.dsel_col;
+        const float lo = d2[c] * (1.0f - 2e-5f), hi = d2[c] * (1.0f + 2e-5f);
+        int below = 0;
+        for (int t = lane; t < cnt; t += 32) below += d2[t] < lo;
+        below = warp_sum(below);
+        const double xi = A.pos[3 * size_t(pi)], yi = A.pos[3 * size_t(pi) + 1], zi = A.pos[3 * size_t(pi) + 2];
+        double best = INFINITY;
+        int rank_need = c - below;  // rank of the wanted entry among the ambiguous ones
+        for (int t = lane; t < 64; t += 32) {
+            double v = INFINITY;
+            int tag = 0x7fffffff;
+            if (t < cnt && d2[t] >= lo && d2[t] <= hi) {
+                const int pj = A.perm[idx[t]];
+                const double dx = xi - A.pos[3 * size_t(pj)], dy = yi - A.pos[3 * size_t(pj) + 1],
+                             dz = zi - A.pos[3 * size_t(pj) + 2];
+                v = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+                tag = pj;
+            }
+            dd[t] = v;
+            di[t] = tag;
+        }
+        __syncwarp();
+        warp_bitonic(dd, di, 64);
+        best = dd[max(0, rank_need)];
+        for (int t = lane; t < k; t += 32) {
+            if (A.nb32) A.nb32[size_t(oq) * A.ld32 + t] = A.perm[idx[t]];
+            if (A.nb) A.nb[size_t(oq) * k + t] = A.perm[idx[t]];
+        }
+        if (A.dsel && lane == 0) A.dsel[oq] = __dsqrt_rn(best);
+        __syncwarp();
+        return;
+    }
+    // the k nearest and everything within float32 rounding of the k-th distance
+    const float thr = d2[k - 1] * (1.0f + 2e-5f);
+    int m = 0;
+    for (int t = lane; t < cnt; t += 32) m += d2[t] <= thr;
+    m = min(64, warp_sum(m));
+    const double xi = A.pos[3 * size_t(pi)], yi = A.pos[3 * size_t(pi) + 1], zi = A.pos[3 * size_t(pi) + 2];
+    for (int t = lane; t < 64; t += 32) {
+        double v = INFINITY;
+        int tag = 0x7fffffff;
+        if (t < m) {
+            const int pj = A.perm[idx[t]];
+            const double dx = xi - A.pos[3 * size_t(pj)], dy = yi - A.pos[3 * size_t(pj) + 1],
+                         dz = zi - A.pos[3 * size_t(pj) + 2];
+            v = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+            tag = pj;
+        }
+        dd[t] = v;
+        di[t] = tag;
+    }
+    __syncwarp();
+    warp_bitonic(dd, di, 64);
+    for (int t = lane; t < k; t += 32) {
+        if (A.nb) A.nb[size_t(oq) * k + t] = di[t];
+        if (A.dist) A.dist[size_t(oq) * k + t] = __dsqrt_rn(dd[t]);
+        if (A.nb32) A.nb32[size_t(oq) * A.ld32 + t] = di[t];
+        if (A.dsel && t == A.dsel_col) A.dsel[oq] = __dsqrt_rn(dd[t]);
+    }
+    __syncwarp();
+}
+
+__device__ void knn_fail_output(const KnnArgs& A, int q, bool stack) {
+    const int lane = threadIdx.x & 31;
+    const int oq = A.perm[q];
+    if (lane == 0) raise_status(A.status, stack ? GF_ERR_WALK_STACK : GF_ERR_KNN);
+    for (int t = lane; t < A.k; t += 32) {
+        if (A.nb) A.nb[size_t(oq) * A.k + t] = -1;
+        if (A.dist) A.dist[size_t(oq) * A.k + t] = INFINITY;
+        if (A.nb32) A.nb32[size_t(oq) * A.ld32 + t] = -1;
+    }
+    if (A.dsel && lane == 0) A.dsel[oq] = INFINITY;
+}
+
+// Radius step of the count-to-k iteration: Newton on count ~ R^3 until the count is
+// bracketed by [lo, hi], bisection afterwards.
+__device__ __forceinline__ float knn_next_radius(float R, int cnt, int k, int cap, float& lo, float& hi) {
+    float next;
+    if (cnt < k) {
+        lo = R;
+        next = R * (cnt >= 4 ? cbrtf(1.3f * float(k) / float(cnt)) : 2.0f);
+    } else {
+        hi = R;
+        next = R * cbrtf(0.75f * float(cap) / float(cnt));
+    }
+    if (lo > 0.f && hi < INFINITY) next = 0.5f * (lo + hi);
+    return next;
+}
+
+// One warp per query: walk from the smallest ancestor cell containing the search sphere.
 __global__ void __launch_bounds__(kKnnWarps * 32) k_knn(KnnArgs A) {
     __shared__ KnnSmem smem_all[kKnnWarps];
     KnnSmem& S = smem_all[threadIdx.x >> 5];
@@ -360,78 +508,26 @@ __global__ void __launch_bounds__(kKnnWarps * 32) k_knn(KnnArgs A) {
             R = 2.0f * half * cbrtf(float(k) / float(c));
         }
         if (!(R > 0.f) || !isfinite(R)) R = 1e-3f;
-        // Newton steps on count ~ R^3 until the count is bracketed, then bisection: the
-        // count lands in [k, kKnnCap] unless > kKnnCap - k points share one distance.
+        const int cap = kKnnCap;  // count window [k, cap]
         int cnt = 0, it = 0;
         bool ok = false;
         float lo = 0.f, hi = INFINITY;
+        const int leaf = A.leaf_of[q];
         for (; it < 48; ++it) {
-            cnt = knn_collect(A, S, xh, xl, R * R);
+            cnt = knn_collect(A, S, xh, xl, R * R, leaf, R);
             if (cnt < 0) break;
-            if (cnt >= k && cnt <= kKnnCap) {
+            if (cnt >= k && cnt <= cap) {
                 ok = true;
                 break;
             }
-            float next;
-            if (cnt < k) {
-                lo = R;
-                next = R * (cnt >= 4 ? cbrtf(1.3f * float(k) / float(cnt)) : 2.0f);
-            } else {
-                hi = R;
-                next = R * cbrtf(0.75f * float(kKnnCap) / float(cnt));
-            }
-            if (lo > 0.f && hi < INFINITY) next = 0.5f * (lo + hi);
-            R = next;
+            R = knn_next_radius(R, cnt, k, cap, lo, hi);
         }
         if (lane == 0 && A.iters) atomicAdd(A.iters, (unsigned long long)(it + 1));
         if (!ok) {
-            if (lane == 0) raise_status(A.status, cnt < 0 ? GF_ERR_WALK_STACK : GF_ERR_KNN);
-            for (int t = lane; t < k; t += 32) {
-                if (A.nb) A.nb[size_t(oq) * k + t] = -1;
-                if (A.dist) A.dist[size_t(oq) * k + t] = INFINITY;
-                if (A.nb32) A.nb32[size_t(oq) * A.ld32 + t] = -1;
-            }
-            if (A.dsel && lane == 0) A.dsel[oq] = INFINITY;
+            knn_fail_output(A, q, cnt < 0);
             continue;
         }
-        // float32 sort of the collected points
-        int P = 64;
-        while (P < cnt) P <<= 1;
-        for (int t = cnt + lane; t < P; t += 32) {
-            S.d2[t] = INFINITY;
-            S.idx[t] = 0x7fffffff;
-        }
-        __syncwarp();
-        warp_bitonic(S.d2, S.idx, P);
-        // the k nearest and everything within float32 rounding of the k-th distance
-        const float thr = S.d2[k - 1] * (1.0f + 2e-5f);
-        int m = 0;
-        for (int t = lane; t < cnt; t += 32) m += S.d2[t] <= thr;
-        m = min(64, warp_sum(m));
-        const int pi = A.perm[q];
-        const double xi = A.pos[3 * size_t(pi)], yi = A.pos[3 * size_t(pi) + 1], zi = A.pos[3 * size_t(pi) + 2];
-        for (int t = lane; t < 64; t += 32) {
-            double dd = INFINITY;
-            int tag = 0x7fffffff;
-            if (t < m) {
-                const int pj = A.perm[S.idx[t]];
-                const double dx = xi - A.pos[3 * size_t(pj)], dy = yi - A.pos[3 * size_t(pj) + 1],
-                             dz = zi - A.pos[3 * size_t(pj) + 2];
-                dd = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-                tag = pj;
-            }
-            S.dd[t] = dd;
-            S.di[t] = tag;
-        }
-        __syncwarp();
-        warp_bitonic(S.dd, S.di, 64);
-        for (int t = lane; t < k; t += 32) {
-            if (A.nb) A.nb[size_t(oq) * k + t] = S.di[t];
-            if (A.dist) A.dist[size_t(oq) * k + t] = __dsqrt_rn(S.dd[t]);
-            if (A.nb32) A.nb32[size_t(oq) * A.ld32 + t] = S.di[t];
-            if (A.dsel && t == A.dsel_col) A.dsel[oq] = __dsqrt_rn(S.dd[t]);
-        }
-        __syncwarp();
+        knn_finish(A, S.d2, S.idx, S.dd, S.di, cnt, q);
     }
 }
 
@@ -448,7 +544,7 @@ void sph_kernel_values(int n, const double* r, const double* h, double* w, doubl
 template <class Idx>
 void sph_forces(SphScratch& S, int n, int k, int ld, const double* pos, const double* vel, const double* mass,
                 const Idx* nb, const double* h, const double* u, double gamma, double alpha,
-                double beta, double* rho, double* acc, double* dudt, double* dt_i, cudaStream_t s) {
+                double beta, double* rho, double* acc, double* dudt, double* dt_i, cudaStream_t s, float* divv) {
     if (n <= 0) return;
     const int grid = div_up(n, kThreads);
     {
@@ -462,15 +558,15 @@ void sph_forces(SphScratch& S, int n, int k, int ld, const double* pos, const do
     GF_CHECK_LAUNCH();
     ProfScope ps(kStSphForce, s);
     k_sph_force<Idx><<<grid, kThreads, 0, s>>>(n, k, ld, pos, vel, mass, nb, h, rho, pr2, cs, alpha, beta,
-                                               acc, dudt, dt_i);
+                                               acc, dudt, dt_i, divv);
     GF_CHECK_LAUNCH();
 }
 template void sph_forces<int64_t>(SphScratch&, int, int, int, const double*, const double*, const double*,
                                   const int64_t*, const double*, const double*, double, double, double,
-                                  double*, double*, double*, double*, cudaStream_t);
+                                  double*, double*, double*, double*, cudaStream_t, float*);
 template void sph_forces<int>(SphScratch&, int, int, int, const double*, const double*, const double*,
                               const int*, const double*, const double*, double, double, double,
-                              double*, double*, double*, double*, cudaStream_t);
+                              double*, double*, double*, double*, cudaStream_t, float*);
 
 void knn_from_candidates(int n, int m, const double* pos, const int64_t* cand, int k, int64_t* nb,
                          double* dist, int* d_ok, cudaStream_t s) {
@@ -480,12 +576,48 @@ void knn_from_candidates(int n, int m, const double* pos, const int64_t* cand, i
     GF_CHECK_LAUNCH();
 }
 
+// Features of the smoothing-length guess, per gas particle (caller order):
+// (log cell density of its leaf, log previous h, leaf count, previous velocity divergence).
+__global__ void k_hfeatures(int n, const int* __restrict__ perm, const int* __restrict__ leaf_of,
+                            const float4* __restrict__ wb, const float4* __restrict__ wgeo, const int* __restrict__ gidx,
+                            const double* __restrict__ hprev, const float* __restrict__ divv, float* __restrict__ X) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const int i = perm[q];
+    const int lf = leaf_of[q];
+    const float c = float(max(1, -__float_as_int(wb[lf].z)));
+    const float side = 2.f * wgeo[lf].w;
+    const int g = gidx ? gidx[i] : i;
+    const double hp = hprev ? hprev[g] : 0.0;
+    X[4 * size_t(i) + 0] = logf(c / fmaxf(side * side * side, 1e-30f));
+    X[4 * size_t(i) + 1] = hp > 0 ? float(log(hp)) : 0.f;
+    X[4 * size_t(i) + 2] = c;
+    X[4 * size_t(i) + 3] = divv ? divv[g] : 0.f;
+}
+
+__global__ void k_guess_from_logh(int n, const float* __restrict__ Y, float* __restrict__ rg) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) rg[i] = 2.4f * expf(Y[i]);
+}
+
 void knn_exact(Octree& T, int n, const double* pos, int k, const float* r_guess, int64_t* nb,
                double* dist, unsigned long long* d_iters, cudaStream_t s, int* nb32, int ld32,
-               double* dsel, int dsel_col) {
+               double* dsel, int dsel_col, const HGuess* hg) {
     if (n <= 0) return;
     T.want_knn = true;
     T.build(n, pos, nullptr, 0.7, s);
+    if (hg && hg->X) {  // features for the learned guess (and for training pairs)
+        k_hfeatures<<<div_up(n, kThreads), kThreads, 0, s>>>(n, T.perm.as<int>(), T.leaf_of.as<int>(),
+                                                             T.w_b.as<float4>(), T.w_geo.as<float4>(), hg->gidx,
+                                                             hg->hprev, hg->divv, hg->X);
+        GF_CHECK_LAUNCH();
+        if (hg->use_mlp) {
+            mlp().predict(n, hg->X, hg->Y, s);
+            k_guess_from_logh<<<div_up(n, kThreads), kThreads, 0, s>>>(n, hg->Y, hg->rg);
+            GF_CHECK_LAUNCH();
+            r_guess = hg->rg;
+        }
+    }
     KnnArgs A{};
     A.n = n;
     A.k = k;
@@ -504,10 +636,12 @@ void knn_exact(Octree& T, int n, const double* pos, int k, const float* r_guess,
     A.ld32 = ld32;
     A.dsel = dsel;
     A.dsel_col = dsel_col;
+    A.exact_order = (nb != nullptr || dist != nullptr || dsel_col < 0) ? 1 : 0;
     A.status = ctx().d_status;
     A.iters = d_iters;
-    const int blocks = std::min(div_up(n, kKnnWarps), 16 * ctx().sms);
+    A.wparent = T.w_parent.as<int>();
     ProfScope ps(kStKnn, s);
+    const int blocks = std::min(div_up(n, kKnnWarps), 16 * ctx().sms);
     k_knn<<<blocks, kKnnWarps * 32, 0, s>>>(A);
     GF_CHECK_LAUNCH();
 }
@@ -601,7 +735,7 @@ extern "C" int gf_sph_forces_noalloc_dev(int n, int k, const double* pos, const 
     k_sph_density<int64_t><<<grid, kThreads, 0, s>>>(n, k, k, pos, mass, nb, h, rho);
     k_sph_eos<<<grid, kThreads, 0, s>>>(n, rho, u, gamma, pr2, cs);
     k_sph_force<int64_t><<<grid, kThreads, 0, s>>>(n, k, k, pos, vel, mass, nb, h, rho, pr2, cs, alpha,
-                                                   beta, acc, dudt, dt_i);
+                                                   beta, acc, dudt, dt_i, nullptr);
     e = cudaGetLastError();
     if (e != cudaSuccess) return noalloc_fail(GF_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
     c.launches += 3;

@@ -15,7 +15,32 @@ void sph_kernel_values(int n, const double* r, const double* h, double* w, doubl
 template <class Idx>
 void sph_forces(SphScratch& S, int n, int k, int ld, const double* pos, const double* vel, const double* mass,
                 const Idx* nb, const double* h, const double* u, double gamma, double alpha,
-                double beta, double* rho, double* acc, double* dudt, double* dt_i, cudaStream_t s);
+                double beta, double* rho, double* acc, double* dudt, double* dt_i, cudaStream_t s,
+                float* divv = nullptr);
+
+// Inputs of the learned smoothing-length guess inside a neighbour search: X (n x 4) receives
+// the features; with use_mlp the network's log h gives the starting radius 2.4 h.
+struct HGuess {
+    const int* gidx;      // caller index -> global particle index (null: identity)
+    const double* hprev;  // previous h per global index (null: none)
+    const float* divv;    // previous velocity divergence per global index (null: none)
+    float* X;             // n x 4 features (out)
+    float* Y;             // n predictions (scratch)
+    float* rg;            // n starting radii (scratch)
+    bool use_mlp;
+};
+
+struct Sph32Scratch {
+    DevBuf A, B, C, D;
+};
+
+// Mixed-precision sph_forces (float32 arithmetic, Kahan sums; float64 in and out). order
+// (optional): the visiting order of the particles.
+template <class Idx>
+void sph_forces32(Sph32Scratch& S, int n, int k, int ld, const int* order, const double* pos, const double* vel,
+                  const double* mass, const Idx* nb, const double* h, const double* u, double gamma, double alpha,
+                  double beta, double* rho, double* acc, double* dudt, double* dt_i, cudaStream_t s,
+                  float* divv = nullptr);
 
 void knn_from_candidates(int n, int m, const double* pos, const int64_t* cand, int k, int64_t* nb,
                          double* dist, int* d_ok, cudaStream_t s);
@@ -26,7 +51,7 @@ void knn_from_candidates(int n, int m, const double* pos, const int64_t* cand, i
 // neighbour `dsel_col` in dsel (n,).
 void knn_exact(Octree& T, int n, const double* pos, int k, const float* r_guess, int64_t* nb,
                double* dist, unsigned long long* d_iters, cudaStream_t s, int* nb32 = nullptr,
-               int ld32 = 0, double* dsel = nullptr, int dsel_col = -1);
+               int ld32 = 0, double* dsel = nullptr, int dsel_col = -1, const HGuess* hg = nullptr);
 
 void direct_sum(int n, const double* pos, const double* mass, int nt, const int64_t* targets,
                 double* acc, double eps, cudaStream_t s);

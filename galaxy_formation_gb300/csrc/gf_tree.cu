@@ -78,16 +78,25 @@ __global__ void k_bbox_partial(const double* __restrict__ pos, int n, double* __
 
 __global__ void k_bbox_final(const double* __restrict__ part, int nparts, RootBox* __restrict__ root,
                              uint32_t* status) {
-    if (threadIdx.x != 0) return;
+    // one warp reduces the block partials
     double lo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, hi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
     double bad = 0;
-    for (int b = 0; b < nparts; ++b) {
+    for (int b = threadIdx.x; b < nparts; b += 32) {
         for (int a = 0; a < 3; ++a) {
             lo[a] = fmin(lo[a], part[7 * b + a]);
             hi[a] = fmax(hi[a], part[7 * b + 3 + a]);
         }
         bad = fmax(bad, part[7 * b + 6]);
     }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = fmin(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+            hi[a] = fmax(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+        }
+        bad = fmax(bad, __shfl_xor_sync(0xffffffffu, bad, o));
+    }
+    if (threadIdx.x != 0) return;
     if (bad > 0) raise_status(status, GF_ERR_NONFINITE);
     RootBox R;
     double ext = 0;
@@ -472,16 +481,88 @@ __global__ void k_moments(MomentArgs A) {
     }
 }
 
+// Traceless quadrupole Q = sum m (3 d d - |d|^2 I) about each node's (float32) centre of
+// mass, bottom-up like k_moments: leaves from their particles, parents from their children
+// shifted by the parallel-axis term. Float32 with Kahan-compensated sums (mixed form).
+struct QuadArgs {
+    int nn;
+    const int4* n_i4;
+    const int* parent;
+    const int* nchild;
+    int* counter;
+    const float4* mom;
+    const float4* p4;
+    float4* q4;   // Qxx, Qyy, Qxy, Qxz
+    float2* qyz;  // Qyz, T = sum m |d|^2 (trace of the second moment, for the softened kernel)
+};
+
+struct QuadSum {
+    KahanF xx, yy, xy, xz, yz, tr;
+    __device__ __forceinline__ void point(float m, float dx, float dy, float dz) {
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        xx.add(m * (3.f * dx * dx - r2));
+        yy.add(m * (3.f * dy * dy - r2));
+        xy.add(3.f * m * dx * dy);
+        xz.add(3.f * m * dx * dz);
+        yz.add(3.f * m * dy * dz);
+        tr.add(m * r2);
+    }
+};
+
+__global__ void k_quad(QuadArgs A) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= A.nn) return;
+    const int4 q = A.n_i4[k];
+    if (!(q.w & 1)) return;
+    {
+        const float4 c = A.mom[k];
+        QuadSum S;
+        for (int i = q.x; i < q.x + q.y; ++i) {
+            const float4 p = A.p4[i];
+            S.point(p.w, p.x - c.x, p.y - c.y, p.z - c.z);
+        }
+        A.q4[k] = make_float4(S.xx.s, S.yy.s, S.xy.s, S.xz.s);
+        A.qyz[k] = make_float2(S.yz.s, S.tr.s);
+    }
+    __threadfence();
+    int p = A.parent[k];
+    while (p >= 0) {
+        const int arrived = atomicAdd(&A.counter[p], 1);
+        if (arrived != A.nchild[p] - 1) return;
+        __threadfence();
+        const float4 cp = A.mom[p];
+        QuadSum S;
+        const int end = A.n_i4[p].z;
+        int seen = 0;
+        for (int c = p + 1; c < end && seen < 8; c = A.n_i4[c].z, ++seen) {
+            const float4 cm = A.mom[c];
+            const float4 qc = __ldcg(&A.q4[c]);
+            S.xx.add(qc.x);
+            S.yy.add(qc.y);
+            S.xy.add(qc.z);
+            S.xz.add(qc.w);
+            const float2 yt = __ldcg(&A.qyz[c]);
+            S.yz.add(yt.x);
+            S.tr.add(yt.y);
+            S.point(cm.w, cm.x - cp.x, cm.y - cp.y, cm.z - cp.z);
+        }
+        A.q4[p] = make_float4(S.xx.s, S.yy.s, S.xy.s, S.xz.s);
+        A.qyz[p] = make_float2(S.yz.s, S.tr.s);
+        __threadfence();
+        p = A.parent[p];
+    }
+}
+
 // ---------------------------------------------------------------------------- groups + layout
 
-__global__ void k_group_flag(int nn, const int4* __restrict__ n_i4, const int* __restrict__ parent,
+__global__ void k_group_flag(int nn, int gmax, const int4* __restrict__ n_i4, const int* __restrict__ parent,
                              int* __restrict__ flag) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nn) return;
     const int4 q = n_i4[k];
-    const bool candidate = q.y <= kGroupMax || (q.w & 1);
+    const bool candidate = q.y <= gmax || (q.w & 1);
     const int p = parent[k];
-    flag[k] = candidate && (p < 0 || n_i4[p].y > kGroupMax) ? 1 : 0;
+    flag[k] = candidate && (p < 0 || n_i4[p].y > gmax) ? 1 : 0;
 }
 
 __global__ void k_group_write(int nn, const int* __restrict__ flag, const int* __restrict__ scan,
@@ -509,7 +590,10 @@ __global__ void k_walk_fill(int nn, const int4* __restrict__ n_i4, const int* __
                             const int* __restrict__ bfs, const float4* __restrict__ mom,
                             const float* __restrict__ open_r, const float4* __restrict__ geo,
                             float4* __restrict__ wa, float4* __restrict__ wb,
-                            float4* __restrict__ wgeo, int* __restrict__ leaf_of) {
+                            float4* __restrict__ wgeo, int* __restrict__ leaf_of,
+                            const float4* __restrict__ q4, const float2* __restrict__ qyz,
+                            float4* __restrict__ wq, const int* __restrict__ parent, int* __restrict__ wparent,
+                            float* __restrict__ wt) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nn) return;
     const int4 q = n_i4[k];
@@ -525,8 +609,13 @@ __global__ void k_walk_fill(int nn, const int4* __restrict__ n_i4, const int* __
         code = nchild[k];
     }
     wa[b] = mom[k];
-    wb[b] = make_float4(open_r[k], __int_as_float(first), __int_as_float(code), 0.f);
+    wb[b] = make_float4(open_r[k], __int_as_float(first), __int_as_float(code), q4 ? qyz[k].x : 0.f);
     if (wgeo) wgeo[b] = geo[k];
+    if (q4) {
+        wq[b] = q4[k];
+        wt[b] = qyz[k].y;
+    }
+    if (wparent) wparent[b] = parent[k] < 0 ? -1 : bfs[parent[k]];
 }
 
 // ---------------------------------------------------------------------------- deep cells
@@ -628,6 +717,8 @@ __global__ void k_deep_sort(int n, const uint64_t* __restrict__ k0, uint64_t* __
 
 static Octree g_tree;
 Octree& gravity_tree() { return g_tree; }
+static Octree* g_last_walked = nullptr;
+Octree*& last_walked() { return g_last_walked; }
 
 void Octree::build(int n_, const double* pos, const double* mass, double theta, cudaStream_t s) {
     Context& C = ctx();
@@ -734,9 +825,16 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
     k_moments<<<ngrid, kThreads, 0, s>>>(A);
     GF_CHECK_LAUNCH();
 
+    if (quad) {
+        QuadArgs Q{nn, i4, par, nch, ctr, A.mom, pp, n_quad.get<float4>(nn), n_qyz.get<float2>(nn)};
+        GF_CUDA(cudaMemsetAsync(ctr, 0, sizeof(int) * size_t(nn), s));
+        k_quad<<<ngrid, kThreads, 0, s>>>(Q);
+        GF_CHECK_LAUNCH();
+    }
+
     int* gf_ = gflag.get<int>(nn);
     int* gs = gscan.get<int>(nn);
-    k_group_flag<<<ngrid, kThreads, 0, s>>>(nn, i4, par, gf_);
+    k_group_flag<<<ngrid, kThreads, 0, s>>>(nn, group_max, i4, par, gf_);
     GF_CHECK_LAUNCH();
     exclusive_scan(gf_, gs, nn, &cnt->num_groups, s);
     k_group_write<<<ngrid, kThreads, 0, s>>>(nn, gf_, gs, groups.get<int>(nn));
@@ -752,7 +850,11 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
     GF_CHECK_LAUNCH();
     k_walk_fill<<<ngrid, kThreads, 0, s>>>(nn, i4, nch, bfs, A.mom, A.open_r, geo, w_a.get<float4>(nn),
                                            w_b.get<float4>(nn), want_knn ? w_geo.get<float4>(nn) : nullptr,
-                                           want_knn ? leaf_of.get<int>(n) : nullptr);
+                                           want_knn ? leaf_of.get<int>(n) : nullptr,
+                                           quad ? n_quad.as<float4>() : nullptr, quad ? n_qyz.as<float2>() : nullptr,
+                                           quad ? w_q.get<float4>(nn) : nullptr, par,
+                                           want_knn ? w_parent.get<int>(nn) : nullptr,
+                                           quad ? w_t.get<float>(nn) : nullptr);
     GF_CHECK_LAUNCH();
     valid = true;
 }
@@ -784,10 +886,20 @@ void Octree::refit(const double* pos, const double* mass, cudaStream_t s) {
     A.pdisp = pd;
     k_moments<<<ngrid, kThreads, 0, s>>>(A);
     GF_CHECK_LAUNCH();
+    if (quad) {
+        QuadArgs Q{nn, A.n_i4, A.parent, A.nchild, A.counter, A.mom, pp, n_quad.as<float4>(), n_qyz.as<float2>()};
+        GF_CUDA(cudaMemsetAsync(A.counter, 0, sizeof(int) * size_t(nn), s));
+        k_quad<<<ngrid, kThreads, 0, s>>>(Q);
+        GF_CHECK_LAUNCH();
+    }
     k_walk_fill<<<ngrid, kThreads, 0, s>>>(nn, A.n_i4, A.nchild, n_bfs.as<int>(), A.mom, A.open_r,
                                            A.n_geo, w_a.as<float4>(), w_b.as<float4>(),
                                            want_knn ? w_geo.as<float4>() : nullptr,
-                                           want_knn ? leaf_of.as<int>() : nullptr);
+                                           want_knn ? leaf_of.as<int>() : nullptr,
+                                           quad ? n_quad.as<float4>() : nullptr, quad ? n_qyz.as<float2>() : nullptr,
+                                           quad ? w_q.as<float4>() : nullptr, A.parent,
+                                           want_knn ? w_parent.as<int>() : nullptr,
+                                           quad ? w_t.as<float>() : nullptr);
     GF_CHECK_LAUNCH();
 }
 

@@ -57,11 +57,17 @@ struct Octree {
                       //   code > 0: internal, `code` children from BFS index `first`;
                       //   code < 0: leaf, -code particles from tree position `first`
     DevBuf w_geo;     // float4 {gx, gy, gz, half} of the cell, breadth-first order
+    DevBuf w_q;       // float4 {Qxx, Qyy, Qxy, Qxz} (quadrupole trees; Qyz in w_b.w)
+    DevBuf w_t;       // float T = sum m |d|^2 about the centre of mass (quadrupole trees)
+    DevBuf n_quad, n_qyz;  // traceless quadrupole about the centre of mass, preorder
     DevBuf bfs_key, bfs_key_alt, bfs_val, bfs_val_alt;
     // neighbour search extras (tree order): float32 remainders x - float(x) and the
     // breadth-first index of each particle's leaf
-    DevBuf plo, leaf_of;
+    DevBuf plo, leaf_of, w_parent;
     bool want_knn = false;
+    int group_max = kGroupMax;   // walk groups: shallowest nodes with <= group_max particles
+    bool quad = false;           // also build quadrupole moments (mixed-precision form)
+    bool kahan = false;          // walk: compensated accumulation of the tile sums
     // groups and walk work list
     DevBuf gflag, gscan, groups, work, sphere;
     DevBuf root, counts;
@@ -75,5 +81,7 @@ struct Octree {
 };
 
 Octree& gravity_tree();
+// The tree walked most recently (for the pair counter).
+Octree*& last_walked();
 
 }  // namespace gf

@@ -78,9 +78,17 @@ __global__ void k_group_prep(const int* __restrict__ groups, const int4* __restr
     }
 }
 
+// Shared memory of one warp. QUAD (mixed form) adds a tile of accepted nodes with their
+// quadrupoles; particles of opened leaves always go to the monopole tile.
+template <bool QUAD>
 struct WarpSmem {
-    int stack[kStackCap];
+    static constexpr int kStack = QUAD ? 768 : kStackCap;
+    static constexpr int kNodeTile = QUAD ? 96 : 1;
+    int stack[kStack];
     float4 tile[kTileCap];
+    float4 ntA[kNodeTile];   // centre of mass, mass
+    float4 ntQ[kNodeTile];   // Qxx, Qyy, Qxy, Qxz
+    float2 ntYZ[kNodeTile];  // Qyz, T
     int lanemap[32];
     int slot_pos[64];
 };
@@ -96,13 +104,78 @@ __device__ __forceinline__ void pair_acc(const float4 e, float x, float y, float
     az += f * ez;
 }
 
-__global__ void __launch_bounds__(kWalkWarps * 32) k_walk_mono(
-    const float4* __restrict__ wa, const float4* __restrict__ wb, const float4* __restrict__ p4,
-    const int* __restrict__ perm, const uint8_t* __restrict__ active, const int4* __restrict__ work,
-    const float4* __restrict__ sphere, TreeCounts* cnt, int nn, float eps2, double* __restrict__ acc,
-    uint32_t* status) {
-    __shared__ WarpSmem smem_all[kWalkWarps];
-    WarpSmem& S = smem_all[threadIdx.x >> 5];
+// Second-order expansion of the Plummer-softened field of a node about its centre of mass,
+// at d = com - x, r^2 = |d|^2 + eps^2, Q the traceless quadrupole and T = sum m |y|^2:
+//   a = M d / r^3 - Q d / r^5 + (5/2) (d.Q.d) d / r^7 - (5/2) T eps^2 d / r^7.
+// The last term comes from the trace of the second moment, which the softened potential
+// (unlike 1/r) does not annihilate; it matters for cells accepted within a few eps.
+__device__ __forceinline__ void quad_acc(const float4 e, const float4 q, float2 yt, float x, float y, float z,
+                                         float eps2, float& ax, float& ay, float& az) {
+    const float qyz = yt.x;
+    const float dx = e.x - x, dy = e.y - y, dz = e.z - z;
+    const float r2 = dx * dx + dy * dy + dz * dz + eps2;
+    const float inv = rsqrtf(r2);
+    const float inv2 = inv * inv;
+    const float inv3 = inv2 * inv;
+    const float inv5 = inv3 * inv2;
+    const float qzz = -(q.x + q.y);
+    const float qdx = q.x * dx + q.z * dy + q.w * dz;
+    const float qdy = q.z * dx + q.y * dy + qyz * dz;
+    const float qdz = q.w * dx + qyz * dy + qzz * dz;
+    const float dqd = dx * qdx + dy * qdy + dz * qdz;
+    const float f = e.w * inv3 + 2.5f * (dqd - yt.y * eps2) * inv5 * inv2;
+    ax += f * dx - inv5 * qdx;
+    ay += f * dy - inv5 * qdy;
+    az += f * dz - inv5 * qdz;
+}
+
+// Evaluates the tile entries [0, fill) for the lane's particle(s).
+__device__ __forceinline__ void eval_tile(const float4* tile, int fill, bool two, int r, int sub, float eps2,
+                                          float x0, float y0, float z0, float x1, float y1, float z1,
+                                          float& ax0, float& ay0, float& az0, float& ax1, float& ay1,
+                                          float& az1) {
+    if (two) {
+#pragma unroll 2
+        for (int j = 0; j < fill; ++j) {
+            const float4 e = tile[j];
+            pair_acc(e, x0, y0, z0, eps2, ax0, ay0, az0);
+            pair_acc(e, x1, y1, z1, eps2, ax1, ay1, az1);
+        }
+    } else if (r == 1) {
+#pragma unroll 4
+        for (int j = 0; j < fill; ++j) pair_acc(tile[j], x0, y0, z0, eps2, ax0, ay0, az0);
+    } else {
+#pragma unroll 4
+        for (int j = sub; j < fill; j += r) pair_acc(tile[j], x0, y0, z0, eps2, ax0, ay0, az0);
+    }
+}
+
+__device__ __forceinline__ void eval_nodes(const float4* ntA, const float4* ntQ, const float2* ntYZ, int fill,
+                                           bool two, int r, int sub, float eps2, float x0, float y0, float z0,
+                                           float x1, float y1, float z1, float& ax0, float& ay0, float& az0,
+                                           float& ax1, float& ay1, float& az1) {
+    if (two) {
+        for (int j = 0; j < fill; ++j) {
+            const float4 e = ntA[j], q = ntQ[j];
+            const float2 qyz = ntYZ[j];
+            quad_acc(e, q, qyz, x0, y0, z0, eps2, ax0, ay0, az0);
+            quad_acc(e, q, qyz, x1, y1, z1, eps2, ax1, ay1, az1);
+        }
+    } else {
+#pragma unroll 2
+        for (int j = sub; j < fill; j += r) quad_acc(ntA[j], ntQ[j], ntYZ[j], x0, y0, z0, eps2, ax0, ay0, az0);
+    }
+}
+
+template <bool QUAD>
+__global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
+    const float4* __restrict__ wa, const float4* __restrict__ wb, const float4* __restrict__ wq,
+    const float* __restrict__ wt, const float4* __restrict__ p4, const int* __restrict__ perm, const uint8_t* __restrict__ active,
+    const int4* __restrict__ work, const float4* __restrict__ sphere, TreeCounts* cnt, int nn, float eps2,
+    double* __restrict__ acc, uint32_t* status) {
+    using Smem = WarpSmem<QUAD>;
+    __shared__ Smem smem_all[kWalkWarps];
+    Smem& S = smem_all[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     const unsigned lt = lanemask_lt();
     const int nwork = cnt->num_work;
@@ -147,26 +220,34 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk_mono(
             const float4 p = p4[S.slot_pos[slot1]];
             x1 = p.x; y1 = p.y; z1 = p.z;
         }
+        // reference form: one float32 running sum per component; mixed form: each tile's
+        // partial sums are added to Kahan-compensated totals
         float ax0 = 0.f, ay0 = 0.f, az0 = 0.f, ax1 = 0.f, ay1 = 0.f, az1 = 0.f;
+        KahanF kx0, ky0, kz0, kx1, ky1, kz1;
         const bool two = P > 32;
 
-        int fill = 0;
+        int fill = 0, fillN = 0;
         unsigned long long listlen = 0;
-        auto flush = [&]() {
-            listlen += fill;
-            __syncwarp();
-            if (two) {
-                for (int j = 0; j < fill; ++j) {
-                    const float4 e = S.tile[j];
-                    pair_acc(e, x0, y0, z0, eps2, ax0, ay0, az0);
-                    pair_acc(e, x1, y1, z1, eps2, ax1, ay1, az1);
-                }
-            } else {
-                for (int j = sub; j < fill; j += r) pair_acc(S.tile[j], x0, y0, z0, eps2, ax0, ay0, az0);
-            }
-            __syncwarp();
-            fill = 0;
-        };
+#define GF_WALK_FLUSH()                                                                              \
+    do {                                                                                             \
+        listlen += fill + fillN;                                                                     \
+        __syncwarp();                                                                                \
+        if (QUAD) {                                                                                  \
+            float px0 = 0.f, py0 = 0.f, pz0 = 0.f, px1 = 0.f, py1 = 0.f, pz1 = 0.f;                  \
+            eval_tile(S.tile, fill, two, r, sub, eps2, x0, y0, z0, x1, y1, z1, px0, py0, pz0, px1,   \
+                      py1, pz1);                                                                     \
+            eval_nodes(S.ntA, S.ntQ, S.ntYZ, fillN, two, r, sub, eps2, x0, y0, z0, x1, y1, z1, px0,  \
+                       py0, pz0, px1, py1, pz1);                                                     \
+            kx0.add(px0); ky0.add(py0); kz0.add(pz0);                                                \
+            kx1.add(px1); ky1.add(py1); kz1.add(pz1);                                                \
+        } else {                                                                                     \
+            eval_tile(S.tile, fill, two, r, sub, eps2, x0, y0, z0, x1, y1, z1, ax0, ay0, az0, ax1,   \
+                      ay1, az1);                                                                     \
+        }                                                                                            \
+        __syncwarp();                                                                                \
+        fill = 0;                                                                                    \
+        fillN = 0;                                                                                   \
+    } while (0)
 
         int sp = 1;
         if (lane == 0) S.stack[0] = (0 << 4) | 1;  // root: range (first 0, count 1)
@@ -224,19 +305,30 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk_mono(
             // opened internal nodes: push their child ranges
             const unsigned om = __ballot_sync(0xffffffffu, open);
             const int npush = __popc(om);
-            if (sp + npush > kStackCap) {
+            if (sp + npush > Smem::kStack) {
                 overflow = true;
                 break;
             }
             if (open) S.stack[sp + __popc(om & lt)] = (first << 4) | code;
             sp += npush;
 
-            // accepted nodes: monopole entries
+            // accepted nodes: monopole (reference) or monopole + quadrupole (mixed) entries
             const unsigned am = __ballot_sync(0xffffffffu, accept);
             const int na = __popc(am);
-            if (fill + na > kTileCap) flush();
-            if (accept) S.tile[fill + __popc(am & lt)] = A;
-            fill += na;
+            if (QUAD) {
+                if (fillN + na > Smem::kNodeTile) GF_WALK_FLUSH();
+                if (accept) {
+                    const int slot = fillN + __popc(am & lt);
+                    S.ntA[slot] = A;
+                    S.ntQ[slot] = wq[node];
+                    S.ntYZ[slot] = make_float2(B.w, wt[node]);
+                }
+                fillN += na;
+            } else {
+                if (fill + na > kTileCap) GF_WALK_FLUSH();
+                if (accept) S.tile[fill + __popc(am & lt)] = A;
+                fill += na;
+            }
 
             // opened leaves: their particles
             const int lc = leaf ? -code : 0;
@@ -244,7 +336,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk_mono(
             const int lexcl = lincl - lc;
             const int ltot = __shfl_sync(0xffffffffu, lincl, 31);
             for (int done = 0; done < ltot;) {
-                if (fill == kTileCap) flush();
+                if (fill == kTileCap) GF_WALK_FLUSH();
                 const int chunk = min(kTileCap - fill, ltot - done);
                 if (leaf) {
                     const int a0 = max(lexcl, done), a1 = min(lexcl + lc, done + chunk);
@@ -259,7 +351,12 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk_mono(
             if (lane == 0) raise_status(status, GF_ERR_WALK_STACK);
             break;
         }
-        flush();
+        GF_WALK_FLUSH();
+#undef GF_WALK_FLUSH
+        if (QUAD) {
+            ax0 = kx0.s; ay0 = ky0.s; az0 = kz0.s;
+            ax1 = kx1.s; ay1 = ky1.s; az1 = kz1.s;
+        }
 
         // combine the partial sums of the lanes that share a particle
         for (int o = r >> 1; o > 0; o >>= 1) {
@@ -304,16 +401,25 @@ void Octree::prepare_walk(const uint8_t* active, cudaStream_t s) {
 void Octree::walk(double eps, double* acc, cudaStream_t s) {
     Context& C = ctx();
     const float eps2 = float(eps * eps);
-    static int blocks_per_sm = 0;
-    if (!blocks_per_sm) {
-        GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_walk_mono,
-                                                              kWalkWarps * 32, 0));
-        blocks_per_sm = std::max(1, blocks_per_sm);
+    static int bps_mono = 0, bps_quad = 0;
+    if (!bps_mono) {
+        GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps_mono, k_walk<false>, kWalkWarps * 32, 0));
+        GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps_quad, k_walk<true>, kWalkWarps * 32, 0));
+        bps_mono = std::max(1, bps_mono);
+        bps_quad = std::max(1, bps_quad);
     }
     ProfScope ps(kStWalk, s);
-    k_walk_mono<<<blocks_per_sm * C.sms, kWalkWarps * 32, 0, s>>>(
-        w_a.as<float4>(), w_b.as<float4>(), p4.as<float4>(), perm.as<int>(), active_ptr,
-        work.as<int4>(), sphere.as<float4>(), counts.as<TreeCounts>(), nn, eps2, acc, C.d_status);
+    last_walked() = this;
+    if (quad) {
+        k_walk<true><<<bps_quad * C.sms, kWalkWarps * 32, 0, s>>>(
+            w_a.as<float4>(), w_b.as<float4>(), w_q.as<float4>(), w_t.as<float>(), p4.as<float4>(), perm.as<int>(),
+            active_ptr,
+            work.as<int4>(), sphere.as<float4>(), counts.as<TreeCounts>(), nn, eps2, acc, C.d_status);
+    } else {
+        k_walk<false><<<bps_mono * C.sms, kWalkWarps * 32, 0, s>>>(
+            w_a.as<float4>(), w_b.as<float4>(), nullptr, nullptr, p4.as<float4>(), perm.as<int>(), active_ptr,
+            work.as<int4>(), sphere.as<float4>(), counts.as<TreeCounts>(), nn, eps2, acc, C.d_status);
+    }
     GF_CHECK_LAUNCH();
 }
 

@@ -115,6 +115,14 @@ int gf_sph_forces(int n, int k, const double* pos, const double* vel, const doub
                   const int64_t* nb, const double* h, const double* u, double gamma,
                   double alpha, double beta, double* rho, double* acc, double* dudt,
                   double* dt_i);
+/* sph_forces in the mixed-precision form (no reference counterpart): the same formulas in
+ * float32 arithmetic with hi/lo split positions and Kahan-compensated neighbour sums;
+ * float64 inputs and outputs, host pointers, same arguments as gf_sph_forces. */
+int gf_sph_forces_mixed(int n, int k, const double* pos, const double* vel, const double* mass,
+                        const int64_t* nb, const double* h, const double* u, double gamma,
+                        double alpha, double beta, double* rho, double* acc, double* dudt,
+                        double* dt_i);
+
 /* Particles accepted by gf_sph_forces_noalloc_dev (its fixed scratch: 16 bytes each). */
 #define GF_SPH_NOALLOC_MAX_N 262144
 
@@ -177,10 +185,75 @@ int gf_accelerations(int n, const double* pos, const double* vel, const double* 
                      const int8_t* kind, const double* u, double theta, double eps, double gamma,
                      double alpha, double beta, const uint8_t* active, int rebuild, int sph,
                      int fresh_nb, double* acc, double* dt_ind);
+/* ---- the step loop (galaxy_formation/simulation.py:114-149) ----------------------------- */
+
+/* Loads a particle set onto the GPU (host pointers, copied) and computes its initial
+ * accelerations, as GalaxyFormation.__init__ does (simulation.py:51-54). kind: 0 gas,
+ * 1 star, 2 dark matter. */
+int gf_sim_init(int n, const double* pos, const double* vel, const double* mass,
+                const int8_t* kind, const double* u, double theta, double eps, double gamma,
+                double alpha, double beta);
+/* One long step of the hierarchical kick-drift-kick leapfrog of GalaxyFormation.step
+ * (simulation.py:114-149), device-resident, without the sub-grid physics hooks
+ * (_thermodynamics, _stars). taken: its length; substeps: sub-steps done (1 for a global
+ * step). */
+int gf_sim_step(double dt_max, double* taken, int* substeps);
+/* Copies the state out (host pointers; any may be NULL): pos, vel, acc (n,3), dt_ind (n),
+ * and the simulated time t. */
+int gf_sim_read(double* pos, double* vel, double* acc, double* dt_ind, double* t);
+
+/* Options of the fused force evaluation (no reference counterpart):
+ *   GF_OPT_SPH_FLOAT32  0 = float64 SPH arithmetic (the reference's, default);
+ *                       1 = mixed precision: float32 arithmetic with hi/lo split positions
+ *                           and Kahan-compensated neighbour sums. */
+#define GF_OPT_SPH_FLOAT32 0
+/*   GF_OPT_GRAVITY_QUAD 0 = the reference's monopole Barnes-Hut (default);
+ *                       1 = mixed form: nodes carry traceless quadrupoles (float32, Kahan
+ *                           sums), accepted nodes are evaluated to quadrupole order and the
+ *                           walk adds its tile sums with Kahan compensation. The fused path
+ *                           keeps its own tree; nbody_accel_active is never affected. */
+#define GF_OPT_GRAVITY_QUAD 1
+/*   GF_OPT_HGUESS       start of the neighbour-count iteration of a full search:
+ *                       0 = 2.4 x the previous h (default), 1 = the density of the particle's
+ *                       tree cell only, 2 = the learned guess (gf_mlp_*); the iteration always
+ *                       runs to the exact 48 nearest, so only the iteration count changes. */
+#define GF_OPT_HGUESS 2
+/*   GF_OPT_COLLECT      capacity (rows) of a device buffer that every later full search
+ *                       fills with (features, log of the converged h) pairs for training;
+ *                       setting it clears the buffer; gf_get_option returns the rows kept. */
+#define GF_OPT_COLLECT 3
+int gf_set_option(int key, double value);
+/* Current value of an option (-1 for an unknown key). */
+double gf_get_option(int key);
+/* ---- learned smoothing-length guess (no reference counterpart) ----------------------- */
+/* A 4 -> 64 -> 64 -> 1 ReLU MLP with bfloat16 weights and float32 accumulation predicting log h
+ * from (log cell density, log previous h, leaf count, velocity divergence), standardised by
+ * gf_mlp_set_norm. Parameters: flat float32 vector of 4545 values, W1 (64x4), b1, W2 (64x64),
+ * b2, w3 (64), b3. */
+int gf_mlp_init(int seed);
+int gf_mlp_set_params(const float* params);
+int gf_mlp_get_params(float* params);
+int gf_mlp_set_norm(const float* mean4, const float* std4, double t_mean, double t_std);
+/* log h of n samples (X: n x 4), host pointers. */
+int gf_mlp_predict(int n, const float* X, float* Y);
+/* Gradient of 0.5 mean((y - t)^2) (standardised target t) over the n samples w.r.t. the flat
+ * parameters, host pointers. */
+int gf_mlp_gradient(int n, const float* X, const float* T, float* grad);
+/* Copies up to max_rows collected training pairs (X rows of 4, T) to the host; returns the
+ * rows copied (with X and T NULL: the rows available). */
+long long gf_mlp_collected(float* X, float* T, long long max_rows);
+/* Adam steps on random minibatches of the collected pairs; loss: the last minibatch's
+ * mean loss in standardised units. */
+int gf_mlp_train(int steps, int batch, double lr, double* loss);
+
 /* Scalars of the last force evaluation: gas count, dt_grav = 0.3 sqrt(eps / max |a|),
  * dt_gas = min Courant step (inf without hydro), search-radius iterations of the last full
  * neighbour search. Any pointer may be NULL. Synchronises the device. */
 int gf_force_info(int* n_gas, double* dt_grav, double* dt_gas, long long* knn_iters);
+/* Up to nout statistics of the fused evaluation, in this order: gas count, dt_grav, dt_gas,
+ * search-radius iterations of the last full search, 0 (reserved), full searches so far,
+ * Verlet reselections so far, nodes of the gas octree. Synchronises the device. */
+int gf_force_stats(double* out, int nout);
 
 /* ---- measurement hooks (no reference counterpart) ----------------------------------- */
 
@@ -194,7 +267,7 @@ int gf_profile(int on);
 int gf_profile_stage(int stage, double* total_ms, int* launches);
 /* Kernels launched by the library since it was loaded. */
 long long gf_launch_count(void);
-/* Particle-list pair interactions evaluated by the last gravity walk (synchronises). */
+/* Particle-list pair interactions evaluated by the most recent gravity walk (synchronises). */
 long long gf_walk_pairs(void);
 /* Measures the float32 FFMA throughput of the GPU (TFLOP/s, an FMA counting 2 flops): the
  * roofline peak of the float32 walk. */

@@ -84,3 +84,55 @@ class ForceOracle:
         self.dt_ind = np.minimum(0.3 * np.sqrt(self.eps / np.maximum(a_mag, 1e-30)), self.dt_courant)
         self.dt_grav = 0.3 * np.sqrt(self.eps / max(a_mag.max(), 1e-30))
         return acc
+
+
+class StepOracle:
+    """GalaxyFormation.step (galaxy_formation/simulation.py:114-149) restated on ForceOracle,
+    without the sub-grid physics hooks (_thermodynamics, _stars) that sit outside the force
+    path. State: pos, vel, mass, kind, u (float64, updated in place)."""
+
+    def __init__(self, pos, vel, mass, kind, u, theta, eps, **kw):
+        self.pos, self.vel = pos.copy(), vel.copy()
+        self.mass, self.kind, self.u = mass, kind, u
+        self.eps = eps
+        self.f = ForceOracle(len(mass), theta, eps, **kw)
+        self.t = 0.0
+        self.acc = self.accelerations()
+
+    def accelerations(self, active=None, rebuild=True, sph=True, fresh_nb=True):
+        acc = self.f.accelerations(self.pos, self.vel, self.mass, self.kind, self.u, active, rebuild,
+                                   sph, fresh_nb)
+        self.dt_ind, self.dt_grav = self.f.dt_ind, self.f.dt_grav
+        self.dt_gas = self.f.dt_gas if sph else self.dt_gas
+        return acc
+
+    def step(self, dt_max):
+        dt_min = min(self.dt_gas, self.dt_grav, dt_max)
+        D = min(dt_max, np.percentile(self.dt_ind, 10))
+        self.substeps = 0
+        if D <= 1.5 * dt_min:
+            self.vel += 0.5 * dt_min * self.acc
+            self.pos += dt_min * self.vel
+            self.acc = self.accelerations()
+            self.vel += 0.5 * dt_min * self.acc
+            self.t += dt_min
+            self.substeps = 1
+            return dt_min
+        fast = (self.dt_ind < D) | (self.kind == GAS)
+        slow = ~fast
+        self.vel[slow] += 0.5 * D * self.acc[slow]
+        tau = 0.0
+        first = True
+        while tau < D * (1 - 1e-9):
+            dt = min(self.dt_ind[fast].min(), D - tau)
+            self.vel[fast] += 0.5 * dt * self.acc[fast]
+            self.pos += dt * self.vel
+            self.acc = self.accelerations(active=fast, rebuild=False, fresh_nb=first)
+            first = False
+            self.vel[fast] += 0.5 * dt * self.acc[fast]
+            tau += dt
+            self.t += dt
+            self.substeps += 1
+        self.acc = self.accelerations(active=slow, rebuild=True, sph=False)
+        self.vel[slow] += 0.5 * D * self.acc[slow]
+        return D

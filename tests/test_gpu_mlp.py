@@ -1,0 +1,110 @@
+"""The learned smoothing-length guess (gf_mlp_*, BF16 weights, float32 accumulation).
+
+* forward and gradient kernels against the float64 oracle (oracle/mlp_ref.py) evaluated
+  with the same bfloat16-rounded weights;
+* training on the GPU lowers the loss;
+* end to end: trained on (features, converged h) pairs collected from the simulator's own
+  force evaluations, the guess needs fewer radius iterations than the start from the cell
+  density alone, and the converged neighbours / h (hence accelerations) do not change.
+"""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def mref():
+    import mlp_ref
+
+    return mlp_ref
+
+
+def _identity_norm(lib):
+    from galaxy_formation_gb300 import _lib
+
+    _lib.check(lib.gf_mlp_set_norm(np.zeros(4, np.float32), np.ones(4, np.float32), 0.0, 1.0))
+
+
+def test_forward_and_gradient_match_float64(gpulib, mref):
+    from galaxy_formation_gb300 import _lib
+
+    lib = gpulib
+    _lib.check(lib.gf_mlp_init(11))
+    _identity_norm(lib)
+    p = np.zeros(_lib.MLP_PARAMS, np.float32)
+    _lib.check(lib.gf_mlp_get_params(p))
+    pb = mref.bf16_round(p)               # the weights the kernels actually use
+    rng = np.random.default_rng(0)
+    X = rng.normal(size=(300, 4)).astype(np.float32)
+    T = rng.normal(size=300).astype(np.float32)
+    Y = np.zeros(300, np.float32)
+    _lib.check(lib.gf_mlp_predict(300, X, Y))
+    y_ref, _ = mref.forward(pb, X.astype(np.float64))
+    assert np.max(np.abs(Y - y_ref)) < 1e-4 * max(1.0, np.abs(y_ref).max())
+    g = np.zeros(_lib.MLP_PARAMS, np.float32)
+    _lib.check(lib.gf_mlp_gradient(300, X, T, g))
+    _, g_ref = mref.loss_and_grad(pb, X.astype(np.float64), T.astype(np.float64))
+    rel = np.linalg.norm(g - g_ref) / np.linalg.norm(g_ref)
+    assert rel < 1e-4, rel
+    # every block of the parameter vector individually
+    H = 64
+    for a, b in ((0, 4 * H), (4 * H, 5 * H), (5 * H, 5 * H + H * H), (5 * H + H * H, 6 * H + H * H),
+                 (6 * H + H * H, 7 * H + H * H)):
+        assert np.linalg.norm(g[a:b] - g_ref[a:b]) <= 1e-4 * np.linalg.norm(g_ref[a:b]) + 1e-9
+
+
+def test_training_lowers_the_loss(gpulib, oracle):
+    """Collect pairs from the simulator's own evaluations, then fit them on the GPU."""
+    import ctypes
+
+    from galaxy_formation_gb300 import _lib, params, synthetic
+
+    lib = gpulib
+    d = synthetic.make_config(1, scale=0.1)
+    n = len(d["mass"])
+    acc, dt = np.empty((n, 3)), np.empty(n)
+
+    def force(fresh=1):
+        _lib.check(lib.gf_accelerations(n, d["pos"], d["vel"], d["mass"], d["kind"], d["u"], params.THETA,
+                                        params.EPS, params.GAMMA, 1.0, 2.0, None, 1, 1, fresh, acc, dt))
+
+    lib.gf_set_option(_lib.OPT_HGUESS, 0)
+    force()
+    lib.gf_set_option(_lib.OPT_COLLECT, 200_000)
+    for _ in range(4):     # drift by the local time steps, then search again
+        d["pos"] = np.ascontiguousarray(d["pos"] + 0.5 * dt[:, None] * d["vel"])
+        force()
+    rows = lib.gf_mlp_collected(None, None, 0)
+    assert rows >= 30_000
+    X = np.zeros((rows, 4), np.float32)
+    T = np.zeros(rows, np.float32)
+    lib.gf_mlp_collected(X.ctypes.data, T.ctypes.data, rows)
+    assert np.all(np.isfinite(X)) and np.all(np.isfinite(T))
+    _lib.check(lib.gf_mlp_init(3))
+    mu, sd = X.mean(0), X.std(0) + 1e-6
+    _lib.check(lib.gf_mlp_set_norm(mu.astype(np.float32), sd.astype(np.float32), float(T.mean()), float(T.std())))
+    loss0, loss1 = ctypes.c_double(), ctypes.c_double()
+    _lib.check(lib.gf_mlp_train(1, 4096, 1e-3, ctypes.byref(loss0)))
+    _lib.check(lib.gf_mlp_train(1500, 4096, 2e-3, ctypes.byref(loss1)))
+    assert loss1.value < 0.2 * loss0.value, (loss0.value, loss1.value)
+
+    # the guess in use: fewer iterations than the cell-density start, same converged result
+    st = np.zeros(8)
+    d["pos"] = np.ascontiguousarray(d["pos"] + 0.5 * dt[:, None] * d["vel"])
+    pos_next = d["pos"].copy()
+    res = {}
+    for mode in (1, 2, 0):
+        lib.gf_set_option(_lib.OPT_COLLECT, 0)
+        lib.gf_set_option(_lib.OPT_HGUESS, mode)
+        d["pos"] = pos_next.copy()
+        force()
+        lib.gf_force_stats(st, 8)
+        res[mode] = (st[3] / st[0], acc.copy(), dt.copy())
+    lib.gf_set_option(_lib.OPT_HGUESS, 0)
+    it_cell, it_mlp = res[1][0], res[2][0]
+    assert it_mlp < it_cell, (it_cell, it_mlp)
+    for mode in (2, 0):
+        assert np.allclose(res[mode][1], res[1][1], rtol=1e-12, atol=0)
+        assert np.allclose(res[mode][2], res[1][2], rtol=1e-12, atol=0)
