@@ -55,6 +55,10 @@ SIGNATURES = {
                      _cd, _cd, _cd, _cd, _cd], _ci),
     "gf_sim_step": ([_cd, ctypes.POINTER(_cd), ctypes.POINTER(_ci)], _ci),
     "gf_sim_read": ([_vp, _vp, _vp, _vp, ctypes.POINTER(_cd)], _ci),
+    "gf_sim_blocks": ([_ci, _ci, ctypes.POINTER(_cd)], _ci),
+    "gf_sim_updates": ([], _cd),
+    "gf_stream": ([], _vp),
+    "gf_sim_levels": ([_ci, _dbl], _ci),
     "gf_set_option": ([_ci, _cd], _ci),
     "gf_get_option": ([_ci], _cd),
     "gf_force_stats": ([_dbl, _ci], _ci),

@@ -459,6 +459,15 @@ int gf_profile_stage(int stage, double* total_ms, int* launches) {
 
 long long gf_launch_count(void) { return ctx().launches; }
 
+void* gf_stream(void) {
+    try {
+        ensure_ready();
+        return ctx().stream;
+    } catch (...) {
+        return nullptr;
+    }
+}
+
 int gf_fp32_peak(double* tflops) {
     return guarded([&] {
         require(tflops != nullptr, "null pointer");
@@ -529,6 +538,25 @@ int gf_sim_step(double dt_max, double* taken, int* substeps) {
         const double D = sim_step(dt_max, substeps);
         if (taken) *taken = D;
         collect_status(ctx().stream);
+    });
+}
+
+double gf_sim_updates(void) { return sim_updates(); }
+
+int gf_sim_blocks(int nblocks, int nlev, double* updates) {
+    return guarded([&] {
+        require(nblocks >= 0 && nlev >= 1 && nlev <= 8, "need nblocks >= 0 and 1 <= nlev <= 8");
+        require(simulation_ready(), "gf_sim_init first");
+        const double u = block_run(nblocks, nlev);
+        if (updates) *updates = u;
+        collect_status(ctx().stream);
+    });
+}
+
+int gf_sim_levels(int nlev, double* frac) {
+    return guarded([&] {
+        require(nlev >= 1 && nlev <= 8 && frac, "bad arguments");
+        block_levels(nlev, frac);
     });
 }
 

@@ -37,6 +37,10 @@ struct Error : std::runtime_error {
         ++gf::ctx().launches;           \
     } while (0)
 
+// Bumped whenever any DevBuf (re)allocates: a captured CUDA graph that bakes buffer
+// addresses is valid only while this stays unchanged.
+extern unsigned long long g_alloc_generation;
+
 // A grow-only device allocation.
 struct DevBuf {
     void* p = nullptr;
@@ -50,6 +54,7 @@ struct DevBuf {
             bytes = 0;
             GF_CUDA(cudaMalloc(&p, need));
             bytes = need;
+            ++g_alloc_generation;
         }
         return static_cast<T*>(p);
     }

@@ -16,6 +16,7 @@
 namespace gf {
 
 static Context g_ctx;
+unsigned long long g_alloc_generation = 0;
 
 Context& ctx() { return g_ctx; }
 

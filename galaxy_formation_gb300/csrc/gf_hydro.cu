@@ -66,12 +66,13 @@ constexpr int kSelWarps = 8;
 __global__ void __launch_bounds__(kSelWarps * 32) k_verlet_select(
     int ng, const int* __restrict__ gidx, const int* __restrict__ row, const int* __restrict__ cache,
     const int* __restrict__ loc, const double* __restrict__ gpos, int* __restrict__ nb, double* __restrict__ d31,
-    int* __restrict__ fail) {
+    int* __restrict__ fail, const uint8_t* __restrict__ gact) {
     __shared__ double s_key[kSelWarps][64];
     __shared__ int s_tag[kSelWarps][64];
     __shared__ int s_loc[kSelWarps][64];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int i = blockIdx.x * kSelWarps + w; i < ng; i += gridDim.x * kSelWarps) {
+        if (gact && !gact[i]) continue;
         const int r = row[gidx[i]];
         if (r < 0) continue;  // handled by k_verlet_prep's flag
         const double xi = gpos[3 * size_t(i)], yi = gpos[3 * size_t(i) + 1], zi = gpos[3 * size_t(i) + 2];
@@ -142,9 +143,9 @@ __global__ void k_guess(int ng, const int* __restrict__ gidx, const double* __re
 }
 
 __global__ void k_smoothing(int ng, const double* __restrict__ d31, double eps, const int* __restrict__ gidx,
-                            double* __restrict__ h, double* __restrict__ hprev) {
+                            double* __restrict__ h, double* __restrict__ hprev, const uint8_t* __restrict__ gact) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ng) return;
+    if (i >= ng || (gact && !gact[i])) return;
     const double v = fmax(0.5 * d31[i], 0.5 * eps);  // simulation.py:84
     h[i] = v;
     hprev[gidx[i]] = 0.5 * d31[i] > 0 ? 0.5 * d31[i] : v;
@@ -165,6 +166,12 @@ __global__ void k_scatter_f(int ng, const int* __restrict__ gidx, const float* _
     if (i < ng) out[gidx[i]] = v[i];
 }
 
+__global__ void k_gas_active(int ng, const int* __restrict__ gidx, const uint8_t* __restrict__ active,
+                             uint8_t* __restrict__ gact) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ng) gact[i] = active[gidx[i]];
+}
+
 __global__ void k_fill(int n, double* __restrict__ a, double v) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) a[i] = v;
@@ -172,10 +179,11 @@ __global__ void k_fill(int n, double* __restrict__ a, double v) {
 
 __global__ void k_scatter_sph(int ng, const int* __restrict__ gidx, const double* __restrict__ a,
                               const double* __restrict__ dti, double* __restrict__ acc_sph,
-                              double* __restrict__ dt_courant, unsigned long long* __restrict__ dtmin_bits) {
+                              double* __restrict__ dt_courant, unsigned long long* __restrict__ dtmin_bits,
+                              const uint8_t* __restrict__ gact) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double v = INFINITY;
-    if (i < ng) {
+    if (i < ng && !(gact && !gact[i])) {
         const int g = gidx[i];
         for (int c = 0; c < 3; ++c) acc_sph[3 * size_t(g) + c] = a[3 * size_t(i) + c];
         dt_courant[g] = dti[i];
@@ -241,12 +249,15 @@ void ForceEngine::evaluate(const ForceArgs& a, cudaStream_t s) {
 
     // gravity (simulation.py:64)
     Octree& T = grav;
-    if (a.rebuild || !T.valid || T.n != n || T.quad != (gravity_quad != 0)) {
+    if (a.nosync) {
+        if (a.rebuild || !T.valid || T.n != n) throw Error(GF_ERR_ARG, "a synchronisation-free evaluation refits");
+        T.refit(a.pos, a.mass, s, true);
+    } else if (a.rebuild || !T.valid || T.n != n || T.quad != (gravity_quad != 0)) {
         T.quad = gravity_quad != 0;
         T.build(n, a.pos, a.mass, a.theta, s);
-    }
-    else
+    } else {
         T.refit(a.pos, a.mass, s);
+    }
     T.prepare_walk(a.active, s);
     T.walk(a.eps, acc_grav.as<double>(), s);
 
@@ -270,25 +281,33 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
     HydroScalars* sc = scalars.as<HydroScalars>();
     double* as = acc_sph.as<double>();
     double* dtc = dt_courant.as<double>();
-    GF_CUDA(cudaMemsetAsync(as, 0, sizeof(double) * 3 * size_t(n), s));  // simulation.py:75-76
-    k_fill<<<grid, kThreads, 0, s>>>(n, dtc, INFINITY);
-    GF_CHECK_LAUNCH();
+    const bool partial = a.sph_active != nullptr;
+    if (!partial) {
+        GF_CUDA(cudaMemsetAsync(as, 0, sizeof(double) * 3 * size_t(n), s));  // simulation.py:75-76
+        k_fill<<<grid, kThreads, 0, s>>>(n, dtc, INFINITY);
+        GF_CHECK_LAUNCH();
+    }
 
     int* fl = flag.get<int>(n);
     int* sc_ = scan.get<int>(n);
-    k_gas_flag<<<grid, kThreads, 0, s>>>(n, a.kind, fl);
-    GF_CHECK_LAUNCH();
-    GF_CUDA(cudaMemsetAsync(sc, 0, sizeof(HydroScalars), s));
-    GF_CUDA(cudaMemsetAsync(&sc->dtmin_bits, 0x7f, sizeof(unsigned long long), s));
-    exclusive_scan(fl, sc_, n, &sc->ng, s);
-    GF_CUDA(cudaMemcpyAsync(&scalars_h->ng, &sc->ng, sizeof(int), cudaMemcpyDeviceToHost, s));
-    GF_CUDA(cudaStreamSynchronize(s));
-    ng = scalars_h->ng;
-    if (ng <= 40) {  // simulation.py:80
-        ng_valid = 0;
-        return;
+    if (!a.nosync) {
+        k_gas_flag<<<grid, kThreads, 0, s>>>(n, a.kind, fl);
+        GF_CHECK_LAUNCH();
+        GF_CUDA(cudaMemsetAsync(sc, 0, sizeof(HydroScalars), s));
+        GF_CUDA(cudaMemsetAsync(&sc->dtmin_bits, 0x7f, sizeof(unsigned long long), s));
+        exclusive_scan(fl, sc_, n, &sc->ng, s);
+        GF_CUDA(cudaMemcpyAsync(&scalars_h->ng, &sc->ng, sizeof(int), cudaMemcpyDeviceToHost, s));
+        GF_CUDA(cudaStreamSynchronize(s));
+        ng = scalars_h->ng;
+        if (ng <= 40) {  // simulation.py:80
+            ng_valid = 0;
+            return;
+        }
+        ng_valid = ng;
+    } else {
+        if (ng_valid == 0) return;  // gas set of the last regular call
+        GF_CUDA(cudaMemsetAsync(&sc->dtmin_bits, 0x7f, sizeof(unsigned long long), s));
     }
-    ng_valid = ng;
     int* gi = gidx.get<int>(ng);
     double* gp = gpos.get<double>(3 * size_t(ng));
     double* gv = gvel.get<double>(3 * size_t(ng));
@@ -300,6 +319,12 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
     const int ggrid = div_up(ng, kThreads);
     int* nb = nb48.get<int>(size_t(ng) * kCand);
     double* d31 = dsel.get<double>(ng);
+    uint8_t* ga = nullptr;
+    if (partial) {
+        ga = gact.get<uint8_t>(ng);
+        k_gas_active<<<ggrid, kThreads, 0, s>>>(ng, gi, a.sph_active, ga);
+        GF_CHECK_LAUNCH();
+    }
     bool have_nb = false;
     if (!a.fresh_nb && cache_valid) {
         int* lc = loc.as<int>();
@@ -310,13 +335,18 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
         const int blocks = std::min(div_up(ng, kSelWarps), 16 * ctx().sms);
         ProfScope pv(kStVerlet, s);
         k_verlet_select<<<blocks, kSelWarps * 32, 0, s>>>(ng, gi, row.as<int>(), cache.as<int>(), lc, gp, nb,
-                                                          d31, &sc->fail);
+                                                          d31, &sc->fail, ga);
         GF_CHECK_LAUNCH();
-        GF_CUDA(cudaMemcpyAsync(&scalars_h->fail, &sc->fail, sizeof(int), cudaMemcpyDeviceToHost, s));
-        GF_CUDA(cudaStreamSynchronize(s));
-        have_nb = scalars_h->fail == 0;
+        if (a.nosync) {  // the gas set is the cached one: every particle keeps its candidates
+            have_nb = true;
+        } else {
+            GF_CUDA(cudaMemcpyAsync(&scalars_h->fail, &sc->fail, sizeof(int), cudaMemcpyDeviceToHost, s));
+            GF_CUDA(cudaStreamSynchronize(s));
+            have_nb = scalars_h->fail == 0;
+        }
         verlet_hits += have_nb ? 1 : 0;
     }
+    if (!have_nb && a.nosync) throw Error(GF_ERR_ARG, "a synchronisation-free evaluation needs a neighbour cache");
     if (!have_nb) {  // full search, 48 candidates (sph.py:165-169)
         const int kq = std::min(kCand, ng);
         float* rg = nullptr;
@@ -350,28 +380,28 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
         order_ng = ng;
     }
     double* hh = h.get<double>(ng);
-    k_smoothing<<<ggrid, kThreads, 0, s>>>(ng, d31, a.eps, gi, hh, h_prev.as<double>());
+    k_smoothing<<<ggrid, kThreads, 0, s>>>(ng, d31, a.eps, gi, hh, h_prev.as<double>(), ga);
     GF_CHECK_LAUNCH();
     have_hprev = true;
 
     double* r = rho.get<double>(ng);
-    double* ga = gacc.get<double>(3 * size_t(ng));
+    double* gacc_ = gacc.get<double>(3 * size_t(ng));
     double* du = dudt.get<double>(ng);
     double* dti = dt_i.get<double>(ng);
     float* dv = gdivv.get<float>(ng);
     if (sph_float32) {
         // visit the gas in the Morton order of the last neighbour-search tree (same gas set)
         const int* order = order_ng == ng ? knn_tree.perm.as<int>() : nullptr;
-        sph_forces32<int>(sph32, ng, kNgb, kCand, order, gp, gv, gm, nb, hh, gu, a.gamma, a.alpha, a.beta, r, ga,
-                          du, dti, s, dv);
+        sph_forces32<int>(sph32, ng, kNgb, kCand, order, gp, gv, gm, nb, hh, gu, a.gamma, a.alpha, a.beta, r,
+                          gacc_, du, dti, s, dv, ga);
     } else {
-        sph_forces<int>(sph, ng, kNgb, kCand, gp, gv, gm, nb, hh, gu, a.gamma, a.alpha, a.beta, r, ga, du, dti, s,
-                        dv);
+        sph_forces<int>(sph, ng, kNgb, kCand, gp, gv, gm, nb, hh, gu, a.gamma, a.alpha, a.beta, r, gacc_, du, dti,
+                        s, dv, ga);
     }
     k_scatter_f<<<ggrid, kThreads, 0, s>>>(ng, gi, dv, divv_prev.as<float>());
     GF_CHECK_LAUNCH();
     have_divv = true;
-    k_scatter_sph<<<ggrid, kThreads, 0, s>>>(ng, gi, ga, dti, as, dtc, &sc->dtmin_bits);
+    k_scatter_sph<<<ggrid, kThreads, 0, s>>>(ng, gi, gacc_, dti, as, dtc, &sc->dtmin_bits, ga);
     GF_CHECK_LAUNCH();
 }
 

@@ -26,6 +26,12 @@ struct ForceArgs {
     int rebuild, sph, fresh_nb;
     double* acc;     // (n,3) out
     double* dt_ind;  // (n,) out
+    // block time steps: SPH recomputed only for the gas flagged here (others keep their last
+    // density, forces and Courant step); null = all gas, as in the reference
+    const uint8_t* sph_active = nullptr;
+    // no host synchronisation (for CUDA-graph capture): gas set, neighbour cache and tree are
+    // those of the last regular call; gravity refits with device-side node counts
+    int nosync = 0;
 };
 
 struct ForceEngine {
@@ -48,10 +54,15 @@ struct ForceEngine {
     DevBuf acc_grav, acc_sph, dt_courant, h_prev, row, loc, cache;
     DevBuf flag, scan, gidx, gpos, gvel, gmass, gu_, nb48, dsel, rguess, h, rho, gacc, dudt, dt_i;
     DevBuf scalars;
-    DevBuf divv_prev, gdivv, hX, hY, hrg, colX, colT;
+    DevBuf divv_prev, gdivv, hX, hY, hrg, colX, colT, gact;
     HydroScalars* scalars_h = nullptr;  // pinned copy, valid after the stream synchronises
 
     void evaluate(const ForceArgs& a, cudaStream_t s);
+    // allocates the buffers that only synchronisation-free evaluations touch
+    void reserve_nosync(int n) {
+        grav.pdisp.get<float>(n);
+        if (ng > 0) gact.get<uint8_t>(ng);
+    }
     void hydro(const ForceArgs& a, cudaStream_t s);
 };
 
@@ -61,6 +72,12 @@ ForceEngine& force_engine();
 void sim_init(int n, const double* pos, const double* vel, const double* mass, const int8_t* kind, const double* u,
               double theta, double eps, double gamma, double alpha, double beta);
 double sim_step(double dt_max, int* substeps);
+double sim_updates();
 void sim_read(double* pos, double* vel, double* acc, double* dt_ind, double* t);
+// Block time steps (the batched form): advances nblocks blocks of 2^(nlev-1) sub-steps;
+// returns the particle-updates done.
+double block_run(int nblocks, int nlev);
+bool simulation_ready();
+void block_levels(int nlev, double* frac);
 
 }  // namespace gf

@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 #include "gf_hydro.cuh"
 
@@ -51,6 +52,14 @@ __global__ void k_keys_of(int n, const double* __restrict__ v, uint64_t* __restr
     val[i] = i;
 }
 
+__global__ void k_count_forced(int n, const uint8_t* __restrict__ active, const int8_t* __restrict__ kind, int sph,
+                               unsigned long long* __restrict__ count) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool f = i < n && (active[i] || (sph && kind[i] == 0));
+    const unsigned m = __ballot_sync(0xffffffffu, f);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(count, (unsigned long long)__popc(m));
+}
+
 __global__ void k_masked_min(int n, const double* __restrict__ v, const uint8_t* __restrict__ mask,
                              unsigned long long* __restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -68,12 +77,20 @@ struct Simulation {
     double t = 0, theta = 0.7, eps = 0, gamma = 5.0 / 3.0, alpha = 1, beta = 2;
     double dt_grav = 0, dt_gas = INFINITY;
     int last_substeps = 0;
+    double updates = 0;  // particle-updates of the last step (forces computed)
     DevBuf pos, vel, acc, mass, kind, u, dt_ind, fast, slow, keys, keys_alt, vals, vals_alt, scal;
     unsigned long long* h_scal = nullptr;
 
     cudaStream_t s() const { return ctx().stream; }
 
     void accelerations(const uint8_t* active, int rebuild, int sph, int fresh) {
+        if (active) {  // particles receiving new forces: the active ones, plus the gas under SPH
+            unsigned long long* d = scal.get<unsigned long long>(2);
+            GF_CUDA(cudaMemsetAsync(d + 1, 0, sizeof(unsigned long long), s()));
+            k_count_forced<<<div_up(n, kThreads), kThreads, 0, s()>>>(n, active, kind.as<int8_t>(), sph, d + 1);
+            GF_CHECK_LAUNCH();
+            GF_CUDA(cudaMemcpyAsync(h_scal + 1, d + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s()));
+        }
         ForceArgs a{n, pos.as<double>(), vel.as<double>(), mass.as<double>(), kind.as<int8_t>(), u.as<double>(),
                     theta, eps, gamma, alpha, beta, active, rebuild, sph, fresh, acc.as<double>(),
                     dt_ind.as<double>()};
@@ -82,6 +99,7 @@ struct Simulation {
         GF_CUDA(cudaStreamSynchronize(s()));
         dt_grav = F.scalars_h->dt_grav;
         if (sph) dt_gas = F.scalars_h->dt_gas;
+        updates += active ? double(h_scal[1]) : double(n);
     }
 
     void kick(const uint8_t* mask, double h) {
@@ -128,6 +146,7 @@ struct Simulation {
     }
 
     double step(double dt_max) {
+        updates = 0;
         const double dt_min = std::min(std::min(dt_gas, dt_grav), dt_max);
         const double D = std::min(dt_max, percentile(10.0));
         last_substeps = 0;
@@ -166,6 +185,204 @@ struct Simulation {
 
 static Simulation g_sim;
 Simulation& simulation() { return g_sim; }
+bool simulation_ready() { return g_sim.n > 0; }
+
+// ---------------------------------------------------------------------------------------
+// Block time steps (the batched form). Every particle sits on a power-of-two level j:
+// its step is 2^j delta, delta = min dt_ind (the finest step), j = floor(log2(dt_ind /
+// delta)) clamped to [0, nlev-1]; a block is 2^(nlev-1) finest sub-steps, so every level
+// is synchronised at block boundaries. Leapfrog per particle: an opening half-kick at the
+// block start, a full kick (closing + opening) at each of its force evaluations inside the
+// block, a closing half-kick at the block end. Sub-step s evaluates forces (gravity on the
+// refitted tree, SPH) for the particles with s mod 2^j == 0 only — from 100 % of them at
+// s = 0 down to the finest level alone at odd s. The 2^(nlev-1) - 1 inner sub-steps plus the
+// last drift are captured once as a CUDA graph and replayed every block; the block-end
+// evaluation (rebuilt tree, fresh neighbour search, all particles) runs outside the graph.
+// The graph is recaptured whenever a device buffer moved (g_alloc_generation).
+
+namespace {
+
+__global__ void k_levels(int n, const double* __restrict__ dt_ind, const unsigned long long* __restrict__ dbits,
+                         int nlev, int8_t* __restrict__ level) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double delta = __longlong_as_double((long long)*dbits);
+    int j = int(floor(log2(dt_ind[i] / delta)));
+    level[i] = int8_t(min(max(j, 0), nlev - 1));
+}
+
+// mode 0: opening half-kick (all); 1: full kick of the particles active at sub-step s;
+// 2: closing half-kick (all)
+__global__ void k_kick_levels(int n, double* __restrict__ vel, const double* __restrict__ acc,
+                              const int8_t* __restrict__ level, const unsigned long long* __restrict__ dbits,
+                              int mode, int s) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int j = level[i];
+    if (mode == 1 && (s & ((1 << j) - 1))) return;
+    const double step = __longlong_as_double((long long)*dbits) * double(1 << j);
+    const double h = mode == 1 ? step : 0.5 * step;
+    for (int c = 0; c < 3; ++c) vel[3 * size_t(i) + c] += h * acc[3 * size_t(i) + c];
+}
+
+__global__ void k_drift_bits(int n, double* __restrict__ pos, const double* __restrict__ vel,
+                             const unsigned long long* __restrict__ dbits) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double dt = __longlong_as_double((long long)*dbits);
+    for (int c = 0; c < 3; ++c) pos[3 * size_t(i) + c] += dt * vel[3 * size_t(i) + c];
+}
+
+__global__ void k_active_at(int n, const int8_t* __restrict__ level, int s, uint8_t* __restrict__ act,
+                            unsigned long long* __restrict__ count) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool a = i < n && !(s & ((1 << level[i]) - 1));
+    if (i < n) act[i] = a;
+    const unsigned m = __ballot_sync(0xffffffffu, a);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(count, (unsigned long long)__popc(m));
+}
+
+}  // namespace
+
+struct BlockIntegrator {
+    int nlev = 7;
+    bool started = false;
+    DevBuf level, act, scal;  // scal: [0] delta bits, [1] active-count accumulator
+    unsigned long long* h_cnt = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long gen = ~0ull;
+    int cap_n = -1, cap_nlev = -1;
+    double last_updates = 0;
+    int captures = 0;
+
+    int nsub() const { return 1 << (nlev - 1); }
+
+    void levels_and_open(Simulation& S) {
+        cudaStream_t s = S.s();
+        unsigned long long* d = scal.as<unsigned long long>();
+        GF_CUDA(cudaMemsetAsync(d, 0x7f, sizeof(unsigned long long), s));
+        k_masked_min<<<div_up(S.n, 256), 256, 0, s>>>(S.n, S.dt_ind.as<double>(), nullptr, d);
+        GF_CHECK_LAUNCH();
+        k_levels<<<div_up(S.n, 256), 256, 0, s>>>(S.n, S.dt_ind.as<double>(), d, nlev, level.as<int8_t>());
+        GF_CHECK_LAUNCH();
+        k_kick_levels<<<div_up(S.n, 256), 256, 0, s>>>(S.n, S.vel.as<double>(), S.acc.as<double>(),
+                                                       level.as<int8_t>(), d, 0, 0);
+        GF_CHECK_LAUNCH();
+    }
+
+    void force(Simulation& S, const uint8_t* active, bool nosync) {
+        ForceArgs a{S.n, S.pos.as<double>(), S.vel.as<double>(), S.mass.as<double>(), S.kind.as<int8_t>(),
+                    S.u.as<double>(), S.theta, S.eps, S.gamma, S.alpha, S.beta, active, nosync ? 0 : 1, 1,
+                    nosync ? 0 : 1, S.acc.as<double>(), S.dt_ind.as<double>()};
+        a.sph_active = active;
+        a.nosync = nosync ? 1 : 0;
+        force_engine().evaluate(a, S.s());
+    }
+
+    void capture(Simulation& S) {
+        cudaStream_t s = S.s();
+        if (exec) {
+            cudaGraphExecDestroy(exec);
+            exec = nullptr;
+        }
+        Context& C = ctx();
+        force_engine().reserve_nosync(S.n);  // nothing may allocate inside the capture
+        const bool prof = C.prof.on;
+        C.prof.on = false;
+        unsigned long long* d = scal.as<unsigned long long>();
+        uint8_t* ac = act.as<uint8_t>();
+        GF_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeGlobal));
+        try {
+            for (int sub = 1; sub < nsub(); ++sub) {
+                k_drift_bits<<<div_up(S.n, 256), 256, 0, s>>>(S.n, S.pos.as<double>(), S.vel.as<double>(), d);
+                GF_CHECK_LAUNCH();
+                k_active_at<<<div_up(S.n, 256), 256, 0, s>>>(S.n, level.as<int8_t>(), sub, ac, d + 1);
+                GF_CHECK_LAUNCH();
+                force(S, ac, true);
+                k_kick_levels<<<div_up(S.n, 256), 256, 0, s>>>(S.n, S.vel.as<double>(), S.acc.as<double>(),
+                                                               level.as<int8_t>(), d, 1, sub);
+                GF_CHECK_LAUNCH();
+            }
+            k_drift_bits<<<div_up(S.n, 256), 256, 0, s>>>(S.n, S.pos.as<double>(), S.vel.as<double>(), d);
+            GF_CHECK_LAUNCH();
+        } catch (...) {
+            cudaGraph_t g;
+            cudaStreamEndCapture(s, &g);
+            if (g) cudaGraphDestroy(g);
+            C.prof.on = prof;
+            throw;
+        }
+        cudaGraph_t g;
+        GF_CUDA(cudaStreamEndCapture(s, &g));
+        GF_CUDA(cudaGraphInstantiate(&exec, g, 0));
+        GF_CUDA(cudaGraphDestroy(g));
+        C.prof.on = prof;
+        gen = g_alloc_generation;
+        cap_n = S.n;
+        cap_nlev = nlev;
+        ++captures;
+    }
+
+    // Advances nblocks blocks; returns particle-updates done (forces computed).
+    double run(Simulation& S, int nblocks) {
+        cudaStream_t s = S.s();
+        if (!h_cnt) GF_CUDA(cudaMallocHost(&h_cnt, 2 * sizeof(unsigned long long)));
+        level.get<int8_t>(S.n);
+        act.get<uint8_t>(S.n);
+        scal.get<unsigned long long>(2);
+        double updates = 0;
+        if (!started) {  // block start: forces of everybody on a rebuilt tree, levels, opening kicks
+            force(S, nullptr, false);
+            levels_and_open(S);
+            updates += S.n;
+            started = true;
+        }
+        for (int b = 0; b < nblocks; ++b) {
+            if (!exec || gen != g_alloc_generation || cap_n != S.n || cap_nlev != nlev) capture(S);
+            unsigned long long* d = scal.as<unsigned long long>();
+            GF_CUDA(cudaMemsetAsync(d + 1, 0, sizeof(unsigned long long), s));
+            GF_CUDA(cudaGraphLaunch(exec, s));
+            GF_CUDA(cudaMemcpyAsync(h_cnt, d, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+            force(S, nullptr, false);  // block end: synchronised, rebuilt tree, fresh neighbours
+            GF_CUDA(cudaStreamSynchronize(s));
+            double delta;
+            memcpy(&delta, &h_cnt[0], sizeof delta);
+            updates += double(h_cnt[1]) + S.n;
+            S.t += delta * nsub();
+            k_kick_levels<<<div_up(S.n, 256), 256, 0, s>>>(S.n, S.vel.as<double>(), S.acc.as<double>(),
+                                                           level.as<int8_t>(), d, 2, 0);  // closing
+            GF_CHECK_LAUNCH();
+            levels_and_open(S);  // new levels from the new dt_ind, opening kicks
+        }
+        GF_CUDA(cudaStreamSynchronize(s));
+        last_updates = updates;
+        return updates;
+    }
+};
+
+static BlockIntegrator g_block;
+
+double block_run(int nblocks, int nlev) {
+    if (g_block.nlev != nlev) {
+        g_block.nlev = nlev;
+        g_block.started = false;
+    }
+    return g_block.run(g_sim, nblocks);
+}
+
+void block_reset() { g_block.started = false; }
+
+// Fraction of particles on each level (levels 0..nlev-1) of the current block.
+void block_levels(int nlev, double* frac) {
+    Simulation& S = g_sim;
+    std::vector<int8_t> lv(S.n);
+    GF_CUDA(cudaMemcpy(lv.data(), g_block.level.p, S.n, cudaMemcpyDeviceToHost));
+    for (int j = 0; j < nlev; ++j) frac[j] = 0;
+    for (int8_t v : lv)
+        if (v >= 0 && v < nlev) frac[v] += 1.0 / S.n;
+}
+
+void sim_init_reset_blocks() { g_block.started = false; }
 
 void sim_init(int n, const double* pos, const double* vel, const double* mass, const int8_t* kind, const double* u,
               double theta, double eps, double gamma, double alpha, double beta) {
@@ -187,9 +404,12 @@ void sim_init(int n, const double* pos, const double* vel, const double* mass, c
     S.acc.get<double>(3 * size_t(n));
     S.dt_ind.get<double>(n);
     force_engine().n_total = -1;  // fresh force state (simulation.py:51-54)
+    g_block.started = false;
     S.dt_gas = INFINITY;
     S.accelerations(nullptr, 1, 1, 1);
 }
+
+double sim_updates() { return g_sim.updates; }
 
 double sim_step(double dt_max, int* substeps) {
     const double D = g_sim.step(dt_max);

@@ -73,9 +73,9 @@ __global__ void k_sph_kernel(int n, const double* __restrict__ r, const double* 
 template <class Idx>
 __global__ void k_sph_density(int n, int k, int ld, const double* __restrict__ pos, const double* __restrict__ mass,
                               const Idx* __restrict__ nb, const double* __restrict__ h,
-                              double* __restrict__ rho) {
+                              double* __restrict__ rho, const uint8_t* __restrict__ act) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || (act && !act[i])) return;
     const double xi = pos[3 * size_t(i)], yi = pos[3 * size_t(i) + 1], zi = pos[3 * size_t(i) + 2];
     const double hi = h[i];
     double s = 0.0;
@@ -120,9 +120,9 @@ __global__ void k_sph_force(int n, int k, int ld, const double* __restrict__ pos
                             const double* __restrict__ h, const double* __restrict__ rho,
                             const double* __restrict__ pr2, const double* __restrict__ cs, double alpha,
                             double beta, double* __restrict__ acc, double* __restrict__ dudt,
-                            double* __restrict__ dt_i, float* __restrict__ divv) {
+                            double* __restrict__ dt_i, float* __restrict__ divv, const uint8_t* __restrict__ act) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || (act && !act[i])) return;
     const double xi = pos[3 * size_t(i)], yi = pos[3 * size_t(i) + 1], zi = pos[3 * size_t(i) + 2];
     const double vxi = vel[3 * size_t(i)], vyi = vel[3 * size_t(i) + 1], vzi = vel[3 * size_t(i) + 2];
     const double hi = h[i], rhoi = rho[i], pri = pr2[i], ci = cs[i];
@@ -544,12 +544,13 @@ void sph_kernel_values(int n, const double* r, const double* h, double* w, doubl
 template <class Idx>
 void sph_forces(SphScratch& S, int n, int k, int ld, const double* pos, const double* vel, const double* mass,
                 const Idx* nb, const double* h, const double* u, double gamma, double alpha,
-                double beta, double* rho, double* acc, double* dudt, double* dt_i, cudaStream_t s, float* divv) {
+                double beta, double* rho, double* acc, double* dudt, double* dt_i, cudaStream_t s, float* divv,
+                const uint8_t* act) {
     if (n <= 0) return;
     const int grid = div_up(n, kThreads);
     {
         ProfScope ps(kStSphDensity, s);
-        k_sph_density<Idx><<<grid, kThreads, 0, s>>>(n, k, ld, pos, mass, nb, h, rho);
+        k_sph_density<Idx><<<grid, kThreads, 0, s>>>(n, k, ld, pos, mass, nb, h, rho, act);
         GF_CHECK_LAUNCH();
     }
     double* pr2 = S.pr2.get<double>(n);
@@ -558,15 +559,15 @@ void sph_forces(SphScratch& S, int n, int k, int ld, const double* pos, const do
     GF_CHECK_LAUNCH();
     ProfScope ps(kStSphForce, s);
     k_sph_force<Idx><<<grid, kThreads, 0, s>>>(n, k, ld, pos, vel, mass, nb, h, rho, pr2, cs, alpha, beta,
-                                               acc, dudt, dt_i, divv);
+                                               acc, dudt, dt_i, divv, act);
     GF_CHECK_LAUNCH();
 }
 template void sph_forces<int64_t>(SphScratch&, int, int, int, const double*, const double*, const double*,
                                   const int64_t*, const double*, const double*, double, double, double,
-                                  double*, double*, double*, double*, cudaStream_t, float*);
+                                  double*, double*, double*, double*, cudaStream_t, float*, const uint8_t*);
 template void sph_forces<int>(SphScratch&, int, int, int, const double*, const double*, const double*,
                               const int*, const double*, const double*, double, double, double,
-                              double*, double*, double*, double*, cudaStream_t, float*);
+                              double*, double*, double*, double*, cudaStream_t, float*, const uint8_t*);
 
 void knn_from_candidates(int n, int m, const double* pos, const int64_t* cand, int k, int64_t* nb,
                          double* dist, int* d_ok, cudaStream_t s) {
@@ -732,10 +733,10 @@ extern "C" int gf_sph_forces_noalloc_dev(int n, int k, const double* pos, const 
     double* cs = scratch + kNoallocMaxN;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int grid = div_up(n, kThreads);
-    k_sph_density<int64_t><<<grid, kThreads, 0, s>>>(n, k, k, pos, mass, nb, h, rho);
+    k_sph_density<int64_t><<<grid, kThreads, 0, s>>>(n, k, k, pos, mass, nb, h, rho, nullptr);
     k_sph_eos<<<grid, kThreads, 0, s>>>(n, rho, u, gamma, pr2, cs);
     k_sph_force<int64_t><<<grid, kThreads, 0, s>>>(n, k, k, pos, vel, mass, nb, h, rho, pr2, cs, alpha,
-                                                   beta, acc, dudt, dt_i, nullptr);
+                                                   beta, acc, dudt, dt_i, nullptr, nullptr);
     e = cudaGetLastError();
     if (e != cudaSuccess) return noalloc_fail(GF_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
     c.launches += 3;

@@ -387,6 +387,7 @@ __global__ void k_gather(int n, const int* __restrict__ perm, const double* __re
 
 struct MomentArgs {
     int nn;
+    const int* nn_dev;  // when set: node count read on the device
     bool refit;
     float theta;
     const int4* n_i4;
@@ -432,7 +433,7 @@ __device__ __forceinline__ void finalize(const MomentArgs& A, int k, double M, d
 
 __global__ void k_moments(MomentArgs A) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= A.nn) return;
+    if (k >= (A.nn_dev ? *A.nn_dev : A.nn)) return;
     const int4 q = A.n_i4[k];
     if (!(q.w & 1)) return;
     double M = 0, sx = 0, sy = 0, sz = 0;
@@ -486,6 +487,7 @@ __global__ void k_moments(MomentArgs A) {
 // shifted by the parallel-axis term. Float32 with Kahan-compensated sums (mixed form).
 struct QuadArgs {
     int nn;
+    const int* nn_dev;
     const int4* n_i4;
     const int* parent;
     const int* nchild;
@@ -511,7 +513,7 @@ struct QuadSum {
 
 __global__ void k_quad(QuadArgs A) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= A.nn) return;
+    if (k >= (A.nn_dev ? *A.nn_dev : A.nn)) return;
     const int4 q = A.n_i4[k];
     if (!(q.w & 1)) return;
     {
@@ -593,9 +595,9 @@ __global__ void k_walk_fill(int nn, const int4* __restrict__ n_i4, const int* __
                             float4* __restrict__ wgeo, int* __restrict__ leaf_of,
                             const float4* __restrict__ q4, const float2* __restrict__ qyz,
                             float4* __restrict__ wq, const int* __restrict__ parent, int* __restrict__ wparent,
-                            float* __restrict__ wt) {
+                            float* __restrict__ wt, const int* __restrict__ nn_dev) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nn) return;
+    if (k >= (nn_dev ? *nn_dev : nn)) return;
     const int4 q = n_i4[k];
     const int b = bfs[k];
     int first, code;
@@ -784,16 +786,18 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
         GF_CUDA(cudaStreamSynchronize(s));
     }
     nn = h_counts->total_nodes;
+    if (nn > node_cap) node_cap = nn + nn / 4 + 1024;  // headroom: later rebuilds rarely move buffers
+    const int cap = node_cap;
 
-    int4* i4 = n_i4.get<int4>(nn);
-    double4* cd = n_cd.get<double4>(nn);
-    float4* geo = n_geo.get<float4>(nn);
-    int* par = n_parent.get<int>(nn);
+    int4* i4 = n_i4.get<int4>(cap);
+    double4* cd = n_cd.get<double4>(cap);
+    float4* geo = n_geo.get<float4>(cap);
+    int* par = n_parent.get<int>(cap);
     k_emit<<<grid, kThreads, 0, s>>>(K, n, R, ld, ds, ns, nb, cnt, i4, cd, geo, par);
     GF_CHECK_LAUNCH();
     const int ngrid = div_up(nn, kThreads);
-    int* nch = n_nchild.get<int>(nn);
-    int* ctr = n_counter.get<int>(nn);
+    int* nch = n_nchild.get<int>(cap);
+    int* ctr = n_counter.get<int>(cap);
     k_nchild<<<ngrid, kThreads, 0, s>>>(nn, i4, nch, ctr);
     GF_CHECK_LAUNCH();
     k_leaf_sort<<<ngrid, kThreads, 0, s>>>(nn, i4, pm);
@@ -816,9 +820,9 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
     A.counter = ctr;
     A.n_cd = cd;
     A.n_geo = geo;
-    A.mom = n_mom.get<float4>(nn);
-    A.open_r = n_open.get<float>(nn);
-    A.ndisp = n_disp.get<float>(nn);
+    A.mom = n_mom.get<float4>(cap);
+    A.open_r = n_open.get<float>(cap);
+    A.ndisp = n_disp.get<float>(cap);
     A.perm = pm;
     A.pos = pos;
     A.mass = mass;
@@ -826,51 +830,54 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
     GF_CHECK_LAUNCH();
 
     if (quad) {
-        QuadArgs Q{nn, i4, par, nch, ctr, A.mom, pp, n_quad.get<float4>(nn), n_qyz.get<float2>(nn)};
+        QuadArgs Q{nn, nullptr, i4, par, nch, ctr, A.mom, pp, n_quad.get<float4>(cap), n_qyz.get<float2>(cap)};
         GF_CUDA(cudaMemsetAsync(ctr, 0, sizeof(int) * size_t(nn), s));
         k_quad<<<ngrid, kThreads, 0, s>>>(Q);
         GF_CHECK_LAUNCH();
     }
 
-    int* gf_ = gflag.get<int>(nn);
-    int* gs = gscan.get<int>(nn);
+    int* gf_ = gflag.get<int>(cap);
+    int* gs = gscan.get<int>(cap);
     k_group_flag<<<ngrid, kThreads, 0, s>>>(nn, group_max, i4, par, gf_);
     GF_CHECK_LAUNCH();
     exclusive_scan(gf_, gs, nn, &cnt->num_groups, s);
-    k_group_write<<<ngrid, kThreads, 0, s>>>(nn, gf_, gs, groups.get<int>(nn));
+    k_group_write<<<ngrid, kThreads, 0, s>>>(nn, gf_, gs, groups.get<int>(cap));
     GF_CHECK_LAUNCH();
 
-    uint64_t* bk = bfs_key.get<uint64_t>(nn);
-    int* bv = bfs_val.get<int>(nn);
+    uint64_t* bk = bfs_key.get<uint64_t>(cap);
+    int* bv = bfs_val.get<int>(cap);
     k_bfs_keys<<<ngrid, kThreads, 0, s>>>(nn, i4, bk, bv);
     GF_CHECK_LAUNCH();
-    radix_sort_pairs(bk, bv, bfs_key_alt.get<uint64_t>(nn), bfs_val_alt.get<int>(nn), nn, 0, 8, s);
-    int* bfs = n_bfs.get<int>(nn);
+    radix_sort_pairs(bk, bv, bfs_key_alt.get<uint64_t>(cap), bfs_val_alt.get<int>(cap), nn, 0, 8, s);
+    int* bfs = n_bfs.get<int>(cap);
     k_bfs_index<<<ngrid, kThreads, 0, s>>>(nn, bv, bfs);
     GF_CHECK_LAUNCH();
-    k_walk_fill<<<ngrid, kThreads, 0, s>>>(nn, i4, nch, bfs, A.mom, A.open_r, geo, w_a.get<float4>(nn),
-                                           w_b.get<float4>(nn), want_knn ? w_geo.get<float4>(nn) : nullptr,
+    k_walk_fill<<<ngrid, kThreads, 0, s>>>(nn, i4, nch, bfs, A.mom, A.open_r, geo, w_a.get<float4>(cap),
+                                           w_b.get<float4>(cap), want_knn ? w_geo.get<float4>(cap) : nullptr,
                                            want_knn ? leaf_of.get<int>(n) : nullptr,
                                            quad ? n_quad.as<float4>() : nullptr, quad ? n_qyz.as<float2>() : nullptr,
-                                           quad ? w_q.get<float4>(nn) : nullptr, par,
-                                           want_knn ? w_parent.get<int>(nn) : nullptr,
-                                           quad ? w_t.get<float>(nn) : nullptr);
+                                           quad ? w_q.get<float4>(cap) : nullptr, par,
+                                           want_knn ? w_parent.get<int>(cap) : nullptr,
+                                           quad ? w_t.get<float>(cap) : nullptr, nullptr);
     GF_CHECK_LAUNCH();
     valid = true;
 }
 
-void Octree::refit(const double* pos, const double* mass, cudaStream_t s) {
+void Octree::refit(const double* pos, const double* mass, cudaStream_t s, bool graph_safe) {
     ProfScope ps(kStTreeRefit, s);
     const int grid = div_up(n, kThreads);
-    const int ngrid = div_up(nn, kThreads);
+    const int span = graph_safe ? node_cap : nn;  // nodes covered by the launches
+    const int ngrid = div_up(span, kThreads);
+    const int* nn_dev = graph_safe ? &counts.as<TreeCounts>()->total_nodes : nullptr;
     float4* pp = p4.as<float4>();
     float* pd = pdisp.get<float>(n);
     k_gather<<<grid, kThreads, 0, s>>>(n, perm.as<int>(), pos, mass, xbuild.as<double>(), pp, pd,
                                        want_knn ? plo.get<float4>(n) : nullptr);
     GF_CHECK_LAUNCH();
-    GF_CUDA(cudaMemsetAsync(n_counter.as<int>(), 0, sizeof(int) * size_t(nn), s));
+    GF_CUDA(cudaMemsetAsync(n_counter.as<int>(), 0, sizeof(int) * size_t(span), s));
     MomentArgs A{};
     A.nn = nn;
+    A.nn_dev = nn_dev;
     A.refit = true;
     A.theta = theta_f;
     A.n_i4 = n_i4.as<int4>();
@@ -887,8 +894,9 @@ void Octree::refit(const double* pos, const double* mass, cudaStream_t s) {
     k_moments<<<ngrid, kThreads, 0, s>>>(A);
     GF_CHECK_LAUNCH();
     if (quad) {
-        QuadArgs Q{nn, A.n_i4, A.parent, A.nchild, A.counter, A.mom, pp, n_quad.as<float4>(), n_qyz.as<float2>()};
-        GF_CUDA(cudaMemsetAsync(A.counter, 0, sizeof(int) * size_t(nn), s));
+        QuadArgs Q{nn, nn_dev, A.n_i4, A.parent, A.nchild, A.counter, A.mom, pp, n_quad.as<float4>(),
+                   n_qyz.as<float2>()};
+        GF_CUDA(cudaMemsetAsync(A.counter, 0, sizeof(int) * size_t(span), s));
         k_quad<<<ngrid, kThreads, 0, s>>>(Q);
         GF_CHECK_LAUNCH();
     }
@@ -899,7 +907,7 @@ void Octree::refit(const double* pos, const double* mass, cudaStream_t s) {
                                            quad ? n_quad.as<float4>() : nullptr, quad ? n_qyz.as<float2>() : nullptr,
                                            quad ? w_q.as<float4>() : nullptr, A.parent,
                                            want_knn ? w_parent.as<int>() : nullptr,
-                                           quad ? w_t.as<float>() : nullptr);
+                                           quad ? w_t.as<float>() : nullptr, nn_dev);
     GF_CHECK_LAUNCH();
 }
 

@@ -37,6 +37,7 @@ struct Octree {
     int nn = 0;       // nodes
     int ng = 0;       // groups
     int max_depth = 0;
+    int node_cap = 0; // node buffers are sized to this (grows with headroom, never shrinks)
     float theta_f = 0.7f;
     bool valid = false;
     const uint8_t* active_ptr = nullptr;  // active flags of the current walk (device)
@@ -74,7 +75,9 @@ struct Octree {
     TreeCounts* h_counts = nullptr;  // pinned
 
     void build(int n, const double* pos, const double* mass, double theta, cudaStream_t s);
-    void refit(const double* pos, const double* mass, cudaStream_t s);
+    // graph_safe: grids sized to node_cap and node count read on the device, so the launch
+    // sequence stays valid (e.g. inside a captured CUDA graph) across later rebuilds.
+    void refit(const double* pos, const double* mass, cudaStream_t s, bool graph_safe = false);
     // Work list of groups with at least one active particle (active may be null).
     void prepare_walk(const uint8_t* active, cudaStream_t s);
     void walk(double eps, double* acc, cudaStream_t s);

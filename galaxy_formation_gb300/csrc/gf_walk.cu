@@ -390,7 +390,7 @@ void Octree::prepare_walk(const uint8_t* active, cudaStream_t s) {
     GF_CUDA(cudaMemsetAsync(&cnt->num_work, 0, 2 * sizeof(int), s));  // num_work, walk_next
     GF_CUDA(cudaMemsetAsync(&cnt->pairs, 0, sizeof(unsigned long long), s));
     ProfScope ps(kStGroupPrep, s);
-    const int cap = std::max(1, nn);
+    const int cap = std::max(1, node_cap);
     active_ptr = active;
     k_group_prep<<<4 * C.sms, 256, 0, s>>>(groups.as<int>(), n_i4.as<int4>(), p4.as<float4>(),
                                           perm.as<int>(), active, cnt, work.get<int4>(cap),
@@ -414,11 +414,11 @@ void Octree::walk(double eps, double* acc, cudaStream_t s) {
         k_walk<true><<<bps_quad * C.sms, kWalkWarps * 32, 0, s>>>(
             w_a.as<float4>(), w_b.as<float4>(), w_q.as<float4>(), w_t.as<float>(), p4.as<float4>(), perm.as<int>(),
             active_ptr,
-            work.as<int4>(), sphere.as<float4>(), counts.as<TreeCounts>(), nn, eps2, acc, C.d_status);
+            work.as<int4>(), sphere.as<float4>(), counts.as<TreeCounts>(), node_cap, eps2, acc, C.d_status);
     } else {
         k_walk<false><<<bps_mono * C.sms, kWalkWarps * 32, 0, s>>>(
             w_a.as<float4>(), w_b.as<float4>(), nullptr, nullptr, p4.as<float4>(), perm.as<int>(), active_ptr,
-            work.as<int4>(), sphere.as<float4>(), counts.as<TreeCounts>(), nn, eps2, acc, C.d_status);
+            work.as<int4>(), sphere.as<float4>(), counts.as<TreeCounts>(), node_cap, eps2, acc, C.d_status);
     }
     GF_CHECK_LAUNCH();
 }

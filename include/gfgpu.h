@@ -198,6 +198,19 @@ int gf_sim_init(int n, const double* pos, const double* vel, const double* mass,
  * (_thermodynamics, _stars). taken: its length; substeps: sub-steps done (1 for a global
  * step). */
 int gf_sim_step(double dt_max, double* taken, int* substeps);
+/* The batched form of the step loop (no reference counterpart): block time steps. Each
+ * particle sits on a power-of-two level j (step 2^j delta, delta = min dt_ind, j =
+ * floor(log2(dt_ind / delta)) clamped to [0, nlev-1]); a block is 2^(nlev-1) finest
+ * sub-steps, at each of which only the particles due (s mod 2^j == 0) get new forces
+ * (gravity on the refitted tree, SPH with the neighbours' last densities) and kicks. The
+ * inner sub-steps of a block run as one captured CUDA graph; block boundaries rebuild the
+ * tree and search neighbours afresh. updates: particle-updates done (forces computed). */
+int gf_sim_blocks(int nblocks, int nlev, double* updates);
+/* Fraction of the particles on each level 0..nlev-1 of the current block. */
+int gf_sim_levels(int nlev, double* frac);
+/* Particle-updates of the last gf_sim_step: particles that received freshly computed forces
+ * (the active set of every force evaluation, plus all gas whenever SPH ran). */
+double gf_sim_updates(void);
 /* Copies the state out (host pointers; any may be NULL): pos, vel, acc (n,3), dt_ind (n),
  * and the simulated time t. */
 int gf_sim_read(double* pos, double* vel, double* acc, double* dt_ind, double* t);
@@ -267,6 +280,9 @@ int gf_profile(int on);
 int gf_profile_stage(int stage, double* total_ms, int* launches);
 /* Kernels launched by the library since it was loaded. */
 long long gf_launch_count(void);
+/* The library's own CUDA stream (cudaStream_t as void*), on which the host-pointer entry
+ * points and the step loops run (NULL when no GPU is usable). */
+void* gf_stream(void);
 /* Particle-list pair interactions evaluated by the most recent gravity walk (synchronises). */
 long long gf_walk_pairs(void);
 /* Measures the float32 FFMA throughput of the GPU (TFLOP/s, an FMA counting 2 flops): the

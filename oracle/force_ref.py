@@ -136,3 +136,42 @@ class StepOracle:
         self.acc = self.accelerations(active=slow, rebuild=True, sph=False)
         self.vel[slow] += 0.5 * D * self.acc[slow]
         return D
+
+
+class BlockOracle:
+    """CPU restatement of the block time-step scheme of the library's batched form (power-of-two
+    levels, gravity of the particles due at each sub-step on a refitted tree, opening /
+    full / closing kicks). Gravity only: for particle sets without gas."""
+
+    def __init__(self, pos, vel, mass, theta, eps, nlev):
+        self.pos, self.vel, self.mass = pos.copy(), vel.copy(), mass
+        self.theta, self.eps, self.nlev = theta, eps, nlev
+        self.acc = np.zeros_like(pos)
+        self.t = 0.0
+        self._force(None, True)
+        self._levels_and_open()
+
+    def _force(self, active, rebuild):
+        oracle.accel_active(self.pos, self.mass, self.acc, self.theta, self.eps, active, rebuild)
+        a = np.sqrt(np.einsum("ij,ij->i", self.acc, self.acc))
+        self.dt_ind = 0.3 * np.sqrt(self.eps / np.maximum(a, 1e-30))
+
+    def _levels_and_open(self):
+        self.delta = self.dt_ind.min()
+        j = np.floor(np.log2(self.dt_ind / self.delta)).astype(int)
+        self.level = np.clip(j, 0, self.nlev - 1)
+        self.vel += (0.5 * self.delta * 2.0 ** self.level)[:, None] * self.acc
+
+    def block(self):
+        nsub = 1 << (self.nlev - 1)
+        step = self.delta * 2.0 ** self.level
+        for s in range(1, nsub):
+            self.pos += self.delta * self.vel
+            act = (s % (1 << self.level)) == 0
+            self._force(act.astype(np.uint8), False)
+            self.vel[act] += step[act][:, None] * self.acc[act]
+        self.pos += self.delta * self.vel
+        self._force(None, True)
+        self.vel += (0.5 * step)[:, None] * self.acc
+        self.t += self.delta * nsub
+        self._levels_and_open()
