@@ -1,25 +1,36 @@
 #!/usr/bin/env python
 """Benchmark: particle-updates/s of the gravity + SPH force evaluation at 1M particles.
 
-Workload (default): 1,000,000 particles (500,000 gas + 500,000 dark matter), the seeded
-synthetic disk + 1/r halo snapshot (galaxy_formation_gb300.synthetic, seed 3). One step =
-one full force evaluation of every particle: Barnes-Hut tree build + group walk (theta 0.7,
-eps 0.4 kpc, monopole, the reference's float32 arithmetic), full 48-candidate neighbour
-search of the gas, smoothing lengths, SPH density + pressure/viscosity forces (float64)
-and the time-step glue (simulation.py:61-95). One particle-update = one particle receiving
-a freshly computed total acceleration.
+Workload: 1,000,000 particles (500,000 gas + 500,000 dark matter), the seeded synthetic disk +
+1/r halo snapshot (galaxy_formation_gb300.synthetic, seed 3), eps 0.4 kpc. One step = one full
+force evaluation of every particle: Barnes-Hut tree build + group walk, full 48-candidate
+neighbour search of the gas, smoothing lengths, SPH density + pressure/viscosity forces and
+the time-step glue (simulation.py:61-95). One particle-update = one particle receiving a
+freshly computed total acceleration.
+
+Forms measured (same snapshot, same evaluation):
+  plain          the reference's arithmetic: float32 monopole walk at theta 0.7 (its
+                 default), float64 SPH, search radius from the previous h;
+  plain_matched  the same arithmetic at the opening angle whose gravity error against the
+                 float64 direct sum meets p99 <= 1e-3 (theta 0.15);
+  mixed_learned  the headline: quadrupole walk in float32 with Kahan tile sums at theta 0.5
+                 (p99 <= 1e-3), float32 + Kahan SPH, search radius from the learned MLP guess
+                 (trained first on pairs the simulator produced, on the GPU);
+plus the batched form (block time steps, CUDA-graph replay, autotuned) as particle-updates/s
+over a 64-sub-step block.
+
+`value` = mixed_learned, timed on the device with CUDA events on the launching stream around
+each step, inputs resident in HBM, L2 flushed (256 MB write) between steps; `e2e` = the same
+form through the C ABI with host buffers (copies in and out included). `--impl reference`
+times the reference's CPU algorithm on this host's cores (the oracle restatement of
+cpp/nbody.cpp + scipy cKDTree + the restated sph_forces) on the same workload.
+Multi-GPU (torchrun): independent replicas, one per GPU, no collective on the data path.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
-
-`value` is timed on the device with CUDA events around each step, inputs resident in HBM,
-L2 flushed (256 MB write) between steps; `e2e` is the same metric through the C ABI with
-host (pageable NumPy) buffers, copies in and out included. `--impl reference` times the
-reference's CPU algorithm on this host's cores (the oracle restatement of cpp/nbody.cpp +
-the reference's scipy cKDTree call + the restated SPH forces) on the same workload.
-Multi-GPU (torchrun): independent replicas, one per GPU, no collective on the data path.
 """
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -38,14 +49,27 @@ UNIT = "particle-updates/s"
 CONFIG_IDX = 2
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
+# (theta, quadrupole walk, float32 SPH, h guess mode)
+FORMS = {
+    "plain": (0.7, 0, 0, 0),
+    "plain_matched": (0.15, 0, 0, 0),
+    "mixed_learned": (0.5, 1, 1, 2),
+}
+# flops per interaction (an FMA counting 2): monopole pair (cpp/nbody.cpp:398-402 in float32)
+# and the softened quadrupole node term of the mixed walk
+FLOPS_MONO, FLOPS_QUAD = 20, 57
+
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--scale", type=float, default=1.0, help="shrink the workload (testing only)")
+    ap.add_argument("--forms", default="plain,plain_matched,mixed_learned",
+                    help="comma list of forms to time (the last one given is the headline)")
+    ap.add_argument("--blocks", type=int, default=3, help="64-sub-step blocks of the batched form (0: skip)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
@@ -201,126 +225,265 @@ def load_traffic():
     return {}
 
 
-def run_gpu(args, world, rank, local):
-    import torch
+class Gpu:
+    """The workload resident on one GPU and the library's entry points around it."""
 
-    from galaxy_formation_gb300 import _lib, build, params
-    from galaxy_formation_gb300.engine import Engine
+    def __init__(self, args, local):
+        import torch
 
-    build.build()
-    lib = _lib.load()
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    d = workload(args.scale)
-    n = len(d["mass"])
-    n_gas = int((d["kind"] == 0).sum())
-    T = {k: torch.from_numpy(np.ascontiguousarray(d[k])).to(dev) for k in ("pos", "vel", "mass", "kind", "u")}
-    acc = torch.empty((n, 3), dtype=torch.float64, device=dev)
-    dt_ind = torch.empty(n, dtype=torch.float64, device=dev)
-    stream = torch.cuda.current_stream(dev)
-    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
+        from galaxy_formation_gb300 import _lib, build, params
 
-    def step():
-        st = lib.gf_accelerations_dev(n, T["pos"].data_ptr(), T["vel"].data_ptr(), T["mass"].data_ptr(),
-                                      T["kind"].data_ptr(), T["u"].data_ptr(), params.THETA, params.EPS,
-                                      params.GAMMA, params.ALPHA, params.BETA, None, 1, 1, 1,
-                                      acc.data_ptr(), dt_ind.data_ptr(), stream.cuda_stream)
+        build.build()
+        self.torch, self._lib, self.params = torch, _lib, params
+        self.lib = _lib.load()
+        torch.cuda.set_device(local)
+        self.dev = torch.device("cuda", local)
+        self.d = workload(args.scale)
+        self.n = len(self.d["mass"])
+        self.n_gas = int((self.d["kind"] == 0).sum())
+        self.T = {k: torch.from_numpy(np.ascontiguousarray(self.d[k])).to(self.dev)
+                  for k in ("pos", "vel", "mass", "kind", "u")}
+        self.acc = torch.empty((self.n, 3), dtype=torch.float64, device=self.dev)
+        self.dt = torch.empty(self.n, dtype=torch.float64, device=self.dev)
+        self.stream = torch.cuda.current_stream(self.dev)
+        self.flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=self.dev)  # 256 MB > L2
+
+    def set_form(self, form):
+        theta, quad, sph32, hguess = FORMS[form]
+        L, lib = self._lib, self.lib
+        lib.gf_set_option(L.OPT_GRAVITY_QUAD, quad)
+        lib.gf_set_option(L.OPT_SPH_FLOAT32, sph32)
+        lib.gf_set_option(L.OPT_HGUESS, hguess)
+        return theta
+
+    def step(self, theta, pos=None, kind=None, sph=1):
+        T, p = self.T, self.params
+        st = self.lib.gf_accelerations_dev(
+            self.n, (pos if pos is not None else T["pos"]).data_ptr(), T["vel"].data_ptr(), T["mass"].data_ptr(),
+            (kind if kind is not None else T["kind"]).data_ptr(), T["u"].data_ptr(), theta, p.EPS, p.GAMMA,
+            p.ALPHA, p.BETA, None, 1, sph, 1, self.acc.data_ptr(), self.dt.data_ptr(), self.stream.cuda_stream)
         if st:
-            _lib.check(st)
+            self._lib.check(st)
 
-    for _ in range(args.warmup):
-        step()
-        flush.zero_()
-    torch.cuda.synchronize()
+    def knn_iters(self):
+        info = [ctypes.c_int(), ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()]
+        self.lib.gf_force_info(*[ctypes.byref(x) for x in info])
+        return info[3].value / max(1, info[0].value)
+
+    def time_form(self, form, steps, warmup):
+        """Device time of `steps` evaluations (CUDA events on the launching stream, L2 flushed
+        between steps), stages, launches, walk interactions."""
+        torch, lib, L = self.torch, self.lib, self._lib
+        theta = self.set_form(form)
+        for _ in range(warmup):
+            self.step(theta)
+            self.flush.zero_()
+        torch.cuda.synchronize()
+        lib.gf_profile(1)
+        launches0 = lib.gf_launch_count()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        torch.cuda.synchronize()
+        for e0, e1 in evs:
+            e0.record(self.stream)
+            self.step(theta)
+            e1.record(self.stream)
+            self.flush.zero_()
+        torch.cuda.synchronize()
+        launches = lib.gf_launch_count() - launches0
+        times = [e0.elapsed_time(e1) for e0, e1 in evs]
+        stages = {}
+        for i, name in enumerate(L.STAGES):
+            ms, cnt = ctypes.c_double(), ctypes.c_int()
+            lib.gf_profile_stage(i, ctypes.byref(ms), ctypes.byref(cnt))
+            if cnt.value:
+                stages[name] = {"ms_per_launch": ms.value / cnt.value, "launches": cnt.value}
+        lib.gf_profile(0)
+        return {"theta": theta, "times_ms": times, "launches": launches, "stages": stages,
+                "pairs": lib.gf_walk_pairs(), "qpairs": lib.gf_walk_quad_pairs(), "knn_iters": self.knn_iters()}
+
+    def gravity_error(self, form, targets, exact):
+        """p99 / median relative error of the form's gravity against the float64 direct sum:
+        the fused evaluation with every particle flagged dark matter (no hydro term)."""
+        theta = self.set_form(form)
+        dm = torch_full_like(self.torch, self.T["kind"], 2)
+        self.step(theta, kind=dm)
+        a = self.acc.cpu().numpy()[targets]
+        e = np.linalg.norm(a - exact, axis=1) / np.linalg.norm(exact, axis=1)
+        return float(np.percentile(e, 99)), float(np.median(e))
+
+    def train_hguess(self, rows=2_000_000, collect_steps=4):
+        """Learned smoothing-length guess: (features, converged log h) pairs from the
+        simulator's own evaluations of drifting copies of the snapshot, then Adam on the GPU."""
+        torch, lib, L = self.torch, self.lib, self._lib
+        theta = self.set_form("plain")
+        lib.gf_set_option(L.OPT_HGUESS, 0)
+        pos = self.T["pos"].clone()
+        self.step(theta, pos=pos)
+        lib.gf_set_option(L.OPT_COLLECT, rows)
+        for _ in range(collect_steps):
+            pos += 0.5 * self.dt[:, None] * self.T["vel"]
+            self.step(theta, pos=pos)
+        torch.cuda.synchronize()
+        m = lib.gf_mlp_collected(None, None, 0)
+        X = np.zeros((m, 4), np.float32)
+        Y = np.zeros(m, np.float32)
+        lib.gf_mlp_collected(X.ctypes.data, Y.ctypes.data, m)
+        L.check(lib.gf_mlp_init(7))
+        mu, sd = X.mean(0), X.std(0) + 1e-6
+        L.check(lib.gf_mlp_set_norm(mu.astype(np.float32), sd.astype(np.float32), float(Y.mean()), float(Y.std())))
+        loss0, loss1 = ctypes.c_double(), ctypes.c_double()
+        t0 = time.perf_counter()
+        L.check(lib.gf_mlp_train(1, 4096, 1e-3, ctypes.byref(loss0)))
+        L.check(lib.gf_mlp_train(2000, 4096, 2e-3, ctypes.byref(loss1)))
+        train_s = time.perf_counter() - t0
+        lib.gf_set_option(L.OPT_COLLECT, 0)  # stop collecting (clears the pairs)
+        # iterations of the count-to-48 search on a drifted snapshot: previous h, cell density
+        # alone, learned guess (the converged neighbours are the same in all three)
+        its = {}
+        for mode, name in ((0, "previous_h"), (1, "cell_density"), (2, "learned")):
+            lib.gf_set_option(L.OPT_HGUESS, 0)
+            self.step(theta, pos=pos)
+            nxt = pos + 0.5 * self.dt[:, None] * self.T["vel"]
+            lib.gf_set_option(L.OPT_HGUESS, mode)
+            lib.gf_profile(1)
+            self.step(theta, pos=nxt)
+            torch.cuda.synchronize()
+            ms, cnt = ctypes.c_double(), ctypes.c_int()
+            lib.gf_profile_stage(L.STAGES.index("knn"), ctypes.byref(ms), ctypes.byref(cnt))
+            lib.gf_profile(0)
+            its[name] = {"iterations_per_gas": self.knn_iters(), "knn_ms": ms.value}
+        lib.gf_set_option(L.OPT_HGUESS, 0)
+        return {"training_rows": int(m), "loss_start": loss0.value, "loss_end": loss1.value,
+                "train_s": train_s, "adam_steps": 2000, "batch": 4096, "search_on_drifted_snapshot": its}
+
+    def batched(self, blocks, nlev=7):
+        """Block time steps at the mixed + learned form: autotune, one warm block, then
+        `blocks` blocks timed with CUDA events on the library's stream."""
+        torch, lib, L, p = self.torch, self.lib, self._lib, self.params
+        theta = self.set_form("mixed_learned")
+        d = self.d
+        L.check(lib.gf_sim_init(self.n, d["pos"], d["vel"], d["mass"], d["kind"], d["u"], theta, p.EPS,
+                                p.GAMMA, p.ALPHA, p.BETA))
+        chunk = np.zeros(nlev - 1, np.int32)
+        every, gms = ctypes.c_int(), ctypes.c_double()
+        t0 = time.perf_counter()
+        L.check(lib.gf_sim_block_autotune(nlev, chunk.ctypes.data, ctypes.byref(every), ctypes.byref(gms)))
+        tune_s = time.perf_counter() - t0
+        upd = ctypes.c_double()
+        L.check(lib.gf_sim_blocks(1, nlev, ctypes.byref(upd)))
+        frac = np.zeros(nlev)
+        L.check(lib.gf_sim_levels(nlev, frac))
+        s = torch.cuda.ExternalStream(lib.gf_stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        launches0 = lib.gf_launch_count()
+        e0.record(s)
+        L.check(lib.gf_sim_blocks(blocks, nlev, ctypes.byref(upd)))
+        e1.record(s)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        return {"value": upd.value / (ms * 1e-3), "unit": UNIT, "blocks": blocks, "substeps_per_block": 1 << (nlev - 1),
+                "levels": nlev, "level_fractions": [round(float(x), 5) for x in frac],
+                "updates": upd.value, "ms": ms, "ms_per_block": ms / blocks,
+                "autotune": {"chunk_per_bin": chunk.tolist(), "rebuild_every": every.value, "seconds": tune_s},
+                "launches_outside_graphs": lib.gf_launch_count() - launches0,
+                "note": "an update = a particle given a freshly computed force at one of its own steps; "
+                        "each block = 63 sub-steps replayed as one CUDA graph + a full evaluation"}
+
+
+def torch_full_like(torch, t, v):
+    return torch.full_like(t, v)
+
+
+def run_gpu(args, world, rank, local):
+    G = Gpu(args, local)
+    torch, lib, L, params = G.torch, G.lib, G._lib, G.params
+    n, n_gas = G.n, G.n_gas
+    forms = [f for f in args.forms.split(",") if f]
+    head = forms[-1]
+
+    learned = None
+    if any(FORMS[f][3] == 2 for f in forms):
+        learned = G.train_hguess()
+
     barrier(world)
-
     vis = os.environ.get("CUDA_VISIBLE_DEVICES")
     gpu_index = vis.split(",")[local] if vis else str(local)
-    clocks = ClockSampler(gpu_index)
-    lib.gf_profile(1)
-    launches0 = lib.gf_launch_count()
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in range(args.steps)]
-    torch.cuda.synchronize()
-    clocks.start()
-    for e0, e1 in evs:
-        e0.record(stream)
-        step()
-        e1.record(stream)
-        flush.zero_()
-    torch.cuda.synchronize()
-    clk = clocks.stop()
+    res = {}
+    clk = None
+    for f in forms:
+        steps = args.steps if FORMS[f][0] >= 0.3 else max(3, args.steps // 5)
+        if f == head:
+            clocks = ClockSampler(gpu_index)
+            clocks.start()
+        res[f] = G.time_form(f, steps, args.warmup)
+        if f == head:
+            clk = clocks.stop()
     barrier(world)
-    launches = lib.gf_launch_count() - launches0
-    times = [e0.elapsed_time(e1) for e0, e1 in evs]
-    total_ms = allmax(world, sum(times))
-    ms_per_step = total_ms / args.steps
-    value = world * n / (ms_per_step * 1e-3)
-
-    import ctypes
-
-    stages = {}
-    for i, name in enumerate(_lib.STAGES):
-        ms, cnt = ctypes.c_double(), ctypes.c_int()
-        lib.gf_profile_stage(i, ctypes.byref(ms), ctypes.byref(cnt))
-        if cnt.value:
-            stages[name] = {"ms_per_launch": ms.value / cnt.value, "launches": cnt.value}
-    lib.gf_profile(0)
-    pairs = lib.gf_walk_pairs()
-    info = [ctypes.c_int(), ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()]
-    lib.gf_force_info(*[ctypes.byref(x) for x in info])
+    for f in forms:
+        r = res[f]
+        r["ms_per_step"] = allmax(world, sum(r["times_ms"])) / len(r["times_ms"])
+        r["value"] = world * n / (r["ms_per_step"] * 1e-3)
 
     if rank != 0:
         return
 
-    # roofline of the dominant kernel
+    # accuracy of each form's gravity against the float64 direct sum (2000 random targets)
+    tgt = np.random.default_rng(11).choice(n, 2000, replace=False)
+    exact = np.zeros((len(tgt), 3))
+    L.check(lib.gf_accel_direct_targets(n, G.d["pos"], G.d["mass"], len(tgt), tgt.astype(np.int64), exact,
+                                        params.EPS))
+    for f in forms:
+        res[f]["p99"], res[f]["median"] = G.gravity_error(f, tgt, exact)
+
+    batched = G.batched(args.blocks) if args.blocks > 0 else None
+
+    H = res[head]
+    # roofline of the dominant kernel of the headline form
     peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
     hbm = peaks.get("hbm_gbs", 6800.0)
     hbm_src = "measured (MEASURED_PEAKS.json)" if "hbm_gbs" in peaks else "fallback"
     fp32 = ctypes.c_double()
     lib.gf_fp32_peak(ctypes.byref(fp32))
+    stages = H["stages"]
     kernel_stages = {k: v for k, v in stages.items() if k in ("walk", "knn", "sph_density", "sph_force", "verlet")}
     dom = max(kernel_stages, key=lambda k: kernel_stages[k]["ms_per_launch"] * kernel_stages[k]["launches"])
     t_launch = kernel_stages[dom]["ms_per_launch"] * 1e-3
-    # algorithmic work per launch (unit figures are stated in the design doc)
-    bytes_per_gas = {"knn": 24 + 48 * 4 + 8, "sph_density": 32 * 4 + 24 + 8 + 8 + 8,
-                     "sph_force": 32 * 4 + 24 + 24 + 8 + 8 + 8 + 8 + 8 + 24 + 8 + 8, "verlet": 48 * 4 + 24 + 32 * 4 + 8}
     traffic_db = load_traffic()
-    traffic = traffic_db.get(dom, {}).get("bytes_per_launch") if traffic_db.get("particles") == n else None
+    tkey = f"{head}:{dom}"
+    traffic = traffic_db.get(tkey, {}).get("bytes_per_launch") if traffic_db.get("particles") == n else None
+    quad = FORMS[head][1] == 1
     if dom == "walk":
-        work = 20.0 * pairs
-        achieved = work / t_launch / 1e12
-        roof = {"kernel": "k_walk_mono", "bound": "fp32", "achieved": achieved, "peak": fp32.value,
-                "unit": "TFLOP/s", "frac": achieved / fp32.value, "traffic": traffic,
+        mono = H["pairs"] - H["qpairs"]
+        flops = FLOPS_MONO * mono + FLOPS_QUAD * H["qpairs"]
+        achieved = flops / t_launch / 1e12
+        roof = {"kernel": "k_walk<QUAD>" if quad else "k_walk<mono>", "bound": "fp32", "achieved": achieved,
+                "peak": fp32.value, "unit": "TFLOP/s", "frac": achieved / fp32.value, "traffic": traffic,
                 "peak_source": "measured float32 FFMA throughput of this GPU (gf_fp32_peak)",
-                "work_per_launch": {"pair_interactions": pairs, "flops_per_pair": 20}}
+                "work_per_launch": {"monopole_interactions": mono, "quadrupole_interactions": H["qpairs"],
+                                    "flops_per_monopole": FLOPS_MONO, "flops_per_quadrupole": FLOPS_QUAD}}
     else:
+        bytes_per_gas = {"knn": 24 + 48 * 4 + 8, "sph_density": 32 * 4 + 24 + 8 + 8 + 8,
+                         "sph_force": 32 * 4 + 24 + 24 + 8 + 8 + 8 + 8 + 8 + 24 + 8 + 8,
+                         "verlet": 48 * 4 + 24 + 32 * 4 + 8}
         work = bytes_per_gas[dom] * n_gas
         achieved = work / t_launch / 1e9
         roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": traffic, "peak_source": hbm_src,
                 "work_per_launch": {"bytes": work, "bytes_per_gas_particle": bytes_per_gas[dom]}}
 
-    # accuracy of the gravity against the float64 direct sum (2000 random targets)
-    eng = Engine()
-    agrav = np.zeros_like(d["pos"])
-    eng.gravity(d["pos"], d["mass"], agrav, params.THETA, params.EPS)
-    tgt = np.random.default_rng(11).choice(n, 2000, replace=False)
-    exact = eng.gravity_direct_targets(d["pos"], d["mass"], tgt, params.EPS)
-    err = np.linalg.norm(agrav[tgt] - exact, axis=1) / np.linalg.norm(exact, axis=1)
-
     e2e = None
     if not args.no_e2e:
-        host = {k: np.ascontiguousarray(d[k]) for k in ("pos", "vel", "mass", "kind", "u")}
+        theta = G.set_form(head)
+        host = {k: np.ascontiguousarray(G.d[k]) for k in ("pos", "vel", "mass", "kind", "u")}
         a_h = np.empty((n, 3))
         dt_h = np.empty(n)
 
         def host_step():
             st = lib.gf_accelerations(n, host["pos"], host["vel"], host["mass"], host["kind"], host["u"],
-                                      params.THETA, params.EPS, params.GAMMA, params.ALPHA, params.BETA,
+                                      theta, params.EPS, params.GAMMA, params.ALPHA, params.BETA,
                                       None, 1, 1, 1, a_h, dt_h)
             if st:
-                _lib.check(st)
+                L.check(st)
 
         host_step()
         ts = []
@@ -330,35 +493,47 @@ def run_gpu(args, world, rank, local):
             ts.append(time.perf_counter() - t0)
         e2e = {"value": world * n / statistics.mean(ts), "unit": UNIT,
                "h2d_bytes_per_step": n * (24 + 24 + 8 + 1 + 8), "d2h_bytes_per_step": n * (24 + 8),
-               "ms_per_step": statistics.mean(ts) * 1e3}
+               "ms_per_step": statistics.mean(ts) * 1e3, "form": head}
 
     cpu = None
     if world == 1 and not args.no_cpu:
-        sec, cores = time_cpu(d, 3, 1)
+        sec, cores = time_cpu(G.d, 3, 1)
         cpu = {"value": n / sec, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"3 full force evaluations of the {n:,}-particle workload (median) after 1 "
                          "warm-up: oracle restatement of cpp/nbody.cpp (OpenMP) + scipy cKDTree "
-                         "(workers=-1) + restated sph_forces (OpenMP)"}
+                         "(workers=-1) + restated sph_forces (OpenMP), theta 0.7"}
+
+    def summary(f):
+        r = res[f]
+        th, quad_f, sph32, hg = FORMS[f]
+        out = {"value": r["value"], "ms_per_step": r["ms_per_step"], "theta": th,
+               "gravity": "quadrupole float32 + Kahan" if quad_f else "monopole float32 (reference)",
+               "sph": "float32 + Kahan" if sph32 else "float64 (reference)",
+               "h_guess": ["previous h", "cell density", "learned MLP"][hg],
+               "grav_p99_rel_err_vs_f64_direct": r["p99"], "grav_median_rel_err": r["median"],
+               "stages_ms": {k: round(v["ms_per_launch"], 4) for k, v in r["stages"].items()},
+               "knn_iterations_per_gas": r["knn_iters"], "walk_interactions": r["pairs"],
+               "walk_quadrupole_interactions": r["qpairs"], "steps": len(r["times_ms"])}
+        return out
 
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32 gravity + f64 SPH", "data": "synthetic",
+        "metric": METRIC, "value": H["value"], "unit": UNIT, "n_gpus": world, "steps": len(H["times_ms"]),
+        "warmup": args.warmup, "ms_per_step": H["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (Kahan) gravity + f32 (Kahan) SPH, f64 positions" if FORMS[head][2] else "f32 gravity + f64 SPH",
+        "data": "synthetic",
         "config": {"workload": workload_name(n_gas, n - n_gas), "particles": n, "gas": n_gas,
-                   "theta": params.THETA, "eps_kpc": params.EPS_KPC, "form": "plain (reference arithmetic)",
+                   "form": head, "theta": FORMS[head][0], "eps_kpc": params.EPS_KPC,
                    "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
         "roofline": roof,
         "cpu_baseline": cpu,
         "e2e": e2e,
-        "gpu_launches": launches,
+        "gpu_launches": H["launches"],
         "clocks": clk,
-        "stages_ms": {k: round(v["ms_per_launch"], 4) for k, v in stages.items()},
-        "accuracy": {"grav_p99_rel_err_vs_f64_direct": float(np.percentile(err, 99)),
-                     "grav_median": float(np.median(err)), "targets": 2000},
-        "knn_iterations_per_gas": info[3].value / max(1, info[0].value),
-        "walk": {"pair_interactions": pairs,
-                 "tflops": 20.0 * pairs / (stages["walk"]["ms_per_launch"] * 1e-3) / 1e12
-                 if "walk" in stages else None, "fp32_peak_tflops": fp32.value},
+        "forms": {f: summary(f) for f in forms},
+        "speedup_vs_plain": {f"{head}/{f}": H["value"] / res[f]["value"] for f in forms if f != head},
+        "batched": batched,
+        "learned_h": learned,
     }
     print(json.dumps(line), flush=True)
 

@@ -30,6 +30,7 @@ SIGNATURES = {
     "gf_last_error": ([], ctypes.c_char_p),
     "gf_tree_size": ([ctypes.POINTER(_ci), ctypes.POINTER(_ci)], _ci),
     "gf_tree_export": ([_i32, _f32, _i32, _i32], _ci),
+    "gf_tree_rebuild_captured": ([_ci, _dbl, _dbl, _cd], _ci),
     "gf_accel_active_dev": ([_ci, _vp, _vp, _vp, _cd, _cd, _vp, _ci, _vp], _ci),
     "gf_accel_direct_dev": ([_ci, _vp, _vp, _vp, _cd, _vp], _ci),
     "gf_accel_direct_targets": ([_ci, _dbl, _dbl, _ci, _i64, _dbl, _cd], _ci),
@@ -57,6 +58,8 @@ SIGNATURES = {
     "gf_sim_read": ([_vp, _vp, _vp, _vp, ctypes.POINTER(_cd)], _ci),
     "gf_sim_blocks": ([_ci, _ci, ctypes.POINTER(_cd)], _ci),
     "gf_sim_updates": ([], _cd),
+    "gf_sim_block_config": ([_vp, _ci, _ci], _ci),
+    "gf_sim_block_autotune": ([_ci, _vp, _vp, _vp], _ci),
     "gf_stream": ([], _vp),
     "gf_sim_levels": ([_ci, _dbl], _ci),
     "gf_set_option": ([_ci, _cd], _ci),
@@ -74,6 +77,7 @@ SIGNATURES = {
     "gf_profile_stage": ([_ci, ctypes.POINTER(_cd), ctypes.POINTER(_ci)], _ci),
     "gf_launch_count": ([], ctypes.c_longlong),
     "gf_walk_pairs": ([], ctypes.c_longlong),
+    "gf_walk_quad_pairs": ([], ctypes.c_longlong),
     "gf_fp32_peak": ([ctypes.POINTER(_cd)], _ci),
 }
 
@@ -81,6 +85,7 @@ OPT_SPH_FLOAT32 = 0
 OPT_GRAVITY_QUAD = 1
 OPT_HGUESS = 2
 OPT_COLLECT = 3
+OPT_WALK_CHUNK = 4
 MLP_PARAMS = 4545
 
 STAGES = ["tree_build", "tree_refit", "walk", "group_prep", "knn", "knn_tree", "sph_density",

@@ -69,7 +69,7 @@ void accel_active_device(int n, const double* pos, const double* mass, double* a
         T.build(n, pos, mass, theta, s);
     else
         T.refit(pos, mass, s);
-    T.prepare_walk(active, s);
+    T.prepare_walk(active, s, force_engine().walk_chunk);
     T.walk(eps, acc, s);
 }
 
@@ -176,10 +176,11 @@ int gf_tree_size(int* num_nodes, int* num_groups) {
     return guarded([&] {
         Octree& T = gravity_tree();
         int nn = 0, ng = 0;
-        if (T.valid) {
+        if (T.valid) {  // device counts: also right after a captured rebuild
+            GF_CUDA(cudaDeviceSynchronize());
             TreeCounts h;
             GF_CUDA(cudaMemcpy(&h, T.counts.as<TreeCounts>(), sizeof h, cudaMemcpyDeviceToHost));
-            nn = T.nn;
+            nn = h.total_nodes;
             ng = h.num_groups;
         }
         if (num_nodes) *num_nodes = nn;
@@ -192,9 +193,9 @@ int gf_tree_export(int32_t* ints, float* floats, int32_t* order, int32_t* groups
         Octree& T = gravity_tree();
         require(T.valid, "no tree");
         GF_CUDA(cudaDeviceSynchronize());
-        const int nn = T.nn, n = T.n;
         TreeCounts h;
         GF_CUDA(cudaMemcpy(&h, T.counts.as<TreeCounts>(), sizeof h, cudaMemcpyDeviceToHost));
+        const int nn = h.total_nodes, n = T.n;
         std::vector<int4> i4(nn);
         std::vector<float4> mom(nn), geo(nn);
         std::vector<float> open(nn);
@@ -213,6 +214,44 @@ int gf_tree_export(int32_t* ints, float* floats, int32_t* order, int32_t* groups
         }
         GF_CUDA(cudaMemcpy(order, T.perm.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
         GF_CUDA(cudaMemcpy(groups, T.groups.p, sizeof(int32_t) * h.num_groups, cudaMemcpyDeviceToHost));
+    });
+}
+
+int gf_tree_rebuild_captured(int n, const double* pos, const double* mass, double theta) {
+    return guarded([&] {
+        Octree& T = gravity_tree();
+        require(pos && mass, "null array");
+        require(T.valid && T.n == n, "build the tree for n particles first");
+        cudaStream_t s = ctx().stream;
+        double* d_pos = upload(g_st.pos, pos, 3 * size_t(n), s);
+        double* d_mass = upload(g_st.mass, mass, size_t(n), s);
+        T.reserve_graph_build();
+        GF_CUDA(cudaStreamSynchronize(s));
+        Context& C = ctx();
+        const bool prof = C.prof.on;
+        C.prof.on = false;
+        cudaGraph_t g = nullptr;
+        GF_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeGlobal));
+        g_no_alloc = true;
+        try {
+            T.build(n, d_pos, d_mass, theta, s, true);
+        } catch (...) {
+            g_no_alloc = false;
+            cudaStreamEndCapture(s, &g);
+            if (g) cudaGraphDestroy(g);
+            C.prof.on = prof;
+            throw;
+        }
+        g_no_alloc = false;
+        C.prof.on = prof;
+        GF_CUDA(cudaStreamEndCapture(s, &g));
+        cudaGraphExec_t exec = nullptr;
+        GF_CUDA(cudaGraphInstantiate(&exec, g, 0));
+        GF_CUDA(cudaGraphDestroy(g));
+        const cudaError_t e = cudaGraphLaunch(exec, s);
+        cudaGraphExecDestroy(exec);
+        GF_CUDA(e);
+        collect_status(s);
     });
 }
 
@@ -475,16 +514,21 @@ int gf_fp32_peak(double* tflops) {
     });
 }
 
-long long gf_walk_pairs(void) {
+static long long walk_counter(bool quad_only) {
     unsigned long long p = 0;
     guarded([&] {
         Octree* T = last_walked();
         if (!T || !T->valid) return;
         GF_CUDA(cudaDeviceSynchronize());
-        GF_CUDA(cudaMemcpy(&p, &T->counts.as<TreeCounts>()->pairs, sizeof p, cudaMemcpyDeviceToHost));
+        TreeCounts* c = T->counts.as<TreeCounts>();
+        GF_CUDA(cudaMemcpy(&p, quad_only ? &c->qpairs : &c->pairs, sizeof p, cudaMemcpyDeviceToHost));
     });
     return (long long)p;
 }
+
+long long gf_walk_pairs(void) { return walk_counter(false); }
+
+long long gf_walk_quad_pairs(void) { return walk_counter(true); }
 
 int gf_set_option(int key, double value) {
     return guarded([&] {
@@ -506,6 +550,10 @@ int gf_set_option(int key, double value) {
                 }
                 break;
             }
+            case GF_OPT_WALK_CHUNK:
+                require(value >= 0 && value <= 64, "walk chunk is 0..64");
+                F.walk_chunk = int(value);
+                break;
             default: throw Error(GF_ERR_ARG, "unknown option");
         }
     });
@@ -518,6 +566,7 @@ double gf_get_option(int key) {
         case GF_OPT_GRAVITY_QUAD: return F.gravity_quad;
         case GF_OPT_HGUESS: return F.hguess;
         case GF_OPT_COLLECT: return double(F.collect_n);
+        case GF_OPT_WALK_CHUNK: return F.walk_chunk;
         default: return -1.0;
     }
 }
@@ -549,6 +598,25 @@ int gf_sim_blocks(int nblocks, int nlev, double* updates) {
         require(simulation_ready(), "gf_sim_init first");
         const double u = block_run(nblocks, nlev);
         if (updates) *updates = u;
+        collect_status(ctx().stream);
+    });
+}
+
+int gf_sim_block_config(const int* chunk, int nbins, int rebuild_every) {
+    return guarded([&] {
+        require(!chunk || (nbins >= 1 && nbins <= 8), "need 1 <= nbins <= 8");
+        require(rebuild_every >= 0, "rebuild_every < 0");
+        if (chunk)
+            for (int b = 0; b < nbins; ++b) require(chunk[b] >= 0 && chunk[b] <= 64, "chunk out of [0, 64]");
+        block_config(chunk, nbins, rebuild_every);
+    });
+}
+
+int gf_sim_block_autotune(int nlev, int* chunk, int* rebuild_every, double* graph_ms) {
+    return guarded([&] {
+        require(nlev >= 2 && nlev <= 8, "need 2 <= nlev <= 8");
+        require(simulation_ready(), "gf_sim_init first");
+        block_autotune(nlev, chunk, rebuild_every, graph_ms);
         collect_status(ctx().stream);
     });
 }

@@ -40,6 +40,9 @@ struct Error : std::runtime_error {
 // Bumped whenever any DevBuf (re)allocates: a captured CUDA graph that bakes buffer
 // addresses is valid only while this stays unchanged.
 extern unsigned long long g_alloc_generation;
+// Set while a CUDA graph is being captured: a buffer that would have to grow then is an error
+// (an allocation inside a capture fails, and the captured addresses must stay valid).
+extern bool g_no_alloc;
 
 // A grow-only device allocation.
 struct DevBuf {
@@ -49,6 +52,7 @@ struct DevBuf {
     T* get(size_t count) {
         const size_t need = count * sizeof(T) + 256;
         if (need > bytes) {
+            if (g_no_alloc) throw Error(GF_ERR_CAPACITY, "a device buffer would grow inside a captured step");
             if (p) GF_CUDA(cudaFree(p));
             p = nullptr;
             bytes = 0;
@@ -121,10 +125,50 @@ __device__ __forceinline__ void raise_status(uint32_t* st, uint32_t bit) {
 // Device-wide exclusive scan of int32 (n may be 0). `total` (device) receives the sum.
 void exclusive_scan(const int* in, int* out, int n, int* total, cudaStream_t s);
 
+// Sizes the scratch of exclusive_scan / radix_sort_pairs for inputs of up to n elements.
+void reserve_scan_sort(int n);
+
 // Stable LSD radix sort of (key, value) pairs on bits [bit_lo, bit_hi) of the keys.
 // Results end in keys/vals (the alternate buffers are scratch of the same size).
 void radix_sort_pairs(uint64_t* keys, int* vals, uint64_t* keys_alt, int* vals_alt, int n,
                       int bit_lo, int bit_hi, cudaStream_t s);
+
+// A subset of particles to process: idx[0 .. *count) (device memory, count read on the
+// device so the launch stays valid inside a captured graph); idx == null means all n.
+struct Subset {
+    const int* idx = nullptr;
+    const int* count = nullptr;
+};
+
+// Item t of a launch over n slots: false when past the subset; `base` maps t -> particle
+// when processing everything (e.g. a visiting order; null = identity).
+__device__ __forceinline__ bool subset_item(const Subset& S, int t, int n, const int* base, int& i) {
+    if (S.idx) {
+        if (t >= *S.count) return false;
+        i = S.idx[t];
+        return true;
+    }
+    if (t >= n) return false;
+    i = base ? base[t] : t;
+    return true;
+}
+
+// A CUDA event for host-side timing on a stream.
+struct Event {
+    cudaEvent_t e = nullptr;
+    Event() { GF_CUDA(cudaEventCreate(&e)); }
+    ~Event() {
+        if (e) cudaEventDestroy(e);
+    }
+    Event(const Event&) = delete;
+    Event& operator=(const Event&) = delete;
+    void record(cudaStream_t s) { GF_CUDA(cudaEventRecord(e, s)); }
+    float since(const Event& a) const {  // ms from a to this (both recorded and complete)
+        float ms = 0.f;
+        GF_CUDA(cudaEventElapsedTime(&ms, a.e, e));
+        return ms;
+    }
+};
 
 // Timed stages (CUDA events recorded on the launching stream while profiling is on).
 enum Stage {

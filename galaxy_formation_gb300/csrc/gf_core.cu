@@ -17,6 +17,7 @@ namespace gf {
 
 static Context g_ctx;
 unsigned long long g_alloc_generation = 0;
+bool g_no_alloc = false;
 
 Context& ctx() { return g_ctx; }
 
@@ -276,6 +277,14 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_downsweep(
             vout[pos] = v[s];
         }
     }
+}
+
+void reserve_scan_sort(int n) {
+    Context& c = g_ctx;
+    const int rs_tiles = div_up(std::max(n, 1), kRsTile);
+    c.sort_tmp.get<int>(size_t(256) * rs_tiles * 2);
+    const int scan_n = std::max(n, 256 * rs_tiles);
+    c.scan_tmp.get<int>(size_t(div_up(scan_n, kScanTile)) + 1);
 }
 
 void radix_sort_pairs(uint64_t* keys, int* vals, uint64_t* keys_alt, int* vals_alt, int n,

@@ -66,13 +66,14 @@ constexpr int kSelWarps = 8;
 __global__ void __launch_bounds__(kSelWarps * 32) k_verlet_select(
     int ng, const int* __restrict__ gidx, const int* __restrict__ row, const int* __restrict__ cache,
     const int* __restrict__ loc, const double* __restrict__ gpos, int* __restrict__ nb, double* __restrict__ d31,
-    int* __restrict__ fail, const uint8_t* __restrict__ gact) {
-    __shared__ double s_key[kSelWarps][64];
+    int* __restrict__ fail, Subset sub) {
+    __shared__ unsigned long long s_key[kSelWarps][64];  // float64 d^2 bit patterns (see below)
     __shared__ int s_tag[kSelWarps][64];
     __shared__ int s_loc[kSelWarps][64];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int i = blockIdx.x * kSelWarps + w; i < ng; i += gridDim.x * kSelWarps) {
-        if (gact && !gact[i]) continue;
+    for (int q = blockIdx.x * kSelWarps + w;; q += gridDim.x * kSelWarps) {
+        int i;
+        if (!subset_item(sub, q, ng, nullptr, i)) break;
         const int r = row[gidx[i]];
         if (r < 0) continue;  // handled by k_verlet_prep's flag
         const double xi = gpos[3 * size_t(i)], yi = gpos[3 * size_t(i) + 1], zi = gpos[3 * size_t(i) + 2];
@@ -90,7 +91,7 @@ __global__ void __launch_bounds__(kSelWarps * 32) k_verlet_select(
                     ++valid;
                 }
             }
-            s_key[w][jj] = d2;
+            s_key[w][jj] = (unsigned long long)__double_as_longlong(d2);
             s_tag[w][jj] = jj;
             s_loc[w][jj] = j;
         }
@@ -100,14 +101,15 @@ __global__ void __launch_bounds__(kSelWarps * 32) k_verlet_select(
             if (lane == 0) *fail = 1;
             continue;
         }
-        // bitonic sort of 64 (key, slot) pairs
+        // bitonic sort of 64 (key, slot) pairs; non-negative float64 keys compare as their bit
+        // patterns (integer compares: the float64 pipe is narrow on this GPU)
         for (int size = 2; size <= 64; size <<= 1) {
             for (int stride = size >> 1; stride > 0; stride >>= 1) {
                 const int t = lane;
                 const int a = 2 * stride * (t / stride) + (t % stride);
                 const int b = a + stride;
                 const bool up = (a & size) == 0;
-                const double ka = s_key[w][a], kb = s_key[w][b];
+                const unsigned long long ka = s_key[w][a], kb = s_key[w][b];
                 const int ta = s_tag[w][a], tb = s_tag[w][b];
                 const bool gt = ka > kb || (ka == kb && ta > tb);
                 if (gt == up) {
@@ -120,7 +122,7 @@ __global__ void __launch_bounds__(kSelWarps * 32) k_verlet_select(
             }
         }
         nb[size_t(i) * kCand + lane] = s_loc[w][s_tag[w][lane]];
-        if (lane == kNgb - 1) d31[i] = sqrt(s_key[w][lane]);
+        if (lane == kNgb - 1) d31[i] = sqrt(__longlong_as_double((long long)s_key[w][lane]));
         __syncwarp();
     }
 }
@@ -143,9 +145,9 @@ __global__ void k_guess(int ng, const int* __restrict__ gidx, const double* __re
 }
 
 __global__ void k_smoothing(int ng, const double* __restrict__ d31, double eps, const int* __restrict__ gidx,
-                            double* __restrict__ h, double* __restrict__ hprev, const uint8_t* __restrict__ gact) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ng || (gact && !gact[i])) return;
+                            double* __restrict__ h, double* __restrict__ hprev, Subset sub) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!subset_item(sub, i, ng, nullptr, i)) return;
     const double v = fmax(0.5 * d31[i], 0.5 * eps);  // simulation.py:84
     h[i] = v;
     hprev[gidx[i]] = 0.5 * d31[i] > 0 ? 0.5 * d31[i] : v;
@@ -161,9 +163,23 @@ __global__ void k_collect(int ng, long long base, const float* __restrict__ X, c
     colT[r] = float(log(0.5 * d31[i]));
 }
 
-__global__ void k_scatter_f(int ng, const int* __restrict__ gidx, const float* __restrict__ v, float* __restrict__ out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < ng) out[gidx[i]] = v[i];
+__global__ void k_scatter_f(int ng, const int* __restrict__ gidx, const float* __restrict__ v, float* __restrict__ out,
+                            Subset sub) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (subset_item(sub, i, ng, nullptr, i)) out[gidx[i]] = v[i];
+}
+
+// gas-local flags of the particles due, in the visiting order (order: position -> particle)
+__global__ void k_flag_in_order(int ng, const int* __restrict__ order, const uint8_t* __restrict__ gact,
+                                int* __restrict__ flag) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < ng) flag[t] = gact[order ? order[t] : t] ? 1 : 0;
+}
+
+__global__ void k_compact(int ng, const int* __restrict__ order, const int* __restrict__ flag,
+                          const int* __restrict__ scan, int* __restrict__ list) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < ng && flag[t]) list[scan[t]] = order ? order[t] : t;
 }
 
 __global__ void k_gas_active(int ng, const int* __restrict__ gidx, const uint8_t* __restrict__ active,
@@ -177,41 +193,67 @@ __global__ void k_fill(int n, double* __restrict__ a, double v) {
     if (i < n) a[i] = v;
 }
 
+// dtmin_bits (may be null): block minimum of the Courant steps, one atomic per block
 __global__ void k_scatter_sph(int ng, const int* __restrict__ gidx, const double* __restrict__ a,
                               const double* __restrict__ dti, double* __restrict__ acc_sph,
                               double* __restrict__ dt_courant, unsigned long long* __restrict__ dtmin_bits,
-                              const uint8_t* __restrict__ gact) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+                              Subset sub) {
+    __shared__ double s_min[kThreads / 32];
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
     double v = INFINITY;
-    if (i < ng && !(gact && !gact[i])) {
+    if (subset_item(sub, i, ng, nullptr, i)) {
         const int g = gidx[i];
         for (int c = 0; c < 3; ++c) acc_sph[3 * size_t(g) + c] = a[3 * size_t(i) + c];
         dt_courant[g] = dti[i];
         v = dti[i];
     }
+    if (!dtmin_bits) return;
 #pragma unroll
     for (int o = 16; o; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
-    if ((threadIdx.x & 31) == 0 && v >= 0) atomicMin(dtmin_bits, __double_as_longlong(v));
+    if ((threadIdx.x & 31) == 0) s_min[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < kThreads / 32; ++w) v = fmin(v, s_min[w]);
+        if (v >= 0) atomicMin(dtmin_bits, __double_as_longlong(v));
+    }
 }
 
+// f32 (mixed form): |a| and the gravitational step criterion in float32 (two float64
+// square roots and a division per particle are the float64 pipe's bottleneck here)
+// only: when set, the particles whose terms changed (inactive rows would be recomputed to
+// the values they hold); amax_bits (block maximum, one atomic per block) may then be null.
 __global__ void k_combine(int n, const double* __restrict__ ag, const double* __restrict__ as,
                           const double* __restrict__ dtc, double eps, double* __restrict__ acc,
-                          double* __restrict__ dt_ind, unsigned long long* __restrict__ amax_bits) {
+                          double* __restrict__ dt_ind, unsigned long long* __restrict__ amax_bits, int f32,
+                          const uint8_t* __restrict__ only) {
+    __shared__ double s_max[kThreads / 32];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double m = 0;
-    if (i < n) {
+    if (i < n && !(only && !only[i])) {
         double a2 = 0;
         for (int c = 0; c < 3; ++c) {
             const double v = ag[3 * size_t(i) + c] + as[3 * size_t(i) + c];
             acc[3 * size_t(i) + c] = v;
             a2 += v * v;
         }
-        m = sqrt(a2);
-        dt_ind[i] = fmin(0.3 * sqrt(eps / fmax(m, 1e-30)), dtc[i]);
+        if (f32) {
+            const float mf = sqrtf(float(a2));
+            m = mf;
+            dt_ind[i] = fmin(double(0.3f * sqrtf(float(eps) / fmaxf(mf, 1e-30f))), dtc[i]);
+        } else {
+            m = sqrt(a2);
+            dt_ind[i] = fmin(0.3 * sqrt(eps / fmax(m, 1e-30)), dtc[i]);
+        }
     }
+    if (!amax_bits) return;
 #pragma unroll
     for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(amax_bits, __double_as_longlong(m));
+    if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < kThreads / 32; ++w) m = fmax(m, s_max[w]);
+        atomicMax(amax_bits, __double_as_longlong(m));  // |a| >= 0: bit order = numeric order
+    }
 }
 
 __global__ void k_finish(HydroScalars* sc, double eps) {
@@ -249,26 +291,33 @@ void ForceEngine::evaluate(const ForceArgs& a, cudaStream_t s) {
 
     // gravity (simulation.py:64)
     Octree& T = grav;
-    if (a.nosync) {
-        if (a.rebuild || !T.valid || T.n != n) throw Error(GF_ERR_ARG, "a synchronisation-free evaluation refits");
-        T.refit(a.pos, a.mass, s, true);
+    if (a.nosync) {  // inside a captured graph: the tree of the last regular build, rebuilt or refitted
+        if (!T.valid || T.n != n) throw Error(GF_ERR_ARG, "a synchronisation-free evaluation needs a built tree");
+        if (a.rebuild)
+            T.build(n, a.pos, a.mass, a.theta, s, true);
+        else
+            T.refit(a.pos, a.mass, s);
     } else if (a.rebuild || !T.valid || T.n != n || T.quad != (gravity_quad != 0)) {
         T.quad = gravity_quad != 0;
         T.build(n, a.pos, a.mass, a.theta, s);
     } else {
         T.refit(a.pos, a.mass, s);
     }
-    T.prepare_walk(a.active, s);
+    T.prepare_walk(a.active, s, a.walk_chunk ? a.walk_chunk : walk_chunk);
     T.walk(a.eps, acc_grav.as<double>(), s);
 
     if (a.sph) hydro(a, s);
 
     // combination (simulation.py:68-71)
-    GF_CUDA(cudaMemsetAsync(&sc->amax_bits, 0, sizeof(unsigned long long), s));
+    if (!a.nosync) GF_CUDA(cudaMemsetAsync(&sc->amax_bits, 0, sizeof(unsigned long long), s));
+    // inside a captured block only the active rows change, and nothing reads dt_grav
+    const bool only_active = a.nosync && a.active;
     k_combine<<<div_up(n, kThreads), kThreads, 0, s>>>(n, acc_grav.as<double>(), acc_sph.as<double>(),
                                                        dt_courant.as<double>(), a.eps, a.acc, a.dt_ind,
-                                                       &sc->amax_bits);
+                                                       only_active ? nullptr : &sc->amax_bits,
+                                                       gravity_quad ? 1 : 0, only_active ? a.active : nullptr);
     GF_CHECK_LAUNCH();
+    if (a.nosync) return;  // the host reads no scalars inside a captured block
     k_finish<<<1, 1, 0, s>>>(sc, a.eps);
     GF_CHECK_LAUNCH();
     GF_CUDA(cudaMemcpyAsync(scalars_h, sc, sizeof(HydroScalars), cudaMemcpyDeviceToHost, s));
@@ -319,23 +368,37 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
     const int ggrid = div_up(ng, kThreads);
     int* nb = nb48.get<int>(size_t(ng) * kCand);
     double* d31 = dsel.get<double>(ng);
-    uint8_t* ga = nullptr;
+    // partial: the gas due, compacted in the visiting order of the last neighbour-search tree
+    Subset sub;
     if (partial) {
-        ga = gact.get<uint8_t>(ng);
+        uint8_t* ga = gact.get<uint8_t>(ng);
         k_gas_active<<<ggrid, kThreads, 0, s>>>(ng, gi, a.sph_active, ga);
         GF_CHECK_LAUNCH();
+        const int* vorder = order_ng == ng ? knn_tree.perm.as<int>() : nullptr;
+        int* fl2 = aflag.get<int>(ng);
+        int* sc2 = ascan.get<int>(ng);
+        int* lst = alist.get<int>(ng);
+        k_flag_in_order<<<ggrid, kThreads, 0, s>>>(ng, vorder, ga, fl2);
+        GF_CHECK_LAUNCH();
+        exclusive_scan(fl2, sc2, ng, &sc->nact, s);
+        k_compact<<<ggrid, kThreads, 0, s>>>(ng, vorder, fl2, sc2, lst);
+        GF_CHECK_LAUNCH();
+        sub = Subset{lst, &sc->nact};
     }
     bool have_nb = false;
     if (!a.fresh_nb && cache_valid) {
-        int* lc = loc.as<int>();
-        GF_CUDA(cudaMemsetAsync(lc, 0xff, sizeof(int) * size_t(n), s));
-        GF_CUDA(cudaMemsetAsync(&sc->fail, 0, sizeof(int), s));
-        k_verlet_prep<<<ggrid, kThreads, 0, s>>>(ng, gi, row.as<int>(), lc, &sc->fail);
-        GF_CHECK_LAUNCH();
+        // inside a captured block the gas set is the cached one: local index == cache row
+        int* lc = a.nosync ? row.as<int>() : loc.as<int>();
+        if (!a.nosync) {
+            GF_CUDA(cudaMemsetAsync(lc, 0xff, sizeof(int) * size_t(n), s));
+            GF_CUDA(cudaMemsetAsync(&sc->fail, 0, sizeof(int), s));
+            k_verlet_prep<<<ggrid, kThreads, 0, s>>>(ng, gi, row.as<int>(), lc, &sc->fail);
+            GF_CHECK_LAUNCH();
+        }
         const int blocks = std::min(div_up(ng, kSelWarps), 16 * ctx().sms);
         ProfScope pv(kStVerlet, s);
         k_verlet_select<<<blocks, kSelWarps * 32, 0, s>>>(ng, gi, row.as<int>(), cache.as<int>(), lc, gp, nb,
-                                                          d31, &sc->fail, ga);
+                                                          d31, &sc->fail, sub);
         GF_CHECK_LAUNCH();
         if (a.nosync) {  // the gas set is the cached one: every particle keeps its candidates
             have_nb = true;
@@ -380,7 +443,7 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
         order_ng = ng;
     }
     double* hh = h.get<double>(ng);
-    k_smoothing<<<ggrid, kThreads, 0, s>>>(ng, d31, a.eps, gi, hh, h_prev.as<double>(), ga);
+    k_smoothing<<<ggrid, kThreads, 0, s>>>(ng, d31, a.eps, gi, hh, h_prev.as<double>(), sub);
     GF_CHECK_LAUNCH();
     have_hprev = true;
 
@@ -393,15 +456,15 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
         // visit the gas in the Morton order of the last neighbour-search tree (same gas set)
         const int* order = order_ng == ng ? knn_tree.perm.as<int>() : nullptr;
         sph_forces32<int>(sph32, ng, kNgb, kCand, order, gp, gv, gm, nb, hh, gu, a.gamma, a.alpha, a.beta, r,
-                          gacc_, du, dti, s, dv, ga);
+                          gacc_, du, dti, s, dv, sub);
     } else {
         sph_forces<int>(sph, ng, kNgb, kCand, gp, gv, gm, nb, hh, gu, a.gamma, a.alpha, a.beta, r, gacc_, du, dti,
-                        s, dv, ga);
+                        s, dv, sub);
     }
-    k_scatter_f<<<ggrid, kThreads, 0, s>>>(ng, gi, dv, divv_prev.as<float>());
+    k_scatter_f<<<ggrid, kThreads, 0, s>>>(ng, gi, dv, divv_prev.as<float>(), sub);
     GF_CHECK_LAUNCH();
     have_divv = true;
-    k_scatter_sph<<<ggrid, kThreads, 0, s>>>(ng, gi, gacc_, dti, as, dtc, &sc->dtmin_bits, ga);
+    k_scatter_sph<<<ggrid, kThreads, 0, s>>>(ng, gi, gacc_, dti, as, dtc, a.nosync ? nullptr : &sc->dtmin_bits, sub);
     GF_CHECK_LAUNCH();
 }
 

@@ -11,6 +11,7 @@ struct HydroScalars {
     unsigned long long amax_bits;    // max |a| (float64 bits, non-negative)
     unsigned long long dtmin_bits;   // min Courant step of the gas (float64 bits)
     unsigned long long knn_iters;    // search-radius iterations of the last full search
+    int nact;                        // gas due in a partial (block time-step) call
     double dt_grav, dt_gas;
 };
 
@@ -32,12 +33,16 @@ struct ForceArgs {
     // no host synchronisation (for CUDA-graph capture): gas set, neighbour cache and tree are
     // those of the last regular call; gravity refits with device-side node counts
     int nosync = 0;
+    // walk work items of <= walk_chunk active particles with their own spheres (0: the
+    // reference's groups); used with an active set
+    int walk_chunk = 0;
 };
 
 struct ForceEngine {
     // options (gf_set_option)
     int sph_float32 = 0;     // 1: mixed-precision SPH (float32 + Kahan), 0: float64
     int gravity_quad = 0;    // 1: quadrupole moments + Kahan tile sums, 0: the reference's monopole
+    int walk_chunk = 0;      // walk items for active-set walks (0: the reference's groups)
     int hguess = 0;          // start of the neighbour-count iteration: 0 previous h, 1 cell
                              // density only, 2 the learned guess (MLP)
     long long collect_cap = 0, collect_n = 0;  // (features, log h) training pairs kept
@@ -54,14 +59,20 @@ struct ForceEngine {
     DevBuf acc_grav, acc_sph, dt_courant, h_prev, row, loc, cache;
     DevBuf flag, scan, gidx, gpos, gvel, gmass, gu_, nb48, dsel, rguess, h, rho, gacc, dudt, dt_i;
     DevBuf scalars;
-    DevBuf divv_prev, gdivv, hX, hY, hrg, colX, colT, gact;
+    DevBuf divv_prev, gdivv, hX, hY, hrg, colX, colT, gact, aflag, ascan, alist;
     HydroScalars* scalars_h = nullptr;  // pinned copy, valid after the stream synchronises
 
     void evaluate(const ForceArgs& a, cudaStream_t s);
     // allocates the buffers that only synchronisation-free evaluations touch
+    // every buffer a captured (synchronisation-free) evaluation touches, at its final size
     void reserve_nosync(int n) {
-        grav.pdisp.get<float>(n);
-        if (ng > 0) gact.get<uint8_t>(ng);
+        grav.reserve_graph_build();
+        if (ng > 0) {
+            gact.get<uint8_t>(ng);
+            aflag.get<int>(ng);
+            ascan.get<int>(ng);
+            alist.get<int>(ng);
+        }
     }
     void hydro(const ForceArgs& a, cudaStream_t s);
 };
@@ -72,6 +83,8 @@ ForceEngine& force_engine();
 void sim_init(int n, const double* pos, const double* vel, const double* mass, const int8_t* kind, const double* u,
               double theta, double eps, double gamma, double alpha, double beta);
 double sim_step(double dt_max, int* substeps);
+void block_config(const int* chunk, int nbins, int rebuild_every);
+void block_autotune(int nlev, int* chunk, int* rebuild_every, double* graph_ms);
 double sim_updates();
 void sim_read(double* pos, double* vel, double* acc, double* dt_ind, double* t);
 // Block time steps (the batched form): advances nblocks blocks of 2^(nlev-1) sub-steps;

@@ -244,18 +244,30 @@ __global__ void k_active_at(int n, const int8_t* __restrict__ level, int s, uint
 
 }  // namespace
 
+// Launch shape of the batched step, per sub-step bin (bin = number of trailing zero bits of
+// the sub-step index: levels 0..bin are due). Chosen by BlockIntegrator::autotune.
+struct BlockTuning {
+    int chunk[8] = {4, 8, 8, 16, 16, 32, 64, 64};  // walk items of <= chunk active particles (0: groups)
+    int rebuild_every = 8;  // captured tree rebuild every this many sub-steps (0: refit only)
+};
+
 struct BlockIntegrator {
     int nlev = 7;
     bool started = false;
     DevBuf level, act, scal;  // scal: [0] delta bits, [1] active-count accumulator
+    DevBuf save_pos, save_vel, tune_acc;
     unsigned long long* h_cnt = nullptr;
     cudaGraphExec_t exec = nullptr;
     unsigned long long gen = ~0ull;
     int cap_n = -1, cap_nlev = -1;
     double last_updates = 0;
     int captures = 0;
+    BlockTuning tune;
+    bool tune_changed = true;
+    double last_graph_ms = 0;  // device time of the last replayed graph
 
     int nsub() const { return 1 << (nlev - 1); }
+    static int bin_of(int sub) { return std::min(7, __builtin_ctz(unsigned(sub))); }
 
     void levels_and_open(Simulation& S) {
         cudaStream_t s = S.s();
@@ -270,12 +282,15 @@ struct BlockIntegrator {
         GF_CHECK_LAUNCH();
     }
 
-    void force(Simulation& S, const uint8_t* active, bool nosync) {
+    // nosync: inside the captured graph (rebuild = captured tree rebuild, else refit);
+    // otherwise a regular evaluation of everybody on a rebuilt tree with fresh neighbours
+    void force(Simulation& S, const uint8_t* active, bool nosync, bool rebuild = false, int chunk = 0) {
         ForceArgs a{S.n, S.pos.as<double>(), S.vel.as<double>(), S.mass.as<double>(), S.kind.as<int8_t>(),
-                    S.u.as<double>(), S.theta, S.eps, S.gamma, S.alpha, S.beta, active, nosync ? 0 : 1, 1,
-                    nosync ? 0 : 1, S.acc.as<double>(), S.dt_ind.as<double>()};
+                    S.u.as<double>(), S.theta, S.eps, S.gamma, S.alpha, S.beta, active,
+                    nosync ? (rebuild ? 1 : 0) : 1, 1, nosync ? 0 : 1, S.acc.as<double>(), S.dt_ind.as<double>()};
         a.sph_active = active;
         a.nosync = nosync ? 1 : 0;
+        a.walk_chunk = chunk;
         force_engine().evaluate(a, S.s());
     }
 
@@ -292,13 +307,15 @@ struct BlockIntegrator {
         unsigned long long* d = scal.as<unsigned long long>();
         uint8_t* ac = act.as<uint8_t>();
         GF_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeGlobal));
+        g_no_alloc = true;
         try {
             for (int sub = 1; sub < nsub(); ++sub) {
                 k_drift_bits<<<div_up(S.n, 256), 256, 0, s>>>(S.n, S.pos.as<double>(), S.vel.as<double>(), d);
                 GF_CHECK_LAUNCH();
                 k_active_at<<<div_up(S.n, 256), 256, 0, s>>>(S.n, level.as<int8_t>(), sub, ac, d + 1);
                 GF_CHECK_LAUNCH();
-                force(S, ac, true);
+                const bool rb = tune.rebuild_every > 0 && sub % tune.rebuild_every == 0;
+                force(S, ac, true, rb, tune.chunk[bin_of(sub)]);
                 k_kick_levels<<<div_up(S.n, 256), 256, 0, s>>>(S.n, S.vel.as<double>(), S.acc.as<double>(),
                                                                level.as<int8_t>(), d, 1, sub);
                 GF_CHECK_LAUNCH();
@@ -306,12 +323,14 @@ struct BlockIntegrator {
             k_drift_bits<<<div_up(S.n, 256), 256, 0, s>>>(S.n, S.pos.as<double>(), S.vel.as<double>(), d);
             GF_CHECK_LAUNCH();
         } catch (...) {
-            cudaGraph_t g;
+            g_no_alloc = false;
+            cudaGraph_t g = nullptr;
             cudaStreamEndCapture(s, &g);
             if (g) cudaGraphDestroy(g);
             C.prof.on = prof;
             throw;
         }
+        g_no_alloc = false;
         cudaGraph_t g;
         GF_CUDA(cudaStreamEndCapture(s, &g));
         GF_CUDA(cudaGraphInstantiate(&exec, g, 0));
@@ -320,31 +339,40 @@ struct BlockIntegrator {
         gen = g_alloc_generation;
         cap_n = S.n;
         cap_nlev = nlev;
+        tune_changed = false;
         ++captures;
+    }
+
+    void start(Simulation& S) {  // block start: forces of everybody on a rebuilt tree, levels, opening kicks
+        level.get<int8_t>(S.n);
+        act.get<uint8_t>(S.n);
+        scal.get<unsigned long long>(2);
+        if (!h_cnt) GF_CUDA(cudaMallocHost(&h_cnt, 2 * sizeof(unsigned long long)));
+        force(S, nullptr, false);
+        levels_and_open(S);
+        started = true;
     }
 
     // Advances nblocks blocks; returns particle-updates done (forces computed).
     double run(Simulation& S, int nblocks) {
         cudaStream_t s = S.s();
-        if (!h_cnt) GF_CUDA(cudaMallocHost(&h_cnt, 2 * sizeof(unsigned long long)));
-        level.get<int8_t>(S.n);
-        act.get<uint8_t>(S.n);
-        scal.get<unsigned long long>(2);
         double updates = 0;
-        if (!started) {  // block start: forces of everybody on a rebuilt tree, levels, opening kicks
-            force(S, nullptr, false);
-            levels_and_open(S);
+        if (!started) {
+            start(S);
             updates += S.n;
-            started = true;
         }
+        Event e0, e1;
         for (int b = 0; b < nblocks; ++b) {
-            if (!exec || gen != g_alloc_generation || cap_n != S.n || cap_nlev != nlev) capture(S);
+            if (!exec || gen != g_alloc_generation || cap_n != S.n || cap_nlev != nlev || tune_changed) capture(S);
             unsigned long long* d = scal.as<unsigned long long>();
             GF_CUDA(cudaMemsetAsync(d + 1, 0, sizeof(unsigned long long), s));
+            e0.record(s);
             GF_CUDA(cudaGraphLaunch(exec, s));
+            e1.record(s);
             GF_CUDA(cudaMemcpyAsync(h_cnt, d, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
             force(S, nullptr, false);  // block end: synchronised, rebuilt tree, fresh neighbours
             GF_CUDA(cudaStreamSynchronize(s));
+            last_graph_ms = e1.since(e0);
             double delta;
             memcpy(&delta, &h_cnt[0], sizeof delta);
             updates += double(h_cnt[1]) + S.n;
@@ -358,6 +386,96 @@ struct BlockIntegrator {
         last_updates = updates;
         return updates;
     }
+
+    // Autotuner. The state (positions, velocities, time) is saved first and restored at the
+    // end; the next block then starts with a full evaluation, so tuning leaves no trace in the
+    // trajectory. Two knobs:
+    //   * walk items per bin: for the particles due at the first sub-step of each bin, the
+    //     gravity walk alone (on the block-start tree, into a scratch array) is timed for each
+    //     candidate chunk; the fastest wins;
+    //   * tree rebuild cadence: one whole block per candidate, graph time compared.
+    void autotune(Simulation& S, int* chunk_out, int* rebuild_out, double* graph_ms_out) {
+        cudaStream_t s = S.s();
+        const size_t n3 = 3 * size_t(S.n);
+        double* sp = save_pos.get<double>(n3);
+        double* sv = save_vel.get<double>(n3);
+        GF_CUDA(cudaMemcpyAsync(sp, S.pos.as<double>(), sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
+        GF_CUDA(cudaMemcpyAsync(sv, S.vel.as<double>(), sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
+        const double t0 = S.t;
+        ForceEngine& F = force_engine();
+        const long long collect = F.collect_cap;
+        F.collect_cap = F.collect_n;  // no training rows from trial runs
+        Context& C = ctx();
+        const bool prof = C.prof.on;
+        C.prof.on = false;
+        try {
+            start(S);
+            Octree& T = F.grav;
+            double* ta = tune_acc.get<double>(n3);
+            unsigned long long* d = scal.as<unsigned long long>();
+            static const int cand[] = {0, 2, 4, 8, 16, 32, 64};
+            Event e0, e1;
+            for (int bin = 0; bin < nlev - 1; ++bin) {
+                k_active_at<<<div_up(S.n, 256), 256, 0, s>>>(S.n, level.as<int8_t>(), 1 << bin, act.as<uint8_t>(),
+                                                             d + 1);
+                GF_CHECK_LAUNCH();
+                double best = INFINITY;
+                int best_c = 0;
+                for (int c : cand) {
+                    double ms[3];
+                    for (int r = 0; r < 3; ++r) {
+                        e0.record(s);
+                        T.prepare_walk(act.as<uint8_t>(), s, c);
+                        T.walk(S.eps, ta, s);
+                        e1.record(s);
+                        GF_CUDA(cudaStreamSynchronize(s));
+                        ms[r] = e1.since(e0);
+                    }
+                    std::sort(ms, ms + 3);
+                    if (ms[1] < best * 0.97) {  // prefer the earlier (coarser) candidate on near-ties
+                        best = ms[1];
+                        best_c = c;
+                    }
+                }
+                tune.chunk[bin] = best_c;
+            }
+            for (int bin = nlev - 1; bin < 8; ++bin) tune.chunk[bin] = tune.chunk[std::max(0, nlev - 2)];
+            // rebuild cadence: whole blocks from the same start
+            static const int every[] = {0, 32, 16, 8, 4};
+            double best = INFINITY;
+            int best_r = 0;
+            for (int r : every) {
+                if (r >= nsub()) continue;
+                GF_CUDA(cudaMemcpyAsync(S.pos.as<double>(), sp, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
+                GF_CUDA(cudaMemcpyAsync(S.vel.as<double>(), sv, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
+                tune.rebuild_every = r;
+                tune_changed = true;
+                started = false;
+                run(S, 1);
+                if (last_graph_ms < best) {
+                    best = last_graph_ms;
+                    best_r = r;
+                }
+            }
+            tune.rebuild_every = best_r;
+            tune_changed = true;
+            if (graph_ms_out) *graph_ms_out = best;
+        } catch (...) {
+            F.collect_cap = collect;
+            C.prof.on = prof;
+            throw;
+        }
+        F.collect_cap = collect;
+        C.prof.on = prof;
+        GF_CUDA(cudaMemcpyAsync(S.pos.as<double>(), sp, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
+        GF_CUDA(cudaMemcpyAsync(S.vel.as<double>(), sv, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
+        GF_CUDA(cudaStreamSynchronize(s));
+        S.t = t0;
+        started = false;
+        if (chunk_out)
+            for (int b = 0; b < nlev - 1; ++b) chunk_out[b] = tune.chunk[b];
+        if (rebuild_out) *rebuild_out = tune.rebuild_every;
+    }
 };
 
 static BlockIntegrator g_block;
@@ -368,6 +486,18 @@ double block_run(int nblocks, int nlev) {
         g_block.started = false;
     }
     return g_block.run(g_sim, nblocks);
+}
+
+void block_config(const int* chunk, int nbins, int rebuild_every) {
+    BlockTuning& t = g_block.tune;
+    for (int b = 0; b < 8; ++b) t.chunk[b] = chunk ? chunk[std::min(b, nbins - 1)] : 0;
+    t.rebuild_every = rebuild_every;
+    g_block.tune_changed = true;
+}
+
+void block_autotune(int nlev, int* chunk, int* rebuild_every, double* graph_ms) {
+    g_block.nlev = nlev;
+    g_block.autotune(g_sim, chunk, rebuild_every, graph_ms);
 }
 
 void block_reset() { g_block.started = false; }

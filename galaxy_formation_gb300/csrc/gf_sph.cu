@@ -73,9 +73,9 @@ __global__ void k_sph_kernel(int n, const double* __restrict__ r, const double* 
 template <class Idx>
 __global__ void k_sph_density(int n, int k, int ld, const double* __restrict__ pos, const double* __restrict__ mass,
                               const Idx* __restrict__ nb, const double* __restrict__ h,
-                              double* __restrict__ rho, const uint8_t* __restrict__ act) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || (act && !act[i])) return;
+                              double* __restrict__ rho, Subset sub) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!subset_item(sub, i, n, nullptr, i)) return;
     const double xi = pos[3 * size_t(i)], yi = pos[3 * size_t(i) + 1], zi = pos[3 * size_t(i) + 2];
     const double hi = h[i];
     double s = 0.0;
@@ -89,9 +89,9 @@ __global__ void k_sph_density(int n, int k, int ld, const double* __restrict__ p
 
 // P / rho^2 and the sound speed of every particle (the per-j factors of sph.py:88-89)
 __global__ void k_sph_eos(int n, const double* __restrict__ rho, const double* __restrict__ u,
-                          double gamma, double* __restrict__ pr2, double* __restrict__ cs) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+                          double gamma, double* __restrict__ pr2, double* __restrict__ cs, Subset sub) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!subset_item(sub, i, n, nullptr, i)) return;
     const double P = (gamma - 1) * rho[i] * u[i];
     pr2[i] = P / (rho[i] * rho[i]);
     cs[i] = sqrt(gamma * (gamma - 1) * u[i]);
@@ -120,9 +120,9 @@ __global__ void k_sph_force(int n, int k, int ld, const double* __restrict__ pos
                             const double* __restrict__ h, const double* __restrict__ rho,
                             const double* __restrict__ pr2, const double* __restrict__ cs, double alpha,
                             double beta, double* __restrict__ acc, double* __restrict__ dudt,
-                            double* __restrict__ dt_i, float* __restrict__ divv, const uint8_t* __restrict__ act) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || (act && !act[i])) return;
+                            double* __restrict__ dt_i, float* __restrict__ divv, Subset sub) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!subset_item(sub, i, n, nullptr, i)) return;
     const double xi = pos[3 * size_t(i)], yi = pos[3 * size_t(i) + 1], zi = pos[3 * size_t(i) + 2];
     const double vxi = vel[3 * size_t(i)], vyi = vel[3 * size_t(i) + 1], vzi = vel[3 * size_t(i) + 2];
     const double hi = h[i], rhoi = rho[i], pri = pr2[i], ci = cs[i];
@@ -166,7 +166,9 @@ __global__ void k_sph_force(int n, int k, int ld, const double* __restrict__ pos
 // ------------------------------------------------------------------- warp bitonic sorts
 
 // In-place ascending bitonic sort of P (power of two <= 128) keys in shared memory by the
-// calling warp; ties broken by the integer tag.
+// calling warp; ties broken by the integer tag. Non-negative float64 distances are sorted by
+// their bit patterns as unsigned 64-bit integers (the same order, including +inf): integer
+// compares avoid the float64 pipe, which is narrow on this GPU.
 template <class K>
 __device__ void warp_bitonic(K* key, int* tag, int P) {
     const int lane = threadIdx.x & 31;
@@ -198,10 +200,10 @@ constexpr int kCandWarps = 8;
 __global__ void __launch_bounds__(kCandWarps * 32) k_knn_cand(
     int n, int m, const double* __restrict__ pos, const int64_t* __restrict__ cand, int k,
     int64_t* __restrict__ nb, double* __restrict__ dist, int* __restrict__ all_ok) {
-    __shared__ double s_key[kCandWarps][64];
+    __shared__ unsigned long long s_key[kCandWarps][64];
     __shared__ int s_tag[kCandWarps][64];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    double* key = s_key[w];
+    unsigned long long* key = s_key[w];
     int* tag = s_tag[w];
     const int nwarps = gridDim.x * kCandWarps;
     for (int i = blockIdx.x * kCandWarps + w; i < n; i += nwarps) {
@@ -217,7 +219,7 @@ __global__ void __launch_bounds__(kCandWarps * 32) k_knn_cand(
                     ++valid;
                 }
             }
-            key[jj] = d2;
+            key[jj] = (unsigned long long)__double_as_longlong(d2);
             tag[jj] = jj;
         }
         valid = warp_sum(valid);
@@ -229,7 +231,7 @@ __global__ void __launch_bounds__(kCandWarps * 32) k_knn_cand(
         warp_bitonic(key, tag, 64);
         for (int t = lane; t < k; t += 32) {
             nb[size_t(i) * k + t] = cand[size_t(i) * m + tag[t]];
-            dist[size_t(i) * k + t] = sqrt(key[t]);
+            dist[size_t(i) * k + t] = sqrt(__longlong_as_double((long long)key[t]));
         }
         __syncwarp();
     }
@@ -245,7 +247,7 @@ struct KnnSmem {
     int stack[kKnnStack];
     float d2[kKnnCap];
     int idx[kKnnCap];
-    double dd[64];
+    unsigned long long dd[64];  // float64 squared distances as bit patterns
     int di[64];
     int lanemap[32];
 };
@@ -382,7 +384,8 @@ __device__ int knn_collect(const KnnArgs& A, KnnSmem& S, float4 xh, float4 xl, f
 // Sorts the cnt (<= kKnnCap) collected points of query q (tree position) held in d2/idx,
 // re-measures the k nearest and the float32 near-ties in float64, sorts those and writes the
 // k nearest (ascending, ties by index) in the caller's order.
-__device__ void knn_finish(const KnnArgs& A, float* d2, int* idx, double* dd, int* di, int cnt, int q) {
+__device__ void knn_finish(const KnnArgs& A, float* d2, int* idx, unsigned long long* dd, int* di, int cnt,
+                           int q) {
     const int lane = threadIdx.x & 31;
     const int k = A.k;
     const int oq = A.perm[q];
@@ -417,12 +420,12 @@ __device__ void knn_finish(const KnnArgs& A, float* d2, int* idx, double* dd, in
                 v = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
                 tag = pj;
             }
-            dd[t] = v;
+            dd[t] = (unsigned long long)__double_as_longlong(v);
             di[t] = tag;
         }
         __syncwarp();
         warp_bitonic(dd, di, 64);
-        best = dd[max(0, rank_need)];
+        best = __longlong_as_double((long long)dd[max(0, rank_need)]);
         for (int t = lane; t < k; t += 32) {
             if (A.nb32) A.nb32[size_t(oq) * A.ld32 + t] = A.perm[idx[t]];
             if (A.nb) A.nb[size_t(oq) * k + t] = A.perm[idx[t]];
@@ -447,16 +450,17 @@ __device__ void knn_finish(const KnnArgs& A, float* d2, int* idx, double* dd, in
             v = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
             tag = pj;
         }
-        dd[t] = v;
+        dd[t] = (unsigned long long)__double_as_longlong(v);
         di[t] = tag;
     }
     __syncwarp();
     warp_bitonic(dd, di, 64);
     for (int t = lane; t < k; t += 32) {
+        const double dt = __longlong_as_double((long long)dd[t]);
         if (A.nb) A.nb[size_t(oq) * k + t] = di[t];
-        if (A.dist) A.dist[size_t(oq) * k + t] = __dsqrt_rn(dd[t]);
+        if (A.dist) A.dist[size_t(oq) * k + t] = __dsqrt_rn(dt);
         if (A.nb32) A.nb32[size_t(oq) * A.ld32 + t] = di[t];
-        if (A.dsel && t == A.dsel_col) A.dsel[oq] = __dsqrt_rn(dd[t]);
+        if (A.dsel && t == A.dsel_col) A.dsel[oq] = __dsqrt_rn(dt);
     }
     __syncwarp();
 }
@@ -545,29 +549,29 @@ template <class Idx>
 void sph_forces(SphScratch& S, int n, int k, int ld, const double* pos, const double* vel, const double* mass,
                 const Idx* nb, const double* h, const double* u, double gamma, double alpha,
                 double beta, double* rho, double* acc, double* dudt, double* dt_i, cudaStream_t s, float* divv,
-                const uint8_t* act) {
+                Subset sub) {
     if (n <= 0) return;
     const int grid = div_up(n, kThreads);
     {
         ProfScope ps(kStSphDensity, s);
-        k_sph_density<Idx><<<grid, kThreads, 0, s>>>(n, k, ld, pos, mass, nb, h, rho, act);
+        k_sph_density<Idx><<<grid, kThreads, 0, s>>>(n, k, ld, pos, mass, nb, h, rho, sub);
         GF_CHECK_LAUNCH();
     }
     double* pr2 = S.pr2.get<double>(n);
     double* cs = S.cs.get<double>(n);
-    k_sph_eos<<<grid, kThreads, 0, s>>>(n, rho, u, gamma, pr2, cs);
+    k_sph_eos<<<grid, kThreads, 0, s>>>(n, rho, u, gamma, pr2, cs, sub);
     GF_CHECK_LAUNCH();
     ProfScope ps(kStSphForce, s);
     k_sph_force<Idx><<<grid, kThreads, 0, s>>>(n, k, ld, pos, vel, mass, nb, h, rho, pr2, cs, alpha, beta,
-                                               acc, dudt, dt_i, divv, act);
+                                               acc, dudt, dt_i, divv, sub);
     GF_CHECK_LAUNCH();
 }
 template void sph_forces<int64_t>(SphScratch&, int, int, int, const double*, const double*, const double*,
                                   const int64_t*, const double*, const double*, double, double, double,
-                                  double*, double*, double*, double*, cudaStream_t, float*, const uint8_t*);
+                                  double*, double*, double*, double*, cudaStream_t, float*, Subset);
 template void sph_forces<int>(SphScratch&, int, int, int, const double*, const double*, const double*,
                               const int*, const double*, const double*, double, double, double,
-                              double*, double*, double*, double*, cudaStream_t, float*, const uint8_t*);
+                              double*, double*, double*, double*, cudaStream_t, float*, Subset);
 
 void knn_from_candidates(int n, int m, const double* pos, const int64_t* cand, int k, int64_t* nb,
                          double* dist, int* d_ok, cudaStream_t s) {
@@ -733,10 +737,10 @@ extern "C" int gf_sph_forces_noalloc_dev(int n, int k, const double* pos, const 
     double* cs = scratch + kNoallocMaxN;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int grid = div_up(n, kThreads);
-    k_sph_density<int64_t><<<grid, kThreads, 0, s>>>(n, k, k, pos, mass, nb, h, rho, nullptr);
-    k_sph_eos<<<grid, kThreads, 0, s>>>(n, rho, u, gamma, pr2, cs);
+    k_sph_density<int64_t><<<grid, kThreads, 0, s>>>(n, k, k, pos, mass, nb, h, rho, Subset());
+    k_sph_eos<<<grid, kThreads, 0, s>>>(n, rho, u, gamma, pr2, cs, Subset());
     k_sph_force<int64_t><<<grid, kThreads, 0, s>>>(n, k, k, pos, vel, mass, nb, h, rho, pr2, cs, alpha,
-                                                   beta, acc, dudt, dt_i, nullptr, nullptr);
+                                                   beta, acc, dudt, dt_i, nullptr, Subset());
     e = cudaGetLastError();
     if (e != cudaSuccess) return noalloc_fail(GF_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
     c.launches += 3;

@@ -16,7 +16,7 @@ template <class Idx>
 void sph_forces(SphScratch& S, int n, int k, int ld, const double* pos, const double* vel, const double* mass,
                 const Idx* nb, const double* h, const double* u, double gamma, double alpha,
                 double beta, double* rho, double* acc, double* dudt, double* dt_i, cudaStream_t s,
-                float* divv = nullptr, const uint8_t* act = nullptr);
+                float* divv = nullptr, Subset sub = Subset());
 
 // Inputs of the learned smoothing-length guess inside a neighbour search: X (n x 4) receives
 // the features; with use_mlp the network's log h gives the starting radius 2.4 h.
@@ -35,12 +35,13 @@ struct Sph32Scratch {
 };
 
 // Mixed-precision sph_forces (float32 arithmetic, Kahan sums; float64 in and out). order
-// (optional): the visiting order of the particles.
+// (optional): the visiting order of the particles. sub (both forms): only these particles get
+// new density, forces and Courant step (the others keep theirs, and serve as neighbours).
 template <class Idx>
 void sph_forces32(Sph32Scratch& S, int n, int k, int ld, const int* order, const double* pos, const double* vel,
                   const double* mass, const Idx* nb, const double* h, const double* u, double gamma, double alpha,
                   double beta, double* rho, double* acc, double* dudt, double* dt_i, cudaStream_t s,
-                  float* divv = nullptr, const uint8_t* act = nullptr);
+                  float* divv = nullptr, Subset sub = Subset());
 
 void knn_from_candidates(int n, int m, const double* pos, const int64_t* cand, int k, int64_t* nb,
                          double* dist, int* d_ok, cudaStream_t s);

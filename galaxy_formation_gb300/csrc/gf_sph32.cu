@@ -67,11 +67,10 @@ template <class Idx>
 __global__ void k_sph32_density(int n, int k, int ld, const Idx* __restrict__ nb, const int* __restrict__ order,
                                 const float4* __restrict__ A, const float4* __restrict__ B,
                                 const double* __restrict__ u, float gamma, float4* __restrict__ D,
-                                double* __restrict__ rho_out, const uint8_t* __restrict__ act) {
+                                double* __restrict__ rho_out, Subset sub) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    const int i = order ? order[t] : t;
-    if (act && !act[i]) return;  // keeps its last density record
+    int i;
+    if (!subset_item(sub, t, n, order, i)) return;  // others keep their last density record
     const float4 ai = A[i], bi = B[i];
     const float inv_h = 1.f / ai.w;
     Kahan s;
@@ -95,11 +94,10 @@ __global__ void k_sph32_force(int n, int k, int ld, const Idx* __restrict__ nb, 
                               const float4* __restrict__ A, const float4* __restrict__ B,
                               const float4* __restrict__ C, const float4* __restrict__ D, float alpha,
                               float beta, double* __restrict__ acc, double* __restrict__ dudt,
-                              double* __restrict__ dt_i, float* __restrict__ divv, const uint8_t* __restrict__ act) {
+                              double* __restrict__ dt_i, float* __restrict__ divv, Subset sub) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    const int i = order ? order[t] : t;
-    if (act && !act[i]) return;
+    int i;
+    if (!subset_item(sub, t, n, order, i)) return;
     const float4 ai = A[i], bi = B[i], ci = C[i], di = D[i];
     const float hi = ai.w, inv_hi = di.w, rhoi = di.x, pri = di.y, csi = di.z;
     const float ih2 = inv_hi * inv_hi;
@@ -150,7 +148,7 @@ template <class Idx>
 void sph_forces32(Sph32Scratch& S, int n, int k, int ld, const int* order, const double* pos, const double* vel,
                   const double* mass, const Idx* nb, const double* h, const double* u, double gamma, double alpha,
                   double beta, double* rho, double* acc, double* dudt, double* dt_i, cudaStream_t s, float* divv,
-                  const uint8_t* act) {
+                  Subset sub) {
     if (n <= 0) return;
     const int grid = div_up(n, kThreads);
     float4* A = S.A.get<float4>(n);
@@ -161,21 +159,21 @@ void sph_forces32(Sph32Scratch& S, int n, int k, int ld, const int* order, const
     GF_CHECK_LAUNCH();
     {
         ProfScope ps(kStSphDensity, s);
-        k_sph32_density<Idx><<<grid, kThreads, 0, s>>>(n, k, ld, nb, order, A, B, u, float(gamma), D, rho, act);
+        k_sph32_density<Idx><<<grid, kThreads, 0, s>>>(n, k, ld, nb, order, A, B, u, float(gamma), D, rho, sub);
         GF_CHECK_LAUNCH();
     }
     ProfScope ps(kStSphForce, s);
     k_sph32_force<Idx><<<grid, kThreads, 0, s>>>(n, k, ld, nb, order, A, B, C, D, float(alpha), float(beta), acc,
-                                                 dudt, dt_i, divv, act);
+                                                 dudt, dt_i, divv, sub);
     GF_CHECK_LAUNCH();
 }
 
 template void sph_forces32<int64_t>(Sph32Scratch&, int, int, int, const int*, const double*, const double*,
                                     const double*, const int64_t*, const double*, const double*, double, double,
                                     double, double*, double*, double*, double*, cudaStream_t, float*,
-                                    const uint8_t*);
+                                    Subset);
 template void sph_forces32<int>(Sph32Scratch&, int, int, int, const int*, const double*, const double*,
                                 const double*, const int*, const double*, const double*, double, double, double,
-                                double*, double*, double*, double*, cudaStream_t, float*, const uint8_t*);
+                                double*, double*, double*, double*, cudaStream_t, float*, Subset);
 
 }  // namespace gf

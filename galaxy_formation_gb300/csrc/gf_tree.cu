@@ -289,7 +289,7 @@ __global__ void k_emit(KeyView K, int n, const RootBox* __restrict__ rootp,
                        const int* __restrict__ nstart, const int* __restrict__ nbase,
                        const TreeCounts* __restrict__ cnt, int4* __restrict__ n_i4,
                        double4* __restrict__ n_cd, float4* __restrict__ n_geo,
-                       int* __restrict__ n_parent) {
+                       int* __restrict__ n_parent, int cap) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || nstart[i] == 0) return;
     const RootBox R = *rootp;
@@ -313,6 +313,7 @@ __global__ void k_emit(KeyView K, int n, const RootBox* __restrict__ rootp,
             c[2] = __dadd_rn(c[2], (o & 4) ? h : -h);
         }
         const int id = base + (d - ds);
+        if (id >= cap) return;  // reported by k_node_cap_check
         const int end = run_end(K, n, i, d);
         const int next = end < n ? nbase[end] : total;
         int parent;
@@ -331,10 +332,22 @@ __global__ void k_emit(KeyView K, int n, const RootBox* __restrict__ rootp,
     }
 }
 
-__global__ void k_nchild(int nn, const int4* __restrict__ n_i4, int* __restrict__ nchild,
-                         int* __restrict__ counter) {
+__global__ void k_node_cap_check(TreeCounts* cnt, int cap, uint32_t* status) {
+    if (cnt->total_nodes > cap) {
+        raise_status(status, GF_ERR_CAPACITY);
+        cnt->total_nodes = 0;
+    }
+}
+
+// Node kernels: launched over [0, span); the live node count is *nn_dev.
+__device__ __forceinline__ int live_nodes(int span, const int* nn_dev) {
+    return nn_dev ? min(span, *nn_dev) : span;
+}
+
+__global__ void k_nchild(int span, const int* __restrict__ nn_dev, const int4* __restrict__ n_i4,
+                         int* __restrict__ nchild, int* __restrict__ counter) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nn) return;
+    if (k >= live_nodes(span, nn_dev)) return;
     const int4 q = n_i4[k];
     int c = 0;
     if (!(q.w & 1)) {
@@ -345,9 +358,10 @@ __global__ void k_nchild(int nn, const int4* __restrict__ n_i4, int* __restrict_
 }
 
 // Inside a leaf the reference keeps increasing particle index (stable partitions).
-__global__ void k_leaf_sort(int nn, const int4* __restrict__ n_i4, int* __restrict__ perm) {
+__global__ void k_leaf_sort(int span, const int* __restrict__ nn_dev, const int4* __restrict__ n_i4,
+                            int* __restrict__ perm) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nn) return;
+    if (k >= live_nodes(span, nn_dev)) return;
     const int4 q = n_i4[k];
     if (!(q.w & 1) || q.y > 64) return;  // larger leaves hold identical keys: already sorted
     int* p = perm + q.x;
@@ -364,7 +378,8 @@ __global__ void k_leaf_sort(int nn, const int4* __restrict__ n_i4, int* __restri
 
 __global__ void k_gather(int n, const int* __restrict__ perm, const double* __restrict__ pos,
                          const double* __restrict__ mass, const double* __restrict__ xbuild,
-                         float4* __restrict__ p4, float* __restrict__ pdisp, float4* __restrict__ plo) {
+                         float4* __restrict__ p4, float* __restrict__ pdisp, float4* __restrict__ plo,
+                         int disp32 = 0) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int j = perm[i];
@@ -373,7 +388,11 @@ __global__ void k_gather(int n, const int* __restrict__ perm, const double* __re
     const float fx = float(x), fy = float(y), fz = float(z);
     p4[i] = make_float4(fx, fy, fz, float(m));
     if (plo) plo[i] = make_float4(float(x - double(fx)), float(y - double(fy)), float(z - double(fz)), 0.f);
-    if (pdisp) {  // refit: displacement since the build (cpp/nbody.cpp:273-275)
+    if (pdisp && disp32) {  // mixed form: float64 differences, float32 length
+        const float dx = float(x - xbuild[3 * size_t(j)]), dy = float(y - xbuild[3 * size_t(j) + 1]),
+                    dz = float(z - xbuild[3 * size_t(j) + 2]);
+        pdisp[i] = m > 0 ? sqrtf(dx * dx + dy * dy + dz * dz) : 0.0f;
+    } else if (pdisp) {  // refit: displacement since the build (cpp/nbody.cpp:273-275)
         const double dx = __dsub_rn(x, xbuild[3 * size_t(j)]);
         const double dy = __dsub_rn(y, xbuild[3 * size_t(j) + 1]);
         const double dz = __dsub_rn(z, xbuild[3 * size_t(j) + 2]);
@@ -433,7 +452,7 @@ __device__ __forceinline__ void finalize(const MomentArgs& A, int k, double M, d
 
 __global__ void k_moments(MomentArgs A) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= (A.nn_dev ? *A.nn_dev : A.nn)) return;
+    if (k >= live_nodes(A.nn, A.nn_dev)) return;
     const int4 q = A.n_i4[k];
     if (!(q.w & 1)) return;
     double M = 0, sx = 0, sy = 0, sz = 0;
@@ -482,22 +501,44 @@ __global__ void k_moments(MomentArgs A) {
     }
 }
 
-// Traceless quadrupole Q = sum m (3 d d - |d|^2 I) about each node's (float32) centre of
-// mass, bottom-up like k_moments: leaves from their particles, parents from their children
-// shifted by the parallel-axis term. Float32 with Kahan-compensated sums (mixed form).
-struct QuadArgs {
+// Mixed form: monopole and traceless quadrupole in one bottom-up pass, float32 with
+// Kahan-compensated sums. A leaf sums its particles; the last child to finish a parent
+// (arrival counter) combines the children's masses and centres, then their quadrupoles shifted
+// by the parallel-axis term. open_r = 2 (half + displacement) / theta + |com - cell centre|
+// as in the float64 pass, evaluated in float32.
+struct Mom32Args {
     int nn;
     const int* nn_dev;
+    bool refit;
+    float theta;
     const int4* n_i4;
     const int* parent;
     const int* nchild;
     int* counter;
-    const float4* mom;
+    const float4* n_geo;
+    float4* mom;
+    float* open_r;
+    float* ndisp;
     const float4* p4;
+    const float* pdisp;
     float4* q4;   // Qxx, Qyy, Qxy, Qxz
-    float2* qyz;  // Qyz, T = sum m |d|^2 (trace of the second moment, for the softened kernel)
+    float2* qyz;  // Qyz, T = sum m |d|^2
 };
 
+__device__ __forceinline__ float4 finalize32(const Mom32Args& A, int k, const KahanF& M, const KahanF& sx,
+                                             const KahanF& sy, const KahanF& sz, float dm) {
+    const float inv = M.s > 0.f ? 1.f / M.s : 0.f;
+    const float4 c = make_float4(sx.s * inv, sy.s * inv, sz.s * inv, M.s);
+    A.mom[k] = c;
+    const float4 g = A.n_geo[k];
+    const float first = 2.f * (g.w + dm) / A.theta;
+    if (A.refit) A.ndisp[k] = dm;
+    const float ox = c.x - g.x, oy = c.y - g.y, oz = c.z - g.z;
+    A.open_r[k] = first + sqrtf(ox * ox + oy * oy + oz * oz);
+    return c;
+}
+
+// Traceless quadrupole Q = sum m (3 d d - |d|^2 I) and trace T = sum m |d|^2 about a centre.
 struct QuadSum {
     KahanF xx, yy, xy, xz, yz, tr;
     __device__ __forceinline__ void point(float m, float dx, float dy, float dz) {
@@ -511,13 +552,23 @@ struct QuadSum {
     }
 };
 
-__global__ void k_quad(QuadArgs A) {
+__global__ void k_moments_quad32(Mom32Args A) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= (A.nn_dev ? *A.nn_dev : A.nn)) return;
+    if (k >= live_nodes(A.nn, A.nn_dev)) return;
     const int4 q = A.n_i4[k];
     if (!(q.w & 1)) return;
     {
-        const float4 c = A.mom[k];
+        KahanF M, sx, sy, sz;
+        float dm = 0.f;
+        for (int i = q.x; i < q.x + q.y; ++i) {
+            const float4 p = A.p4[i];
+            M.add(p.w);
+            sx.add(p.w * p.x);
+            sy.add(p.w * p.y);
+            sz.add(p.w * p.z);
+            if (A.refit) dm = fmaxf(dm, A.pdisp[i]);
+        }
+        const float4 c = finalize32(A, k, M, sx, sy, sz, dm);
         QuadSum S;
         for (int i = q.x; i < q.x + q.y; ++i) {
             const float4 p = A.p4[i];
@@ -532,18 +583,29 @@ __global__ void k_quad(QuadArgs A) {
         const int arrived = atomicAdd(&A.counter[p], 1);
         if (arrived != A.nchild[p] - 1) return;
         __threadfence();
-        const float4 cp = A.mom[p];
-        QuadSum S;
         const int end = A.n_i4[p].z;
+        KahanF M, sx, sy, sz;
+        float dm = 0.f;
         int seen = 0;
+        for (int c = p + 1; c < end && seen < 8; c = A.n_i4[c].z, ++seen) {  // octant order
+            const float4 cm = __ldcg(&A.mom[c]);
+            M.add(cm.w);
+            sx.add(cm.w * cm.x);
+            sy.add(cm.w * cm.y);
+            sz.add(cm.w * cm.z);
+            if (A.refit) dm = fmaxf(dm, __ldcg(&A.ndisp[c]));
+        }
+        const float4 cp = finalize32(A, p, M, sx, sy, sz, dm);
+        QuadSum S;
+        seen = 0;
         for (int c = p + 1; c < end && seen < 8; c = A.n_i4[c].z, ++seen) {
-            const float4 cm = A.mom[c];
+            const float4 cm = __ldcg(&A.mom[c]);
             const float4 qc = __ldcg(&A.q4[c]);
+            const float2 yt = __ldcg(&A.qyz[c]);
             S.xx.add(qc.x);
             S.yy.add(qc.y);
             S.xy.add(qc.z);
             S.xz.add(qc.w);
-            const float2 yt = __ldcg(&A.qyz[c]);
             S.yz.add(yt.x);
             S.tr.add(yt.y);
             S.point(cm.w, cm.x - cp.x, cm.y - cp.y, cm.z - cp.z);
@@ -555,36 +617,156 @@ __global__ void k_quad(QuadArgs A) {
     }
 }
 
+// Refit of the mixed form directly in the breadth-first walk layout: the same float32 + Kahan
+// monopole / quadrupole / open_r as k_moments_quad32, with the same summation order (the
+// children of a node are contiguous there, in octant order), but a parent reads its children
+// with independent loads instead of following `next` links, and the walk arrays are written
+// in place (no k_walk_fill pass). Thread per breadth-first node; leaves start the chains.
+struct RefitBfsArgs {
+    int span;
+    const int* nn_dev;
+    float theta;
+    const int* wparent;
+    const float4* wgeo;
+    int* counter;
+    float4* wa;   // com, m
+    float4* wb;   // open_r, first, code, Qyz
+    float4* wq;   // Qxx, Qyy, Qxy, Qxz
+    float* wt;    // T
+    float* ndisp; // breadth-first
+    const float4* p4;
+    const float* pdisp;
+};
+
+__device__ __forceinline__ float4 finalize_bfs(const RefitBfsArgs& A, int b, const KahanF& M, const KahanF& sx,
+                                               const KahanF& sy, const KahanF& sz, float dm) {
+    const float inv = M.s > 0.f ? 1.f / M.s : 0.f;
+    const float4 c = make_float4(sx.s * inv, sy.s * inv, sz.s * inv, M.s);
+    A.wa[b] = c;
+    const float4 g = A.wgeo[b];
+    const float ox = c.x - g.x, oy = c.y - g.y, oz = c.z - g.z;
+    A.wb[b].x = 2.f * (g.w + dm) / A.theta + sqrtf(ox * ox + oy * oy + oz * oz);
+    A.ndisp[b] = dm;
+    return c;
+}
+
+__global__ void k_refit_bfs_quad32(RefitBfsArgs A) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= live_nodes(A.span, A.nn_dev)) return;
+    const float4 wb = A.wb[b];
+    const int first = __float_as_int(wb.y), code = __float_as_int(wb.z);
+    if (code >= 0) return;  // internal: reached by the last of its children
+    {
+        KahanF M, sx, sy, sz;
+        float dm = 0.f;
+        for (int i = first; i < first - code; ++i) {
+            const float4 p = A.p4[i];
+            M.add(p.w);
+            sx.add(p.w * p.x);
+            sy.add(p.w * p.y);
+            sz.add(p.w * p.z);
+            dm = fmaxf(dm, A.pdisp[i]);
+        }
+        const float4 c = finalize_bfs(A, b, M, sx, sy, sz, dm);
+        QuadSum S;
+        for (int i = first; i < first - code; ++i) {
+            const float4 p = A.p4[i];
+            S.point(p.w, p.x - c.x, p.y - c.y, p.z - c.z);
+        }
+        A.wq[b] = make_float4(S.xx.s, S.yy.s, S.xy.s, S.xz.s);
+        A.wb[b].w = S.yz.s;
+        A.wt[b] = S.tr.s;
+    }
+    __threadfence();
+    int p = A.wparent[b];
+    while (p >= 0) {
+        const float4 pb = A.wb[p];
+        const int c0 = __float_as_int(pb.y), nc = __float_as_int(pb.z);
+        const int arrived = atomicAdd(&A.counter[p], 1);
+        if (arrived != nc - 1) return;
+        __threadfence();
+        float4 cm[8];
+        float dmc[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            if (c < nc) {
+                cm[c] = __ldcg(&A.wa[c0 + c]);
+                dmc[c] = __ldcg(&A.ndisp[c0 + c]);
+            }
+        }
+        KahanF M, sx, sy, sz;
+        float dm = 0.f;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            if (c < nc) {
+                M.add(cm[c].w);
+                sx.add(cm[c].w * cm[c].x);
+                sy.add(cm[c].w * cm[c].y);
+                sz.add(cm[c].w * cm[c].z);
+                dm = fmaxf(dm, dmc[c]);
+            }
+        }
+        const float4 cp = finalize_bfs(A, p, M, sx, sy, sz, dm);
+        QuadSum S;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            if (c < nc) {
+                const float4 qc = __ldcg(&A.wq[c0 + c]);
+                const float yz = __ldcg(&A.wb[c0 + c]).w;
+                const float tc = __ldcg(&A.wt[c0 + c]);
+                S.xx.add(qc.x);
+                S.yy.add(qc.y);
+                S.xy.add(qc.z);
+                S.xz.add(qc.w);
+                S.yz.add(yz);
+                S.tr.add(tc);
+                S.point(cm[c].w, cm[c].x - cp.x, cm[c].y - cp.y, cm[c].z - cp.z);
+            }
+        }
+        A.wq[p] = make_float4(S.xx.s, S.yy.s, S.xy.s, S.xz.s);
+        A.wb[p].w = S.yz.s;
+        A.wt[p] = S.tr.s;
+        __threadfence();
+        p = A.wparent[p];
+    }
+}
+
 // ---------------------------------------------------------------------------- groups + layout
 
-__global__ void k_group_flag(int nn, int gmax, const int4* __restrict__ n_i4, const int* __restrict__ parent,
-                             int* __restrict__ flag) {
+__global__ void k_group_flag(int span, const int* __restrict__ nn_dev, int gmax, const int4* __restrict__ n_i4,
+                             const int* __restrict__ parent, int* __restrict__ flag) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nn) return;
+    if (k >= span) return;
+    if (k >= live_nodes(span, nn_dev)) {  // past the live nodes: no group (the scan covers span)
+        flag[k] = 0;
+        return;
+    }
     const int4 q = n_i4[k];
     const bool candidate = q.y <= gmax || (q.w & 1);
     const int p = parent[k];
     flag[k] = candidate && (p < 0 || n_i4[p].y > gmax) ? 1 : 0;
 }
 
-__global__ void k_group_write(int nn, const int* __restrict__ flag, const int* __restrict__ scan,
-                              int* __restrict__ groups) {
+__global__ void k_group_write(int span, const int* __restrict__ nn_dev, const int* __restrict__ flag,
+                              const int* __restrict__ scan, int* __restrict__ groups) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nn) return;
+    if (k >= live_nodes(span, nn_dev)) return;
     if (flag[k]) groups[scan[k]] = k;
 }
 
-__global__ void k_bfs_keys(int nn, const int4* __restrict__ n_i4, uint64_t* __restrict__ key,
-                           int* __restrict__ val) {
+// breadth-first order = stable sort by depth; slots past the live nodes sort last
+__global__ void k_bfs_keys(int span, const int* __restrict__ nn_dev, const int4* __restrict__ n_i4,
+                           uint64_t* __restrict__ key, int* __restrict__ val) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nn) return;
-    key[k] = uint64_t(n_i4[k].w >> 8);
+    if (k >= span) return;
+    key[k] = k < live_nodes(span, nn_dev) ? uint64_t(n_i4[k].w >> 8) : 255u;
     val[k] = k;
 }
 
-__global__ void k_bfs_index(int nn, const int* __restrict__ val, int* __restrict__ bfs) {
+__global__ void k_bfs_index(int span, const int* __restrict__ nn_dev, const int* __restrict__ val,
+                            int* __restrict__ bfs) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nn) return;
+    if (b >= live_nodes(span, nn_dev)) return;
     bfs[val[b]] = b;
 }
 
@@ -597,7 +779,7 @@ __global__ void k_walk_fill(int nn, const int4* __restrict__ n_i4, const int* __
                             float4* __restrict__ wq, const int* __restrict__ parent, int* __restrict__ wparent,
                             float* __restrict__ wt, const int* __restrict__ nn_dev) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= (nn_dev ? *nn_dev : nn)) return;
+    if (k >= live_nodes(nn, nn_dev)) return;
     const int4 q = n_i4[k];
     const int b = bfs[k];
     int first, code;
@@ -722,12 +904,34 @@ Octree& gravity_tree() { return g_tree; }
 static Octree* g_last_walked = nullptr;
 Octree*& last_walked() { return g_last_walked; }
 
-void Octree::build(int n_, const double* pos, const double* mass, double theta, cudaStream_t s) {
+void Octree::reserve_graph_build() {
+    if (!valid || n <= 0) throw Error(GF_ERR_ARG, "a captured rebuild needs a regular build first");
+    key1.get<uint64_t>(n);
+    key2.get<uint64_t>(n);
+    pdisp.get<float>(n);
+    work.get<int4>(std::max(size_t(node_cap), size_t(n)) + 1);
+    sphere.get<float4>(std::max(size_t(node_cap), size_t(n)) + 1);
+    reserve_scan_sort(std::max(n, node_cap));
+    deep_sort_attr();
+}
+
+void Octree::deep_sort_attr() {
+    static bool attr = false;
+    if (!attr) {
+        const size_t sm = size_t(kDeepRunMax) * (2 * sizeof(uint64_t) + sizeof(int));
+        GF_CUDA(cudaFuncSetAttribute(k_deep_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)));
+        attr = true;
+    }
+}
+
+void Octree::build(int n_, const double* pos, const double* mass, double theta, cudaStream_t s, bool graph_safe) {
     Context& C = ctx();
     ProfScope ps(want_knn ? kStKnnTree : kStTreeBuild, s);
+    if (graph_safe && (!valid || n != n_ || node_cap <= 0))
+        throw Error(GF_ERR_ARG, "a captured rebuild needs a regular build of the same particle set first");
     n = n_;
     theta_f = float(theta);
-    valid = false;
+    if (!graph_safe) valid = false;
     if (!h_counts) GF_CUDA(cudaMallocHost(&h_counts, sizeof(TreeCounts)));
     TreeCounts* cnt = counts.get<TreeCounts>(1);
     RootBox* R = root.get<RootBox>(1);
@@ -753,27 +957,29 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
     int8_t* ds = dsplit.get<int8_t>(n);
     int* ns = nstart.get<int>(n);
     KeyView K{k0, nullptr, nullptr};
-    k_cpl9<<<grid, kThreads, 0, s>>>(K, n, c9, cnt);
-    GF_CHECK_LAUNCH();
-    k_nstart<<<grid, kThreads, 0, s>>>(K, n, c9, ld, ds, ns);
-    GF_CHECK_LAUNCH();
-    exclusive_scan(ns, nb, n, &cnt->total_nodes, s);
-    GF_CUDA(cudaMemcpyAsync(h_counts, cnt, sizeof(TreeCounts), cudaMemcpyDeviceToHost, s));
-    GF_CUDA(cudaStreamSynchronize(s));
-
-    if (h_counts->deep) {
+    // Deep cells (> 8 particles in one level-21 cell) need extension keys. A regular build
+    // finds out on the host; a captured one always computes them (zero outside deep runs,
+    // where they leave every common-prefix length the tree uses unchanged).
+    bool deep = graph_safe;
+    if (!graph_safe) {
+        k_cpl9<<<grid, kThreads, 0, s>>>(K, n, c9, cnt);
+        GF_CHECK_LAUNCH();
+        k_nstart<<<grid, kThreads, 0, s>>>(K, n, c9, ld, ds, ns);
+        GF_CHECK_LAUNCH();
+        exclusive_scan(ns, nb, n, &cnt->total_nodes, s);
+        GF_CUDA(cudaMemcpyAsync(h_counts, cnt, sizeof(TreeCounts), cudaMemcpyDeviceToHost, s));
+        GF_CUDA(cudaStreamSynchronize(s));
+        deep = h_counts->deep != 0;
+    }
+    if (deep) {
         uint64_t* e1 = key1.get<uint64_t>(n);
         uint64_t* e2 = key2.get<uint64_t>(n);
         int* starts = reinterpret_cast<int*>(key_alt.get<uint64_t>(n));  // scratch
         int* nst = &cnt->pad[0];
         k_deep_keys<<<grid, kThreads, 0, s>>>(n, k0, pm, pos, R, e1, e2, starts, nst);
         GF_CHECK_LAUNCH();
+        deep_sort_attr();
         const size_t sm = size_t(kDeepRunMax) * (2 * sizeof(uint64_t) + sizeof(int));
-        static bool attr = false;
-        if (!attr) {
-            GF_CUDA(cudaFuncSetAttribute(k_deep_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)));
-            attr = true;
-        }
         k_deep_sort<<<2 * C.sms, 512, sm, s>>>(n, k0, e1, e2, pm, starts, nst, C.d_status);
         GF_CHECK_LAUNCH();
         K = KeyView{k0, e1, e2};
@@ -782,25 +988,36 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
         k_nstart<<<grid, kThreads, 0, s>>>(K, n, c9, ld, ds, ns);
         GF_CHECK_LAUNCH();
         exclusive_scan(ns, nb, n, &cnt->total_nodes, s);
-        GF_CUDA(cudaMemcpyAsync(h_counts, cnt, sizeof(TreeCounts), cudaMemcpyDeviceToHost, s));
-        GF_CUDA(cudaStreamSynchronize(s));
+        if (!graph_safe) {
+            GF_CUDA(cudaMemcpyAsync(h_counts, cnt, sizeof(TreeCounts), cudaMemcpyDeviceToHost, s));
+            GF_CUDA(cudaStreamSynchronize(s));
+        }
     }
-    nn = h_counts->total_nodes;
-    if (nn > node_cap) node_cap = nn + nn / 4 + 1024;  // headroom: later rebuilds rarely move buffers
+    if (!graph_safe) {
+        nn = h_counts->total_nodes;
+        if (nn > node_cap) node_cap = nn + nn / 4 + 1024;  // headroom: captured rebuilds stay inside
+    }
     const int cap = node_cap;
+    // node kernels cover [0, span) and read the live count on the device
+    const int span = graph_safe ? cap : nn;
+    const int* nn_dev = &cnt->total_nodes;
+    const int ngrid = div_up(span, kThreads);
 
     int4* i4 = n_i4.get<int4>(cap);
     double4* cd = n_cd.get<double4>(cap);
     float4* geo = n_geo.get<float4>(cap);
     int* par = n_parent.get<int>(cap);
-    k_emit<<<grid, kThreads, 0, s>>>(K, n, R, ld, ds, ns, nb, cnt, i4, cd, geo, par);
+    k_emit<<<grid, kThreads, 0, s>>>(K, n, R, ld, ds, ns, nb, cnt, i4, cd, geo, par, cap);
     GF_CHECK_LAUNCH();
-    const int ngrid = div_up(nn, kThreads);
+    if (graph_safe) {  // more nodes than the buffers hold: flag, and leave an empty tree
+        k_node_cap_check<<<1, 1, 0, s>>>(cnt, cap, C.d_status);
+        GF_CHECK_LAUNCH();
+    }
     int* nch = n_nchild.get<int>(cap);
     int* ctr = n_counter.get<int>(cap);
-    k_nchild<<<ngrid, kThreads, 0, s>>>(nn, i4, nch, ctr);
+    k_nchild<<<ngrid, kThreads, 0, s>>>(span, nn_dev, i4, nch, ctr);
     GF_CHECK_LAUNCH();
-    k_leaf_sort<<<ngrid, kThreads, 0, s>>>(nn, i4, pm);
+    k_leaf_sort<<<ngrid, kThreads, 0, s>>>(span, nn_dev, i4, pm);
     GF_CHECK_LAUNCH();
 
     float4* pp = p4.get<float4>(n);
@@ -810,102 +1027,113 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
     double* xb = xbuild.get<double>(3 * size_t(n));
     GF_CUDA(cudaMemcpyAsync(xb, pos, sizeof(double) * 3 * size_t(n), cudaMemcpyDeviceToDevice, s));
 
-    MomentArgs A{};
-    A.nn = nn;
-    A.refit = false;
-    A.theta = theta_f;
-    A.n_i4 = i4;
-    A.parent = par;
-    A.nchild = nch;
-    A.counter = ctr;
-    A.n_cd = cd;
-    A.n_geo = geo;
-    A.mom = n_mom.get<float4>(cap);
-    A.open_r = n_open.get<float>(cap);
-    A.ndisp = n_disp.get<float>(cap);
-    A.perm = pm;
-    A.pos = pos;
-    A.mass = mass;
-    k_moments<<<ngrid, kThreads, 0, s>>>(A);
-    GF_CHECK_LAUNCH();
-
-    if (quad) {
-        QuadArgs Q{nn, nullptr, i4, par, nch, ctr, A.mom, pp, n_quad.get<float4>(cap), n_qyz.get<float2>(cap)};
-        GF_CUDA(cudaMemsetAsync(ctr, 0, sizeof(int) * size_t(nn), s));
-        k_quad<<<ngrid, kThreads, 0, s>>>(Q);
+    float4* mom = n_mom.get<float4>(cap);
+    float* opr = n_open.get<float>(cap);
+    float* ndp = n_disp.get<float>(cap);
+    if (quad) {  // mixed form: float32 monopole + quadrupole in one pass
+        Mom32Args A{span, nn_dev, false, theta_f, i4, par, nch, ctr, geo, mom, opr, ndp, pp, nullptr,
+                    n_quad.get<float4>(cap), n_qyz.get<float2>(cap)};
+        k_moments_quad32<<<ngrid, kThreads, 0, s>>>(A);
+        GF_CHECK_LAUNCH();
+    } else {
+        MomentArgs A{};
+        A.nn = span;
+        A.nn_dev = nn_dev;
+        A.refit = false;
+        A.theta = theta_f;
+        A.n_i4 = i4;
+        A.parent = par;
+        A.nchild = nch;
+        A.counter = ctr;
+        A.n_cd = cd;
+        A.n_geo = geo;
+        A.mom = mom;
+        A.open_r = opr;
+        A.ndisp = ndp;
+        A.perm = pm;
+        A.pos = pos;
+        A.mass = mass;
+        k_moments<<<ngrid, kThreads, 0, s>>>(A);
         GF_CHECK_LAUNCH();
     }
 
     int* gf_ = gflag.get<int>(cap);
     int* gs = gscan.get<int>(cap);
-    k_group_flag<<<ngrid, kThreads, 0, s>>>(nn, group_max, i4, par, gf_);
+    k_group_flag<<<ngrid, kThreads, 0, s>>>(span, nn_dev, group_max, i4, par, gf_);
     GF_CHECK_LAUNCH();
-    exclusive_scan(gf_, gs, nn, &cnt->num_groups, s);
-    k_group_write<<<ngrid, kThreads, 0, s>>>(nn, gf_, gs, groups.get<int>(cap));
+    exclusive_scan(gf_, gs, span, &cnt->num_groups, s);
+    k_group_write<<<ngrid, kThreads, 0, s>>>(span, nn_dev, gf_, gs, groups.get<int>(cap));
     GF_CHECK_LAUNCH();
 
     uint64_t* bk = bfs_key.get<uint64_t>(cap);
     int* bv = bfs_val.get<int>(cap);
-    k_bfs_keys<<<ngrid, kThreads, 0, s>>>(nn, i4, bk, bv);
+    k_bfs_keys<<<ngrid, kThreads, 0, s>>>(span, nn_dev, i4, bk, bv);
     GF_CHECK_LAUNCH();
-    radix_sort_pairs(bk, bv, bfs_key_alt.get<uint64_t>(cap), bfs_val_alt.get<int>(cap), nn, 0, 8, s);
+    radix_sort_pairs(bk, bv, bfs_key_alt.get<uint64_t>(cap), bfs_val_alt.get<int>(cap), span, 0, 8, s);
     int* bfs = n_bfs.get<int>(cap);
-    k_bfs_index<<<ngrid, kThreads, 0, s>>>(nn, bv, bfs);
+    k_bfs_index<<<ngrid, kThreads, 0, s>>>(span, nn_dev, bv, bfs);
     GF_CHECK_LAUNCH();
-    k_walk_fill<<<ngrid, kThreads, 0, s>>>(nn, i4, nch, bfs, A.mom, A.open_r, geo, w_a.get<float4>(cap),
-                                           w_b.get<float4>(cap), want_knn ? w_geo.get<float4>(cap) : nullptr,
+    // breadth-first geometry and parents: the neighbour search, and the mixed form's refit
+    const bool bfs_geo = want_knn || quad;
+    k_walk_fill<<<ngrid, kThreads, 0, s>>>(span, i4, nch, bfs, mom, opr, geo, w_a.get<float4>(cap),
+                                           w_b.get<float4>(cap), bfs_geo ? w_geo.get<float4>(cap) : nullptr,
                                            want_knn ? leaf_of.get<int>(n) : nullptr,
                                            quad ? n_quad.as<float4>() : nullptr, quad ? n_qyz.as<float2>() : nullptr,
                                            quad ? w_q.get<float4>(cap) : nullptr, par,
-                                           want_knn ? w_parent.get<int>(cap) : nullptr,
-                                           quad ? w_t.get<float>(cap) : nullptr, nullptr);
+                                           bfs_geo ? w_parent.get<int>(cap) : nullptr,
+                                           quad ? w_t.get<float>(cap) : nullptr, nn_dev);
     GF_CHECK_LAUNCH();
     valid = true;
 }
 
-void Octree::refit(const double* pos, const double* mass, cudaStream_t s, bool graph_safe) {
+// Node kernels cover node_cap and read the live node count on the device, so a refit stays
+// valid after a rebuild inside a captured graph (whose node count the host never sees).
+void Octree::refit(const double* pos, const double* mass, cudaStream_t s) {
     ProfScope ps(kStTreeRefit, s);
     const int grid = div_up(n, kThreads);
-    const int span = graph_safe ? node_cap : nn;  // nodes covered by the launches
+    const int span = std::max(node_cap, nn);
     const int ngrid = div_up(span, kThreads);
-    const int* nn_dev = graph_safe ? &counts.as<TreeCounts>()->total_nodes : nullptr;
+    const int* nn_dev = &counts.as<TreeCounts>()->total_nodes;
     float4* pp = p4.as<float4>();
     float* pd = pdisp.get<float>(n);
     k_gather<<<grid, kThreads, 0, s>>>(n, perm.as<int>(), pos, mass, xbuild.as<double>(), pp, pd,
-                                       want_knn ? plo.get<float4>(n) : nullptr);
+                                       want_knn ? plo.get<float4>(n) : nullptr, quad ? 1 : 0);
     GF_CHECK_LAUNCH();
-    GF_CUDA(cudaMemsetAsync(n_counter.as<int>(), 0, sizeof(int) * size_t(span), s));
-    MomentArgs A{};
-    A.nn = nn;
-    A.nn_dev = nn_dev;
-    A.refit = true;
-    A.theta = theta_f;
-    A.n_i4 = n_i4.as<int4>();
-    A.parent = n_parent.as<int>();
-    A.nchild = n_nchild.as<int>();
-    A.counter = n_counter.as<int>();
-    A.n_cd = n_cd.as<double4>();
-    A.n_geo = n_geo.as<float4>();
-    A.mom = n_mom.as<float4>();
-    A.open_r = n_open.as<float>();
-    A.ndisp = n_disp.as<float>();
-    A.p4 = pp;
-    A.pdisp = pd;
-    k_moments<<<ngrid, kThreads, 0, s>>>(A);
-    GF_CHECK_LAUNCH();
-    if (quad) {
-        QuadArgs Q{nn, nn_dev, A.n_i4, A.parent, A.nchild, A.counter, A.mom, pp, n_quad.as<float4>(),
-                   n_qyz.as<float2>()};
-        GF_CUDA(cudaMemsetAsync(A.counter, 0, sizeof(int) * size_t(span), s));
-        k_quad<<<ngrid, kThreads, 0, s>>>(Q);
+    int* ctr = n_counter.as<int>();
+    GF_CUDA(cudaMemsetAsync(ctr, 0, sizeof(int) * size_t(span), s));
+    if (quad) {  // mixed form: straight into the walk layout
+        RefitBfsArgs A{span, nn_dev, theta_f, w_parent.as<int>(), w_geo.as<float4>(), ctr, w_a.as<float4>(),
+                       w_b.as<float4>(), w_q.as<float4>(), w_t.as<float>(), n_disp.as<float>(), pp, pd};
+        k_refit_bfs_quad32<<<ngrid, kThreads, 0, s>>>(A);
+        GF_CHECK_LAUNCH();
+        return;
+    } else {
+        MomentArgs A{};
+        A.nn = span;
+        A.nn_dev = nn_dev;
+        A.refit = true;
+        A.theta = theta_f;
+        A.n_i4 = n_i4.as<int4>();
+        A.parent = n_parent.as<int>();
+        A.nchild = n_nchild.as<int>();
+        A.counter = ctr;
+        A.n_cd = n_cd.as<double4>();
+        A.n_geo = n_geo.as<float4>();
+        A.mom = n_mom.as<float4>();
+        A.open_r = n_open.as<float>();
+        A.ndisp = n_disp.as<float>();
+        A.p4 = pp;
+        A.pdisp = pd;
+        k_moments<<<ngrid, kThreads, 0, s>>>(A);
         GF_CHECK_LAUNCH();
     }
-    k_walk_fill<<<ngrid, kThreads, 0, s>>>(nn, A.n_i4, A.nchild, n_bfs.as<int>(), A.mom, A.open_r,
-                                           A.n_geo, w_a.as<float4>(), w_b.as<float4>(),
+    k_walk_fill<<<ngrid, kThreads, 0, s>>>(span, n_i4.as<int4>(), n_nchild.as<int>(), n_bfs.as<int>(),
+                                           n_mom.as<float4>(), n_open.as<float>(), n_geo.as<float4>(),
+                                           w_a.as<float4>(), w_b.as<float4>(),
                                            want_knn ? w_geo.as<float4>() : nullptr,
                                            want_knn ? leaf_of.as<int>() : nullptr,
                                            quad ? n_quad.as<float4>() : nullptr, quad ? n_qyz.as<float2>() : nullptr,
-                                           quad ? w_q.as<float4>() : nullptr, A.parent,
+                                           quad ? w_q.as<float4>() : nullptr, n_parent.as<int>(),
                                            want_knn ? w_parent.as<int>() : nullptr,
                                            quad ? w_t.as<float>() : nullptr, nn_dev);
     GF_CHECK_LAUNCH();

@@ -29,7 +29,8 @@ struct TreeCounts {
     int num_work;
     int walk_next;    // dynamic scheduler of the walk
     int pad[3];
-    unsigned long long pairs;  // particle-list interactions evaluated by the last walk
+    unsigned long long pairs;   // list interactions evaluated by the last walk (all kinds)
+    unsigned long long qpairs;  // of which with quadrupole nodes (mixed form)
 };
 
 struct Octree {
@@ -74,12 +75,18 @@ struct Octree {
     DevBuf root, counts;
     TreeCounts* h_counts = nullptr;  // pinned
 
-    void build(int n, const double* pos, const double* mass, double theta, cudaStream_t s);
-    // graph_safe: grids sized to node_cap and node count read on the device, so the launch
-    // sequence stays valid (e.g. inside a captured CUDA graph) across later rebuilds.
-    void refit(const double* pos, const double* mass, cudaStream_t s, bool graph_safe = false);
-    // Work list of groups with at least one active particle (active may be null).
-    void prepare_walk(const uint8_t* active, cudaStream_t s);
+    // graph_safe: no host synchronisation and no allocation (inside a captured CUDA graph):
+    // needs a regular build of the same particle set first (node_cap from it; a tree that
+    // outgrows node_cap raises GF_ERR_CAPACITY and is left empty).
+    void build(int n, const double* pos, const double* mass, double theta, cudaStream_t s,
+               bool graph_safe = false);
+    void reserve_graph_build();
+    void deep_sort_attr();
+    // Node kernels read the live node count on the device (valid after captured rebuilds).
+    void refit(const double* pos, const double* mass, cudaStream_t s);
+    // Work list of groups with at least one active particle (active may be null); chunk > 0
+    // cuts each group's active particles into items of <= chunk with their own spheres.
+    void prepare_walk(const uint8_t* active, cudaStream_t s, int chunk = 0);
     void walk(double eps, double* acc, cudaStream_t s);
 };
 

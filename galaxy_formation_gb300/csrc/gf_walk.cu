@@ -28,12 +28,20 @@ constexpr int kWalkWarps = 4;
 constexpr int kStackCap = 1024;   // child ranges per warp
 constexpr int kTileCap = 256;     // interaction entries per warp
 
-// Work list: groups with at least one active particle and a massive member.
+// Work list: groups with at least one active particle and a massive member, as work items
+// {first particle, particle count, active particles to evaluate, rank of the first of them
+// among the group's active particles}.
+//   chunk == 0: one item per group with the reference's sphere (all massive members);
+//   chunk  > 0: the group's active particles in tree order, cut into items of <= chunk,
+//               each with the bounding sphere of its own particles. Sparse active sets
+//               (block time steps) then spread over many warps with tight spheres instead of
+//               one warp walking a whole group for a few particles.
 __global__ void k_group_prep(const int* __restrict__ groups, const int4* __restrict__ n_i4,
                              const float4* __restrict__ p4, const int* __restrict__ perm,
                              const uint8_t* __restrict__ active, TreeCounts* cnt,
-                             int4* __restrict__ work, float4* __restrict__ sphere) {
+                             int4* __restrict__ work, float4* __restrict__ sphere, int chunk) {
     const int lane = threadIdx.x & 31;
+    const unsigned lt = lanemask_lt();
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const int ng = cnt->num_groups;
@@ -41,6 +49,62 @@ __global__ void k_group_prep(const int* __restrict__ groups, const int4* __restr
         const int node = groups[g];
         const int4 q = n_i4[node];
         const int b = q.x, e = q.x + q.y;
+        if (chunk > 0) {
+            // pass over the group per item: rank of each active particle by ballot
+            int base = 0, r0 = 0;
+            for (;;) {  // items [r0, r0 + chunk)
+                float x0 = 1e30f, y0 = 1e30f, z0 = 1e30f, x1 = -1e30f, y1 = -1e30f, z1 = -1e30f;
+                int rank_base = 0, in_item = 0;
+                for (int i0 = b; i0 < e; i0 += 32) {
+                    const int i = i0 + lane;
+                    const bool a = i < e && active[perm[i]] != 0;
+                    const unsigned m = __ballot_sync(0xffffffffu, a);
+                    const int rank = rank_base + __popc(m & lt);
+                    if (a && rank >= r0 && rank < r0 + chunk) {
+                        const float4 p = p4[i];
+                        x0 = fminf(x0, p.x); x1 = fmaxf(x1, p.x);
+                        y0 = fminf(y0, p.y); y1 = fmaxf(y1, p.y);
+                        z0 = fminf(z0, p.z); z1 = fmaxf(z1, p.z);
+                        ++in_item;
+                    }
+                    rank_base += __popc(m);
+                    if (rank_base >= r0 + chunk) break;
+                }
+                base = rank_base;
+                const int P = warp_sum(in_item);
+                if (P == 0) break;
+                x0 = warp_min(x0); y0 = warp_min(y0); z0 = warp_min(z0);
+                x1 = warp_max(x1); y1 = warp_max(y1); z1 = warp_max(z1);
+                const float bx = 0.5f * (x0 + x1), by = 0.5f * (y0 + y1), bz = 0.5f * (z0 + z1);
+                float br2 = 0.f;
+                int rb = 0;
+                for (int i0 = b; i0 < e && rb < r0 + chunk; i0 += 32) {
+                    const int i = i0 + lane;
+                    const bool a = i < e && active[perm[i]] != 0;
+                    const unsigned m = __ballot_sync(0xffffffffu, a);
+                    const int rank = rb + __popc(m & lt);
+                    if (a && rank >= r0 && rank < r0 + chunk) {
+                        const float4 p = p4[i];
+                        const float dx = p.x - bx, dy = p.y - by, dz = p.z - bz;
+                        br2 = fmaxf(br2, dx * dx + dy * dy + dz * dz);
+                    }
+                    rb += __popc(m);
+                }
+                br2 = warp_max(br2);
+                int slot = 0;
+                if (lane == 0) slot = atomicAdd(&cnt->num_work, 1);
+                slot = __shfl_sync(0xffffffffu, slot, 0);
+                if (lane == 0) {
+                    work[slot] = make_int4(b, q.y, P, r0);
+                    // float32 rounding of the centre: pad so every member stays inside
+                    sphere[slot] = make_float4(bx, by, bz, sqrtf(br2) * (1.f + 1e-6f));
+                }
+                if (P < chunk) break;
+                r0 += chunk;
+            }
+            (void)base;
+            continue;
+        }
         int nact = 0;
         float x0 = 1e30f, y0 = 1e30f, z0 = 1e30f, x1 = -1e30f, y1 = -1e30f, z1 = -1e30f;
         for (int i = b + lane; i < e; i += 32) {
@@ -72,7 +136,7 @@ __global__ void k_group_prep(const int* __restrict__ groups, const int4* __restr
         if (lane == 0) slot = atomicAdd(&cnt->num_work, 1);
         slot = __shfl_sync(0xffffffffu, slot, 0);
         if (lane == 0) {
-            work[slot] = make_int4(b, q.y, nact, node);
+            work[slot] = make_int4(b, q.y, nact, 0);
             sphere[slot] = make_float4(bx, by, bz, sqrtf(br2));
         }
     }
@@ -187,7 +251,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
         if (g >= nwork) break;
         const int4 w = work[g];
         const float4 sph = sphere[g];
-        const int b = w.x, count = w.y, Pall = w.z;
+        const int b = w.x, count = w.y, Pall = w.z, r0 = w.w;
         // Groups hold <= 64 particles except depth-48 leaves of coincident points; those are
         // evaluated in batches of 64 active particles, each batch walking the tree again.
         for (int pb = 0; pb < Pall; pb += 64) {
@@ -200,7 +264,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
             const bool a = i0 + lane < count && (active ? active[perm[i]] != 0 : true);
             const unsigned m = __ballot_sync(0xffffffffu, a);
             const int rank = nslot + __popc(m & lt);
-            if (a && rank >= pb && rank < pb + P) S.slot_pos[rank - pb] = i;
+            if (a && rank >= r0 + pb && rank < r0 + pb + P) S.slot_pos[rank - r0 - pb] = i;
             nslot += __popc(m);
         }
         __syncwarp();
@@ -227,10 +291,11 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
         const bool two = P > 32;
 
         int fill = 0, fillN = 0;
-        unsigned long long listlen = 0;
+        unsigned long long listlen = 0, nodelen = 0;
 #define GF_WALK_FLUSH()                                                                              \
     do {                                                                                             \
         listlen += fill + fillN;                                                                     \
+        nodelen += fillN;                                                                            \
         __syncwarp();                                                                                \
         if (QUAD) {                                                                                  \
             float px0 = 0.f, py0 = 0.f, pz0 = 0.f, px1 = 0.f, py1 = 0.f, pz1 = 0.f;                  \
@@ -364,7 +429,10 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
             ay0 += __shfl_xor_sync(0xffffffffu, ay0, o);
             az0 += __shfl_xor_sync(0xffffffffu, az0, o);
         }
-        if (lane == 0) atomicAdd(&cnt->pairs, listlen * (unsigned long long)P);
+        if (lane == 0) {
+            atomicAdd(&cnt->pairs, listlen * (unsigned long long)P);
+            if (QUAD) atomicAdd(&cnt->qpairs, nodelen * (unsigned long long)P);
+        }
         if (has0 && sub == 0) {
             const int k = perm[S.slot_pos[slot0]];
             acc[3 * size_t(k)] = ax0;
@@ -384,17 +452,18 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
 
 }  // namespace
 
-void Octree::prepare_walk(const uint8_t* active, cudaStream_t s) {
+void Octree::prepare_walk(const uint8_t* active, cudaStream_t s, int chunk) {
     Context& C = ctx();
     TreeCounts* cnt = counts.as<TreeCounts>();
     GF_CUDA(cudaMemsetAsync(&cnt->num_work, 0, 2 * sizeof(int), s));  // num_work, walk_next
-    GF_CUDA(cudaMemsetAsync(&cnt->pairs, 0, sizeof(unsigned long long), s));
+    GF_CUDA(cudaMemsetAsync(&cnt->pairs, 0, 2 * sizeof(unsigned long long), s));  // pairs, qpairs
     ProfScope ps(kStGroupPrep, s);
-    const int cap = std::max(1, node_cap);
+    // items: one per group (<= nodes), or at most one per active particle with chunks
+    const size_t cap = std::max<size_t>(1, std::max(size_t(node_cap), size_t(n)));
     active_ptr = active;
     k_group_prep<<<4 * C.sms, 256, 0, s>>>(groups.as<int>(), n_i4.as<int4>(), p4.as<float4>(),
                                           perm.as<int>(), active, cnt, work.get<int4>(cap),
-                                          sphere.get<float4>(cap));
+                                          sphere.get<float4>(cap), active ? chunk : 0);
     GF_CHECK_LAUNCH();
 }
 

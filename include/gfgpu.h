@@ -85,6 +85,12 @@ int gf_tree_size(int* num_nodes, int* num_groups);
  * particle index (cpp/nbody.cpp:62 idx); groups (ng,) node ids (cpp/nbody.cpp:235-243).
  * Host pointers. No reference counterpart (test hook). */
 int gf_tree_export(int32_t* ints, float* floats, int32_t* order, int32_t* groups);
+/* Rebuilds the gravity tree from pos / mass (host pointers) inside a captured CUDA graph —
+ * the synchronisation-free build that the batched form (gf_sim_blocks) replays — and runs
+ * it once. The tree must already hold n particles (e.g. from nbody_accel_active with
+ * rebuild), whose node buffers bound the new tree (GF_ERR_CAPACITY if it outgrows them).
+ * No reference counterpart (test hook: gf_tree_export then shows the captured build). */
+int gf_tree_rebuild_captured(int n, const double* pos, const double* mass, double theta);
 
 /* ---- device-resident gravity -------------------------------------------------------- */
 
@@ -206,6 +212,19 @@ int gf_sim_step(double dt_max, double* taken, int* substeps);
  * inner sub-steps of a block run as one captured CUDA graph; block boundaries rebuild the
  * tree and search neighbours afresh. updates: particle-updates done (forces computed). */
 int gf_sim_blocks(int nblocks, int nlev, double* updates);
+/* Launch shape of gf_sim_blocks per sub-step bin (bin b = sub-steps whose index has b
+ * trailing zero bits, i.e. levels 0..b due): chunk[b] = active particles per walk item
+ * (0: the reference's walk groups with their spheres; 1..64: items of <= chunk[b] active
+ * particles in tree order, each with its own bounding sphere); bins past nbins reuse
+ * chunk[nbins-1]; chunk NULL = groups everywhere. rebuild_every > 0 rebuilds the tree inside
+ * the captured block every that many sub-steps (0: refit only). */
+int gf_sim_block_config(const int* chunk, int nbins, int rebuild_every);
+/* Autotuner of that launch shape on the current state: times the gravity walk of each bin's
+ * active set per chunk candidate, then one block per rebuild cadence; keeps the fastest and
+ * writes them to chunk (nlev-1 entries) / rebuild_every; graph_ms = the best block's graph
+ * time. Positions, velocities and time are restored afterwards (the next block starts with
+ * a full evaluation). */
+int gf_sim_block_autotune(int nlev, int* chunk, int* rebuild_every, double* graph_ms);
 /* Fraction of the particles on each level 0..nlev-1 of the current block. */
 int gf_sim_levels(int nlev, double* frac);
 /* Particle-updates of the last gf_sim_step: particles that received freshly computed forces
@@ -235,6 +254,12 @@ int gf_sim_read(double* pos, double* vel, double* acc, double* dt_ind, double* t
  *                       fills with (features, log of the converged h) pairs for training;
  *                       setting it clears the buffer; gf_get_option returns the rows kept. */
 #define GF_OPT_COLLECT 3
+/*   GF_OPT_WALK_CHUNK   walks of an active subset (gf_accel_active*, gf_accelerations with an
+ *                       active mask): 0 = the reference's groups and spheres (default);
+ *                       1..64 = items of <= that many active particles in tree order, each
+ *                       with the bounding sphere of its own particles (no reference
+ *                       counterpart: same opening criterion per particle, tighter spheres). */
+#define GF_OPT_WALK_CHUNK 4
 int gf_set_option(int key, double value);
 /* Current value of an option (-1 for an unknown key). */
 double gf_get_option(int key);
@@ -285,6 +310,8 @@ long long gf_launch_count(void);
 void* gf_stream(void);
 /* Particle-list pair interactions evaluated by the most recent gravity walk (synchronises). */
 long long gf_walk_pairs(void);
+/* Of those, the interactions with quadrupole nodes (mixed form; 0 for the monopole walk). */
+long long gf_walk_quad_pairs(void);
 /* Measures the float32 FFMA throughput of the GPU (TFLOP/s, an FMA counting 2 flops): the
  * roofline peak of the float32 walk. */
 int gf_fp32_peak(double* tflops);

@@ -140,12 +140,16 @@ class StepOracle:
 
 class BlockOracle:
     """CPU restatement of the block time-step scheme of the library's batched form (power-of-two
-    levels, gravity of the particles due at each sub-step on a refitted tree, opening /
+    levels, gravity of the particles due at each sub-step on a refitted tree — or a rebuilt one
+    every `rebuild_every` sub-steps — opening /
     full / closing kicks). Gravity only: for particle sets without gas."""
 
-    def __init__(self, pos, vel, mass, theta, eps, nlev):
+    def __init__(self, pos, vel, mass, theta, eps, nlev, rebuild_every=0, chunk=None):
         self.pos, self.vel, self.mass = pos.copy(), vel.copy(), mass
         self.theta, self.eps, self.nlev = theta, eps, nlev
+        self.rebuild_every = rebuild_every  # tree rebuilt at sub-steps s % rebuild_every == 0
+        # walk items per sub-step bin (trailing zero bits of the sub-step index); None: groups
+        self.chunk = chunk
         self.acc = np.zeros_like(pos)
         self.t = 0.0
         self._force(None, True)
@@ -168,7 +172,12 @@ class BlockOracle:
         for s in range(1, nsub):
             self.pos += self.delta * self.vel
             act = (s % (1 << self.level)) == 0
-            self._force(act.astype(np.uint8), False)
+            rebuild = self.rebuild_every > 0 and s % self.rebuild_every == 0
+            if self.chunk is not None:
+                tz = (s & -s).bit_length() - 1
+                oracle.set_walk_chunk(self.chunk[min(tz, len(self.chunk) - 1)])
+            self._force(act.astype(np.uint8), rebuild)
+            oracle.set_walk_chunk(0)
             self.vel[act] += step[act][:, None] * self.acc[act]
         self.pos += self.delta * self.vel
         self._force(None, True)

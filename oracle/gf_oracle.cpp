@@ -292,11 +292,36 @@ void refit(Octree& T, const double* pos, const double* mass) {
     }
 }
 
+// Walk of one sphere: the interaction list of accepted nodes and opened-leaf particles.
+template <class Append>
+void walk_list(const Octree& T, float bx, float by, float bz, float br, Append&& append) {
+    const Node* nd = T.nodes.data();
+    const int nn = int(T.nodes.size());
+    for (int k = 0; k < nn;) {
+        const Node& q = nd[k];
+        const float dx = q.cx - bx, dy = q.cy - by, dz = q.cz - bz;
+        const float t = q.open_r + br;
+        if (dx * dx + dy * dy + dz * dz > t * t) {
+            append(q.cx, q.cy, q.cz, q.m);
+            k = q.next;
+        } else if (q.leaf) {
+            for (int j = q.start; j < q.start + q.count; ++j) append(T.fx[j], T.fy[j], T.fz[j], T.fm[j]);
+            k = q.next;
+        } else {
+            ++k;
+        }
+    }
+}
+
+// Walk items of <= chunk active particles (the library's GF_OPT_WALK_CHUNK; no reference
+// counterpart): a group's active particles in tree order are cut into items, each walked
+// with the bounding sphere (float32 box centre, radius padded by 1e-6) of its own particles.
+int g_walk_chunk = 0;
+
 // Group walk + list evaluation (cpp/nbody.cpp:323-411).
 void accel(Octree& T, double* acc, double eps, const uint8_t* active) {
     const float eps2 = float(eps * eps);
     const Node* nd = T.nodes.data();
-    const int nn = int(T.nodes.size());
     const int ng = int(T.groups.size());
     const float* px = T.fx.data();
     const float* py = T.fy.data();
@@ -320,10 +345,54 @@ void accel(Octree& T, double* acc, double eps, const uint8_t* active) {
             lm[len] = d;
             ++len;
         };
+        auto eval = [&](int p) {
+            const float x = px[p], y = py[p], z = pz[p];
+            float sx = 0, sy = 0, sz = 0;
+#pragma omp simd reduction(+ : sx, sy, sz)
+            for (int j = 0; j < len; ++j) {
+                const float ex = lx[j] - x, ey = ly[j] - y, ez = lz[j] - z;
+                const float r2 = ex * ex + ey * ey + ez * ez + eps2;
+                const float inv = 1.0f / std::sqrt(r2);
+                const float f = lm[j] * inv * inv * inv;
+                sx += f * ex;
+                sy += f * ey;
+                sz += f * ez;
+            }
+            const int k = T.order[p];
+            acc[3 * k] = sx;
+            acc[3 * k + 1] = sy;
+            acc[3 * k + 2] = sz;
+        };
 #pragma omp for schedule(dynamic, 4)
         for (int g = 0; g < ng; ++g) {
             const Node& G = nd[T.groups[g]];
             const int b = G.start, e = G.start + G.count;
+            if (active && g_walk_chunk > 0) {
+                std::vector<int> act;
+                for (int i = b; i < e; ++i)
+                    if (active[T.order[i]]) act.push_back(i);
+                for (size_t c0 = 0; c0 < act.size(); c0 += size_t(g_walk_chunk)) {
+                    const size_t c1 = std::min(act.size(), c0 + size_t(g_walk_chunk));
+                    float x0 = 1e30f, y0 = 1e30f, z0 = 1e30f, x1 = -1e30f, y1 = -1e30f, z1 = -1e30f;
+                    for (size_t a = c0; a < c1; ++a) {
+                        const int i = act[a];
+                        x0 = std::min(x0, px[i]); x1 = std::max(x1, px[i]);
+                        y0 = std::min(y0, py[i]); y1 = std::max(y1, py[i]);
+                        z0 = std::min(z0, pz[i]); z1 = std::max(z1, pz[i]);
+                    }
+                    const float bx = 0.5f * (x0 + x1), by = 0.5f * (y0 + y1), bz = 0.5f * (z0 + z1);
+                    float br2 = 0;
+                    for (size_t a = c0; a < c1; ++a) {
+                        const int i = act[a];
+                        const float dx = px[i] - bx, dy = py[i] - by, dz = pz[i] - bz;
+                        br2 = std::max(br2, dx * dx + dy * dy + dz * dz);
+                    }
+                    len = 0;
+                    walk_list(T, bx, by, bz, std::sqrt(br2) * (1.f + 1e-6f), append);
+                    for (size_t a = c0; a < c1; ++a) eval(act[a]);
+                }
+                continue;
+            }
             if (active) {
                 bool any = false;
                 for (int i = b; i < e && !any; ++i) any = active[T.order[i]] != 0;
@@ -350,43 +419,10 @@ void accel(Octree& T, double* acc, double eps, const uint8_t* active) {
             const float br = std::sqrt(br2);
 
             len = 0;
-            for (int k = 0; k < nn;) {
-                const Node& q = nd[k];
-                const float dx = q.cx - bx, dy = q.cy - by, dz = q.cz - bz;
-                const float t = q.open_r + br;
-                if (dx * dx + dy * dy + dz * dz > t * t) {
-                    append(q.cx, q.cy, q.cz, q.m);
-                    k = q.next;
-                } else if (q.leaf) {
-                    for (int j = q.start; j < q.start + q.count; ++j) append(px[j], py[j], pz[j], pm[j]);
-                    k = q.next;
-                } else {
-                    ++k;
-                }
-            }
-
-            const float* __restrict ax_ = lx.data();
-            const float* __restrict ay_ = ly.data();
-            const float* __restrict az_ = lz.data();
-            const float* __restrict am_ = lm.data();
+            walk_list(T, bx, by, bz, br, append);
             for (int p = b; p < e; ++p) {
                 if (active && !active[T.order[p]]) continue;
-                const float x = px[p], y = py[p], z = pz[p];
-                float sx = 0, sy = 0, sz = 0;
-#pragma omp simd reduction(+ : sx, sy, sz)
-                for (int j = 0; j < len; ++j) {
-                    const float ex = ax_[j] - x, ey = ay_[j] - y, ez = az_[j] - z;
-                    const float r2 = ex * ex + ey * ey + ez * ez + eps2;
-                    const float inv = 1.0f / std::sqrt(r2);
-                    const float f = am_[j] * inv * inv * inv;
-                    sx += f * ex;
-                    sy += f * ey;
-                    sz += f * ez;
-                }
-                const int k = T.order[p];
-                acc[3 * k] = sx;
-                acc[3 * k + 1] = sy;
-                acc[3 * k + 2] = sz;
+                eval(p);
             }
         }
     }
@@ -433,6 +469,8 @@ int orc_num_threads(void) { return omp_get_max_threads(); }
 void orc_set_threads(int t) {
     if (t > 0) omp_set_num_threads(t);
 }
+
+void orc_set_walk_chunk(int c) { g_walk_chunk = c > 0 ? c : 0; }
 
 // Mirrors nbody_accel_active (cpp/nbody.cpp:422-425): a process-global tree, rebuilt when
 // asked or when n changes, refitted otherwise.

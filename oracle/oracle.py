@@ -50,6 +50,7 @@ def lib():
         L = ctypes.CDLL(LIB)
         L.orc_num_threads.restype = _ci
         L.orc_set_threads.argtypes = [_ci]
+        L.orc_set_walk_chunk.argtypes = [_ci]
         L.orc_accel_active.argtypes = [_ci, _dbl, _dbl, _dbl, _cd, _cd, ctypes.c_void_p, _ci]
         L.orc_accel_direct.argtypes = [_ci, _dbl, _dbl, _dbl, _cd]
         L.orc_accel_direct_targets.argtypes = [_ci, _dbl, _dbl, _ci, _i64, _dbl, _cd]
@@ -75,6 +76,11 @@ def num_threads():
 
 def set_threads(t):
     lib().orc_set_threads(int(t))
+
+
+def set_walk_chunk(c):
+    """Walk items of <= c active particles with their own spheres (0: the reference's groups)."""
+    lib().orc_set_walk_chunk(int(c))
 
 
 def accel_active(pos, mass, acc, theta, eps, active=None, rebuild=True):

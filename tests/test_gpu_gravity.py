@@ -155,6 +155,30 @@ def test_coincident_and_deep_cells(engine, oracle):
     assert np.percentile(rel_err(acc, ref), 99) <= P99_TOL
 
 
+@pytest.mark.parametrize("case", [0, 1, 3, "deep"])
+def test_captured_rebuild_identical_to_oracle(engine, oracle, case):
+    """The synchronisation-free build that the batched form replays inside a CUDA graph
+    (gf_tree_rebuild_captured) gives the regular tree node for node, deep cells included."""
+    from galaxy_formation_gb300 import _lib
+
+    rng = np.random.default_rng(7)
+    if case == "deep":
+        base = rng.normal(size=(3000, 3))
+        pos = np.ascontiguousarray(np.concatenate([base, np.repeat(base[:1], 20, axis=0),
+                                                   base[1] + 1e-9 * rng.normal(size=(30, 3))]))
+        mass = np.full(len(pos), 1.0 / len(pos))
+        theta = 0.7
+        pos1 = pos.copy()
+        pos1[:3000] += 1e-3 * rng.normal(size=(3000, 3))
+    else:
+        _, pos, mass, theta, _ = list(cases())[case]
+        pos1 = pos * (1 + 1e-3 * rng.normal(size=pos.shape))
+    pos1 = np.ascontiguousarray(pos1)
+    engine.build_tree(pos, mass, theta)  # regular build: the node buffers for this set
+    _lib.check(engine.lib.gf_tree_rebuild_captured(len(mass), pos1, mass, theta))
+    compare_trees(engine.tree(), oracle.build_tree(pos1, mass, theta))
+
+
 def test_massless_and_inactive_groups(engine, oracle):
     rng = np.random.default_rng(5)
     pos = np.ascontiguousarray(rng.normal(size=(5000, 3)))
