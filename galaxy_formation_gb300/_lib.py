@@ -86,6 +86,7 @@ OPT_GRAVITY_QUAD = 1
 OPT_HGUESS = 2
 OPT_COLLECT = 3
 OPT_WALK_CHUNK = 4
+OPT_WALK_GROUP = 5
 MLP_PARAMS = 4545
 
 STAGES = ["tree_build", "tree_refit", "walk", "group_prep", "knn", "knn_tree", "sph_density",

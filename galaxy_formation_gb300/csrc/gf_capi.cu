@@ -554,6 +554,11 @@ int gf_set_option(int key, double value) {
                 require(value >= 0 && value <= 64, "walk chunk is 0..64");
                 F.walk_chunk = int(value);
                 break;
+            case GF_OPT_WALK_GROUP:
+                require(value >= 8 && value <= 128, "walk group is 8..128");
+                F.walk_group = int(value);
+                F.grav.valid = false;  // regroup at the next evaluation
+                break;
             default: throw Error(GF_ERR_ARG, "unknown option");
         }
     });
@@ -567,6 +572,7 @@ double gf_get_option(int key) {
         case GF_OPT_HGUESS: return F.hguess;
         case GF_OPT_COLLECT: return double(F.collect_n);
         case GF_OPT_WALK_CHUNK: return F.walk_chunk;
+        case GF_OPT_WALK_GROUP: return F.walk_group;
         default: return -1.0;
     }
 }

@@ -122,16 +122,22 @@ __device__ __forceinline__ void raise_status(uint32_t* st, uint32_t bit) {
     if (st) atomicOr(st, bit);
 }
 
+// Scratch of exclusive_scan / radix_sort_pairs. Work queued on different streams at the same
+// time needs different scratch (null = the context's, for the library's main stream).
+struct ScanScratch {
+    DevBuf scan_tmp, sort_tmp;
+};
+
 // Device-wide exclusive scan of int32 (n may be 0). `total` (device) receives the sum.
-void exclusive_scan(const int* in, int* out, int n, int* total, cudaStream_t s);
+void exclusive_scan(const int* in, int* out, int n, int* total, cudaStream_t s, ScanScratch* sc = nullptr);
 
 // Sizes the scratch of exclusive_scan / radix_sort_pairs for inputs of up to n elements.
-void reserve_scan_sort(int n);
+void reserve_scan_sort(int n, ScanScratch* sc = nullptr);
 
 // Stable LSD radix sort of (key, value) pairs on bits [bit_lo, bit_hi) of the keys.
 // Results end in keys/vals (the alternate buffers are scratch of the same size).
 void radix_sort_pairs(uint64_t* keys, int* vals, uint64_t* keys_alt, int* vals_alt, int n,
-                      int bit_lo, int bit_hi, cudaStream_t s);
+                      int bit_lo, int bit_hi, cudaStream_t s, ScanScratch* sc = nullptr);
 
 // A subset of particles to process: idx[0 .. *count) (device memory, count read on the
 // device so the launch stays valid inside a captured graph); idx == null means all n.

@@ -184,14 +184,13 @@ __global__ void k_scan_tiles(const int* __restrict__ in, int* __restrict__ out, 
     }
 }
 
-void exclusive_scan(const int* in, int* out, int n, int* total, cudaStream_t s) {
-    Context& c = g_ctx;
+void exclusive_scan(const int* in, int* out, int n, int* total, cudaStream_t s, ScanScratch* sc) {
     if (n <= 0) {
         if (total) GF_CUDA(cudaMemsetAsync(total, 0, sizeof(int), s));
         return;
     }
     const int tiles = div_up(n, kScanTile);
-    int* sums = c.scan_tmp.get<int>(size_t(tiles) + 1);
+    int* sums = (sc ? sc->scan_tmp : g_ctx.scan_tmp).get<int>(size_t(tiles) + 1);
     k_scan_tile_sums<<<tiles, kScanThreads, 0, s>>>(in, n, sums);
     GF_CHECK_LAUNCH();
     k_scan_sums<<<1, 1024, 0, s>>>(sums, tiles, total);
@@ -279,20 +278,20 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_downsweep(
     }
 }
 
-void reserve_scan_sort(int n) {
-    Context& c = g_ctx;
+void reserve_scan_sort(int n, ScanScratch* sc) {
+    DevBuf& sort_tmp = sc ? sc->sort_tmp : g_ctx.sort_tmp;
+    DevBuf& scan_tmp = sc ? sc->scan_tmp : g_ctx.scan_tmp;
     const int rs_tiles = div_up(std::max(n, 1), kRsTile);
-    c.sort_tmp.get<int>(size_t(256) * rs_tiles * 2);
+    sort_tmp.get<int>(size_t(256) * rs_tiles * 2);
     const int scan_n = std::max(n, 256 * rs_tiles);
-    c.scan_tmp.get<int>(size_t(div_up(scan_n, kScanTile)) + 1);
+    scan_tmp.get<int>(size_t(div_up(scan_n, kScanTile)) + 1);
 }
 
 void radix_sort_pairs(uint64_t* keys, int* vals, uint64_t* keys_alt, int* vals_alt, int n,
-                      int bit_lo, int bit_hi, cudaStream_t s) {
+                      int bit_lo, int bit_hi, cudaStream_t s, ScanScratch* sc) {
     if (n <= 1) return;
-    Context& c = g_ctx;
     const int tiles = div_up(n, kRsTile);
-    int* hist = c.sort_tmp.get<int>(size_t(256) * tiles * 2);
+    int* hist = (sc ? sc->sort_tmp : g_ctx.sort_tmp).get<int>(size_t(256) * tiles * 2);
     int* offs = hist + size_t(256) * tiles;
     uint64_t *ka = keys, *kb = keys_alt;
     int *va = vals, *vb = vals_alt;
@@ -300,7 +299,7 @@ void radix_sort_pairs(uint64_t* keys, int* vals, uint64_t* keys_alt, int* vals_a
     for (int shift = bit_lo; shift < bit_hi; shift += 8) {
         k_rs_upsweep<<<tiles, kRsThreads, 0, s>>>(ka, n, shift, hist, tiles);
         GF_CHECK_LAUNCH();
-        exclusive_scan(hist, offs, 256 * tiles, nullptr, s);
+        exclusive_scan(hist, offs, 256 * tiles, nullptr, s, sc);
         k_rs_downsweep<<<tiles, kRsThreads, 0, s>>>(ka, va, kb, vb, n, shift, offs, tiles);
         GF_CHECK_LAUNCH();
         std::swap(ka, kb);

@@ -289,24 +289,51 @@ void ForceEngine::evaluate(const ForceArgs& a, cudaStream_t s) {
     if (!scalars_h) GF_CUDA(cudaMallocHost(&scalars_h, sizeof(HydroScalars)));
     HydroScalars* sc = scalars.get<HydroScalars>(1);
 
+    // Gravity on s, hydro on a second stream: the two are independent until the combination.
+    // The gravity chain is queued first and without host synchronisation (a tree of this
+    // particle set was built before: its node buffers bound the new one), so the GPU runs it
+    // while the host drives the hydro chain, whose own synchronisations wait on its stream only.
+    const bool fork = a.sph != 0;
+    if (fork) {
+        if (!s2) {
+            GF_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+            GF_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+            GF_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+        }
+        GF_CUDA(cudaEventRecord(ev_fork, s));
+        GF_CUDA(cudaStreamWaitEvent(s2, ev_fork, 0));
+    }
+
     // gravity (simulation.py:64)
     Octree& T = grav;
+    const int gmax = gravity_quad ? walk_group : kGroupMax;  // the mixed form's groups are tunable
     if (a.nosync) {  // inside a captured graph: the tree of the last regular build, rebuilt or refitted
         if (!T.valid || T.n != n) throw Error(GF_ERR_ARG, "a synchronisation-free evaluation needs a built tree");
         if (a.rebuild)
             T.build(n, a.pos, a.mass, a.theta, s, true);
         else
             T.refit(a.pos, a.mass, s);
-    } else if (a.rebuild || !T.valid || T.n != n || T.quad != (gravity_quad != 0)) {
+    } else if (a.rebuild || !T.valid || T.n != n || T.quad != (gravity_quad != 0) || T.group_max != gmax) {
+        const bool same_set = T.valid && T.n == n && T.quad == (gravity_quad != 0) && T.group_max == gmax;
         T.quad = gravity_quad != 0;
-        T.build(n, a.pos, a.mass, a.theta, s);
+        T.group_max = gmax;
+        if (same_set) {
+            T.reserve_graph_build();
+            T.build(n, a.pos, a.mass, a.theta, s, true);
+        } else {
+            T.build(n, a.pos, a.mass, a.theta, s);
+        }
     } else {
         T.refit(a.pos, a.mass, s);
     }
     T.prepare_walk(a.active, s, a.walk_chunk ? a.walk_chunk : walk_chunk);
     T.walk(a.eps, acc_grav.as<double>(), s);
 
-    if (a.sph) hydro(a, s);
+    if (fork) {
+        hydro(a, s2);
+        GF_CUDA(cudaEventRecord(ev_join, s2));
+        GF_CUDA(cudaStreamWaitEvent(s, ev_join, 0));
+    }
 
     // combination (simulation.py:68-71)
     if (!a.nosync) GF_CUDA(cudaMemsetAsync(&sc->amax_bits, 0, sizeof(unsigned long long), s));
@@ -344,7 +371,7 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
         GF_CHECK_LAUNCH();
         GF_CUDA(cudaMemsetAsync(sc, 0, sizeof(HydroScalars), s));
         GF_CUDA(cudaMemsetAsync(&sc->dtmin_bits, 0x7f, sizeof(unsigned long long), s));
-        exclusive_scan(fl, sc_, n, &sc->ng, s);
+        exclusive_scan(fl, sc_, n, &sc->ng, s, &hscratch);
         GF_CUDA(cudaMemcpyAsync(&scalars_h->ng, &sc->ng, sizeof(int), cudaMemcpyDeviceToHost, s));
         GF_CUDA(cudaStreamSynchronize(s));
         ng = scalars_h->ng;
@@ -380,7 +407,7 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
         int* lst = alist.get<int>(ng);
         k_flag_in_order<<<ggrid, kThreads, 0, s>>>(ng, vorder, ga, fl2);
         GF_CHECK_LAUNCH();
-        exclusive_scan(fl2, sc2, ng, &sc->nact, s);
+        exclusive_scan(fl2, sc2, ng, &sc->nact, s, &hscratch);
         k_compact<<<ggrid, kThreads, 0, s>>>(ng, vorder, fl2, sc2, lst);
         GF_CHECK_LAUNCH();
         sub = Subset{lst, &sc->nact};

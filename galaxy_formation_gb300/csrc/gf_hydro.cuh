@@ -43,6 +43,7 @@ struct ForceEngine {
     int sph_float32 = 0;     // 1: mixed-precision SPH (float32 + Kahan), 0: float64
     int gravity_quad = 0;    // 1: quadrupole moments + Kahan tile sums, 0: the reference's monopole
     int walk_chunk = 0;      // walk items for active-set walks (0: the reference's groups)
+    int walk_group = 64;     // mixed form: walk groups = shallowest nodes with <= this many particles
     int hguess = 0;          // start of the neighbour-count iteration: 0 previous h, 1 cell
                              // density only, 2 the learned guess (MLP)
     long long collect_cap = 0, collect_n = 0;  // (features, log h) training pairs kept
@@ -60,6 +61,9 @@ struct ForceEngine {
     DevBuf flag, scan, gidx, gpos, gvel, gmass, gu_, nb48, dsel, rguess, h, rho, gacc, dudt, dt_i;
     DevBuf scalars;
     DevBuf divv_prev, gdivv, hX, hY, hrg, colX, colT, gact, aflag, ascan, alist;
+    ScanScratch hscratch;    // scans of the hydro stream
+    cudaStream_t s2 = nullptr;               // the hydro chain's stream
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     HydroScalars* scalars_h = nullptr;  // pinned copy, valid after the stream synchronises
 
     void evaluate(const ForceArgs& a, cudaStream_t s);
@@ -67,6 +71,7 @@ struct ForceEngine {
     // every buffer a captured (synchronisation-free) evaluation touches, at its final size
     void reserve_nosync(int n) {
         grav.reserve_graph_build();
+        reserve_scan_sort(n, &hscratch);
         if (ng > 0) {
             gact.get<uint8_t>(ng);
             aflag.get<int>(ng);

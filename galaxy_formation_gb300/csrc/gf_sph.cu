@@ -175,7 +175,7 @@ __device__ void warp_bitonic(K* key, int* tag, int P) {
     for (int size = 2; size <= P; size <<= 1) {
         for (int stride = size >> 1; stride > 0; stride >>= 1) {
             for (int t = lane; t < P / 2; t += 32) {
-                const int a = 2 * stride * (t / stride) + (t % stride);
+                const int a = ((t & ~(stride - 1)) << 1) | (t & (stride - 1));
                 const int b = a + stride;
                 const bool up = (a & size) == 0;
                 const K ka = key[a], kb = key[b];
@@ -186,6 +186,27 @@ __device__ void warp_bitonic(K* key, int* tag, int P) {
                     key[b] = ka;
                     tag[a] = tb;
                     tag[b] = ta;
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// Ascending bitonic sort of P (power of two <= 128) 64-bit keys in shared memory by the
+// calling warp (keys are unique when they carry an index in their low bits).
+__device__ void warp_sort_u64(unsigned long long* key, int P) {
+    const int lane = threadIdx.x & 31;
+    for (int size = 2; size <= P; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int t = lane; t < P / 2; t += 32) {
+                const int a = ((t & ~(stride - 1)) << 1) | (t & (stride - 1));
+                const int b = a + stride;
+                const bool up = (a & size) == 0;
+                const unsigned long long ka = key[a], kb = key[b];
+                if ((ka > kb) == up) {
+                    key[a] = kb;
+                    key[b] = ka;
                 }
             }
             __syncwarp();
@@ -243,10 +264,17 @@ constexpr int kKnnWarps = 8;
 constexpr int kKnnStack = 512;
 constexpr int kKnnCap = 128;
 
+// A collected point: (float32 squared distance bits << 32) | tree position. The bits of a
+// non-negative float order like the float, so sorting the keys orders by distance, then index.
+__device__ __forceinline__ unsigned long long knn_key(float d2, int j) {
+    return ((unsigned long long)__float_as_uint(d2) << 32) | unsigned(j);
+}
+__device__ __forceinline__ float key_d2(unsigned long long k) { return __uint_as_float(unsigned(k >> 32)); }
+__device__ __forceinline__ int key_idx(unsigned long long k) { return int(unsigned(k)); }
+
 struct KnnSmem {
     int stack[kKnnStack];
-    float d2[kKnnCap];
-    int idx[kKnnCap];
+    unsigned long long key[kKnnCap];
     unsigned long long dd[64];  // float64 squared distances as bit patterns
     int di[64];
     int lanemap[32];
@@ -349,16 +377,28 @@ __device__ int knn_collect(const KnnArgs& A, KnnSmem& S, float4 xh, float4 xl, f
         if (sp + npush > kKnnStack) return -1;
         if (inner) S.stack[sp + __popc(om & lt)] = (first << 4) | code;
         sp += npush;
-        int lc = leaf ? -code : 0;
-        int maxc = lc;
+        // particles of the opened leaves, concatenated in lane order and tested 32 at a time:
+        // lane l takes offset o = base + l, owned by the lane whose leaf range covers o
+        const int lc = leaf ? -code : 0;
+        const int lincl = warp_incl_scan(lc);
+        const int lexcl = lincl - lc;
+        const int ltot = __shfl_sync(0xffffffffu, lincl, 31);
+        for (int base = 0; base < ltot; base += 32) {
+            const int o = base + lane;
+            int src = 0;  // lanes whose inclusive end is <= o (branch-free lower bound)
 #pragma unroll
-        for (int o = 16; o; o >>= 1) maxc = max(maxc, __shfl_xor_sync(0xffffffffu, maxc, o));
-        for (int t = 0; t < maxc; ++t) {
+            for (int step = 16; step; step >>= 1) {
+                const int v = __shfl_sync(0xffffffffu, lincl, src + step - 1);
+                if (v <= o) src += step;
+            }
+            src = min(src, 31);
+            const int f_src = __shfl_sync(0xffffffffu, first, src);
+            const int e_src = __shfl_sync(0xffffffffu, lexcl, src);
             bool hit = false;
             float d2 = 0.f;
             int j = 0;
-            if (t < lc) {
-                j = first + t;
+            if (o < ltot) {
+                j = f_src + (o - e_src);
                 const float4 ph = A.p4[j], pl = A.plo[j];
                 const float dx = (ph.x - xh.x) + (pl.x - xl.x);
                 const float dy = (ph.y - xh.y) + (pl.y - xl.y);
@@ -369,10 +409,7 @@ __device__ int knn_collect(const KnnArgs& A, KnnSmem& S, float4 xh, float4 xl, f
             const unsigned hm = __ballot_sync(0xffffffffu, hit);
             if (hit) {
                 const int slot = cnt + __popc(hm & lt);
-                if (slot < kKnnCap) {
-                    S.d2[slot] = d2;
-                    S.idx[slot] = j;
-                }
+                if (slot < kKnnCap) S.key[slot] = knn_key(d2, j);
             }
             cnt += __popc(hm);
         }
@@ -381,73 +418,83 @@ __device__ int knn_collect(const KnnArgs& A, KnnSmem& S, float4 xh, float4 xl, f
     return cnt;
 }
 
-// Sorts the cnt (<= kKnnCap) collected points of query q (tree position) held in d2/idx,
-// re-measures the k nearest and the float32 near-ties in float64, sorts those and writes the
-// k nearest (ascending, ties by index) in the caller's order.
-__device__ void knn_finish(const KnnArgs& A, float* d2, int* idx, unsigned long long* dd, int* di, int cnt,
+// Sorts the cnt (<= kKnnCap) collected points of query q (tree position), re-measures the
+// k nearest and the float32 near-ties in float64 and writes the k nearest (ascending, ties by
+// index) in the caller's order.
+__device__ __forceinline__ double d2_f64(const KnnArgs& A, int pi, int pj) {
+    const double dx = A.pos[3 * size_t(pi)] - A.pos[3 * size_t(pj)];
+    const double dy = A.pos[3 * size_t(pi) + 1] - A.pos[3 * size_t(pj) + 1];
+    const double dz = A.pos[3 * size_t(pi) + 2] - A.pos[3 * size_t(pj) + 2];
+    return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+}
+
+__device__ void knn_finish(const KnnArgs& A, unsigned long long* key, unsigned long long* dd, int* di, int cnt,
                            int q) {
     const int lane = threadIdx.x & 31;
     const int k = A.k;
     const int oq = A.perm[q];
     int P = 64;
     while (P < cnt) P <<= 1;
-    for (int t = cnt + lane; t < P; t += 32) {
-        d2[t] = INFINITY;
-        idx[t] = 0x7fffffff;
-    }
+    for (int t = cnt + lane; t < P; t += 32) key[t] = ~0ull;
     __syncwarp();
-    warp_bitonic(d2, idx, P);
+    warp_sort_u64(key, P);
     const int pi = oq;
     if (!A.exact_order) {
         // Float32 order: the k nearest as a set (only pairs tied to float32 rounding can
         // swap). The neighbour at dsel_col fixes h: the entries within float32 rounding of
         // it are re-measured in float64 and the dsel_col-th smallest is taken.
         const int c = A.dsel_col;
-        const float lo = d2[c] * (1.0f - 2e-5f), hi = d2[c] * (1.0f + 2e-5f);
-        int below = 0;
-        for (int t = lane; t < cnt; t += 32) below += d2[t] < lo;
-        below = warp_sum(below);
-        const double xi = A.pos[3 * size_t(pi)], yi = A.pos[3 * size_t(pi) + 1], zi = A.pos[3 * size_t(pi) + 2];
-        double best = INFINITY;
-        int rank_need = c - below;  // rank of the wanted entry among the ambiguous ones
-        for (int t = lane; t < 64; t += 32) {
-            double v = INFINITY;
-            int tag = 0x7fffffff;
-            if (t < cnt && d2[t] >= lo && d2[t] <= hi) {
-                const int pj = A.perm[idx[t]];
-                const double dx = xi - A.pos[3 * size_t(pj)], dy = yi - A.pos[3 * size_t(pj) + 1],
-                             dz = zi - A.pos[3 * size_t(pj) + 2];
-                v = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-                tag = pj;
-            }
-            dd[t] = (unsigned long long)__double_as_longlong(v);
-            di[t] = tag;
+        const float dc = key_d2(key[c]);
+        const float lo = dc * (1.0f - 2e-5f), hi = dc * (1.0f + 2e-5f);
+        int below = 0, inband = 0;
+        for (int t = lane; t < cnt; t += 32) {
+            const float v = key_d2(key[t]);
+            below += v < lo;
+            inband += v >= lo && v <= hi;
         }
-        __syncwarp();
-        warp_bitonic(dd, di, 64);
-        best = __longlong_as_double((long long)dd[max(0, rank_need)]);
+        below = warp_sum(below);
+        inband = warp_sum(inband);
+        double best;
+        if (inband == 1) {  // no float32 near-tie: entry c itself, measured in float64
+            best = d2_f64(A, pi, A.perm[key_idx(key[c])]);
+        } else {
+            const int rank_need = c - below;  // rank of the wanted entry among the ambiguous ones
+            for (int t = lane; t < 64; t += 32) {
+                double v = INFINITY;
+                int tag = 0x7fffffff;
+                const float vf = t < cnt ? key_d2(key[t]) : INFINITY;
+                if (t < cnt && vf >= lo && vf <= hi) {
+                    const int pj = A.perm[key_idx(key[t])];
+                    v = d2_f64(A, pi, pj);
+                    tag = pj;
+                }
+                dd[t] = (unsigned long long)__double_as_longlong(v);
+                di[t] = tag;
+            }
+            __syncwarp();
+            warp_bitonic(dd, di, 64);
+            best = __longlong_as_double((long long)dd[max(0, rank_need)]);
+        }
         for (int t = lane; t < k; t += 32) {
-            if (A.nb32) A.nb32[size_t(oq) * A.ld32 + t] = A.perm[idx[t]];
-            if (A.nb) A.nb[size_t(oq) * k + t] = A.perm[idx[t]];
+            const int pj = A.perm[key_idx(key[t])];
+            if (A.nb32) A.nb32[size_t(oq) * A.ld32 + t] = pj;
+            if (A.nb) A.nb[size_t(oq) * k + t] = pj;
         }
         if (A.dsel && lane == 0) A.dsel[oq] = __dsqrt_rn(best);
         __syncwarp();
         return;
     }
     // the k nearest and everything within float32 rounding of the k-th distance
-    const float thr = d2[k - 1] * (1.0f + 2e-5f);
+    const float thr = key_d2(key[k - 1]) * (1.0f + 2e-5f);
     int m = 0;
-    for (int t = lane; t < cnt; t += 32) m += d2[t] <= thr;
+    for (int t = lane; t < cnt; t += 32) m += key_d2(key[t]) <= thr;
     m = min(64, warp_sum(m));
-    const double xi = A.pos[3 * size_t(pi)], yi = A.pos[3 * size_t(pi) + 1], zi = A.pos[3 * size_t(pi) + 2];
     for (int t = lane; t < 64; t += 32) {
         double v = INFINITY;
         int tag = 0x7fffffff;
         if (t < m) {
-            const int pj = A.perm[idx[t]];
-            const double dx = xi - A.pos[3 * size_t(pj)], dy = yi - A.pos[3 * size_t(pj) + 1],
-                         dz = zi - A.pos[3 * size_t(pj) + 2];
-            v = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+            const int pj = A.perm[key_idx(key[t])];
+            v = d2_f64(A, pi, pj);
             tag = pj;
         }
         dd[t] = (unsigned long long)__double_as_longlong(v);
@@ -531,7 +578,7 @@ __global__ void __launch_bounds__(kKnnWarps * 32) k_knn(KnnArgs A) {
             knn_fail_output(A, q, cnt < 0);
             continue;
         }
-        knn_finish(A, S.d2, S.idx, S.dd, S.di, cnt, q);
+        knn_finish(A, S.key, S.dd, S.di, cnt, q);
     }
 }
 

@@ -911,7 +911,7 @@ void Octree::reserve_graph_build() {
     pdisp.get<float>(n);
     work.get<int4>(std::max(size_t(node_cap), size_t(n)) + 1);
     sphere.get<float4>(std::max(size_t(node_cap), size_t(n)) + 1);
-    reserve_scan_sort(std::max(n, node_cap));
+    reserve_scan_sort(std::max(n, node_cap), &scratch);
     deep_sort_attr();
 }
 
@@ -950,7 +950,7 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
     int* pm = perm.get<int>(n);
     k_keys<<<grid, kThreads, 0, s>>>(pos, n, R, k0, pm);
     GF_CHECK_LAUNCH();
-    radix_sort_pairs(k0, pm, key_alt.get<uint64_t>(n), perm_alt.get<int>(n), n, 0, 63, s);
+    radix_sort_pairs(k0, pm, key_alt.get<uint64_t>(n), perm_alt.get<int>(n), n, 0, 63, s, &scratch);
 
     int8_t* c9 = cpl9.get<int8_t>(n);
     int8_t* ld = ldepth.get<int8_t>(n);
@@ -966,7 +966,7 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
         GF_CHECK_LAUNCH();
         k_nstart<<<grid, kThreads, 0, s>>>(K, n, c9, ld, ds, ns);
         GF_CHECK_LAUNCH();
-        exclusive_scan(ns, nb, n, &cnt->total_nodes, s);
+        exclusive_scan(ns, nb, n, &cnt->total_nodes, s, &scratch);
         GF_CUDA(cudaMemcpyAsync(h_counts, cnt, sizeof(TreeCounts), cudaMemcpyDeviceToHost, s));
         GF_CUDA(cudaStreamSynchronize(s));
         deep = h_counts->deep != 0;
@@ -987,7 +987,7 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
         GF_CHECK_LAUNCH();
         k_nstart<<<grid, kThreads, 0, s>>>(K, n, c9, ld, ds, ns);
         GF_CHECK_LAUNCH();
-        exclusive_scan(ns, nb, n, &cnt->total_nodes, s);
+        exclusive_scan(ns, nb, n, &cnt->total_nodes, s, &scratch);
         if (!graph_safe) {
             GF_CUDA(cudaMemcpyAsync(h_counts, cnt, sizeof(TreeCounts), cudaMemcpyDeviceToHost, s));
             GF_CUDA(cudaStreamSynchronize(s));
@@ -995,7 +995,8 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
     }
     if (!graph_safe) {
         nn = h_counts->total_nodes;
-        if (nn > node_cap) node_cap = nn + nn / 4 + 1024;  // headroom: captured rebuilds stay inside
+        // headroom: later synchronisation-free rebuilds (captured or not) build inside it
+        if (nn > node_cap) node_cap = nn + nn / 2 + 1024;
     }
     const int cap = node_cap;
     // node kernels cover [0, span) and read the live count on the device
@@ -1061,7 +1062,7 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
     int* gs = gscan.get<int>(cap);
     k_group_flag<<<ngrid, kThreads, 0, s>>>(span, nn_dev, group_max, i4, par, gf_);
     GF_CHECK_LAUNCH();
-    exclusive_scan(gf_, gs, span, &cnt->num_groups, s);
+    exclusive_scan(gf_, gs, span, &cnt->num_groups, s, &scratch);
     k_group_write<<<ngrid, kThreads, 0, s>>>(span, nn_dev, gf_, gs, groups.get<int>(cap));
     GF_CHECK_LAUNCH();
 
@@ -1069,7 +1070,7 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
     int* bv = bfs_val.get<int>(cap);
     k_bfs_keys<<<ngrid, kThreads, 0, s>>>(span, nn_dev, i4, bk, bv);
     GF_CHECK_LAUNCH();
-    radix_sort_pairs(bk, bv, bfs_key_alt.get<uint64_t>(cap), bfs_val_alt.get<int>(cap), span, 0, 8, s);
+    radix_sort_pairs(bk, bv, bfs_key_alt.get<uint64_t>(cap), bfs_val_alt.get<int>(cap), span, 0, 8, s, &scratch);
     int* bfs = n_bfs.get<int>(cap);
     k_bfs_index<<<ngrid, kThreads, 0, s>>>(span, nn_dev, bv, bfs);
     GF_CHECK_LAUNCH();

@@ -73,6 +73,7 @@ struct Octree {
     // groups and walk work list
     DevBuf gflag, gscan, groups, work, sphere;
     DevBuf root, counts;
+    ScanScratch scratch;  // this tree's scan / sort scratch (trees may build on different streams)
     TreeCounts* h_counts = nullptr;  // pinned
 
     // graph_safe: no host synchronisation and no allocation (inside a captured CUDA graph):

@@ -51,7 +51,7 @@ __global__ void k_group_prep(const int* __restrict__ groups, const int4* __restr
         const int b = q.x, e = q.x + q.y;
         if (chunk > 0) {
             // pass over the group per item: rank of each active particle by ballot
-            int base = 0, r0 = 0;
+            int r0 = 0;
             for (;;) {  // items [r0, r0 + chunk)
                 float x0 = 1e30f, y0 = 1e30f, z0 = 1e30f, x1 = -1e30f, y1 = -1e30f, z1 = -1e30f;
                 int rank_base = 0, in_item = 0;
@@ -70,7 +70,6 @@ __global__ void k_group_prep(const int* __restrict__ groups, const int4* __restr
                     rank_base += __popc(m);
                     if (rank_base >= r0 + chunk) break;
                 }
-                base = rank_base;
                 const int P = warp_sum(in_item);
                 if (P == 0) break;
                 x0 = warp_min(x0); y0 = warp_min(y0); z0 = warp_min(z0);
@@ -102,7 +101,6 @@ __global__ void k_group_prep(const int* __restrict__ groups, const int4* __restr
                 if (P < chunk) break;
                 r0 += chunk;
             }
-            (void)base;
             continue;
         }
         int nact = 0;
@@ -148,13 +146,14 @@ template <bool QUAD>
 struct WarpSmem {
     static constexpr int kStack = QUAD ? 768 : kStackCap;
     static constexpr int kNodeTile = QUAD ? 96 : 1;
+    static constexpr int kBatch = QUAD ? 128 : 64;  // active particles evaluated per walk
     int stack[kStack];
     float4 tile[kTileCap];
     float4 ntA[kNodeTile];   // centre of mass, mass
     float4 ntQ[kNodeTile];   // Qxx, Qyy, Qxy, Qxz
     float2 ntYZ[kNodeTile];  // Qyz, T
     int lanemap[32];
-    int slot_pos[64];
+    int slot_pos[kBatch];
 };
 
 __device__ __forceinline__ void pair_acc(const float4 e, float x, float y, float z, float eps2,
@@ -214,20 +213,31 @@ __device__ __forceinline__ void eval_tile(const float4* tile, int fill, bool two
     }
 }
 
-__device__ __forceinline__ void eval_nodes(const float4* ntA, const float4* ntQ, const float2* ntYZ, int fill,
-                                           bool two, int r, int sub, float eps2, float x0, float y0, float z0,
-                                           float x1, float y1, float z1, float& ax0, float& ay0, float& az0,
-                                           float& ax1, float& ay1, float& az1) {
-    if (two) {
-        for (int j = 0; j < fill; ++j) {
-            const float4 e = ntA[j], q = ntQ[j];
-            const float2 qyz = ntYZ[j];
-            quad_acc(e, q, qyz, x0, y0, z0, eps2, ax0, ay0, az0);
-            quad_acc(e, q, qyz, x1, y1, z1, eps2, ax1, ay1, az1);
-        }
-    } else {
-#pragma unroll 2
-        for (int j = sub; j < fill; j += r) quad_acc(ntA[j], ntQ[j], ntYZ[j], x0, y0, z0, eps2, ax0, ay0, az0);
+// Mixed form: entries ksub, ksub + m, ... of both tiles for the lane's 4 particles (each entry
+// loaded once from shared memory serves the 4); the tile's partial sums go to Kahan totals.
+__device__ __forceinline__ void eval_quad4(const float4* tile, const float4* ntA, const float4* ntQ,
+                                           const float2* ntYZ, int fill, int fillN, int ksub, int m, float eps2,
+                                           const float (&x)[4], const float (&y)[4], const float (&z)[4],
+                                           KahanF (&kx)[4], KahanF (&ky)[4], KahanF (&kz)[4]) {
+    float px[4], py[4], pz[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) px[t] = py[t] = pz[t] = 0.f;
+    for (int j = ksub; j < fill; j += m) {
+        const float4 e = tile[j];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) pair_acc(e, x[t], y[t], z[t], eps2, px[t], py[t], pz[t]);
+    }
+    for (int j = ksub; j < fillN; j += m) {
+        const float4 e = ntA[j], q = ntQ[j];
+        const float2 yt = ntYZ[j];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) quad_acc(e, q, yt, x[t], y[t], z[t], eps2, px[t], py[t], pz[t]);
+    }
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        kx[t].add(px[t]);
+        ky[t].add(py[t]);
+        kz[t].add(pz[t]);
     }
 }
 
@@ -252,10 +262,10 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
         const int4 w = work[g];
         const float4 sph = sphere[g];
         const int b = w.x, count = w.y, Pall = w.z, r0 = w.w;
-        // Groups hold <= 64 particles except depth-48 leaves of coincident points; those are
-        // evaluated in batches of 64 active particles, each batch walking the tree again.
-        for (int pb = 0; pb < Pall; pb += 64) {
-        const int P = min(64, Pall - pb);
+        // Items hold <= kBatch particles except depth-48 leaves of coincident points; those
+        // are evaluated in batches, each batch walking the tree again.
+        for (int pb = 0; pb < Pall; pb += Smem::kBatch) {
+        const int P = min(Smem::kBatch, Pall - pb);
 
         // compact the active particles of this batch into slots
         int nslot = 0;
@@ -269,25 +279,48 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
         }
         __syncwarp();
 
-        // lane mapping: r lanes per particle (r = 1 and two slots per lane when P > 32)
-        int r = 1;
-        if (P <= 16) r = P <= 1 ? 32 : P <= 2 ? 16 : P <= 4 ? 8 : P <= 8 ? 4 : 2;
-        const int slot0 = lane / r, sub = lane % r;
-        const int slot1 = slot0 + 32;
-        const bool has0 = slot0 < P, has1 = P > 32 && slot1 < P;
-        float x0 = 0.f, y0 = 0.f, z0 = 0.f, x1 = 0.f, y1 = 0.f, z1 = 0.f;
-        if (has0) {
-            const float4 p = p4[S.slot_pos[slot0]];
-            x0 = p.x; y0 = p.y; z0 = p.z;
+        // Lane mapping.
+        //   monopole (reference form): r lanes per particle splitting the entries (r = 1 and
+        //     two slots per lane when P > 32);
+        //   QUAD (mixed form): every lane holds 4 particles, so each entry read from shared
+        //     memory serves 4 interactions; L = ceil(P / 4) lanes cover the batch and
+        //     m = 32 / L groups of L lanes split the entries (the 4-particle slots of lane
+        //     q hold particles 4q .. 4q + 3).
+        constexpr int kPpl = QUAD ? 4 : 2;
+        int r = 1, sub = 0, m = 1, ksub = 0;
+        bool lane_on = true;
+        int slot[kPpl];
+        if (QUAD) {
+            const int L = (P + 3) >> 2;
+            m = max(1, 32 / L);
+            ksub = lane / L;
+            lane_on = ksub < m;
+            const int q = lane - ksub * L;
+#pragma unroll
+            for (int t = 0; t < kPpl; ++t) slot[t] = 4 * q + t;
+        } else {
+            if (P <= 16) r = P <= 1 ? 32 : P <= 2 ? 16 : P <= 4 ? 8 : P <= 8 ? 4 : 2;
+            slot[0] = lane / r;
+            slot[1] = slot[0] + 32;
+            sub = lane % r;
         }
-        if (has1) {
-            const float4 p = p4[S.slot_pos[slot1]];
-            x1 = p.x; y1 = p.y; z1 = p.z;
+        float x[kPpl], y[kPpl], z[kPpl];
+        bool has[kPpl];
+#pragma unroll
+        for (int t = 0; t < kPpl; ++t) {
+            has[t] = lane_on && slot[t] < P && (QUAD || t == 0 || P > 32);
+            x[t] = y[t] = z[t] = 0.f;
+            if (has[t]) {
+                const float4 p = p4[S.slot_pos[slot[t]]];
+                x[t] = p.x; y[t] = p.y; z[t] = p.z;
+            }
         }
         // reference form: one float32 running sum per component; mixed form: each tile's
         // partial sums are added to Kahan-compensated totals
-        float ax0 = 0.f, ay0 = 0.f, az0 = 0.f, ax1 = 0.f, ay1 = 0.f, az1 = 0.f;
-        KahanF kx0, ky0, kz0, kx1, ky1, kz1;
+        float ax[kPpl], ay[kPpl], az[kPpl];
+        KahanF kx[kPpl], ky[kPpl], kz[kPpl];
+#pragma unroll
+        for (int t = 0; t < kPpl; ++t) ax[t] = ay[t] = az[t] = 0.f;
         const bool two = P > 32;
 
         int fill = 0, fillN = 0;
@@ -297,17 +330,12 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
         listlen += fill + fillN;                                                                     \
         nodelen += fillN;                                                                            \
         __syncwarp();                                                                                \
-        if (QUAD) {                                                                                  \
-            float px0 = 0.f, py0 = 0.f, pz0 = 0.f, px1 = 0.f, py1 = 0.f, pz1 = 0.f;                  \
-            eval_tile(S.tile, fill, two, r, sub, eps2, x0, y0, z0, x1, y1, z1, px0, py0, pz0, px1,   \
-                      py1, pz1);                                                                     \
-            eval_nodes(S.ntA, S.ntQ, S.ntYZ, fillN, two, r, sub, eps2, x0, y0, z0, x1, y1, z1, px0,  \
-                       py0, pz0, px1, py1, pz1);                                                     \
-            kx0.add(px0); ky0.add(py0); kz0.add(pz0);                                                \
-            kx1.add(px1); ky1.add(py1); kz1.add(pz1);                                                \
+        if constexpr (QUAD) {                                                                        \
+            if (lane_on) eval_quad4(S.tile, S.ntA, S.ntQ, S.ntYZ, fill, fillN, ksub, m, eps2, x, y, z, \
+                                    kx, ky, kz);                                                     \
         } else {                                                                                     \
-            eval_tile(S.tile, fill, two, r, sub, eps2, x0, y0, z0, x1, y1, z1, ax0, ay0, az0, ax1,   \
-                      ay1, az1);                                                                     \
+            eval_tile(S.tile, fill, two, r, sub, eps2, x[0], y[0], z[0], x[1], y[1], z[1], ax[0],    \
+                      ay[0], az[0], ax[1], ay[1], az[1]);                                            \
         }                                                                                            \
         __syncwarp();                                                                                \
         fill = 0;                                                                                    \
@@ -383,10 +411,10 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
             if (QUAD) {
                 if (fillN + na > Smem::kNodeTile) GF_WALK_FLUSH();
                 if (accept) {
-                    const int slot = fillN + __popc(am & lt);
-                    S.ntA[slot] = A;
-                    S.ntQ[slot] = wq[node];
-                    S.ntYZ[slot] = make_float2(B.w, wt[node]);
+                    const int slot_n = fillN + __popc(am & lt);
+                    S.ntA[slot_n] = A;
+                    S.ntQ[slot_n] = wq[node];
+                    S.ntYZ[slot_n] = make_float2(B.w, wt[node]);
                 }
                 fillN += na;
             } else {
@@ -418,32 +446,56 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
         }
         GF_WALK_FLUSH();
 #undef GF_WALK_FLUSH
-        if (QUAD) {
-            ax0 = kx0.s; ay0 = ky0.s; az0 = kz0.s;
-            ax1 = kx1.s; ay1 = ky1.s; az1 = kz1.s;
-        }
-
-        // combine the partial sums of the lanes that share a particle
-        for (int o = r >> 1; o > 0; o >>= 1) {
-            ax0 += __shfl_xor_sync(0xffffffffu, ax0, o);
-            ay0 += __shfl_xor_sync(0xffffffffu, ay0, o);
-            az0 += __shfl_xor_sync(0xffffffffu, az0, o);
-        }
         if (lane == 0) {
             atomicAdd(&cnt->pairs, listlen * (unsigned long long)P);
             if (QUAD) atomicAdd(&cnt->qpairs, nodelen * (unsigned long long)P);
         }
-        if (has0 && sub == 0) {
-            const int k = perm[S.slot_pos[slot0]];
-            acc[3 * size_t(k)] = ax0;
-            acc[3 * size_t(k) + 1] = ay0;
-            acc[3 * size_t(k) + 2] = az0;
-        }
-        if (has1) {
-            const int k = perm[S.slot_pos[slot1]];
-            acc[3 * size_t(k)] = ax1;
-            acc[3 * size_t(k) + 1] = ay1;
-            acc[3 * size_t(k) + 2] = az1;
+        if constexpr (QUAD) {
+            // sum the m entry groups of every particle in a fixed order (the tile is free now)
+            float* red = reinterpret_cast<float*>(S.tile);
+            const int L = (P + 3) >> 2;
+            if (lane_on) {
+#pragma unroll
+                for (int t = 0; t < kPpl; ++t) {
+                    float* o = red + 3 * (ksub * 4 * L + slot[t]);
+                    o[0] = kx[t].s;
+                    o[1] = ky[t].s;
+                    o[2] = kz[t].s;
+                }
+            }
+            __syncwarp();
+            for (int p = lane; p < P; p += 32) {
+                float sx = 0.f, sy = 0.f, sz = 0.f;
+                for (int kk = 0; kk < m; ++kk) {
+                    const float* o = red + 3 * (kk * 4 * L + p);
+                    sx += o[0];
+                    sy += o[1];
+                    sz += o[2];
+                }
+                const int kp = perm[S.slot_pos[p]];
+                acc[3 * size_t(kp)] = sx;
+                acc[3 * size_t(kp) + 1] = sy;
+                acc[3 * size_t(kp) + 2] = sz;
+            }
+        } else {
+            // combine the partial sums of the lanes that share a particle
+            for (int o = r >> 1; o > 0; o >>= 1) {
+                ax[0] += __shfl_xor_sync(0xffffffffu, ax[0], o);
+                ay[0] += __shfl_xor_sync(0xffffffffu, ay[0], o);
+                az[0] += __shfl_xor_sync(0xffffffffu, az[0], o);
+            }
+            if (has[0] && sub == 0) {
+                const int kp = perm[S.slot_pos[slot[0]]];
+                acc[3 * size_t(kp)] = ax[0];
+                acc[3 * size_t(kp) + 1] = ay[0];
+                acc[3 * size_t(kp) + 2] = az[0];
+            }
+            if (has[1]) {
+                const int kp = perm[S.slot_pos[slot[1]]];
+                acc[3 * size_t(kp)] = ax[1];
+                acc[3 * size_t(kp) + 1] = ay[1];
+                acc[3 * size_t(kp) + 2] = az[1];
+            }
         }
         __syncwarp();
         }  // batches

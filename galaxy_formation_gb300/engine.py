@@ -19,7 +19,9 @@ def _is_cuda_tensor(x):
 def _stream_ptr():
     import torch
 
-    return torch.cuda.current_stream().cuda_stream
+    # torch's default stream is the legacy default stream (handle 0); the library reads NULL
+    # as its own stream, so the legacy stream goes as cudaStreamLegacy ((cudaStream_t)1)
+    return torch.cuda.current_stream().cuda_stream or 1
 
 
 class Engine:

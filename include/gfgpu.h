@@ -8,7 +8,8 @@
  *
  * Conventions. Pointers of the reference-compatible functions are HOST pointers (the
  * library copies to and from the GPU). Functions with the `_dev` suffix take DEVICE
- * pointers and a CUDA stream (cudaStream_t passed as void*, NULL = the library's stream);
+ * pointers and a CUDA stream (cudaStream_t passed as void*, NULL = the library's stream;
+ * cudaStreamLegacy, (void*)1, for the legacy default stream);
  * they enqueue work and return without synchronising unless stated. Arrays are
  * C-contiguous: positions (n,3) float64 row-major, etc.
  *
@@ -260,6 +261,11 @@ int gf_sim_read(double* pos, double* vel, double* acc, double* dt_ind, double* t
  *                       with the bounding sphere of its own particles (no reference
  *                       counterpart: same opening criterion per particle, tighter spheres). */
 #define GF_OPT_WALK_CHUNK 4
+/*   GF_OPT_WALK_GROUP   mixed form (GF_OPT_GRAVITY_QUAD = 1): walk groups are the shallowest
+ *                       nodes holding <= this many particles, 8..128 (default 64, the
+ *                       reference's kGroupMax of cpp/nbody.cpp:34, which the monopole walk
+ *                       always keeps). */
+#define GF_OPT_WALK_GROUP 5
 int gf_set_option(int key, double value);
 /* Current value of an option (-1 for an unknown key). */
 double gf_get_option(int key);
