@@ -65,8 +65,8 @@ __global__ void k_verlet_prep(int ng, const int* __restrict__ gidx, const int* _
 constexpr int kSelWarps = 8;
 __global__ void __launch_bounds__(kSelWarps * 32) k_verlet_select(
     int ng, const int* __restrict__ gidx, const int* __restrict__ row, const int* __restrict__ cache,
-    const int* __restrict__ loc, const double* __restrict__ gpos, int* __restrict__ nb, double* __restrict__ d31,
-    int* __restrict__ fail, Subset sub) {
+    const int* __restrict__ cgidx, const int* __restrict__ loc, const double* __restrict__ gpos,
+    int* __restrict__ nb, double* __restrict__ d31, int* __restrict__ fail, Subset sub) {
     __shared__ unsigned long long s_key[kSelWarps][64];  // float64 d^2 bit patterns (see below)
     __shared__ int s_tag[kSelWarps][64];
     __shared__ int s_loc[kSelWarps][64];
@@ -82,8 +82,10 @@ __global__ void __launch_bounds__(kSelWarps * 32) k_verlet_select(
             double d2 = INFINITY;
             int j = -1;
             if (jj < kCand) {
+                // cached candidate: its local index at caching time; now (loc: null when the gas
+                // set is the cached one)
                 const int c = cache[size_t(r) * kCand + jj];
-                j = c >= 0 ? loc[c] : -1;
+                j = c < 0 ? -1 : loc ? loc[cgidx[c]] : c;
                 if (j >= 0) {
                     const double dx = xi - gpos[3 * size_t(j)], dy = yi - gpos[3 * size_t(j) + 1],
                                  dz = zi - gpos[3 * size_t(j) + 2];
@@ -127,14 +129,19 @@ __global__ void __launch_bounds__(kSelWarps * 32) k_verlet_select(
     }
 }
 
-// one thread per cache entry (coalesced rows of 48 global indices)
+// one thread per cache entry (coalesced rows of 48 local indices; cgidx keeps the local ->
+// global map of the caching call)
 __global__ void k_cache_store(int ng, int kq, const int* __restrict__ gidx, const int* __restrict__ nb,
-                              int* __restrict__ row, int* __restrict__ cache) {
+                              int* __restrict__ row, int* __restrict__ cache, int* __restrict__ cgidx) {
     const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (t >= size_t(ng) * kCand) return;
     const int i = int(t / kCand), jj = int(t % kCand);
-    if (jj == 0) row[gidx[i]] = i;
-    cache[t] = jj < kq ? gidx[nb[t]] : -1;
+    if (jj == 0) {
+        const int g = gidx[i];
+        row[g] = i;
+        cgidx[i] = g;
+    }
+    cache[t] = jj < kq ? nb[t] : -1;
 }
 
 __global__ void k_guess(int ng, const int* __restrict__ gidx, const double* __restrict__ hprev, float* __restrict__ rg) {
@@ -424,8 +431,8 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
         }
         const int blocks = std::min(div_up(ng, kSelWarps), 16 * ctx().sms);
         ProfScope pv(kStVerlet, s);
-        k_verlet_select<<<blocks, kSelWarps * 32, 0, s>>>(ng, gi, row.as<int>(), cache.as<int>(), lc, gp, nb,
-                                                          d31, &sc->fail, sub);
+        k_verlet_select<<<blocks, kSelWarps * 32, 0, s>>>(ng, gi, row.as<int>(), cache.as<int>(), cgidx.as<int>(),
+                                                          a.nosync ? nullptr : lc, gp, nb, d31, &sc->fail, sub);
         GF_CHECK_LAUNCH();
         if (a.nosync) {  // the gas set is the cached one: every particle keeps its candidates
             have_nb = true;
@@ -463,7 +470,8 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
         int* ca = cache.get<int>(size_t(ng) * kCand);
         int* rw = row.as<int>();
         GF_CUDA(cudaMemsetAsync(rw, 0xff, sizeof(int) * size_t(n), s));
-        k_cache_store<<<div_up(size_t(ng) * kCand, kThreads), kThreads, 0, s>>>(ng, kq, gi, nb, rw, ca);
+        k_cache_store<<<div_up(size_t(ng) * kCand, kThreads), kThreads, 0, s>>>(ng, kq, gi, nb, rw, ca,
+                                                                                cgidx.get<int>(ng));
         GF_CHECK_LAUNCH();
         cache_valid = true;
         full_searches += 1;

@@ -57,7 +57,7 @@ struct ForceEngine {
     Octree knn_tree;
     SphScratch sph;
     Sph32Scratch sph32;
-    DevBuf acc_grav, acc_sph, dt_courant, h_prev, row, loc, cache;
+    DevBuf acc_grav, acc_sph, dt_courant, h_prev, row, loc, cache, cgidx;
     DevBuf flag, scan, gidx, gpos, gvel, gmass, gu_, nb48, dsel, rguess, h, rho, gacc, dudt, dt_i;
     DevBuf scalars;
     DevBuf divv_prev, gdivv, hX, hY, hrg, colX, colT, gact, aflag, ascan, alist;

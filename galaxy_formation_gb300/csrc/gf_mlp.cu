@@ -42,30 +42,59 @@ __device__ __forceinline__ void normalise(const float* x, const MlpNorm& nm, flo
     for (int i = 0; i < 4; ++i) xn[i] = (x[i] - nm.mean[i]) * nm.inv_std[i];
 }
 
-// one thread per sample; a1 staged in shared memory (row per thread)
-constexpr int kFwdThreads = 64;
+// one thread per sample, layer 2 accumulated column by column: for each hidden unit k of
+// layer 1, a1_k is formed and multiplied into the 64 layer-2 sums z (registers) with column k
+// of W2 read from shared memory as float4 (one address for the whole warp: a broadcast per 4
+// multiply-adds).
+constexpr int kFwdThreads = 128;
+struct MlpFwdW {  // float32 in shared memory, W2 transposed (row k = column k of W2)
+    float W1[H * 4], b1[H], W2T[H * H], b2[H], w3[H], b3;
+};
+
 __global__ void __launch_bounds__(kFwdThreads) k_mlp_forward(int n, const float* __restrict__ X, MlpNorm nm,
                                                              const __nv_bfloat16* __restrict__ P, float* __restrict__ Y) {
-    __shared__ MlpW w;
-    __shared__ float sA1[kFwdThreads][H + 1];
-    load_weights(w, P);
-    float* a1 = sA1[threadIdx.x];
+    __shared__ __align__(16) MlpFwdW w;
+    {
+        const int o2 = H * 4 + H;  // offset of W2 in the flat parameter vector
+        for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) {
+            const float v = __bfloat162float(P[i]);
+            if (i >= o2 && i < o2 + H * H) {
+                const int j = (i - o2) / H, k = (i - o2) % H;
+                w.W2T[k * H + j] = v;
+            } else {
+                reinterpret_cast<float*>(&w)[i] = v;
+            }
+        }
+        __syncthreads();
+    }
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float xn[4];
         normalise(X + 4 * size_t(i), nm, xn);
-        for (int j = 0; j < H; ++j) {
-            float z = w.b1[j];
+        float z[H];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) z = fmaf(w.W1[j * 4 + q], xn[q], z);
-            a1[j] = fmaxf(z, 0.f);
+        for (int j = 0; j < H; ++j) z[j] = w.b2[j];
+#pragma unroll 1
+        for (int k = 0; k < H; ++k) {
+            const float4 r = *reinterpret_cast<const float4*>(&w.W1[k * 4]);
+            float a = w.b1[k];
+            a = fmaf(r.x, xn[0], a);
+            a = fmaf(r.y, xn[1], a);
+            a = fmaf(r.z, xn[2], a);
+            a = fmaf(r.w, xn[3], a);
+            a = fmaxf(a, 0.f);
+            const float4* col = reinterpret_cast<const float4*>(&w.W2T[k * H]);
+#pragma unroll
+            for (int j4 = 0; j4 < H / 4; ++j4) {
+                const float4 c = col[j4];
+                z[4 * j4] = fmaf(c.x, a, z[4 * j4]);
+                z[4 * j4 + 1] = fmaf(c.y, a, z[4 * j4 + 1]);
+                z[4 * j4 + 2] = fmaf(c.z, a, z[4 * j4 + 2]);
+                z[4 * j4 + 3] = fmaf(c.w, a, z[4 * j4 + 3]);
+            }
         }
         float y = w.b3;
-        for (int j = 0; j < H; ++j) {
-            float z = w.b2[j];
-#pragma unroll 16
-            for (int k = 0; k < H; ++k) z = fmaf(w.W2[j * H + k], a1[k], z);
-            y = fmaf(w.w3[j], fmaxf(z, 0.f), y);
-        }
+#pragma unroll
+        for (int j = 0; j < H; ++j) y = fmaf(w.w3[j], fmaxf(z[j], 0.f), y);
         Y[i] = y * nm.t_std + nm.t_mean;  // log h
     }
 }
@@ -247,7 +276,7 @@ void Mlp::get_params(float* host, cudaStream_t s) {
 
 void Mlp::predict(int n, const float* X, float* Y, cudaStream_t s) {
     if (n <= 0) return;
-    const int blocks = std::min(div_up(n, kFwdThreads), 16 * ctx().sms);
+    const int blocks = std::min(div_up(n, kFwdThreads), 8 * ctx().sms);
     k_mlp_forward<<<blocks, kFwdThreads, 0, s>>>(n, X, norm, wb.as<__nv_bfloat16>(), Y);
     GF_CHECK_LAUNCH();
 }

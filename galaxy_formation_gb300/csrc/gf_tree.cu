@@ -1031,7 +1031,10 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
     float4* mom = n_mom.get<float4>(cap);
     float* opr = n_open.get<float>(cap);
     float* ndp = n_disp.get<float>(cap);
-    if (quad) {  // mixed form: float32 monopole + quadrupole in one pass
+    if (want_knn) {
+        // a neighbour-search tree needs geometry only: no moments (the walk layout's mass and
+        // opening-radius fields stay unused)
+    } else if (quad) {  // mixed form: float32 monopole + quadrupole in one pass
         Mom32Args A{span, nn_dev, false, theta_f, i4, par, nch, ctr, geo, mom, opr, ndp, pp, nullptr,
                     n_quad.get<float4>(cap), n_qyz.get<float2>(cap)};
         k_moments_quad32<<<ngrid, kThreads, 0, s>>>(A);
