@@ -70,6 +70,11 @@ def parse():
     ap.add_argument("--forms", default="plain,plain_matched,mixed_learned",
                     help="comma list of forms to time (the last one given is the headline)")
     ap.add_argument("--blocks", type=int, default=3, help="64-sub-step blocks of the batched form (0: skip)")
+    ap.add_argument("--workload", default="force", choices=["force", "drift", "learned"],
+                    help="force: the headline (one full evaluation, 1M disk+halo); drift: 4M cloud, "
+                         "plain step loop vs batched mixed+learned blocks over the same simulated time, "
+                         "energy and angular-momentum drift; learned: 1M gas with clumps, search "
+                         "iterations with and without the learned guess")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
@@ -104,10 +109,10 @@ def allmax(world, x):
     return float(t.item())
 
 
-def workload(scale):
+def workload(scale, idx=CONFIG_IDX):
     from galaxy_formation_gb300 import synthetic
 
-    return synthetic.make_config(CONFIG_IDX, seed=3, scale=scale)
+    return synthetic.make_config(idx, seed=3, scale=scale)
 
 
 def workload_name(n_gas, n_dm):
@@ -228,7 +233,7 @@ def load_traffic():
 class Gpu:
     """The workload resident on one GPU and the library's entry points around it."""
 
-    def __init__(self, args, local):
+    def __init__(self, args, local, config_idx=CONFIG_IDX):
         import torch
 
         from galaxy_formation_gb300 import _lib, build, params
@@ -238,7 +243,7 @@ class Gpu:
         self.lib = _lib.load()
         torch.cuda.set_device(local)
         self.dev = torch.device("cuda", local)
-        self.d = workload(args.scale)
+        self.d = workload(args.scale, config_idx)
         self.n = len(self.d["mass"])
         self.n_gas = int((self.d["kind"] == 0).sum())
         self.T = {k: torch.from_numpy(np.ascontiguousarray(self.d[k])).to(self.dev)
@@ -314,19 +319,28 @@ class Gpu:
         e = np.linalg.norm(a - exact, axis=1) / np.linalg.norm(exact, axis=1)
         return float(np.percentile(e, 99)), float(np.median(e))
 
-    def train_hguess(self, rows=2_000_000, collect_steps=4):
-        """Learned smoothing-length guess: (features, converged log h) pairs from the
-        simulator's own evaluations of drifting copies of the snapshot, then Adam on the GPU."""
+    def collect_pairs(self, rows, collect_steps=4, start=True):
+        """(features, converged log h) pairs from the plain method's own evaluations of drifting
+        copies of the snapshot (the collection buffer is cleared when start)."""
         torch, lib, L = self.torch, self.lib, self._lib
         theta = self.set_form("plain")
         lib.gf_set_option(L.OPT_HGUESS, 0)
         pos = self.T["pos"].clone()
         self.step(theta, pos=pos)
-        lib.gf_set_option(L.OPT_COLLECT, rows)
+        if start:
+            lib.gf_set_option(L.OPT_COLLECT, rows)
         for _ in range(collect_steps):
             pos += 0.5 * self.dt[:, None] * self.T["vel"]
             self.step(theta, pos=pos)
         torch.cuda.synchronize()
+        return pos
+
+    def train_hguess(self, rows=2_000_000, collect_steps=4, collected=False):
+        """Learned smoothing-length guess: pairs collected from the simulator (unless already
+        collected), then Adam on the GPU; iteration counts on a drifted snapshot."""
+        torch, lib, L = self.torch, self.lib, self._lib
+        theta = self.set_form("plain")
+        pos = self.T["pos"].clone() if collected else self.collect_pairs(rows, collect_steps)
         m = lib.gf_mlp_collected(None, None, 0)
         X = np.zeros((m, 4), np.float32)
         Y = np.zeros(m, np.float32)
@@ -541,11 +555,144 @@ def run_gpu(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def run_learned(args, world, rank, local):
+    """Learned smoothing-length guess on 1M gas with 200 Plummer clumps: trained on pairs that
+    the plain method produces on the 200k and 1M disk+halo snapshots; search iterations and
+    time with the learned guess, with the cell-density start it replaces, and with the
+    previous h, on a drifted snapshot; the converged neighbours (hence accelerations) must be
+    identical."""
+    if rank != 0:
+        return
+    G1 = Gpu(args, local, 1)
+    G1.collect_pairs(5_000_000, collect_steps=6, start=True)
+    G2 = Gpu(args, local, 2)
+    G2.collect_pairs(5_000_000, collect_steps=4, start=False)
+    G = Gpu(args, local, 3)
+    tr = G.train_hguess(collected=True)
+    torch, lib, L = G.torch, G.lib, G._lib
+    theta = G.set_form("mixed_learned")
+    res = {}
+    pos = G.T["pos"].clone()
+    for mode, name in ((1, "cell_density"), (2, "learned"), (0, "previous_h")):
+        lib.gf_set_option(L.OPT_HGUESS, 0)
+        G.step(theta, pos=pos)
+        nxt = pos + 0.5 * G.dt[:, None] * G.T["vel"]
+        lib.gf_set_option(L.OPT_HGUESS, mode)
+        lib.gf_profile(1)
+        G.step(theta, pos=nxt)
+        torch.cuda.synchronize()
+        ms, cnt = ctypes.c_double(), ctypes.c_int()
+        lib.gf_profile_stage(L.STAGES.index("knn"), ctypes.byref(ms), ctypes.byref(cnt))
+        lib.gf_profile(0)
+        res[name] = {"iterations_per_gas": G.knn_iters(), "knn_ms": ms.value,
+                     "acc": G.acc.clone(), "dt": G.dt.clone()}
+    same = all(torch.equal(res[k]["acc"], res["cell_density"]["acc"]) and
+               torch.equal(res[k]["dt"], res["cell_density"]["dt"]) for k in res)
+    print(json.dumps({
+        "workload": "learned smoothing-length guess: 1,000,000 gas, disk + 200 Plummer clumps (seed 3)",
+        "training": {k: v for k, v in tr.items() if k != "search_on_drifted_snapshot"},
+        "training_pairs_from": "plain-method evaluations of the 200k and 1M disk+halo snapshots",
+        "search": {k: {"iterations_per_gas": v["iterations_per_gas"], "knn_ms": v["knn_ms"]} for k, v in res.items()},
+        "converged_results_identical": bool(same),
+        "speedup_learned_vs_cell_density": res["cell_density"]["knn_ms"] / res["learned"]["knn_ms"],
+    }), flush=True)
+
+
+def run_drift(args, world, rank, local):
+    """4M rotating cloud: the plain form with the reference's step loop against the mixed +
+    batched + learned form (block time steps), over the same simulated time; updates/s and the
+    float64 energy / angular-momentum drift of each."""
+    if rank != 0:
+        return
+    G = Gpu(args, local, 4)
+    torch, lib, L, p = G.torch, G.lib, G._lib, G.params
+    G.collect_pairs(2_000_000, collect_steps=2, start=True)
+    G.train_hguess(collected=True)
+    d, n = G.d, G.n
+    s = torch.cuda.ExternalStream(lib.gf_stream())
+    out = {}
+
+    def diag():
+        q = np.zeros(8)
+        L.check(lib.gf_sim_diagnostics(0.5, q))
+        return q
+
+    def drift(q0, q1):
+        return {"dE_over_E": abs(q1[3] - q0[3]) / abs(q0[3]),
+                "dL_over_L": float(np.linalg.norm(q1[4:7] - q0[4:7]) / np.linalg.norm(q0[4:7])),
+                "E0": q0[3], "E1": q1[3]}
+
+    theta = G.set_form("plain")
+    L.check(lib.gf_sim_init(n, d["pos"], d["vel"], d["mass"], d["kind"], d["u"], theta, p.EPS, p.GAMMA, p.ALPHA,
+                            p.BETA))
+    q0 = diag()
+    tk, sub = ctypes.c_double(), ctypes.c_int()
+    upd, subs = 0.0, 0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(args.steps):
+        L.check(lib.gf_sim_step(1e30, ctypes.byref(tk), ctypes.byref(sub)))
+        upd += lib.gf_sim_updates()
+        subs += sub.value
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    q1 = diag()
+    t_end = q1[7]
+    out["plain_step_loop"] = {"value": upd / (ms * 1e-3), "unit": UNIT, "steps": args.steps, "substeps": subs,
+                              "updates": upd, "ms": ms, "simulated_time": t_end, **drift(q0, q1),
+                              "form": "plain: reference step loop (simulation.py:114-149), theta 0.7, "
+                                      "float32 monopole walk, float64 SPH"}
+
+    theta = G.set_form("mixed_learned")
+    L.check(lib.gf_sim_init(n, d["pos"], d["vel"], d["mass"], d["kind"], d["u"], theta, p.EPS, p.GAMMA, p.ALPHA,
+                            p.BETA))
+    nlev = 7
+    chunk = np.zeros(nlev - 1, np.int32)
+    every, gms = ctypes.c_int(), ctypes.c_double()
+    L.check(lib.gf_sim_block_autotune(nlev, chunk.ctypes.data, ctypes.byref(every), ctypes.byref(gms)))
+    q0 = diag()
+    upd_b = ctypes.c_double()
+    upd, blocks = 0.0, 0
+    e0.record(s)
+    while True:
+        L.check(lib.gf_sim_blocks(1, nlev, ctypes.byref(upd_b)))
+        upd += upd_b.value
+        blocks += 1
+        t = ctypes.c_double()
+        L.check(lib.gf_sim_read(None, None, None, None, ctypes.byref(t)))
+        if t.value >= t_end or blocks >= 10 * args.steps:
+            break
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    q1 = diag()
+    out["mixed_batched_learned"] = {"value": upd / (ms * 1e-3), "unit": UNIT, "blocks": blocks,
+                                    "substeps": blocks * (1 << (nlev - 1)), "updates": upd, "ms": ms,
+                                    "simulated_time": q1[7], **drift(q0, q1),
+                                    "autotune": {"chunk_per_bin": chunk.tolist(), "rebuild_every": every.value},
+                                    "form": "quadrupole float32 + Kahan walk at theta 0.55, float32 + Kahan SPH, "
+                                            "learned h guess, block time steps (7 levels) replayed as CUDA graphs"}
+    r = out["mixed_batched_learned"]["simulated_time"] / out["mixed_batched_learned"]["ms"]
+    r0 = out["plain_step_loop"]["simulated_time"] / out["plain_step_loop"]["ms"]
+    print(json.dumps({
+        "workload": f"rotating 1/r cloud, {int((d['kind'] == 0).sum()):,} gas + {int((d['kind'] != 0).sum()):,} DM "
+                    "(seed 3), the same simulated time for both forms",
+        "forms": out,
+        "simulated_time_per_wall_second_ratio": r / r0,
+        "diagnostics": "gf_sim_diagnostics: float64 sums; potential from a monopole walk at theta 0.5",
+    }), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.workload == "drift":
+        run_drift(args, world, rank, local)
+    elif args.workload == "learned":
+        run_learned(args, world, rank, local)
     else:
         run_gpu(args, world, rank, local)
 

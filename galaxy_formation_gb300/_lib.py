@@ -56,6 +56,7 @@ SIGNATURES = {
                      _cd, _cd, _cd, _cd, _cd], _ci),
     "gf_sim_step": ([_cd, ctypes.POINTER(_cd), ctypes.POINTER(_ci)], _ci),
     "gf_sim_read": ([_vp, _vp, _vp, _vp, ctypes.POINTER(_cd)], _ci),
+    "gf_sim_diagnostics": ([_cd, _dbl], _ci),
     "gf_sim_blocks": ([_ci, _ci, ctypes.POINTER(_cd)], _ci),
     "gf_sim_updates": ([], _cd),
     "gf_sim_block_config": ([_vp, _ci, _ci], _ci),

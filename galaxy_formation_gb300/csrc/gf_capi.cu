@@ -634,6 +634,15 @@ int gf_sim_levels(int nlev, double* frac) {
     });
 }
 
+int gf_sim_diagnostics(double theta, double* out) {
+    return guarded([&] {
+        require(out && theta > 0, "bad arguments");
+        require(simulation_ready(), "gf_sim_init first");
+        sim_diagnostics(theta, out);
+        collect_status(ctx().stream);
+    });
+}
+
 int gf_sim_read(double* pos, double* vel, double* acc, double* dt_ind, double* t) {
     return guarded([&] { sim_read(pos, vel, acc, dt_ind, t); });
 }

@@ -92,6 +92,7 @@ void block_config(const int* chunk, int nbins, int rebuild_every);
 void block_autotune(int nlev, int* chunk, int* rebuild_every, double* graph_ms);
 double sim_updates();
 void sim_read(double* pos, double* vel, double* acc, double* dt_ind, double* t);
+void sim_diagnostics(double theta, double* out);
 // Block time steps (the batched form): advances nblocks blocks of 2^(nlev-1) sub-steps;
 // returns the particle-updates done.
 double block_run(int nblocks, int nlev);

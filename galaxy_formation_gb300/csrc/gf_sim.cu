@@ -547,6 +547,97 @@ double sim_step(double dt_max, int* substeps) {
     return D;
 }
 
+// ---------------------------------------------------------------------------------------
+// Conserved quantities in float64: kinetic, potential (softened, from a monopole Barnes-Hut
+// walk at opening angle theta on a tree of its own), thermal energy and angular momentum.
+// Between blocks of the batched form the velocities carry the opening half-kick of the next
+// block; it is taken off here so the diagnostics see synchronised velocities.
+
+namespace {
+
+constexpr int kDiagThreads = 256;
+constexpr int kDiagQ = 6;  // kinetic, potential, thermal, Lx, Ly, Lz
+
+__global__ void __launch_bounds__(kDiagThreads) k_diag_partial(
+    int n, const double* __restrict__ pos, const double* __restrict__ vel, const double* __restrict__ acc,
+    const double* __restrict__ mass, const int8_t* __restrict__ kind, const double* __restrict__ u,
+    const double* __restrict__ phi, const int8_t* __restrict__ level, const unsigned long long* __restrict__ dbits,
+    double* __restrict__ part) {
+    __shared__ double sm[kDiagQ][kDiagThreads];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double q[kDiagQ] = {0, 0, 0, 0, 0, 0};
+    if (i < n) {
+        const double m = mass[i];
+        double v[3] = {vel[3 * size_t(i)], vel[3 * size_t(i) + 1], vel[3 * size_t(i) + 2]};
+        if (level) {
+            const double h = 0.5 * __longlong_as_double((long long)*dbits) * double(1 << level[i]);
+            for (int c = 0; c < 3; ++c) v[c] -= h * acc[3 * size_t(i) + c];
+        }
+        const double x = pos[3 * size_t(i)], y = pos[3 * size_t(i) + 1], z = pos[3 * size_t(i) + 2];
+        q[0] = 0.5 * m * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        q[1] = 0.5 * m * phi[i];
+        q[2] = kind[i] == 0 ? m * u[i] : 0.0;
+        q[3] = m * (y * v[2] - z * v[1]);
+        q[4] = m * (z * v[0] - x * v[2]);
+        q[5] = m * (x * v[1] - y * v[0]);
+    }
+    for (int c = 0; c < kDiagQ; ++c) sm[c][threadIdx.x] = q[c];
+    __syncthreads();
+    for (int w = kDiagThreads / 2; w > 0; w >>= 1) {  // fixed pairing: deterministic
+        if (threadIdx.x < w)
+            for (int c = 0; c < kDiagQ; ++c) sm[c][threadIdx.x] += sm[c][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x < kDiagQ) part[size_t(blockIdx.x) * kDiagQ + threadIdx.x] = sm[threadIdx.x][0];
+}
+
+__global__ void k_diag_final(int nb, const double* __restrict__ part, double* __restrict__ out) {
+    const int c = threadIdx.x;
+    if (c >= kDiagQ) return;
+    double t = 0;
+    for (int b = 0; b < nb; ++b) t += part[size_t(b) * kDiagQ + c];
+    out[c] = t;
+}
+
+}  // namespace
+
+static Octree g_diag_tree;
+static DevBuf g_diag_acc, g_diag_phi, g_diag_part, g_diag_out;
+
+void sim_diagnostics(double theta, double* out) {
+    Simulation& S = g_sim;
+    cudaStream_t s = ctx().stream;
+    const int n = S.n;
+    Octree& T = g_diag_tree;
+    T.quad = false;
+    T.build(n, S.pos.as<double>(), S.mass.as<double>(), theta, s);
+    T.prepare_walk(nullptr, s);
+    double* phi = g_diag_phi.get<double>(n);
+    T.walk(S.eps, g_diag_acc.get<double>(3 * size_t(n)), s, phi);
+    const int nb = div_up(n, kDiagThreads);
+    double* part = g_diag_part.get<double>(size_t(nb) * kDiagQ);
+    double* dout = g_diag_out.get<double>(kDiagQ);
+    const bool blocks = g_block.started;
+    k_diag_partial<<<nb, kDiagThreads, 0, s>>>(n, S.pos.as<double>(), S.vel.as<double>(), S.acc.as<double>(),
+                                               S.mass.as<double>(), S.kind.as<int8_t>(), S.u.as<double>(), phi,
+                                               blocks ? g_block.level.as<int8_t>() : nullptr,
+                                               blocks ? g_block.scal.as<unsigned long long>() : nullptr, part);
+    GF_CHECK_LAUNCH();
+    k_diag_final<<<1, 32, 0, s>>>(nb, part, dout);
+    GF_CHECK_LAUNCH();
+    double q[kDiagQ];
+    GF_CUDA(cudaMemcpyAsync(q, dout, sizeof q, cudaMemcpyDeviceToHost, s));
+    GF_CUDA(cudaStreamSynchronize(s));
+    out[0] = q[0];
+    out[1] = q[1];
+    out[2] = q[2];
+    out[3] = q[0] + q[1] + q[2];
+    out[4] = q[3];
+    out[5] = q[4];
+    out[6] = q[5];
+    out[7] = S.t;
+}
+
 void sim_read(double* pos, double* vel, double* acc, double* dt_ind, double* t) {
     Simulation& S = g_sim;
     cudaStream_t s = ctx().stream;

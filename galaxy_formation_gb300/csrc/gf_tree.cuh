@@ -88,7 +88,8 @@ struct Octree {
     // Work list of groups with at least one active particle (active may be null); chunk > 0
     // cuts each group's active particles into items of <= chunk with their own spheres.
     void prepare_walk(const uint8_t* active, cudaStream_t s, int chunk = 0);
-    void walk(double eps, double* acc, cudaStream_t s);
+    // pot (monopole trees, may be null): softened potentials of the walked particles
+    void walk(double eps, double* acc, cudaStream_t s, double* pot = nullptr);
 };
 
 Octree& gravity_tree();

@@ -167,6 +167,21 @@ __device__ __forceinline__ void pair_acc(const float4 e, float x, float y, float
     az += f * ez;
 }
 
+// the same pair with the softened potential -m / sqrt(|d|^2 + eps^2) (energy diagnostics;
+// a particle's pair with itself, d = 0, adds nothing)
+__device__ __forceinline__ void pair_acc_pot(const float4 e, float x, float y, float z, float eps2,
+                                             float& ax, float& ay, float& az, float& ph) {
+    const float ex = e.x - x, ey = e.y - y, ez = e.z - z;
+    const float r2 = ex * ex + ey * ey + ez * ez + eps2;
+    const float inv = rsqrtf(r2);
+    const float mi = e.w * inv;
+    const float f = mi * inv * inv;
+    ax += f * ex;
+    ay += f * ey;
+    az += f * ez;
+    ph -= (ex != 0.f || ey != 0.f || ez != 0.f) ? mi : 0.f;  // no self term
+}
+
 // Second-order expansion of the Plummer-softened field of a node about its centre of mass,
 // at d = com - x, r^2 = |d|^2 + eps^2, Q the traceless quadrupole and T = sum m |y|^2:
 //   a = M d / r^3 - Q d / r^5 + (5/2) (d.Q.d) d / r^7 - (5/2) T eps^2 d / r^7.
@@ -192,11 +207,24 @@ __device__ __forceinline__ void quad_acc(const float4 e, const float4 q, float2 
     az += f * dz - inv5 * qdz;
 }
 
-// Evaluates the tile entries [0, fill) for the lane's particle(s).
+// Evaluates the tile entries [0, fill) for the lane's particle(s); POT also sums potentials.
+template <bool POT>
 __device__ __forceinline__ void eval_tile(const float4* tile, int fill, bool two, int r, int sub, float eps2,
                                           float x0, float y0, float z0, float x1, float y1, float z1,
                                           float& ax0, float& ay0, float& az0, float& ax1, float& ay1,
-                                          float& az1) {
+                                          float& az1, float& ph0, float& ph1) {
+    if constexpr (POT) {
+        if (two) {
+            for (int j = 0; j < fill; ++j) {
+                const float4 e = tile[j];
+                pair_acc_pot(e, x0, y0, z0, eps2, ax0, ay0, az0, ph0);
+                pair_acc_pot(e, x1, y1, z1, eps2, ax1, ay1, az1, ph1);
+            }
+        } else {
+            for (int j = sub; j < fill; j += r) pair_acc_pot(tile[j], x0, y0, z0, eps2, ax0, ay0, az0, ph0);
+        }
+        return;
+    }
     if (two) {
 #pragma unroll 2
         for (int j = 0; j < fill; ++j) {
@@ -241,12 +269,14 @@ __device__ __forceinline__ void eval_quad4(const float4* tile, const float4* ntA
     }
 }
 
-template <bool QUAD>
+// POT (monopole form only): also the softened potential of every walked particle, into pot.
+template <bool QUAD, bool POT = false>
 __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
     const float4* __restrict__ wa, const float4* __restrict__ wb, const float4* __restrict__ wq,
     const float* __restrict__ wt, const float4* __restrict__ p4, const int* __restrict__ perm, const uint8_t* __restrict__ active,
     const int4* __restrict__ work, const float4* __restrict__ sphere, TreeCounts* cnt, int nn, float eps2,
-    double* __restrict__ acc, uint32_t* status) {
+    double* __restrict__ acc, uint32_t* status, double* __restrict__ pot = nullptr) {
+    static_assert(!(QUAD && POT), "potentials come from the monopole walk");
     using Smem = WarpSmem<QUAD>;
     __shared__ Smem smem_all[kWalkWarps];
     Smem& S = smem_all[threadIdx.x >> 5];
@@ -317,10 +347,10 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
         }
         // reference form: one float32 running sum per component; mixed form: each tile's
         // partial sums are added to Kahan-compensated totals
-        float ax[kPpl], ay[kPpl], az[kPpl];
+        float ax[kPpl], ay[kPpl], az[kPpl], ph[kPpl];
         KahanF kx[kPpl], ky[kPpl], kz[kPpl];
 #pragma unroll
-        for (int t = 0; t < kPpl; ++t) ax[t] = ay[t] = az[t] = 0.f;
+        for (int t = 0; t < kPpl; ++t) ax[t] = ay[t] = az[t] = ph[t] = 0.f;
         const bool two = P > 32;
 
         int fill = 0, fillN = 0;
@@ -334,8 +364,8 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
             if (lane_on) eval_quad4(S.tile, S.ntA, S.ntQ, S.ntYZ, fill, fillN, ksub, m, eps2, x, y, z, \
                                     kx, ky, kz);                                                     \
         } else {                                                                                     \
-            eval_tile(S.tile, fill, two, r, sub, eps2, x[0], y[0], z[0], x[1], y[1], z[1], ax[0],    \
-                      ay[0], az[0], ax[1], ay[1], az[1]);                                            \
+            eval_tile<POT>(S.tile, fill, two, r, sub, eps2, x[0], y[0], z[0], x[1], y[1], z[1],      \
+                           ax[0], ay[0], az[0], ax[1], ay[1], az[1], ph[0], ph[1]);                  \
         }                                                                                            \
         __syncwarp();                                                                                \
         fill = 0;                                                                                    \
@@ -483,18 +513,21 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
                 ax[0] += __shfl_xor_sync(0xffffffffu, ax[0], o);
                 ay[0] += __shfl_xor_sync(0xffffffffu, ay[0], o);
                 az[0] += __shfl_xor_sync(0xffffffffu, az[0], o);
+                if (POT) ph[0] += __shfl_xor_sync(0xffffffffu, ph[0], o);
             }
             if (has[0] && sub == 0) {
                 const int kp = perm[S.slot_pos[slot[0]]];
                 acc[3 * size_t(kp)] = ax[0];
                 acc[3 * size_t(kp) + 1] = ay[0];
                 acc[3 * size_t(kp) + 2] = az[0];
+                if (POT) pot[kp] = ph[0];
             }
             if (has[1]) {
                 const int kp = perm[S.slot_pos[slot[1]]];
                 acc[3 * size_t(kp)] = ax[1];
                 acc[3 * size_t(kp) + 1] = ay[1];
                 acc[3 * size_t(kp) + 2] = az[1];
+                if (POT) pot[kp] = ph[1];
             }
         }
         __syncwarp();
@@ -519,7 +552,7 @@ void Octree::prepare_walk(const uint8_t* active, cudaStream_t s, int chunk) {
     GF_CHECK_LAUNCH();
 }
 
-void Octree::walk(double eps, double* acc, cudaStream_t s) {
+void Octree::walk(double eps, double* acc, cudaStream_t s, double* pot) {
     Context& C = ctx();
     const float eps2 = float(eps * eps);
     static int bps_mono = 0, bps_quad = 0;
@@ -531,7 +564,12 @@ void Octree::walk(double eps, double* acc, cudaStream_t s) {
     }
     ProfScope ps(kStWalk, s);
     last_walked() = this;
-    if (quad) {
+    if (pot) {
+        if (quad) throw Error(GF_ERR_ARG, "potentials come from the monopole walk");
+        k_walk<false, true><<<bps_mono * C.sms, kWalkWarps * 32, 0, s>>>(
+            w_a.as<float4>(), w_b.as<float4>(), nullptr, nullptr, p4.as<float4>(), perm.as<int>(), active_ptr,
+            work.as<int4>(), sphere.as<float4>(), counts.as<TreeCounts>(), node_cap, eps2, acc, C.d_status, pot);
+    } else if (quad) {
         k_walk<true><<<bps_quad * C.sms, kWalkWarps * 32, 0, s>>>(
             w_a.as<float4>(), w_b.as<float4>(), w_q.as<float4>(), w_t.as<float>(), p4.as<float4>(), perm.as<int>(),
             active_ptr,

@@ -231,6 +231,13 @@ int gf_sim_levels(int nlev, double* frac);
 /* Particle-updates of the last gf_sim_step: particles that received freshly computed forces
  * (the active set of every force evaluation, plus all gas whenever SPH ran). */
 double gf_sim_updates(void);
+/* Conserved quantities of the current state, float64 (no reference counterpart): out[8] =
+ * kinetic, potential, thermal (sum m u of the gas), total energy, angular momentum Lx, Ly, Lz,
+ * time. The potential is 1/2 sum m phi with phi the softened potential of a monopole
+ * Barnes-Hut walk at opening angle theta (a tree of its own); between blocks of
+ * gf_sim_blocks the velocities are synchronised first (the next block's opening half-kick
+ * taken off). */
+int gf_sim_diagnostics(double theta, double* out);
 /* Copies the state out (host pointers; any may be NULL): pos, vel, acc (n,3), dt_ind (n),
  * and the simulated time t. */
 int gf_sim_read(double* pos, double* vel, double* acc, double* dt_ind, double* t);
