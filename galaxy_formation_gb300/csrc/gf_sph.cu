@@ -261,6 +261,10 @@ __global__ void __launch_bounds__(kCandWarps * 32) k_knn_cand(
 // ------------------------------------------------------------------------ exact kNN
 
 constexpr int kKnnWarps = 8;
+// Leaf capacity of the neighbour-search tree. The search is exact for any tree; 16 walks
+// fewer levels per query (7 % faster on the 1M disk) but its coarser leaf counts make the
+// learned guess's features less informative, so the reference's 8 is kept.
+constexpr int kKnnLeaf = kLeafMax;
 constexpr int kKnnStack = 512;
 constexpr int kKnnCap = 128;
 
@@ -657,6 +661,7 @@ void knn_exact(Octree& T, int n, const double* pos, int k, const float* r_guess,
                double* dsel, int dsel_col, const HGuess* hg) {
     if (n <= 0) return;
     T.want_knn = true;
+    T.leaf_max = kKnnLeaf;
     T.build(n, pos, nullptr, 0.7, s);
     if (hg && hg->X) {  // features for the learned guess (and for training pairs)
         k_hfeatures<<<div_up(n, kThreads), kThreads, 0, s>>>(n, T.perm.as<int>(), T.leaf_of.as<int>(),

@@ -208,21 +208,23 @@ __device__ __forceinline__ int digit(const KeyView& K, int i, int l) {
     return int((K.k2[i] >> (3 * (48 - l))) & 7);
 }
 
-__global__ void k_cpl9(KeyView K, int n, int8_t* __restrict__ cpl9, TreeCounts* cnt) {
+// cpl9[i] = common prefix of positions i and i + L (L = leaf capacity): a cell holding both
+// holds L + 1 particles and must split
+__global__ void k_cpl9(KeyView K, int n, int8_t* __restrict__ cpl9, TreeCounts* cnt, int L) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int c = -1;
-    if (i + kLeafMax < n) c = cpl(K, i, i + kLeafMax);
+    if (i + L < n) c = cpl(K, i, i + L);
     if (c == 21 && !K.k1) cnt->deep = 1;
     cpl9[i] = int8_t(c);
 }
 
 __global__ void k_nstart(KeyView K, int n, const int8_t* __restrict__ cpl9, int8_t* __restrict__ ldepth,
-                         int8_t* __restrict__ dsplit, int* __restrict__ nstart) {
+                         int8_t* __restrict__ dsplit, int* __restrict__ nstart, int L) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int m = -1;
-    for (int j = max(0, i - kLeafMax); j <= i; ++j) m = max(m, int(cpl9[j]));
+    for (int j = max(0, i - L); j <= i; ++j) m = max(m, int(cpl9[j]));
     const int ld = min(kDepthMax, m + 1);
     const int ds = i == 0 ? 0 : cpl(K, i - 1, i) + 1;
     ldepth[i] = int8_t(ld);
@@ -808,12 +810,12 @@ __global__ void k_walk_fill(int nn, const int4* __restrict__ n_i4, const int* __
 __global__ void k_deep_keys(int n, const uint64_t* __restrict__ k0, const int* __restrict__ perm,
                             const double* __restrict__ pos, const RootBox* __restrict__ rootp,
                             uint64_t* __restrict__ k1, uint64_t* __restrict__ k2,
-                            int* __restrict__ starts, int* __restrict__ nstarts) {
+                            int* __restrict__ starts, int* __restrict__ nstarts, int L) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     bool deep = false;
-    for (int j = max(0, i - kLeafMax); j <= i && !deep; ++j)
-        deep = j + kLeafMax < n && k0[j] == k0[j + kLeafMax];
+    for (int j = max(0, i - L); j <= i && !deep; ++j)
+        deep = j + L < n && k0[j] == k0[j + L];
     uint64_t a = 0, b = 0;
     if (deep) {
         const RootBox R = *rootp;
@@ -962,9 +964,9 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
     // where they leave every common-prefix length the tree uses unchanged).
     bool deep = graph_safe;
     if (!graph_safe) {
-        k_cpl9<<<grid, kThreads, 0, s>>>(K, n, c9, cnt);
+        k_cpl9<<<grid, kThreads, 0, s>>>(K, n, c9, cnt, leaf_max);
         GF_CHECK_LAUNCH();
-        k_nstart<<<grid, kThreads, 0, s>>>(K, n, c9, ld, ds, ns);
+        k_nstart<<<grid, kThreads, 0, s>>>(K, n, c9, ld, ds, ns, leaf_max);
         GF_CHECK_LAUNCH();
         exclusive_scan(ns, nb, n, &cnt->total_nodes, s, &scratch);
         GF_CUDA(cudaMemcpyAsync(h_counts, cnt, sizeof(TreeCounts), cudaMemcpyDeviceToHost, s));
@@ -976,16 +978,16 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
         uint64_t* e2 = key2.get<uint64_t>(n);
         int* starts = reinterpret_cast<int*>(key_alt.get<uint64_t>(n));  // scratch
         int* nst = &cnt->pad[0];
-        k_deep_keys<<<grid, kThreads, 0, s>>>(n, k0, pm, pos, R, e1, e2, starts, nst);
+        k_deep_keys<<<grid, kThreads, 0, s>>>(n, k0, pm, pos, R, e1, e2, starts, nst, leaf_max);
         GF_CHECK_LAUNCH();
         deep_sort_attr();
         const size_t sm = size_t(kDeepRunMax) * (2 * sizeof(uint64_t) + sizeof(int));
         k_deep_sort<<<2 * C.sms, 512, sm, s>>>(n, k0, e1, e2, pm, starts, nst, C.d_status);
         GF_CHECK_LAUNCH();
         K = KeyView{k0, e1, e2};
-        k_cpl9<<<grid, kThreads, 0, s>>>(K, n, c9, cnt);
+        k_cpl9<<<grid, kThreads, 0, s>>>(K, n, c9, cnt, leaf_max);
         GF_CHECK_LAUNCH();
-        k_nstart<<<grid, kThreads, 0, s>>>(K, n, c9, ld, ds, ns);
+        k_nstart<<<grid, kThreads, 0, s>>>(K, n, c9, ld, ds, ns, leaf_max);
         GF_CHECK_LAUNCH();
         exclusive_scan(ns, nb, n, &cnt->total_nodes, s, &scratch);
         if (!graph_safe) {

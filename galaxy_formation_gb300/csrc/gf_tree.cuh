@@ -68,6 +68,7 @@ struct Octree {
     DevBuf plo, leaf_of, w_parent;
     bool want_knn = false;
     int group_max = kGroupMax;   // walk groups: shallowest nodes with <= group_max particles
+    int leaf_max = kLeafMax;     // leaf capacity (the reference's 8 for gravity trees)
     bool quad = false;           // also build quadrupole moments (mixed-precision form)
     bool kahan = false;          // walk: compensated accumulation of the tile sums
     // groups and walk work list
