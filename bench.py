@@ -21,7 +21,7 @@ over a 64-sub-step block.
 
 `value` = mixed_learned, timed on the device with CUDA events on the launching stream around
 each step, inputs resident in HBM, L2 flushed (256 MB write) between steps; `e2e` = the same
-form through the C ABI with host buffers (copies in and out included). `--impl reference`
+form through the C ABI with pinned host buffers (copies in and out included). `--impl reference`
 times the reference's CPU algorithm on this host's cores (the oracle restatement of
 cpp/nbody.cpp + scipy cKDTree + the restated sph_forces) on the same workload.
 Multi-GPU (torchrun): independent replicas, one per GPU, no collective on the data path.
@@ -491,9 +491,14 @@ def run_gpu(args, world, rank, local):
     e2e = None
     if not args.no_e2e:
         theta = G.set_form(head)
-        host = {k: np.ascontiguousarray(G.d[k]) for k in ("pos", "vel", "mass", "kind", "u")}
-        a_h = np.empty((n, 3))
-        dt_h = np.empty(n)
+
+        def pinned(a):  # page-locked host copy (numpy view of a pinned torch tensor)
+            t = G.torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+            return t.numpy()
+
+        host = {k: pinned(G.d[k]) for k in ("pos", "vel", "mass", "kind", "u")}
+        a_h = pinned(np.empty((n, 3)))
+        dt_h = pinned(np.empty(n))
 
         def host_step():
             st = lib.gf_accelerations(n, host["pos"], host["vel"], host["mass"], host["kind"], host["u"],
@@ -510,7 +515,8 @@ def run_gpu(args, world, rank, local):
             ts.append(time.perf_counter() - t0)
         e2e = {"value": world * n / statistics.mean(ts), "unit": UNIT,
                "h2d_bytes_per_step": n * (24 + 24 + 8 + 1 + 8), "d2h_bytes_per_step": n * (24 + 8),
-               "ms_per_step": statistics.mean(ts) * 1e3, "form": head}
+               "ms_per_step": statistics.mean(ts) * 1e3, "form": head,
+               "host_buffers": "pinned (page-locked); copies in and out inside each timed call"}
 
     cpu = None
     if world == 1 and not args.no_cpu:
