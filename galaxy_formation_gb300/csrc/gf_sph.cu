@@ -267,6 +267,7 @@ constexpr int kKnnWarps = 8;
 constexpr int kKnnLeaf = kLeafMax;
 constexpr int kKnnStack = 512;
 constexpr int kKnnCap = 128;
+constexpr int kKnnRound = 64;  // nodes tested per round of a neighbour walk (two per lane)
 
 // A collected point: (float32 squared distance bits << 32) | tree position. The bits of a
 // non-negative float order like the float, so sorting the keys orders by distance, then index.
@@ -281,7 +282,7 @@ struct KnnSmem {
     unsigned long long key[kKnnCap];
     unsigned long long dd[64];  // float64 squared distances as bit patterns
     int di[64];
-    int lanemap[32];
+    int lanemap[kKnnRound];
 };
 
 struct KnnArgs {
@@ -331,6 +332,7 @@ __device__ int knn_collect(const KnnArgs& A, KnnSmem& S, float4 xh, float4 xl, f
     __syncwarp();
     for (int rounds = 0; sp > 0; ++rounds) {
         if (rounds > A.nn) return -1;  // each node is popped at most once
+        // pop up to 64 nodes (two per lane: their loads overlap)
         const int kk = min(sp, 32);
         int e = 0, c = 0;
         if (lane < kk) {
@@ -339,51 +341,63 @@ __device__ int knn_collect(const KnnArgs& A, KnnSmem& S, float4 xh, float4 xl, f
         }
         const int incl = warp_incl_scan(c);
         const int excl = incl - c;
-        const unsigned fullm = __ballot_sync(0xffffffffu, lane < kk && incl <= 32);
+        const unsigned fullm = __ballot_sync(0xffffffffu, lane < kk && incl <= kKnnRound);
         const int nfull = __popc(fullm);
         int nnodes = __shfl_sync(0xffffffffu, incl, kk - 1);
         int take = c;
         if (nfull < kk) {
-            nnodes = 32;
+            nnodes = kKnnRound;
             if (lane == nfull) {
-                take = 32 - excl;
+                take = kKnnRound - excl;
                 S.stack[sp - 1 - lane] = (((e >> 4) + take) << 4) | (c - take);
             }
         }
         __syncwarp();
         if (lane < kk && lane <= nfull) {
             const int first = e >> 4;
-            for (int t = 0; t < take && excl + t < 32; ++t) S.lanemap[excl + t] = first + t;
+            for (int t = 0; t < take && excl + t < kKnnRound; ++t) S.lanemap[excl + t] = first + t;
         }
         sp -= nfull;
         __syncwarp();
-        const bool valid = lane < nnodes;
-        const int node = valid ? S.lanemap[lane] : 0;
+        int node[2];
+        float4 G[2], B[2];
+#pragma unroll
+        for (int i = 0; i < 2; ++i) node[i] = lane + 32 * i < nnodes ? S.lanemap[lane + 32 * i] : -1;
         __syncwarp();
-        bool open = false;
-        int first = 0, code = 0;
-        if (valid) {
-            const float4 g = A.wgeo[node];
-            const float4 B = A.wb[node];
-            first = __float_as_int(B.y);
-            code = __float_as_int(B.z);
-            // distance from the query to the cell cube, padded for float32 rounding
-            const float pad = 2e-6f * (fabsf(g.x) + fabsf(g.y) + fabsf(g.z) + g.w) + 1e-30f;
-            const float ex = fmaxf(fabsf((g.x - xh.x) - xl.x) - g.w - pad, 0.f);
-            const float ey = fmaxf(fabsf((g.y - xh.y) - xl.y) - g.w - pad, 0.f);
-            const float ez = fmaxf(fabsf((g.z - xh.z) - xl.z) - g.w - pad, 0.f);
-            open = ex * ex + ey * ey + ez * ez <= R2;
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            if (node[i] >= 0) {
+                G[i] = A.wgeo[node[i]];
+                B[i] = A.wb[node[i]];
+            }
         }
-        const bool inner = open && code > 0;
-        const bool leaf = open && code < 0;
-        const unsigned om = __ballot_sync(0xffffffffu, inner);
-        const int npush = __popc(om);
-        if (sp + npush > kKnnStack) return -1;
-        if (inner) S.stack[sp + __popc(om & lt)] = (first << 4) | code;
-        sp += npush;
-        // particles of the opened leaves, concatenated in lane order and tested 32 at a time:
-        // lane l takes offset o = base + l, owned by the lane whose leaf range covers o
-        const int lc = leaf ? -code : 0;
+        int first[2] = {0, 0}, lcs[2] = {0, 0};
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            bool open = false;
+            int code = 0;
+            if (node[i] >= 0) {
+                const float4 g = G[i];
+                first[i] = __float_as_int(B[i].y);
+                code = __float_as_int(B[i].z);
+                // distance from the query to the cell cube, padded for float32 rounding
+                const float pad = 2e-6f * (fabsf(g.x) + fabsf(g.y) + fabsf(g.z) + g.w) + 1e-30f;
+                const float ex = fmaxf(fabsf((g.x - xh.x) - xl.x) - g.w - pad, 0.f);
+                const float ey = fmaxf(fabsf((g.y - xh.y) - xl.y) - g.w - pad, 0.f);
+                const float ez = fmaxf(fabsf((g.z - xh.z) - xl.z) - g.w - pad, 0.f);
+                open = ex * ex + ey * ey + ez * ez <= R2;
+            }
+            const bool inner = open && code > 0;
+            const unsigned om = __ballot_sync(0xffffffffu, inner);
+            const int npush = __popc(om);
+            if (sp + npush > kKnnStack) return -1;
+            if (inner) S.stack[sp + __popc(om & lt)] = (first[i] << 4) | code;
+            sp += npush;
+            lcs[i] = open && code < 0 ? -code : 0;
+        }
+        // particles of the opened leaves, concatenated in lane order (a lane's two leaves in
+        // turn) and tested 32 at a time: lane l takes offset o = base + l
+        const int lc = lcs[0] + lcs[1];
         const int lincl = warp_incl_scan(lc);
         const int lexcl = lincl - lc;
         const int ltot = __shfl_sync(0xffffffffu, lincl, 31);
@@ -396,13 +410,16 @@ __device__ int knn_collect(const KnnArgs& A, KnnSmem& S, float4 xh, float4 xl, f
                 if (v <= o) src += step;
             }
             src = min(src, 31);
-            const int f_src = __shfl_sync(0xffffffffu, first, src);
+            const int f0 = __shfl_sync(0xffffffffu, first[0], src);
+            const int f1 = __shfl_sync(0xffffffffu, first[1], src);
+            const int l0 = __shfl_sync(0xffffffffu, lcs[0], src);
             const int e_src = __shfl_sync(0xffffffffu, lexcl, src);
             bool hit = false;
             float d2 = 0.f;
             int j = 0;
             if (o < ltot) {
-                j = f_src + (o - e_src);
+                const int off = o - e_src;
+                j = off < l0 ? f0 + off : f1 + (off - l0);
                 const float4 ph = A.p4[j], pl = A.plo[j];
                 const float dx = (ph.x - xh.x) + (pl.x - xl.x);
                 const float dy = (ph.y - xh.y) + (pl.y - xl.y);
