@@ -66,6 +66,7 @@ SIGNATURES = {
     "gf_set_option": ([_ci, _cd], _ci),
     "gf_get_option": ([_ci], _cd),
     "gf_force_stats": ([_dbl, _ci], _ci),
+    "gf_mlp_tensor_cores": ([], _ci),
     "gf_mlp_init": ([_ci], _ci),
     "gf_mlp_set_params": ([_f32], _ci),
     "gf_mlp_get_params": ([_f32], _ci),

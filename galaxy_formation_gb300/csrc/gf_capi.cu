@@ -647,6 +647,8 @@ int gf_sim_read(double* pos, double* vel, double* acc, double* dt_ind, double* t
     return guarded([&] { sim_read(pos, vel, acc, dt_ind, t); });
 }
 
+int gf_mlp_tensor_cores(void) { return mlp().tensor_cores; }
+
 int gf_mlp_init(int seed) {
     return guarded([&] { mlp().init(unsigned(seed), ctx().stream); });
 }

@@ -1,6 +1,8 @@
 // gf_mlp.cuh — the smoothing-length MLP (gf_mlp.cu).
 #pragma once
 
+#include <cuda_bf16.h>
+
 #include "gf_common.cuh"
 
 namespace gf {
@@ -26,7 +28,10 @@ struct Mlp {
     int n_data = 0;
     long long step_count = 0;
     MlpNorm norm;
-    DevBuf w, wb, m, v, grad, partial, loss_buf, idx, X, T;
+    DevBuf w, wb, m, v, grad, partial, loss_buf, idx, X, T, check_y;
+    // tensor-core inference: -1 not checked yet, 1 in use (agrees with the CUDA-core kernel
+    // on the first call), 0 not used
+    int tensor_cores = -1;
 
     void init(unsigned seed, cudaStream_t s);
     void set_params(const float* host, cudaStream_t s);
@@ -41,6 +46,8 @@ struct Mlp {
 };
 
 Mlp& mlp();
+// The inference of Mlp::predict with layer 2 on the tensor cores (gf_mlp_tc.cu).
+void mlp_forward_tc(int n, const float* X, const MlpNorm& nm, const __nv_bfloat16* P, float* Y, cudaStream_t s);
 // Adam steps on random minibatches of the device training set (X n x 4, T n); returns the
 // mean loss of the last minibatch (standardised units).
 double train_on(Mlp& M, const float* X, const float* T, int steps, int batch, double lr, cudaStream_t s);

@@ -285,8 +285,13 @@ int gf_mlp_init(int seed);
 int gf_mlp_set_params(const float* params);
 int gf_mlp_get_params(float* params);
 int gf_mlp_set_norm(const float* mean4, const float* std4, double t_mean, double t_std);
-/* log h of n samples (X: n x 4), host pointers. */
+/* log h of n samples (X: n x 4), host pointers. Inference rounds the layer-2 inputs to
+ * bfloat16 and runs layer 2 on the tensor cores (tcgen05) once the first call has checked
+ * them against the CUDA-core kernel. */
 int gf_mlp_predict(int n, const float* X, float* Y);
+/* 1: inference uses the tensor cores; 0: the CUDA-core kernel (the check disagreed);
+ * -1: not checked yet (no prediction since the weights were set). */
+int gf_mlp_tensor_cores(void);
 /* Gradient of 0.5 mean((y - t)^2) (standardised target t) over the n samples w.r.t. the flat
  * parameters, host pointers. */
 int gf_mlp_gradient(int n, const float* X, const float* T, float* grad);

@@ -37,10 +37,14 @@ def unpack(params):
 N_PARAMS = H * 4 + H + H * H + H + H + 1
 
 
-def forward(params, x):
+def forward(params, x, act_bf16=False):
+    """act_bf16: the layer-2 inputs rounded to bfloat16, as the inference kernels feed the
+    tensor cores (training keeps them in float32)."""
     W1, b1, W2, b2, w3, b3 = unpack(params)
     z1 = x @ W1.T + b1
     a1 = np.maximum(z1, 0)
+    if act_bf16:
+        a1 = bf16_round(a1.astype(np.float32))
     z2 = a1 @ W2.T + b2
     a2 = np.maximum(z2, 0)
     y = a2 @ w3 + b3

@@ -41,7 +41,8 @@ def test_forward_and_gradient_match_float64(gpulib, mref):
     T = rng.normal(size=300).astype(np.float32)
     Y = np.zeros(300, np.float32)
     _lib.check(lib.gf_mlp_predict(300, X, Y))
-    y_ref, _ = mref.forward(pb, X.astype(np.float64))
+    # inference: bfloat16 layer-2 inputs (the tensor-core operands), float32 accumulation
+    y_ref, _ = mref.forward(pb, X.astype(np.float64), act_bf16=True)
     assert np.max(np.abs(Y - y_ref)) < 1e-4 * max(1.0, np.abs(y_ref).max())
     g = np.zeros(_lib.MLP_PARAMS, np.float32)
     _lib.check(lib.gf_mlp_gradient(300, X, T, g))
@@ -108,3 +109,28 @@ def test_training_lowers_the_loss(gpulib, oracle):
     for mode in (2, 0):
         assert np.allclose(res[mode][1], res[1][1], rtol=1e-12, atol=0)
         assert np.allclose(res[mode][2], res[1][2], rtol=1e-12, atol=0)
+
+
+def test_inference_on_tensor_cores(gpulib, mref):
+    """The layer-2 contraction of the inference runs on the tensor cores (tcgen05): the
+    library's first-call check against the CUDA-core kernel passed, and a large batch (many
+    128-sample tiles, a partial last tile) matches the float64 oracle."""
+    from galaxy_formation_gb300 import _lib
+
+    lib = gpulib
+    _lib.check(lib.gf_mlp_init(5))
+    _lib.check(lib.gf_mlp_set_norm(np.zeros(4, np.float32), np.ones(4, np.float32), 0.0, 1.0))
+    p = np.zeros(_lib.MLP_PARAMS, np.float32)
+    _lib.check(lib.gf_mlp_get_params(p))
+    rng = np.random.default_rng(1)
+    n = 100_003
+    X = rng.normal(size=(n, 4)).astype(np.float32)
+    Y = np.zeros(n, np.float32)
+    _lib.check(lib.gf_mlp_predict(n, X, Y))
+    assert lib.gf_mlp_tensor_cores() == 1
+    y_ref, _ = mref.forward(mref.bf16_round(p), X.astype(np.float64), act_bf16=True)
+    err = np.abs(Y - y_ref) / max(1.0, np.abs(y_ref).max())
+    # float32 accumulation order only, except where a layer-1 activation sits on a bfloat16
+    # rounding boundary (the kernel's float32 layer 1 and the oracle's float64 one then round
+    # it to neighbouring bfloat16 values)
+    assert np.percentile(err, 99.9) < 1e-5 and err.max() < 5e-3, (np.percentile(err, 99.9), err.max())
