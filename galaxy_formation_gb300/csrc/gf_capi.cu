@@ -613,7 +613,9 @@ int gf_sim_block_config(const int* chunk, int nbins, int rebuild_every) {
         require(!chunk || (nbins >= 1 && nbins <= 8), "need 1 <= nbins <= 8");
         require(rebuild_every >= 0, "rebuild_every < 0");
         if (chunk)
-            for (int b = 0; b < nbins; ++b) require(chunk[b] >= 0 && chunk[b] <= 64, "chunk out of [0, 64]");
+            for (int b = 0; b < nbins; ++b)
+                require((chunk[b] >= 0 && chunk[b] <= 64) || (chunk[b] >= 100 && chunk[b] <= 164),
+                        "chunk out of [0, 64] (+100)");
         block_config(chunk, nbins, rebuild_every);
     });
 }

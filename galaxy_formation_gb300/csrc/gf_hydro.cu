@@ -334,7 +334,7 @@ void ForceEngine::evaluate(const ForceArgs& a, cudaStream_t s) {
         T.refit(a.pos, a.mass, s);
     }
     T.prepare_walk(a.active, s, a.walk_chunk ? a.walk_chunk : walk_chunk);
-    T.walk(a.eps, acc_grav.as<double>(), s);
+    T.walk(a.eps, acc_grav.as<double>(), s, nullptr, a.walk_npl);
 
     if (fork) {
         hydro(a, s2);

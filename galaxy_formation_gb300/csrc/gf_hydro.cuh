@@ -36,6 +36,7 @@ struct ForceArgs {
     // walk work items of <= walk_chunk active particles with their own spheres (0: the
     // reference's groups); used with an active set
     int walk_chunk = 0;
+    int walk_npl = 2;  // mixed walk: nodes per lane and round (2, or 8 for walks of a few items)
 };
 
 struct ForceEngine {

@@ -248,6 +248,7 @@ __global__ void k_active_at(int n, const int8_t* __restrict__ level, int s, uint
 // the sub-step index: levels 0..bin are due). Chosen by BlockIntegrator::autotune.
 struct BlockTuning {
     int chunk[8] = {4, 8, 8, 16, 16, 32, 64, 64};  // walk items of <= chunk active particles (0: groups)
+    int npl[8] = {8, 8, 8, 2, 2, 2, 2, 2};         // mixed walk: nodes per lane and round (2 or 8)
     int rebuild_every = 8;  // captured tree rebuild every this many sub-steps (0: refit only)
 };
 
@@ -284,13 +285,14 @@ struct BlockIntegrator {
 
     // nosync: inside the captured graph (rebuild = captured tree rebuild, else refit);
     // otherwise a regular evaluation of everybody on a rebuilt tree with fresh neighbours
-    void force(Simulation& S, const uint8_t* active, bool nosync, bool rebuild = false, int chunk = 0) {
+    void force(Simulation& S, const uint8_t* active, bool nosync, bool rebuild = false, int chunk = 0, int npl = 2) {
         ForceArgs a{S.n, S.pos.as<double>(), S.vel.as<double>(), S.mass.as<double>(), S.kind.as<int8_t>(),
                     S.u.as<double>(), S.theta, S.eps, S.gamma, S.alpha, S.beta, active,
                     nosync ? (rebuild ? 1 : 0) : 1, 1, nosync ? 0 : 1, S.acc.as<double>(), S.dt_ind.as<double>()};
         a.sph_active = active;
         a.nosync = nosync ? 1 : 0;
         a.walk_chunk = chunk;
+        a.walk_npl = npl;
         force_engine().evaluate(a, S.s());
     }
 
@@ -315,7 +317,7 @@ struct BlockIntegrator {
                 k_active_at<<<div_up(S.n, 256), 256, 0, s>>>(S.n, level.as<int8_t>(), sub, ac, d + 1);
                 GF_CHECK_LAUNCH();
                 const bool rb = tune.rebuild_every > 0 && sub % tune.rebuild_every == 0;
-                force(S, ac, true, rb, tune.chunk[bin_of(sub)]);
+                force(S, ac, true, rb, tune.chunk[bin_of(sub)], tune.npl[bin_of(sub)]);
                 k_kick_levels<<<div_up(S.n, 256), 256, 0, s>>>(S.n, S.vel.as<double>(), S.acc.as<double>(),
                                                                level.as<int8_t>(), d, 1, sub);
                 GF_CHECK_LAUNCH();
@@ -420,26 +422,34 @@ struct BlockIntegrator {
                                                              d + 1);
                 GF_CHECK_LAUNCH();
                 double best = INFINITY;
-                int best_c = 0;
-                for (int c : cand) {
-                    double ms[3];
-                    for (int r = 0; r < 3; ++r) {
-                        e0.record(s);
-                        T.prepare_walk(act.as<uint8_t>(), s, c);
-                        T.walk(S.eps, ta, s);
-                        e1.record(s);
-                        GF_CUDA(cudaStreamSynchronize(s));
-                        ms[r] = e1.since(e0);
-                    }
-                    std::sort(ms, ms + 3);
-                    if (ms[1] < best * 0.97) {  // prefer the earlier (coarser) candidate on near-ties
-                        best = ms[1];
-                        best_c = c;
+                int best_c = 0, best_p = 2;
+                for (int npl : {2, 8}) {
+                    if (npl != 2 && !T.quad) continue;  // the monopole walk has one width
+                    for (int c : cand) {
+                        double ms[3];
+                        for (int r = 0; r < 3; ++r) {
+                            e0.record(s);
+                            T.prepare_walk(act.as<uint8_t>(), s, c);
+                            T.walk(S.eps, ta, s, nullptr, npl);
+                            e1.record(s);
+                            GF_CUDA(cudaStreamSynchronize(s));
+                            ms[r] = e1.since(e0);
+                        }
+                        std::sort(ms, ms + 3);
+                        if (ms[1] < best * 0.97) {  // prefer the earlier candidate on near-ties
+                            best = ms[1];
+                            best_c = c;
+                            best_p = npl;
+                        }
                     }
                 }
                 tune.chunk[bin] = best_c;
+                tune.npl[bin] = best_p;
             }
-            for (int bin = nlev - 1; bin < 8; ++bin) tune.chunk[bin] = tune.chunk[std::max(0, nlev - 2)];
+            for (int bin = nlev - 1; bin < 8; ++bin) {
+                tune.chunk[bin] = tune.chunk[std::max(0, nlev - 2)];
+                tune.npl[bin] = tune.npl[std::max(0, nlev - 2)];
+            }
             // rebuild cadence: whole blocks from the same start
             static const int every[] = {0, 32, 16, 8, 4};
             double best = INFINITY;
@@ -472,8 +482,8 @@ struct BlockIntegrator {
         GF_CUDA(cudaStreamSynchronize(s));
         S.t = t0;
         started = false;
-        if (chunk_out)
-            for (int b = 0; b < nlev - 1; ++b) chunk_out[b] = tune.chunk[b];
+        if (chunk_out)  // chunk, with 100 added where the 8-nodes-per-lane walk won
+            for (int b = 0; b < nlev - 1; ++b) chunk_out[b] = tune.chunk[b] + (tune.npl[b] > 2 ? 100 : 0);
         if (rebuild_out) *rebuild_out = tune.rebuild_every;
     }
 };
@@ -490,7 +500,11 @@ double block_run(int nblocks, int nlev) {
 
 void block_config(const int* chunk, int nbins, int rebuild_every) {
     BlockTuning& t = g_block.tune;
-    for (int b = 0; b < 8; ++b) t.chunk[b] = chunk ? chunk[std::min(b, nbins - 1)] : 0;
+    for (int b = 0; b < 8; ++b) {
+        const int c = chunk ? chunk[std::min(b, nbins - 1)] : 0;
+        t.chunk[b] = c % 100;
+        t.npl[b] = c >= 100 ? 8 : 2;
+    }
     t.rebuild_every = rebuild_every;
     g_block.tune_changed = true;
 }

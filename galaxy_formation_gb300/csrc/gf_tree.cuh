@@ -90,7 +90,8 @@ struct Octree {
     // cuts each group's active particles into items of <= chunk with their own spheres.
     void prepare_walk(const uint8_t* active, cudaStream_t s, int chunk = 0);
     // pot (monopole trees, may be null): softened potentials of the walked particles
-    void walk(double eps, double* acc, cudaStream_t s, double* pot = nullptr);
+    // npl: nodes per lane and round of the mixed walk (2, or 8 for walks of a few items)
+    void walk(double eps, double* acc, cudaStream_t s, double* pot = nullptr, int npl = 2);
 };
 
 Octree& gravity_tree();

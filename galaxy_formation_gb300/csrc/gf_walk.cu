@@ -27,9 +27,10 @@ namespace {
 constexpr int kWalkWarps = 4;
 constexpr int kStackCap = 1024;   // child ranges per warp
 constexpr int kTileCap = 256;     // interaction entries per warp
-// nodes tested per lane and round of the walk: 2 for the mixed form (its rounds' loads then
-// overlap; measured 10 % faster at 1M), 1 for the reference form (2 measured 3 % slower)
-constexpr int kMaxNodesPerLane = 2;
+// Nodes tested per lane and round of the walk (their loads are issued together, so one
+// round's memory latency covers them all): 2 for the mixed form's full evaluations (10 %
+// faster at 1M than 1), 1 for the reference form (2 measured 3 % slower); 8 for walks of a
+// few items (block time steps), which are bound by the latency of their rounds, not by work.
 
 // Work list: groups with at least one active particle and a massive member, as work items
 // {first particle, particle count, active particles to evaluate, rank of the first of them
@@ -145,17 +146,18 @@ __global__ void k_group_prep(const int* __restrict__ groups, const int4* __restr
 
 // Shared memory of one warp. QUAD (mixed form) adds a tile of accepted nodes with their
 // quadrupoles; particles of opened leaves always go to the monopole tile.
-template <bool QUAD>
+template <bool QUAD, int NPL>
 struct WarpSmem {
     static constexpr int kStack = QUAD ? 768 : kStackCap;
+    static constexpr int kTile = (QUAD && NPL > 2) ? 128 : kTileCap;  // particle entries
     static constexpr int kNodeTile = QUAD ? 96 : 1;
     static constexpr int kBatch = QUAD ? 128 : 64;  // active particles evaluated per walk
     int stack[kStack];
-    float4 tile[kTileCap];
+    float4 tile[kTile];
     float4 ntA[kNodeTile];   // centre of mass, mass
     float4 ntQ[kNodeTile];   // Qxx, Qyy, Qxy, Qxz
     float2 ntYZ[kNodeTile];  // Qyz, T
-    int lanemap[32 * kMaxNodesPerLane];
+    int lanemap[32 * NPL];
     int slot_pos[kBatch];
 };
 
@@ -273,15 +275,15 @@ __device__ __forceinline__ void eval_quad4(const float4* tile, const float4* ntA
 }
 
 // POT (monopole form only): also the softened potential of every walked particle, into pot.
-template <bool QUAD, bool POT = false>
+template <bool QUAD, bool POT = false, int NPL = (QUAD ? 2 : 1)>
 __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
     const float4* __restrict__ wa, const float4* __restrict__ wb, const float4* __restrict__ wq,
     const float* __restrict__ wt, const float4* __restrict__ p4, const int* __restrict__ perm, const uint8_t* __restrict__ active,
     const int4* __restrict__ work, const float4* __restrict__ sphere, TreeCounts* cnt, int nn, float eps2,
     double* __restrict__ acc, uint32_t* status, double* __restrict__ pot = nullptr) {
     static_assert(!(QUAD && POT), "potentials come from the monopole walk");
-    using Smem = WarpSmem<QUAD>;
-    constexpr int kNodesPerLane = QUAD ? 2 : 1;
+    using Smem = WarpSmem<QUAD, NPL>;
+    constexpr int kNodesPerLane = NPL;
     constexpr int kRound = 32 * kNodesPerLane;
     __shared__ Smem smem_all[kWalkWarps];
     Smem& S = smem_all[threadIdx.x >> 5];
@@ -468,7 +470,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
                 }
                 fillN += na;
             } else {
-                if (fill + na > kTileCap) GF_WALK_FLUSH();
+                if (fill + na > Smem::kTile) GF_WALK_FLUSH();
                 if (accept) S.tile[fill + __popc(am & lt)] = A;
                 fill += na;
             }
@@ -479,8 +481,8 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
             const int lexcl = lincl - lc;
             const int ltot = __shfl_sync(0xffffffffu, lincl, 31);
             for (int done = 0; done < ltot;) {
-                if (fill == kTileCap) GF_WALK_FLUSH();
-                const int chunk = min(kTileCap - fill, ltot - done);
+                if (fill == Smem::kTile) GF_WALK_FLUSH();
+                const int chunk = min(Smem::kTile - fill, ltot - done);
                 if (leaf) {
                     const int a0 = max(lexcl, done), a1 = min(lexcl + lc, done + chunk);
                     for (int q = a0; q < a1; ++q) S.tile[fill + q - done] = p4[first + q - lexcl];
@@ -574,7 +576,7 @@ void Octree::prepare_walk(const uint8_t* active, cudaStream_t s, int chunk) {
     GF_CHECK_LAUNCH();
 }
 
-void Octree::walk(double eps, double* acc, cudaStream_t s, double* pot) {
+void Octree::walk(double eps, double* acc, cudaStream_t s, double* pot, int npl) {
     Context& C = ctx();
     const float eps2 = float(eps * eps);
     static int bps_mono = 0, bps_quad = 0;
@@ -591,6 +593,11 @@ void Octree::walk(double eps, double* acc, cudaStream_t s, double* pot) {
         k_walk<false, true><<<bps_mono * C.sms, kWalkWarps * 32, 0, s>>>(
             w_a.as<float4>(), w_b.as<float4>(), nullptr, nullptr, p4.as<float4>(), perm.as<int>(), active_ptr,
             work.as<int4>(), sphere.as<float4>(), counts.as<TreeCounts>(), node_cap, eps2, acc, C.d_status, pot);
+    } else if (quad && npl > 2) {
+        k_walk<true, false, 8><<<bps_quad * C.sms, kWalkWarps * 32, 0, s>>>(
+            w_a.as<float4>(), w_b.as<float4>(), w_q.as<float4>(), w_t.as<float>(), p4.as<float4>(), perm.as<int>(),
+            active_ptr,
+            work.as<int4>(), sphere.as<float4>(), counts.as<TreeCounts>(), node_cap, eps2, acc, C.d_status);
     } else if (quad) {
         k_walk<true><<<bps_quad * C.sms, kWalkWarps * 32, 0, s>>>(
             w_a.as<float4>(), w_b.as<float4>(), w_q.as<float4>(), w_t.as<float>(), p4.as<float4>(), perm.as<int>(),

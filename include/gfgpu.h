@@ -216,14 +216,16 @@ int gf_sim_blocks(int nblocks, int nlev, double* updates);
 /* Launch shape of gf_sim_blocks per sub-step bin (bin b = sub-steps whose index has b
  * trailing zero bits, i.e. levels 0..b due): chunk[b] = active particles per walk item
  * (0: the reference's walk groups with their spheres; 1..64: items of <= chunk[b] active
- * particles in tree order, each with its own bounding sphere); bins past nbins reuse
- * chunk[nbins-1]; chunk NULL = groups everywhere. rebuild_every > 0 rebuilds the tree inside
- * the captured block every that many sub-steps (0: refit only). */
+ * particles in tree order, each with its own bounding sphere), plus 100 to walk with 8 nodes
+ * per lane and round instead of 2 (mixed form; for bins of a few items, whose walks are bound
+ * by the latency of their rounds); bins past nbins reuse chunk[nbins-1]; chunk NULL =
+ * groups everywhere. rebuild_every > 0 rebuilds the tree inside the captured block every
+ * that many sub-steps (0: refit only). */
 int gf_sim_block_config(const int* chunk, int nbins, int rebuild_every);
 /* Autotuner of that launch shape on the current state: times the gravity walk of each bin's
- * active set per chunk candidate, then one block per rebuild cadence; keeps the fastest and
- * writes them to chunk (nlev-1 entries) / rebuild_every; graph_ms = the best block's graph
- * time. Positions, velocities and time are restored afterwards (the next block starts with
+ * active set per chunk candidate and walk width, then one block per rebuild cadence; keeps
+ * the fastest and writes them to chunk (nlev-1 entries, in gf_sim_block_config's encoding) /
+ * rebuild_every; graph_ms = the best block's graph time. Positions, velocities and time are restored afterwards (the next block starts with
  * a full evaluation). */
 int gf_sim_block_autotune(int nlev, int* chunk, int* rebuild_every, double* graph_ms);
 /* Fraction of the particles on each level 0..nlev-1 of the current block. */

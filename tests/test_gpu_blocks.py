@@ -140,7 +140,7 @@ def test_block_autotune_restores_state(gpulib):
     every = ctypes.c_int()
     ms = ctypes.c_double()
     _lib.check(lib.gf_sim_block_autotune(4, chunk.ctypes.data, ctypes.byref(every), ctypes.byref(ms)))
-    assert set(chunk.tolist()) <= {0, 2, 4, 8, 16, 32, 64}
+    assert {c % 100 for c in chunk.tolist()} <= {0, 2, 4, 8, 16, 32, 64}
     assert every.value in (0, 4) and ms.value > 0
     p1, v1, t1 = _state(lib, n)
     assert t1 == t0
@@ -148,3 +148,34 @@ def test_block_autotune_restores_state(gpulib):
     _lib.check(lib.gf_sim_blocks(2, 4, ctypes.byref(upd)))
     p2, v2, t2 = _state(lib, n)
     assert t2 > t1 and np.all(np.isfinite(p2)) and np.all(np.isfinite(v2))
+
+
+def test_wide_rounds_walk_matches(gpulib):
+    """The mixed walk with 8 nodes per lane and round (bins of a few items) evaluates the same
+    interactions as the 2-per-lane walk: block runs of the two agree to float32 summation
+    order."""
+    from galaxy_formation_gb300 import _lib, params, synthetic
+
+    lib = gpulib
+    _plain(lib)
+    lib.gf_set_option(_lib.OPT_GRAVITY_QUAD, 1)
+    d = synthetic.rotating_cloud(3000, 3000, seed=12)
+    d["kind"][:] = params.DM
+    d["u"][:] = 0.0
+    n = len(d["mass"])
+    out = {}
+    for name, chunk in (("two", [4, 8, 16]), ("eight", [104, 108, 116])):
+        ch = np.array(chunk, np.int32)
+        _lib.check(lib.gf_sim_block_config(ch.ctypes.data, 3, 0))
+        _lib.check(lib.gf_sim_init(n, d["pos"], d["vel"], d["mass"], d["kind"], d["u"], 0.55, params.EPS,
+                                   params.GAMMA, params.ALPHA, params.BETA))
+        upd = ctypes.c_double()
+        _lib.check(lib.gf_sim_blocks(2, 4, ctypes.byref(upd)))
+        out[name] = _state(lib, n)
+    lib.gf_set_option(_lib.OPT_GRAVITY_QUAD, 0)
+    (p2, v2, t2), (p8, v8, t8) = out["two"], out["eight"]
+    assert abs(t2 - t8) <= 1e-6 * t2
+    scale = np.linalg.norm(p2, axis=1).mean()
+    assert np.percentile(np.linalg.norm(p8 - p2, axis=1), 99) < 1e-5 * scale
+    vs = np.linalg.norm(v2, axis=1).mean()
+    assert np.percentile(np.linalg.norm(v8 - v2, axis=1), 99) < 1e-4 * vs
