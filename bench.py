@@ -50,10 +50,13 @@ CONFIG_IDX = 2
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 # (theta, quadrupole walk, float32 SPH, h guess mode)
+# theta, quadrupole gravity, float32 SPH, h guess (0 previous h, 2 learned), relative opening
+# tolerance (0: geometric criterion at theta; > 0: the relative criterion once every particle
+# has a previous gravity, with theta used for the first evaluation)
 FORMS = {
-    "plain": (0.7, 0, 0, 0),
-    "plain_matched": (0.15, 0, 0, 0),
-    "mixed_learned": (0.55, 1, 1, 2),
+    "plain": (0.7, 0, 0, 0, 0.0),
+    "plain_matched": (0.15, 0, 0, 0, 0.0),
+    "mixed_learned": (0.55, 1, 1, 2, 2.5e-3),
 }
 # flops per interaction (an FMA counting 2): monopole pair (cpp/nbody.cpp:398-402 in float32)
 # and the softened quadrupole node term of the mixed walk
@@ -257,11 +260,12 @@ class Gpu:
         self.flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=self.dev)  # 256 MB > L2
 
     def set_form(self, form):
-        theta, quad, sph32, hguess = FORMS[form]
+        theta, quad, sph32, hguess, rel = FORMS[form]
         L, lib = self._lib, self.lib
         lib.gf_set_option(L.OPT_GRAVITY_QUAD, quad)
         lib.gf_set_option(L.OPT_SPH_FLOAT32, sph32)
         lib.gf_set_option(L.OPT_HGUESS, hguess)
+        lib.gf_set_option(L.OPT_GRAVITY_REL, rel)  # the next evaluation sets the error scale
         return theta
 
     def step(self, theta, pos=None, kind=None, sph=1):
@@ -314,6 +318,9 @@ class Gpu:
         the fused evaluation with every particle flagged dark matter (no hydro term)."""
         theta = self.set_form(form)
         dm = torch_full_like(self.torch, self.T["kind"], 2)
+        # twice: the relative criterion takes its error scale from the previous evaluation,
+        # as in every timed step
+        self.step(theta, kind=dm)
         self.step(theta, kind=dm)
         a = self.acc.cpu().numpy()[targets]
         e = np.linalg.norm(a - exact, axis=1) / np.linalg.norm(exact, axis=1)
@@ -528,9 +535,12 @@ def run_gpu(args, world, rank, local):
 
     def summary(f):
         r = res[f]
-        th, quad_f, sph32, hg = FORMS[f]
+        th, quad_f, sph32, hg, rel = FORMS[f]
         out = {"value": r["value"], "ms_per_step": r["ms_per_step"], "theta": th,
                "gravity": "quadrupole float32 + Kahan" if quad_f else "monopole float32 (reference)",
+               "opening": (f"relative, alpha {rel:g} with a geometric floor at theta 1 (error scale: the "
+                           f"previous evaluation's gravity; theta {th} before it)") if rel else
+                          f"geometric, theta {th} (cpp/nbody.cpp:104-106)",
                "sph": "float32 + Kahan" if sph32 else "float64 (reference)",
                "h_guess": ["previous h", "cell density", "learned MLP"][hg],
                "grav_p99_rel_err_vs_f64_direct": r["p99"], "grav_median_rel_err": r["median"],
@@ -546,7 +556,8 @@ def run_gpu(args, world, rank, local):
         "dtype": "f32 (Kahan) gravity + f32 (Kahan) SPH, f64 positions" if FORMS[head][2] else "f32 gravity + f64 SPH",
         "data": "synthetic",
         "config": {"workload": workload_name(n_gas, n - n_gas), "particles": n, "gas": n_gas,
-                   "form": head, "theta": FORMS[head][0], "eps_kpc": params.EPS_KPC,
+                   "form": head, "theta": FORMS[head][0], "relative_opening_alpha": FORMS[head][4],
+                   "eps_kpc": params.EPS_KPC,
                    "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
         "roofline": roof,
         "cpu_baseline": cpu,

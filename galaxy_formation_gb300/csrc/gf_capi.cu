@@ -559,6 +559,11 @@ int gf_set_option(int key, double value) {
                 F.walk_group = int(value);
                 F.grav.valid = false;  // regroup at the next evaluation
                 break;
+            case GF_OPT_GRAVITY_REL:
+                require(value >= 0 && value < 1, "relative opening tolerance is in [0, 1)");
+                F.grav_rel = value;
+                F.have_aold = false;  // the next evaluation sets the error scale
+                break;
             default: throw Error(GF_ERR_ARG, "unknown option");
         }
     });
@@ -573,6 +578,7 @@ double gf_get_option(int key) {
         case GF_OPT_COLLECT: return double(F.collect_n);
         case GF_OPT_WALK_CHUNK: return F.walk_chunk;
         case GF_OPT_WALK_GROUP: return F.walk_group;
+        case GF_OPT_GRAVITY_REL: return F.grav_rel;
         default: return -1.0;
     }
 }

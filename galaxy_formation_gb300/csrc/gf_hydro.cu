@@ -289,6 +289,7 @@ void ForceEngine::evaluate(const ForceArgs& a, cudaStream_t s) {
         cache_valid = false;
         have_hprev = false;
         have_divv = false;
+        have_aold = false;
         GF_CUDA(cudaMemsetAsync(divv_prev.get<float>(n), 0, sizeof(float) * size_t(n), s));
         row.get<int>(n);
         loc.get<int>(n);
@@ -314,10 +315,12 @@ void ForceEngine::evaluate(const ForceArgs& a, cudaStream_t s) {
     // gravity (simulation.py:64)
     Octree& T = grav;
     const int gmax = gravity_quad ? walk_group : kGroupMax;  // the mixed form's groups are tunable
+    const bool rel = gravity_quad && grav_rel > 0 && have_aold;
+    const double theta = rel ? kRelFloorTheta : a.theta;
     if (a.nosync) {  // inside a captured graph: the tree of the last regular build, rebuilt or refitted
         if (!T.valid || T.n != n) throw Error(GF_ERR_ARG, "a synchronisation-free evaluation needs a built tree");
         if (a.rebuild)
-            T.build(n, a.pos, a.mass, a.theta, s, true);
+            T.build(n, a.pos, a.mass, theta, s, true);
         else
             T.refit(a.pos, a.mass, s);
     } else if (a.rebuild || !T.valid || T.n != n || T.quad != (gravity_quad != 0) || T.group_max != gmax) {
@@ -326,15 +329,17 @@ void ForceEngine::evaluate(const ForceArgs& a, cudaStream_t s) {
         T.group_max = gmax;
         if (same_set) {
             T.reserve_graph_build();
-            T.build(n, a.pos, a.mass, a.theta, s, true);
+            T.build(n, a.pos, a.mass, theta, s, true);
         } else {
-            T.build(n, a.pos, a.mass, a.theta, s);
+            T.build(n, a.pos, a.mass, theta, s);
         }
     } else {
         T.refit(a.pos, a.mass, s);
     }
-    T.prepare_walk(a.active, s, a.walk_chunk ? a.walk_chunk : walk_chunk);
+    T.prepare_walk(a.active, s, a.walk_chunk ? a.walk_chunk : walk_chunk, rel ? acc_grav.as<double>() : nullptr,
+                   rel ? float(grav_rel) : 0.f);
     T.walk(a.eps, acc_grav.as<double>(), s, nullptr, a.walk_npl);
+    if (!a.active) have_aold = true;  // every particle has a previous gravity now
 
     if (fork) {
         hydro(a, s2);

@@ -1,6 +1,9 @@
 // gf_hydro.cuh — the fused, device-resident force evaluation (simulation.py:61-95).
 #pragma once
 
+#include <cstring>
+#include <initializer_list>
+
 #include "gf_sph.cuh"
 
 namespace gf {
@@ -45,6 +48,14 @@ struct ForceEngine {
     int gravity_quad = 0;    // 1: quadrupole moments + Kahan tile sums, 0: the reference's monopole
     int walk_chunk = 0;      // walk items for active-set walks (0: the reference's groups)
     int walk_group = 64;     // mixed form: walk groups = shallowest nodes with <= this many particles
+    // mixed form: relative opening criterion with this tolerance (0 = the geometric criterion
+    // at the caller's theta). It takes the gravity of the previous evaluation of the same
+    // particle set as the error scale: the first evaluation (and every one before an
+    // evaluation of all particles) uses the geometric criterion; later ones a geometric floor
+    // at theta = kRelFloorTheta combined with the relative test.
+    double grav_rel = 0.0;
+    bool have_aold = false;
+    static constexpr double kRelFloorTheta = 1.0;
     int hguess = 0;          // start of the neighbour-count iteration: 0 previous h, 1 cell
                              // density only, 2 the learned guess (MLP)
     long long collect_cap = 0, collect_n = 0;  // (features, log h) training pairs kept
@@ -68,6 +79,17 @@ struct ForceEngine {
     HydroScalars* scalars_h = nullptr;  // pinned copy, valid after the stream synchronises
 
     void evaluate(const ForceArgs& a, cudaStream_t s);
+    // The options a captured evaluation bakes in: a graph captured under other values is stale.
+    unsigned long long option_key() const {
+        unsigned long long rel_bits;
+        memcpy(&rel_bits, &grav_rel, sizeof rel_bits);
+        unsigned long long k = 1469598103934665603ull;
+        for (unsigned long long v : {(unsigned long long)sph_float32, (unsigned long long)gravity_quad,
+                                     (unsigned long long)walk_chunk, (unsigned long long)walk_group,
+                                     (unsigned long long)hguess, rel_bits, (unsigned long long)have_aold})
+            k = (k ^ v) * 1099511628211ull;
+        return k;
+    }
     // allocates the buffers that only synchronisation-free evaluations touch
     // every buffer a captured (synchronisation-free) evaluation touches, at its final size
     void reserve_nosync(int n) {

@@ -261,6 +261,7 @@ struct BlockIntegrator {
     cudaGraphExec_t exec = nullptr;
     unsigned long long gen = ~0ull;
     int cap_n = -1, cap_nlev = -1;
+    unsigned long long cap_key = 0;  // force-engine options the graph was captured under
     double last_updates = 0;
     int captures = 0;
     BlockTuning tune;
@@ -341,6 +342,7 @@ struct BlockIntegrator {
         gen = g_alloc_generation;
         cap_n = S.n;
         cap_nlev = nlev;
+        cap_key = force_engine().option_key();
         tune_changed = false;
         ++captures;
     }
@@ -365,7 +367,9 @@ struct BlockIntegrator {
         }
         Event e0, e1;
         for (int b = 0; b < nblocks; ++b) {
-            if (!exec || gen != g_alloc_generation || cap_n != S.n || cap_nlev != nlev || tune_changed) capture(S);
+            if (!exec || gen != g_alloc_generation || cap_n != S.n || cap_nlev != nlev || tune_changed ||
+                cap_key != force_engine().option_key())
+                capture(S);
             unsigned long long* d = scal.as<unsigned long long>();
             GF_CUDA(cudaMemsetAsync(d + 1, 0, sizeof(unsigned long long), s));
             e0.record(s);

@@ -503,6 +503,18 @@ __global__ void k_moments(MomentArgs A) {
     }
 }
 
+// Relative opening radius of a quadrupole node: the walk accepts the node for a group sphere
+// (centre c, radius R) when |com - c| - R exceeds rho * (alpha * min |a_old|)^(-1/5), i.e. when
+// the octupole-order estimate M b^3 / r^5 of the truncation error is at most alpha times the
+// group's smallest previous acceleration (the relative criterion of Springel 2005, GADGET-2,
+// to the next order). b bounds the distance of the node's mass from its centre of mass.
+// rho = M^(1/5) b^(3/5) in logarithms, so no intermediate overflows in float32.
+__device__ __forceinline__ float rel_radius(float m, float ox, float oy, float oz, float half) {
+    if (!(m > 0.f)) return 0.f;
+    const float b = sqrtf(ox * ox + oy * oy + oz * oz) + 1.7320508f * half;
+    return exp2f(0.2f * log2f(m) + 0.6f * log2f(b));
+}
+
 // Mixed form: monopole and traceless quadrupole in one bottom-up pass, float32 with
 // Kahan-compensated sums. A leaf sums its particles; the last child to finish a parent
 // (arrival counter) combines the children's masses and centres, then their quadrupoles shifted
@@ -632,9 +644,9 @@ struct RefitBfsArgs {
     const float4* wgeo;
     int* counter;
     float4* wa;   // com, m
-    float4* wb;   // open_r, first, code, Qyz
+    float4* wb;   // open_r, first, code, rho
     float4* wq;   // Qxx, Qyy, Qxy, Qxz
-    float* wt;    // T
+    float2* wt;   // Qyz, T
     float* ndisp; // breadth-first
     const float4* p4;
     const float* pdisp;
@@ -648,6 +660,7 @@ __device__ __forceinline__ float4 finalize_bfs(const RefitBfsArgs& A, int b, con
     const float4 g = A.wgeo[b];
     const float ox = c.x - g.x, oy = c.y - g.y, oz = c.z - g.z;
     A.wb[b].x = 2.f * (g.w + dm) / A.theta + sqrtf(ox * ox + oy * oy + oz * oz);
+    A.wb[b].w = rel_radius(c.w, ox, oy, oz, g.w + dm);
     A.ndisp[b] = dm;
     return c;
 }
@@ -676,8 +689,7 @@ __global__ void k_refit_bfs_quad32(RefitBfsArgs A) {
             S.point(p.w, p.x - c.x, p.y - c.y, p.z - c.z);
         }
         A.wq[b] = make_float4(S.xx.s, S.yy.s, S.xy.s, S.xz.s);
-        A.wb[b].w = S.yz.s;
-        A.wt[b] = S.tr.s;
+        A.wt[b] = make_float2(S.yz.s, S.tr.s);
     }
     __threadfence();
     int p = A.wparent[b];
@@ -714,20 +726,18 @@ __global__ void k_refit_bfs_quad32(RefitBfsArgs A) {
         for (int c = 0; c < 8; ++c) {
             if (c < nc) {
                 const float4 qc = __ldcg(&A.wq[c0 + c]);
-                const float yz = __ldcg(&A.wb[c0 + c]).w;
-                const float tc = __ldcg(&A.wt[c0 + c]);
+                const float2 yt = __ldcg(&A.wt[c0 + c]);
                 S.xx.add(qc.x);
                 S.yy.add(qc.y);
                 S.xy.add(qc.z);
                 S.xz.add(qc.w);
-                S.yz.add(yz);
-                S.tr.add(tc);
+                S.yz.add(yt.x);
+                S.tr.add(yt.y);
                 S.point(cm[c].w, cm[c].x - cp.x, cm[c].y - cp.y, cm[c].z - cp.z);
             }
         }
         A.wq[p] = make_float4(S.xx.s, S.yy.s, S.xy.s, S.xz.s);
-        A.wb[p].w = S.yz.s;
-        A.wt[p] = S.tr.s;
+        A.wt[p] = make_float2(S.yz.s, S.tr.s);
         __threadfence();
         p = A.wparent[p];
     }
@@ -779,7 +789,7 @@ __global__ void k_walk_fill(int nn, const int4* __restrict__ n_i4, const int* __
                             float4* __restrict__ wgeo, int* __restrict__ leaf_of,
                             const float4* __restrict__ q4, const float2* __restrict__ qyz,
                             float4* __restrict__ wq, const int* __restrict__ parent, int* __restrict__ wparent,
-                            float* __restrict__ wt, const int* __restrict__ nn_dev) {
+                            float2* __restrict__ wt, const int* __restrict__ nn_dev) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= live_nodes(nn, nn_dev)) return;
     const int4 q = n_i4[k];
@@ -794,12 +804,18 @@ __global__ void k_walk_fill(int nn, const int4* __restrict__ n_i4, const int* __
         first = bfs[k + 1];
         code = nchild[k];
     }
-    wa[b] = mom[k];
-    wb[b] = make_float4(open_r[k], __int_as_float(first), __int_as_float(code), q4 ? qyz[k].x : 0.f);
+    const float4 c = mom[k];
+    wa[b] = c;
+    float rho = 0.f;
+    if (q4) {
+        const float4 g = geo[k];
+        rho = rel_radius(c.w, c.x - g.x, c.y - g.y, c.z - g.z, g.w);
+    }
+    wb[b] = make_float4(open_r[k], __int_as_float(first), __int_as_float(code), rho);
     if (wgeo) wgeo[b] = geo[k];
     if (q4) {
         wq[b] = q4[k];
-        wt[b] = qyz[k].y;
+        wt[b] = qyz[k];
     }
     if (wparent) wparent[b] = parent[k] < 0 ? -1 : bfs[parent[k]];
 }
@@ -913,6 +929,7 @@ void Octree::reserve_graph_build() {
     pdisp.get<float>(n);
     work.get<int4>(std::max(size_t(node_cap), size_t(n)) + 1);
     sphere.get<float4>(std::max(size_t(node_cap), size_t(n)) + 1);
+    if (quad) item_gam.get<float>(std::max(size_t(node_cap), size_t(n)) + 1);
     reserve_scan_sort(std::max(n, node_cap), &scratch);
     deep_sort_attr();
 }
@@ -1087,7 +1104,7 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
                                            quad ? n_quad.as<float4>() : nullptr, quad ? n_qyz.as<float2>() : nullptr,
                                            quad ? w_q.get<float4>(cap) : nullptr, par,
                                            bfs_geo ? w_parent.get<int>(cap) : nullptr,
-                                           quad ? w_t.get<float>(cap) : nullptr, nn_dev);
+                                           quad ? w_t.get<float2>(cap) : nullptr, nn_dev);
     GF_CHECK_LAUNCH();
     valid = true;
 }
@@ -1109,7 +1126,7 @@ void Octree::refit(const double* pos, const double* mass, cudaStream_t s) {
     GF_CUDA(cudaMemsetAsync(ctr, 0, sizeof(int) * size_t(span), s));
     if (quad) {  // mixed form: straight into the walk layout
         RefitBfsArgs A{span, nn_dev, theta_f, w_parent.as<int>(), w_geo.as<float4>(), ctr, w_a.as<float4>(),
-                       w_b.as<float4>(), w_q.as<float4>(), w_t.as<float>(), n_disp.as<float>(), pp, pd};
+                       w_b.as<float4>(), w_q.as<float4>(), w_t.as<float2>(), n_disp.as<float>(), pp, pd};
         k_refit_bfs_quad32<<<ngrid, kThreads, 0, s>>>(A);
         GF_CHECK_LAUNCH();
         return;
@@ -1141,7 +1158,7 @@ void Octree::refit(const double* pos, const double* mass, cudaStream_t s) {
                                            quad ? n_quad.as<float4>() : nullptr, quad ? n_qyz.as<float2>() : nullptr,
                                            quad ? w_q.as<float4>() : nullptr, n_parent.as<int>(),
                                            want_knn ? w_parent.as<int>() : nullptr,
-                                           quad ? w_t.as<float>() : nullptr, nn_dev);
+                                           quad ? w_t.as<float2>() : nullptr, nn_dev);
     GF_CHECK_LAUNCH();
 }
 

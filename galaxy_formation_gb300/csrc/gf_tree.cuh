@@ -55,12 +55,14 @@ struct Octree {
     DevBuf n_parent, n_nchild, n_counter, n_disp, n_bfs;
     // walk layout, breadth-first order: children of a node are contiguous
     DevBuf w_a;       // float4 {cx, cy, cz, m}
-    DevBuf w_b;       // float4 {open_r, first (int bits), code (int bits), 0};
+    DevBuf w_b;       // float4 {open_r, first (int bits), code (int bits), rho};
                       //   code > 0: internal, `code` children from BFS index `first`;
-                      //   code < 0: leaf, -code particles from tree position `first`
+                      //   code < 0: leaf, -code particles from tree position `first`;
+                      //   rho (quadrupole trees, else 0) = (M b^3)^(1/5), b = |com - cell centre|
+                      //   + sqrt(3) (half + displacement): the relative opening radius
     DevBuf w_geo;     // float4 {gx, gy, gz, half} of the cell, breadth-first order
-    DevBuf w_q;       // float4 {Qxx, Qyy, Qxy, Qxz} (quadrupole trees; Qyz in w_b.w)
-    DevBuf w_t;       // float T = sum m |d|^2 about the centre of mass (quadrupole trees)
+    DevBuf w_q;       // float4 {Qxx, Qyy, Qxy, Qxz} (quadrupole trees)
+    DevBuf w_t;       // float2 {Qyz, T = sum m |d|^2 about the centre of mass} (quadrupole trees)
     DevBuf n_quad, n_qyz;  // traceless quadrupole about the centre of mass, preorder
     DevBuf bfs_key, bfs_key_alt, bfs_val, bfs_val_alt;
     // neighbour search extras (tree order): float32 remainders x - float(x) and the
@@ -73,6 +75,7 @@ struct Octree {
     bool kahan = false;          // walk: compensated accumulation of the tile sums
     // groups and walk work list
     DevBuf gflag, gscan, groups, work, sphere;
+    DevBuf item_gam;  // per work item: (alpha min |a_old|)^(-1/5), 0 = geometric criterion only
     DevBuf root, counts;
     ScanScratch scratch;  // this tree's scan / sort scratch (trees may build on different streams)
     TreeCounts* h_counts = nullptr;  // pinned
@@ -88,7 +91,10 @@ struct Octree {
     void refit(const double* pos, const double* mass, cudaStream_t s);
     // Work list of groups with at least one active particle (active may be null); chunk > 0
     // cuts each group's active particles into items of <= chunk with their own spheres.
-    void prepare_walk(const uint8_t* active, cudaStream_t s, int chunk = 0);
+    // aold (quadrupole trees, may be null): the previous accelerations (n,3) in original order,
+    // for the relative opening criterion with tolerance alpha.
+    void prepare_walk(const uint8_t* active, cudaStream_t s, int chunk = 0, const double* aold = nullptr,
+                      float alpha = 0.f);
     // pot (monopole trees, may be null): softened potentials of the walked particles
     // npl: nodes per lane and round of the mixed walk (2, or 8 for walks of a few items)
     void walk(double eps, double* acc, cudaStream_t s, double* pot = nullptr, int npl = 2);

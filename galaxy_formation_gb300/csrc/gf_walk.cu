@@ -40,10 +40,23 @@ constexpr int kTileCap = 256;     // interaction entries per warp
 //               each with the bounding sphere of its own particles. Sparse active sets
 //               (block time steps) then spread over many warps with tight spheres instead of
 //               one warp walking a whole group for a few particles.
+//   aold != null: per item, gam = (alpha * a_min)^(-1/5) with a_min the smallest previous
+//               |acceleration| among the item's particles (relative opening criterion; 0, i.e.
+//               geometric only, when that minimum is not positive).
+__device__ __forceinline__ float aold_mag(const double* aold, int k) {
+    const double x = aold[3 * size_t(k)], y = aold[3 * size_t(k) + 1], z = aold[3 * size_t(k) + 2];
+    return float(sqrt(x * x + y * y + z * z));
+}
+
+__device__ __forceinline__ float rel_gamma(float alpha, float amin) {
+    return (alpha > 0.f && amin > 0.f && amin < 3e38f) ? exp2f(-0.2f * log2f(alpha * amin)) : 0.f;
+}
+
 __global__ void k_group_prep(const int* __restrict__ groups, const int4* __restrict__ n_i4,
                              const float4* __restrict__ p4, const int* __restrict__ perm,
                              const uint8_t* __restrict__ active, TreeCounts* cnt,
-                             int4* __restrict__ work, float4* __restrict__ sphere, int chunk) {
+                             int4* __restrict__ work, float4* __restrict__ sphere, int chunk,
+                             const double* __restrict__ aold, float alpha, float* __restrict__ gam) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = lanemask_lt();
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -58,6 +71,7 @@ __global__ void k_group_prep(const int* __restrict__ groups, const int4* __restr
             int r0 = 0;
             for (;;) {  // items [r0, r0 + chunk)
                 float x0 = 1e30f, y0 = 1e30f, z0 = 1e30f, x1 = -1e30f, y1 = -1e30f, z1 = -1e30f;
+                float amin = INFINITY;
                 int rank_base = 0, in_item = 0;
                 for (int i0 = b; i0 < e; i0 += 32) {
                     const int i = i0 + lane;
@@ -69,6 +83,7 @@ __global__ void k_group_prep(const int* __restrict__ groups, const int4* __restr
                         x0 = fminf(x0, p.x); x1 = fmaxf(x1, p.x);
                         y0 = fminf(y0, p.y); y1 = fmaxf(y1, p.y);
                         z0 = fminf(z0, p.z); z1 = fmaxf(z1, p.z);
+                        if (aold) amin = fminf(amin, aold_mag(aold, perm[i]));
                         ++in_item;
                     }
                     rank_base += __popc(m);
@@ -94,6 +109,7 @@ __global__ void k_group_prep(const int* __restrict__ groups, const int4* __restr
                     rb += __popc(m);
                 }
                 br2 = warp_max(br2);
+                amin = warp_min(amin);
                 int slot = 0;
                 if (lane == 0) slot = atomicAdd(&cnt->num_work, 1);
                 slot = __shfl_sync(0xffffffffu, slot, 0);
@@ -101,6 +117,7 @@ __global__ void k_group_prep(const int* __restrict__ groups, const int4* __restr
                     work[slot] = make_int4(b, q.y, P, r0);
                     // float32 rounding of the centre: pad so every member stays inside
                     sphere[slot] = make_float4(bx, by, bz, sqrtf(br2) * (1.f + 1e-6f));
+                    if (gam) gam[slot] = aold ? rel_gamma(alpha, amin) : 0.f;
                 }
                 if (P < chunk) break;
                 r0 += chunk;
@@ -109,9 +126,11 @@ __global__ void k_group_prep(const int* __restrict__ groups, const int4* __restr
         }
         int nact = 0;
         float x0 = 1e30f, y0 = 1e30f, z0 = 1e30f, x1 = -1e30f, y1 = -1e30f, z1 = -1e30f;
+        float amin = INFINITY;
         for (int i = b + lane; i < e; i += 32) {
             const bool a = active ? active[perm[i]] != 0 : true;
             nact += __popc(__ballot_sync(__activemask(), a));
+            if (aold && a) amin = fminf(amin, aold_mag(aold, perm[i]));
             const float4 p = p4[i];
             if (p.w > 0) {
                 x0 = fminf(x0, p.x); x1 = fmaxf(x1, p.x);
@@ -134,12 +153,14 @@ __global__ void k_group_prep(const int* __restrict__ groups, const int4* __restr
             }
         }
         br2 = warp_max(br2);
+        amin = warp_min(amin);
         int slot = 0;
         if (lane == 0) slot = atomicAdd(&cnt->num_work, 1);
         slot = __shfl_sync(0xffffffffu, slot, 0);
         if (lane == 0) {
             work[slot] = make_int4(b, q.y, nact, 0);
             sphere[slot] = make_float4(bx, by, bz, sqrtf(br2));
+            if (gam) gam[slot] = aold ? rel_gamma(alpha, amin) : 0.f;
         }
     }
 }
@@ -278,9 +299,9 @@ __device__ __forceinline__ void eval_quad4(const float4* tile, const float4* ntA
 template <bool QUAD, bool POT = false, int NPL = (QUAD ? 2 : 1)>
 __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
     const float4* __restrict__ wa, const float4* __restrict__ wb, const float4* __restrict__ wq,
-    const float* __restrict__ wt, const float4* __restrict__ p4, const int* __restrict__ perm, const uint8_t* __restrict__ active,
-    const int4* __restrict__ work, const float4* __restrict__ sphere, TreeCounts* cnt, int nn, float eps2,
-    double* __restrict__ acc, uint32_t* status, double* __restrict__ pot = nullptr) {
+    const float2* __restrict__ wt, const float4* __restrict__ p4, const int* __restrict__ perm, const uint8_t* __restrict__ active,
+    const int4* __restrict__ work, const float4* __restrict__ sphere, const float* __restrict__ gam, TreeCounts* cnt,
+    int nn, float eps2, double* __restrict__ acc, uint32_t* status, double* __restrict__ pot = nullptr) {
     static_assert(!(QUAD && POT), "potentials come from the monopole walk");
     using Smem = WarpSmem<QUAD, NPL>;
     constexpr int kNodesPerLane = NPL;
@@ -298,6 +319,9 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
         if (g >= nwork) break;
         const int4 w = work[g];
         const float4 sph = sphere[g];
+        // relative criterion: accept a node when its distance from the sphere exceeds both
+        // open_r (geometric) and rho * gm (rho = B.w: 0 outside quadrupole trees)
+        const float gm = QUAD ? gam[g] : 0.f;
         const int b = w.x, count = w.y, Pall = w.z, r0 = w.w;
         // Items hold <= kBatch particles except depth-48 leaves of coincident points; those
         // are evaluated in batches, each batch walking the tree again.
@@ -441,7 +465,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
             const bool valid = node >= 0;
             const float4 A = As[i], B = Bs[i];
             const float dx = A.x - sph.x, dy = A.y - sph.y, dz = A.z - sph.z;
-            const float t = B.x + sph.w;
+            const float t = (QUAD ? fmaxf(B.x, B.w * gm) : B.x) + sph.w;
             const bool accept = valid && (dx * dx + dy * dy + dz * dz > t * t);
             const int first = __float_as_int(B.y), code = __float_as_int(B.z);
             const bool leaf = valid && !accept && code < 0;
@@ -466,7 +490,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
                     const int slot_n = fillN + __popc(am & lt);
                     S.ntA[slot_n] = A;
                     S.ntQ[slot_n] = wq[node];
-                    S.ntYZ[slot_n] = make_float2(B.w, wt[node]);
+                    S.ntYZ[slot_n] = wt[node];
                 }
                 fillN += na;
             } else {
@@ -561,18 +585,20 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
 
 }  // namespace
 
-void Octree::prepare_walk(const uint8_t* active, cudaStream_t s, int chunk) {
+void Octree::prepare_walk(const uint8_t* active, cudaStream_t s, int chunk, const double* aold, float alpha) {
     Context& C = ctx();
     TreeCounts* cnt = counts.as<TreeCounts>();
     GF_CUDA(cudaMemsetAsync(&cnt->num_work, 0, 2 * sizeof(int), s));  // num_work, walk_next
     GF_CUDA(cudaMemsetAsync(&cnt->pairs, 0, 2 * sizeof(unsigned long long), s));  // pairs, qpairs
     ProfScope ps(kStGroupPrep, s);
     // items: one per group (<= nodes), or at most one per active particle with chunks
-    const size_t cap = std::max<size_t>(1, std::max(size_t(node_cap), size_t(n)));
+    const size_t cap = std::max(size_t(node_cap), size_t(n)) + 1;
     active_ptr = active;
     k_group_prep<<<4 * C.sms, 256, 0, s>>>(groups.as<int>(), n_i4.as<int4>(), p4.as<float4>(),
                                           perm.as<int>(), active, cnt, work.get<int4>(cap),
-                                          sphere.get<float4>(cap), active ? chunk : 0);
+                                          sphere.get<float4>(cap), active ? chunk : 0,
+                                          quad && alpha > 0.f ? aold : nullptr, alpha,
+                                          quad ? item_gam.get<float>(cap) : nullptr);
     GF_CHECK_LAUNCH();
 }
 
@@ -592,21 +618,22 @@ void Octree::walk(double eps, double* acc, cudaStream_t s, double* pot, int npl)
         if (quad) throw Error(GF_ERR_ARG, "potentials come from the monopole walk");
         k_walk<false, true><<<bps_mono * C.sms, kWalkWarps * 32, 0, s>>>(
             w_a.as<float4>(), w_b.as<float4>(), nullptr, nullptr, p4.as<float4>(), perm.as<int>(), active_ptr,
-            work.as<int4>(), sphere.as<float4>(), counts.as<TreeCounts>(), node_cap, eps2, acc, C.d_status, pot);
+            work.as<int4>(), sphere.as<float4>(), nullptr, counts.as<TreeCounts>(), node_cap, eps2, acc, C.d_status,
+            pot);
     } else if (quad && npl > 2) {
         k_walk<true, false, 8><<<bps_quad * C.sms, kWalkWarps * 32, 0, s>>>(
-            w_a.as<float4>(), w_b.as<float4>(), w_q.as<float4>(), w_t.as<float>(), p4.as<float4>(), perm.as<int>(),
-            active_ptr,
-            work.as<int4>(), sphere.as<float4>(), counts.as<TreeCounts>(), node_cap, eps2, acc, C.d_status);
+            w_a.as<float4>(), w_b.as<float4>(), w_q.as<float4>(), w_t.as<float2>(), p4.as<float4>(), perm.as<int>(),
+            active_ptr, work.as<int4>(), sphere.as<float4>(), item_gam.as<float>(), counts.as<TreeCounts>(), node_cap,
+            eps2, acc, C.d_status);
     } else if (quad) {
         k_walk<true><<<bps_quad * C.sms, kWalkWarps * 32, 0, s>>>(
-            w_a.as<float4>(), w_b.as<float4>(), w_q.as<float4>(), w_t.as<float>(), p4.as<float4>(), perm.as<int>(),
-            active_ptr,
-            work.as<int4>(), sphere.as<float4>(), counts.as<TreeCounts>(), node_cap, eps2, acc, C.d_status);
+            w_a.as<float4>(), w_b.as<float4>(), w_q.as<float4>(), w_t.as<float2>(), p4.as<float4>(), perm.as<int>(),
+            active_ptr, work.as<int4>(), sphere.as<float4>(), item_gam.as<float>(), counts.as<TreeCounts>(), node_cap,
+            eps2, acc, C.d_status);
     } else {
         k_walk<false><<<bps_mono * C.sms, kWalkWarps * 32, 0, s>>>(
             w_a.as<float4>(), w_b.as<float4>(), nullptr, nullptr, p4.as<float4>(), perm.as<int>(), active_ptr,
-            work.as<int4>(), sphere.as<float4>(), counts.as<TreeCounts>(), node_cap, eps2, acc, C.d_status);
+            work.as<int4>(), sphere.as<float4>(), nullptr, counts.as<TreeCounts>(), node_cap, eps2, acc, C.d_status);
     }
     GF_CHECK_LAUNCH();
 }

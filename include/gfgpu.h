@@ -275,6 +275,17 @@ int gf_sim_read(double* pos, double* vel, double* acc, double* dt_ind, double* t
  *                       reference's kGroupMax of cpp/nbody.cpp:34, which the monopole walk
  *                       always keeps). */
 #define GF_OPT_WALK_GROUP 5
+/*   GF_OPT_GRAVITY_REL  mixed form (GF_OPT_GRAVITY_QUAD = 1): relative opening criterion with
+ *                       tolerance alpha (0 = off, default; e.g. 2.5e-3). A node is accepted
+ *                       for a walk group when its distance from the group's sphere exceeds
+ *                       both the geometric radius at theta = 1 and (M b^3 / (alpha a_min))^(1/5),
+ *                       where M b^3 bounds the node's octupole and a_min is the group's
+ *                       smallest |gravity| of the previous evaluation of the same particle
+ *                       set. Until the gravity of every particle has been evaluated once
+ *                       (the first call, a new particle count, or after setting this option)
+ *                       the geometric criterion at the caller's theta is used. Set the option
+ *                       again before evaluating an unrelated particle set of the same size. */
+#define GF_OPT_GRAVITY_REL 6
 int gf_set_option(int key, double value);
 /* Current value of an option (-1 for an unknown key). */
 double gf_get_option(int key);

@@ -179,3 +179,39 @@ def test_wide_rounds_walk_matches(gpulib):
     assert np.percentile(np.linalg.norm(p8 - p2, axis=1), 99) < 1e-5 * scale
     vs = np.linalg.norm(v2, axis=1).mean()
     assert np.percentile(np.linalg.norm(v8 - v2, axis=1), 99) < 1e-4 * vs
+
+
+def test_blocks_relative_opening(gpulib):
+    """Block time steps with the relative opening criterion (its error scale is every
+    particle's last gravity, kept on the device across the captured sub-steps) stay within
+    the criterion's accuracy of the geometric walk."""
+    from galaxy_formation_gb300 import _lib, params, synthetic
+
+    lib = gpulib
+    _plain(lib)
+    lib.gf_set_option(_lib.OPT_GRAVITY_QUAD, 1)
+    d = synthetic.rotating_cloud(3000, 3000, seed=12)
+    d["kind"][:] = params.DM
+    d["u"][:] = 0.0
+    n = len(d["mass"])
+    out = {}
+    try:
+        for rel in (0.0, 2.5e-3):
+            lib.gf_set_option(_lib.OPT_GRAVITY_REL, rel)
+            ch = np.array([4, 8, 16], np.int32)
+            _lib.check(lib.gf_sim_block_config(ch.ctypes.data, 3, 2))
+            _lib.check(lib.gf_sim_init(n, d["pos"], d["vel"], d["mass"], d["kind"], d["u"], 0.55, params.EPS,
+                                       params.GAMMA, params.ALPHA, params.BETA))
+            upd = ctypes.c_double()
+            _lib.check(lib.gf_sim_blocks(2, 4, ctypes.byref(upd)))
+            out[rel] = _state(lib, n)
+    finally:
+        lib.gf_set_option(_lib.OPT_GRAVITY_REL, 0)
+        lib.gf_set_option(_lib.OPT_GRAVITY_QUAD, 0)
+    (pg, vg, tg), (pr, vr, tr) = out[0.0], out[2.5e-3]
+    assert np.all(np.isfinite(pr)) and np.all(np.isfinite(vr))
+    assert abs(tr - tg) <= 1e-3 * tg
+    moved = np.percentile(np.linalg.norm(pg - d["pos"], axis=1), 99)
+    assert np.percentile(np.linalg.norm(pr - pg, axis=1), 99) < 1e-2 * moved
+    dv = np.percentile(np.linalg.norm(vg - d["vel"], axis=1), 99)
+    assert np.percentile(np.linalg.norm(vr - vg, axis=1), 99) < 2e-2 * dv
