@@ -52,11 +52,12 @@ PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # (theta, quadrupole walk, float32 SPH, h guess mode)
 # theta, quadrupole gravity, float32 SPH, h guess (0 previous h, 2 learned), relative opening
 # tolerance (0: geometric criterion at theta; > 0: the relative criterion once every particle
-# has a previous gravity, with theta used for the first evaluation)
+# has a previous gravity, with theta used for the first evaluation), walk items merged from
+# sibling groups up to this many particles (0: the reference's groups)
 FORMS = {
-    "plain": (0.7, 0, 0, 0, 0.0),
-    "plain_matched": (0.15, 0, 0, 0, 0.0),
-    "mixed_learned": (0.55, 1, 1, 2, 2.5e-3),
+    "plain": (0.7, 0, 0, 0, 0.0, 0),
+    "plain_matched": (0.15, 0, 0, 0, 0.0, 0),
+    "mixed_learned": (0.55, 1, 1, 2, 3e-3, 64),
 }
 # flops per interaction (an FMA counting 2): monopole pair (cpp/nbody.cpp:398-402 in float32)
 # and the softened quadrupole node term of the mixed walk
@@ -260,12 +261,13 @@ class Gpu:
         self.flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=self.dev)  # 256 MB > L2
 
     def set_form(self, form):
-        theta, quad, sph32, hguess, rel = FORMS[form]
+        theta, quad, sph32, hguess, rel, merge = FORMS[form]
         L, lib = self._lib, self.lib
         lib.gf_set_option(L.OPT_GRAVITY_QUAD, quad)
         lib.gf_set_option(L.OPT_SPH_FLOAT32, sph32)
         lib.gf_set_option(L.OPT_HGUESS, hguess)
         lib.gf_set_option(L.OPT_GRAVITY_REL, rel)  # the next evaluation sets the error scale
+        lib.gf_set_option(L.OPT_WALK_MERGE, merge)
         return theta
 
     def step(self, theta, pos=None, kind=None, sph=1):
@@ -535,12 +537,14 @@ def run_gpu(args, world, rank, local):
 
     def summary(f):
         r = res[f]
-        th, quad_f, sph32, hg, rel = FORMS[f]
+        th, quad_f, sph32, hg, rel, merge = FORMS[f]
         out = {"value": r["value"], "ms_per_step": r["ms_per_step"], "theta": th,
                "gravity": "quadrupole float32 + Kahan" if quad_f else "monopole float32 (reference)",
                "opening": (f"relative, alpha {rel:g} with a geometric floor at theta 1 (error scale: the "
                            f"previous evaluation's gravity; theta {th} before it)") if rel else
                           f"geometric, theta {th} (cpp/nbody.cpp:104-106)",
+               "walk_items": (f"runs of sibling groups of <= {merge} particles, own spheres" if merge else
+                              "the reference's groups (cpp/nbody.cpp:235-243)"),
                "sph": "float32 + Kahan" if sph32 else "float64 (reference)",
                "h_guess": ["previous h", "cell density", "learned MLP"][hg],
                "grav_p99_rel_err_vs_f64_direct": r["p99"], "grav_median_rel_err": r["median"],
@@ -557,6 +561,7 @@ def run_gpu(args, world, rank, local):
         "data": "synthetic",
         "config": {"workload": workload_name(n_gas, n - n_gas), "particles": n, "gas": n_gas,
                    "form": head, "theta": FORMS[head][0], "relative_opening_alpha": FORMS[head][4],
+                   "walk_merge": FORMS[head][5],
                    "eps_kpc": params.EPS_KPC,
                    "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
         "roofline": roof,
@@ -688,7 +693,8 @@ def run_drift(args, world, rank, local):
                                     "substeps": blocks * (1 << (nlev - 1)), "updates": upd, "ms": ms,
                                     "simulated_time": q1[7], **drift(q0, q1),
                                     "autotune": {"chunk_per_bin": chunk.tolist(), "rebuild_every": every.value},
-                                    "form": "quadrupole float32 + Kahan walk at theta 0.55, float32 + Kahan SPH, "
+                                    "form": "quadrupole float32 + Kahan walk (relative opening criterion, alpha "
+                                            f"{FORMS['mixed_learned'][4]:g}; merged walk items), float32 + Kahan SPH, "
                                             "learned h guess, block time steps (7 levels) replayed as CUDA graphs"}
     r = out["mixed_batched_learned"]["simulated_time"] / out["mixed_batched_learned"]["ms"]
     r0 = out["plain_step_loop"]["simulated_time"] / out["plain_step_loop"]["ms"]

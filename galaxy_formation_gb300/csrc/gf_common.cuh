@@ -107,6 +107,57 @@ __device__ __forceinline__ int warp_sum(int v) {
     return v;
 }
 
+// One round of a warp's tree walk over a shared-memory stack of child ranges (entry =
+// first << 4 | count, count 1..8, top at sp - 1): takes whole ranges from the top while they fit
+// in 32 * NPL node slots and the head of the next one (the rest of that range stays on the
+// stack). Slot s = lane + 32 i gets node[i] (-1 when empty); returns the number of nodes taken.
+// The node of a slot is found by a binary search over the ranges' inclusive sums (shuffles
+// only, no shared-memory staging), so the slots past the first 32 cost nothing in rounds that
+// fill fewer. The caller synchronises the warp before the stack is read again.
+template <int NPL>
+__device__ __forceinline__ int pop_round(int* stack, int& sp, int (&node)[NPL]) {
+    constexpr int kRound = 32 * NPL;
+    const int lane = threadIdx.x & 31;
+    const int kk = min(sp, 32);
+    int e = 0, c = 0;
+    if (lane < kk) {
+        e = stack[sp - 1 - lane];
+        c = e & 15;
+    }
+    const int incl = warp_incl_scan(c);
+    const int excl = incl - c;
+    const unsigned fullm = __ballot_sync(0xffffffffu, lane < kk && incl <= kRound);
+    const int nfull = __popc(fullm);
+    int nnodes = __shfl_sync(0xffffffffu, incl, kk - 1);
+    if (nfull < kk) {  // range `nfull` is split: its tail stays on the stack
+        nnodes = kRound;
+        if (lane == nfull) {
+            const int take = kRound - excl;
+            stack[sp - 1 - lane] = (((e >> 4) + take) << 4) | (c - take);
+        }
+    }
+    sp -= nfull;
+    const int incl2 = min(incl, kRound);
+    const int first = e >> 4;
+#pragma unroll
+    for (int i = 0; i < NPL; ++i) {
+        node[i] = -1;
+        if (32 * i < nnodes) {  // warp-uniform
+            const int slot = lane + 32 * i;
+            int src = 0;  // ranges ending at or before the slot
+#pragma unroll
+            for (int step = 16; step; step >>= 1) {
+                const int v = __shfl_sync(0xffffffffu, incl2, src + step - 1);
+                if (v <= slot) src += step;
+            }
+            const int f = __shfl_sync(0xffffffffu, first, src);
+            const int x = __shfl_sync(0xffffffffu, excl, src);
+            if (slot < nnodes) node[i] = f + (slot - x);
+        }
+    }
+    return nnodes;
+}
+
 // Kahan-compensated float32 sum.
 struct KahanF {
     float s = 0.f, c = 0.f;

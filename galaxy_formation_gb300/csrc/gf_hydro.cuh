@@ -48,6 +48,8 @@ struct ForceEngine {
     int gravity_quad = 0;    // 1: quadrupole moments + Kahan tile sums, 0: the reference's monopole
     int walk_chunk = 0;      // walk items for active-set walks (0: the reference's groups)
     int walk_group = 64;     // mixed form: walk groups = shallowest nodes with <= this many particles
+    int walk_merge = 0;      // mixed form: walk items = runs of consecutive sibling groups of <= this
+                             // many particles (0: one item per group)
     // mixed form: relative opening criterion with this tolerance (0 = the geometric criterion
     // at the caller's theta). It takes the gravity of the previous evaluation of the same
     // particle set as the error scale: the first evaluation (and every one before an
@@ -86,7 +88,8 @@ struct ForceEngine {
         unsigned long long k = 1469598103934665603ull;
         for (unsigned long long v : {(unsigned long long)sph_float32, (unsigned long long)gravity_quad,
                                      (unsigned long long)walk_chunk, (unsigned long long)walk_group,
-                                     (unsigned long long)hguess, rel_bits, (unsigned long long)have_aold})
+                                     (unsigned long long)hguess, rel_bits, (unsigned long long)have_aold,
+                                     (unsigned long long)walk_merge})
             k = (k ^ v) * 1099511628211ull;
         return k;
     }

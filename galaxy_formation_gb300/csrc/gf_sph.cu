@@ -282,7 +282,6 @@ struct KnnSmem {
     unsigned long long key[kKnnCap];
     unsigned long long dd[64];  // float64 squared distances as bit patterns
     int di[64];
-    int lanemap[kKnnRound];
 };
 
 struct KnnArgs {
@@ -333,37 +332,9 @@ __device__ int knn_collect(const KnnArgs& A, KnnSmem& S, float4 xh, float4 xl, f
     for (int rounds = 0; sp > 0; ++rounds) {
         if (rounds > A.nn) return -1;  // each node is popped at most once
         // pop up to 64 nodes (two per lane: their loads overlap)
-        const int kk = min(sp, 32);
-        int e = 0, c = 0;
-        if (lane < kk) {
-            e = S.stack[sp - 1 - lane];
-            c = e & 15;
-        }
-        const int incl = warp_incl_scan(c);
-        const int excl = incl - c;
-        const unsigned fullm = __ballot_sync(0xffffffffu, lane < kk && incl <= kKnnRound);
-        const int nfull = __popc(fullm);
-        int nnodes = __shfl_sync(0xffffffffu, incl, kk - 1);
-        int take = c;
-        if (nfull < kk) {
-            nnodes = kKnnRound;
-            if (lane == nfull) {
-                take = kKnnRound - excl;
-                S.stack[sp - 1 - lane] = (((e >> 4) + take) << 4) | (c - take);
-            }
-        }
-        __syncwarp();
-        if (lane < kk && lane <= nfull) {
-            const int first = e >> 4;
-            for (int t = 0; t < take && excl + t < kKnnRound; ++t) S.lanemap[excl + t] = first + t;
-        }
-        sp -= nfull;
-        __syncwarp();
         int node[2];
+        const int nnodes = pop_round<2>(S.stack, sp, node);
         float4 G[2], B[2];
-#pragma unroll
-        for (int i = 0; i < 2; ++i) node[i] = lane + 32 * i < nnodes ? S.lanemap[lane + 32 * i] : -1;
-        __syncwarp();
 #pragma unroll
         for (int i = 0; i < 2; ++i) {
             if (node[i] >= 0) {
@@ -374,6 +345,7 @@ __device__ int knn_collect(const KnnArgs& A, KnnSmem& S, float4 xh, float4 xl, f
         int first[2] = {0, 0}, lcs[2] = {0, 0};
 #pragma unroll
         for (int i = 0; i < 2; ++i) {
+            if (32 * i >= nnodes) break;  // warp-uniform
             bool open = false;
             int code = 0;
             if (node[i] >= 0) {

@@ -70,6 +70,8 @@ struct Octree {
     DevBuf plo, leaf_of, w_parent;
     bool want_knn = false;
     int group_max = kGroupMax;   // walk groups: shallowest nodes with <= group_max particles
+    int merge_cap = 0;           // quadrupole trees: walk items = runs of consecutive sibling
+                                 // groups of <= merge_cap particles (0: one item per group)
     int leaf_max = kLeafMax;     // leaf capacity (the reference's 8 for gravity trees)
     bool quad = false;           // also build quadrupole moments (mixed-precision form)
     bool kahan = false;          // walk: compensated accumulation of the tile sums

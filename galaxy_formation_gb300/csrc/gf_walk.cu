@@ -40,6 +40,7 @@ constexpr int kTileCap = 256;     // interaction entries per warp
 //               each with the bounding sphere of its own particles. Sparse active sets
 //               (block time steps) then spread over many warps with tight spheres instead of
 //               one warp walking a whole group for a few particles.
+//   merge  > 0 (chunk == 0): consecutive sibling groups merged into items of <= merge particles;
 //   aold != null: per item, gam = (alpha * a_min)^(-1/5) with a_min the smallest previous
 //               |acceleration| among the item's particles (relative opening criterion; 0, i.e.
 //               geometric only, when that minimum is not positive).
@@ -52,11 +53,60 @@ __device__ __forceinline__ float rel_gamma(float alpha, float amin) {
     return (alpha > 0.f && amin > 0.f && amin < 3e38f) ? exp2f(-0.2f * log2f(alpha * amin)) : 0.f;
 }
 
+// One work item over the particles [b, e) of the tree (a group, or a run of sibling groups):
+// its active count, the bounding sphere of its massive particles and, with aold, its scale of
+// the relative criterion; items without active or massive particles are dropped.
+__device__ __forceinline__ void emit_item(int b, int e, const float4* __restrict__ p4, const int* __restrict__ perm,
+                                          const uint8_t* __restrict__ active, TreeCounts* cnt,
+                                          int4* __restrict__ work, float4* __restrict__ sphere,
+                                          const double* __restrict__ aold, float alpha, float* __restrict__ gam) {
+    const int lane = threadIdx.x & 31;
+    int nact = 0;
+    float x0 = 1e30f, y0 = 1e30f, z0 = 1e30f, x1 = -1e30f, y1 = -1e30f, z1 = -1e30f;
+    float amin = INFINITY;
+    for (int i = b + lane; i < e; i += 32) {
+        const bool a = active ? active[perm[i]] != 0 : true;
+        nact += __popc(__ballot_sync(__activemask(), a));
+        if (aold && a) amin = fminf(amin, aold_mag(aold, perm[i]));
+        const float4 p = p4[i];
+        if (p.w > 0) {
+            x0 = fminf(x0, p.x); x1 = fmaxf(x1, p.x);
+            y0 = fminf(y0, p.y); y1 = fmaxf(y1, p.y);
+            z0 = fminf(z0, p.z); z1 = fmaxf(z1, p.z);
+        }
+    }
+    nact = __shfl_sync(0xffffffffu, nact, 0);
+    if (nact == 0) return;
+    x0 = warp_min(x0); y0 = warp_min(y0); z0 = warp_min(z0);
+    x1 = warp_max(x1); y1 = warp_max(y1); z1 = warp_max(z1);
+    if (x0 > x1) return;  // massless
+    const float bx = 0.5f * (x0 + x1), by = 0.5f * (y0 + y1), bz = 0.5f * (z0 + z1);
+    float br2 = 0.f;
+    for (int i = b + lane; i < e; i += 32) {
+        const float4 p = p4[i];
+        if (p.w > 0) {
+            const float dx = p.x - bx, dy = p.y - by, dz = p.z - bz;
+            br2 = fmaxf(br2, dx * dx + dy * dy + dz * dz);
+        }
+    }
+    br2 = warp_max(br2);
+    amin = warp_min(amin);
+    int slot = 0;
+    if (lane == 0) slot = atomicAdd(&cnt->num_work, 1);
+    slot = __shfl_sync(0xffffffffu, slot, 0);
+    if (lane == 0) {
+        work[slot] = make_int4(b, e - b, nact, 0);
+        sphere[slot] = make_float4(bx, by, bz, sqrtf(br2));
+        if (gam) gam[slot] = aold ? rel_gamma(alpha, amin) : 0.f;
+    }
+}
+
 __global__ void k_group_prep(const int* __restrict__ groups, const int4* __restrict__ n_i4,
                              const float4* __restrict__ p4, const int* __restrict__ perm,
                              const uint8_t* __restrict__ active, TreeCounts* cnt,
                              int4* __restrict__ work, float4* __restrict__ sphere, int chunk,
-                             const double* __restrict__ aold, float alpha, float* __restrict__ gam) {
+                             const double* __restrict__ aold, float alpha, float* __restrict__ gam,
+                             const int* __restrict__ parent, int merge) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = lanemask_lt();
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -124,44 +174,28 @@ __global__ void k_group_prep(const int* __restrict__ groups, const int4* __restr
             }
             continue;
         }
-        int nact = 0;
-        float x0 = 1e30f, y0 = 1e30f, z0 = 1e30f, x1 = -1e30f, y1 = -1e30f, z1 = -1e30f;
-        float amin = INFINITY;
-        for (int i = b + lane; i < e; i += 32) {
-            const bool a = active ? active[perm[i]] != 0 : true;
-            nact += __popc(__ballot_sync(__activemask(), a));
-            if (aold && a) amin = fminf(amin, aold_mag(aold, perm[i]));
-            const float4 p = p4[i];
-            if (p.w > 0) {
-                x0 = fminf(x0, p.x); x1 = fmaxf(x1, p.x);
-                y0 = fminf(y0, p.y); y1 = fmaxf(y1, p.y);
-                z0 = fminf(z0, p.z); z1 = fmaxf(z1, p.z);
+        if (merge > 0) {
+            // mixed form: runs of consecutive sibling groups (contiguous in tree order) of at
+            // most `merge` particles, one item each, started by the first group of its siblings
+            const int par = parent[node];
+            if (g > 0 && parent[groups[g - 1]] == par) continue;
+            int j = g;
+            while (j < ng) {
+                const int4 qj = n_i4[groups[j]];
+                int rc = qj.y;
+                int j2 = j + 1;
+                for (; j2 < ng && parent[groups[j2]] == par; ++j2) {
+                    const int c2 = n_i4[groups[j2]].y;
+                    if (rc + c2 > merge) break;
+                    rc += c2;
+                }
+                emit_item(qj.x, qj.x + rc, p4, perm, active, cnt, work, sphere, aold, alpha, gam);
+                j = j2;
+                if (j >= ng || parent[groups[j]] != par) break;
             }
+            continue;
         }
-        nact = __shfl_sync(0xffffffffu, nact, 0);
-        if (nact == 0) continue;
-        x0 = warp_min(x0); y0 = warp_min(y0); z0 = warp_min(z0);
-        x1 = warp_max(x1); y1 = warp_max(y1); z1 = warp_max(z1);
-        if (x0 > x1) continue;  // massless group
-        const float bx = 0.5f * (x0 + x1), by = 0.5f * (y0 + y1), bz = 0.5f * (z0 + z1);
-        float br2 = 0.f;
-        for (int i = b + lane; i < e; i += 32) {
-            const float4 p = p4[i];
-            if (p.w > 0) {
-                const float dx = p.x - bx, dy = p.y - by, dz = p.z - bz;
-                br2 = fmaxf(br2, dx * dx + dy * dy + dz * dz);
-            }
-        }
-        br2 = warp_max(br2);
-        amin = warp_min(amin);
-        int slot = 0;
-        if (lane == 0) slot = atomicAdd(&cnt->num_work, 1);
-        slot = __shfl_sync(0xffffffffu, slot, 0);
-        if (lane == 0) {
-            work[slot] = make_int4(b, q.y, nact, 0);
-            sphere[slot] = make_float4(bx, by, bz, sqrtf(br2));
-            if (gam) gam[slot] = aold ? rel_gamma(alpha, amin) : 0.f;
-        }
+        emit_item(b, e, p4, perm, active, cnt, work, sphere, aold, alpha, gam);
     }
 }
 
@@ -178,7 +212,7 @@ struct WarpSmem {
     float4 ntA[kNodeTile];   // centre of mass, mass
     float4 ntQ[kNodeTile];   // Qxx, Qyy, Qxy, Qxz
     float2 ntYZ[kNodeTile];  // Qyz, T
-    int lanemap[32 * NPL];
+    int lanemap[QUAD ? 32 * NPL : 1];  // slot -> node of a round (mixed form)
     int slot_pos[kBatch];
 };
 
@@ -267,28 +301,30 @@ __device__ __forceinline__ void eval_tile(const float4* tile, int fill, bool two
     }
 }
 
-// Mixed form: entries ksub, ksub + m, ... of both tiles for the lane's 4 particles (each entry
-// loaded once from shared memory serves the 4); the tile's partial sums go to Kahan totals.
-__device__ __forceinline__ void eval_quad4(const float4* tile, const float4* ntA, const float4* ntQ,
-                                           const float2* ntYZ, int fill, int fillN, int ksub, int m, float eps2,
-                                           const float (&x)[4], const float (&y)[4], const float (&z)[4],
-                                           KahanF (&kx)[4], KahanF (&ky)[4], KahanF (&kz)[4]) {
-    float px[4], py[4], pz[4];
+// Mixed form: entries ksub, ksub + m, ... of both tiles for the lane's PPL (4) particles (each
+// entry loaded once from shared memory serves the PPL); the tile's partial sums go to Kahan
+// totals.
+template <int PPL>
+__device__ __forceinline__ void eval_quad(const float4* tile, const float4* ntA, const float4* ntQ,
+                                          const float2* ntYZ, int fill, int fillN, int ksub, int m, float eps2,
+                                          const float (&x)[4], const float (&y)[4], const float (&z)[4],
+                                          KahanF (&kx)[4], KahanF (&ky)[4], KahanF (&kz)[4]) {
+    float px[PPL], py[PPL], pz[PPL];
 #pragma unroll
-    for (int t = 0; t < 4; ++t) px[t] = py[t] = pz[t] = 0.f;
+    for (int t = 0; t < PPL; ++t) px[t] = py[t] = pz[t] = 0.f;
     for (int j = ksub; j < fill; j += m) {
         const float4 e = tile[j];
 #pragma unroll
-        for (int t = 0; t < 4; ++t) pair_acc(e, x[t], y[t], z[t], eps2, px[t], py[t], pz[t]);
+        for (int t = 0; t < PPL; ++t) pair_acc(e, x[t], y[t], z[t], eps2, px[t], py[t], pz[t]);
     }
     for (int j = ksub; j < fillN; j += m) {
         const float4 e = ntA[j], q = ntQ[j];
         const float2 yt = ntYZ[j];
 #pragma unroll
-        for (int t = 0; t < 4; ++t) quad_acc(e, q, yt, x[t], y[t], z[t], eps2, px[t], py[t], pz[t]);
+        for (int t = 0; t < PPL; ++t) quad_acc(e, q, yt, x[t], y[t], z[t], eps2, px[t], py[t], pz[t]);
     }
 #pragma unroll
-    for (int t = 0; t < 4; ++t) {
+    for (int t = 0; t < PPL; ++t) {
         kx[t].add(px[t]);
         ky[t].add(py[t]);
         kz[t].add(pz[t]);
@@ -296,8 +332,10 @@ __device__ __forceinline__ void eval_quad4(const float4* tile, const float4* ntA
 }
 
 // POT (monopole form only): also the softened potential of every walked particle, into pot.
+// Blocks per SM: shared memory allows 4 of the mixed form's and 6 of the reference form's;
+// 5 keeps the latter free of register spills; the wide-round variant needs more registers.
 template <bool QUAD, bool POT = false, int NPL = (QUAD ? 2 : 1)>
-__global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
+__global__ void __launch_bounds__(kWalkWarps * 32, QUAD ? (NPL > 2 ? 1 : 4) : 5) k_walk(
     const float4* __restrict__ wa, const float4* __restrict__ wb, const float4* __restrict__ wq,
     const float2* __restrict__ wt, const float4* __restrict__ p4, const int* __restrict__ perm, const uint8_t* __restrict__ active,
     const int4* __restrict__ work, const float4* __restrict__ sphere, const float* __restrict__ gam, TreeCounts* cnt,
@@ -346,19 +384,21 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
         //   QUAD (mixed form): every lane holds 4 particles, so each entry read from shared
         //     memory serves 4 interactions; L = ceil(P / 4) lanes cover the batch and
         //     m = 32 / L groups of L lanes split the entries (the 4-particle slots of lane
-        //     q hold particles 4q .. 4q + 3).
+        //     q hold particles 4q .. 4q + 3). (A second evaluation loop with 3 per lane, for
+        //     batches that leave lanes idle, slowed every batch by ~10 %: it is not kept.)
         constexpr int kPpl = QUAD ? 4 : 2;
-        int r = 1, sub = 0, m = 1, ksub = 0;
+        constexpr int ppl = kPpl;
+        int r = 1, sub = 0, m = 1, ksub = 0, L = 1;
         bool lane_on = true;
         int slot[kPpl];
         if (QUAD) {
-            const int L = (P + 3) >> 2;
+            L = (P + ppl - 1) / ppl;
             m = max(1, 32 / L);
             ksub = lane / L;
             lane_on = ksub < m;
             const int q = lane - ksub * L;
 #pragma unroll
-            for (int t = 0; t < kPpl; ++t) slot[t] = 4 * q + t;
+            for (int t = 0; t < kPpl; ++t) slot[t] = t < ppl ? ppl * q + t : P;  // P: no particle
         } else {
             if (P <= 16) r = P <= 1 ? 32 : P <= 2 ? 16 : P <= 4 ? 8 : P <= 8 ? 4 : 2;
             slot[0] = lane / r;
@@ -392,8 +432,8 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
         nodelen += fillN;                                                                            \
         __syncwarp();                                                                                \
         if constexpr (QUAD) {                                                                        \
-            if (lane_on) eval_quad4(S.tile, S.ntA, S.ntQ, S.ntYZ, fill, fillN, ksub, m, eps2, x, y, z, \
-                                    kx, ky, kz);                                                     \
+            if (lane_on) eval_quad<4>(S.tile, S.ntA, S.ntQ, S.ntYZ, fill, fillN, ksub, m, eps2, x, y, z, \
+                                      kx, ky, kz);                                                   \
         } else {                                                                                     \
             eval_tile<POT>(S.tile, fill, two, r, sub, eps2, x[0], y[0], z[0], x[1], y[1], z[1],      \
                            ax[0], ay[0], az[0], ax[1], ay[1], az[1], ph[0], ph[1]);                  \
@@ -415,40 +455,45 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
             }
             // pop up to kRound nodes from the top ranges (kNodesPerLane per lane: their loads
             // are issued together, so one round's memory latency covers them all)
-            const int k = min(sp, 32);
-            int e = 0, c = 0;
-            if (lane < k) {
-                e = S.stack[sp - 1 - lane];
-                c = e & 15;
-            }
-            const int incl = warp_incl_scan(c);
-            const int excl = incl - c;
-            const unsigned fullm = __ballot_sync(0xffffffffu, lane < k && incl <= kRound);
-            const int nfull = __popc(fullm);
-            int nnodes = __shfl_sync(0xffffffffu, incl, k - 1);
-            int take = c;
-            if (nfull < k) {  // range `nfull` is split: the rest stays on the stack
-                nnodes = kRound;
-                if (lane == nfull) {
-                    take = kRound - excl;
-                    S.stack[sp - 1 - lane] = (((e >> 4) + take) << 4) | (c - take);
-                }
-            }
-            __syncwarp();
-            if (lane < k && lane <= nfull) {
-                const int first = e >> 4;
-                for (int t = 0; t < take && excl + t < kRound; ++t) S.lanemap[excl + t] = first + t;
-            }
-            sp -= nfull;
-            __syncwarp();
             int nodes[kNodesPerLane];
-            float4 As[kNodesPerLane], Bs[kNodesPerLane];
+            int nnodes;
+            if constexpr (!QUAD) {
+                nnodes = pop_round<kNodesPerLane>(S.stack, sp, nodes);
+            } else {  // the slots' nodes staged in shared memory (shorter round latency)
+                const int k = min(sp, 32);
+                int e = 0, c = 0;
+                if (lane < k) {
+                    e = S.stack[sp - 1 - lane];
+                    c = e & 15;
+                }
+                const int incl = warp_incl_scan(c);
+                const int excl = incl - c;
+                const unsigned fullm = __ballot_sync(0xffffffffu, lane < k && incl <= kRound);
+                const int nfull = __popc(fullm);
+                nnodes = __shfl_sync(0xffffffffu, incl, k - 1);
+                int take = c;
+                if (nfull < k) {  // range `nfull` is split: the rest stays on the stack
+                    nnodes = kRound;
+                    if (lane == nfull) {
+                        take = kRound - excl;
+                        S.stack[sp - 1 - lane] = (((e >> 4) + take) << 4) | (c - take);
+                    }
+                }
+                __syncwarp();
+                if (lane < k && lane <= nfull) {
+                    const int first = e >> 4;
+                    for (int t = 0; t < take && excl + t < kRound; ++t) S.lanemap[excl + t] = first + t;
+                }
+                sp -= nfull;
+                __syncwarp();
 #pragma unroll
-            for (int i = 0; i < kNodesPerLane; ++i) {
-                const int slot = lane + 32 * i;
-                nodes[i] = slot < nnodes ? S.lanemap[slot] : -1;
+                for (int i = 0; i < kNodesPerLane; ++i) {
+                    const int slot = lane + 32 * i;
+                    nodes[i] = slot < nnodes ? S.lanemap[slot] : -1;
+                }
+                __syncwarp();
             }
-            __syncwarp();
+            float4 As[kNodesPerLane], Bs[kNodesPerLane];
 #pragma unroll
             for (int i = 0; i < kNodesPerLane; ++i) {
                 As[i] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -507,9 +552,20 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
             for (int done = 0; done < ltot;) {
                 if (fill == Smem::kTile) GF_WALK_FLUSH();
                 const int chunk = min(Smem::kTile - fill, ltot - done);
-                if (leaf) {
-                    const int a0 = max(lexcl, done), a1 = min(lexcl + lc, done + chunk);
-                    for (int q = a0; q < a1; ++q) S.tile[fill + q - done] = p4[first + q - lexcl];
+                // warp-cooperative copy: entry o of the concatenated leaves goes to lane o % 32,
+                // which finds its leaf by a binary search over the inclusive sums (32 loads in
+                // flight at once instead of each leaf's particles one after another)
+                for (int base = 0; base < chunk; base += 32) {
+                    const int o = done + base + lane;
+                    int src = 0;
+#pragma unroll
+                    for (int step = 16; step; step >>= 1) {
+                        const int v = __shfl_sync(0xffffffffu, lincl, src + step - 1);
+                        if (v <= o) src += step;
+                    }
+                    const int f = __shfl_sync(0xffffffffu, first, src);
+                    const int x = __shfl_sync(0xffffffffu, lexcl, src);
+                    if (base + lane < chunk) S.tile[fill + base + lane] = p4[f + (o - x)];
                 }
                 fill += chunk;
                 done += chunk;
@@ -530,22 +586,23 @@ __global__ void __launch_bounds__(kWalkWarps * 32) k_walk(
         }
         if constexpr (QUAD) {
             // sum the m entry groups of every particle in a fixed order (the tile is free now)
-            float* red = reinterpret_cast<float*>(S.tile);
-            const int L = (P + 3) >> 2;
+            float* red = reinterpret_cast<float*>(S.tile);  // m groups x ppl L slots x 3 <= 384 floats
             if (lane_on) {
 #pragma unroll
                 for (int t = 0; t < kPpl; ++t) {
-                    float* o = red + 3 * (ksub * 4 * L + slot[t]);
-                    o[0] = kx[t].s;
-                    o[1] = ky[t].s;
-                    o[2] = kz[t].s;
+                    if (t < ppl) {
+                        float* o = red + 3 * (ksub * ppl * L + slot[t]);
+                        o[0] = kx[t].s;
+                        o[1] = ky[t].s;
+                        o[2] = kz[t].s;
+                    }
                 }
             }
             __syncwarp();
             for (int p = lane; p < P; p += 32) {
                 float sx = 0.f, sy = 0.f, sz = 0.f;
                 for (int kk = 0; kk < m; ++kk) {
-                    const float* o = red + 3 * (kk * 4 * L + p);
+                    const float* o = red + 3 * (kk * ppl * L + p);
                     sx += o[0];
                     sy += o[1];
                     sz += o[2];
@@ -598,7 +655,8 @@ void Octree::prepare_walk(const uint8_t* active, cudaStream_t s, int chunk, cons
                                           perm.as<int>(), active, cnt, work.get<int4>(cap),
                                           sphere.get<float4>(cap), active ? chunk : 0,
                                           quad && alpha > 0.f ? aold : nullptr, alpha,
-                                          quad ? item_gam.get<float>(cap) : nullptr);
+                                          quad ? item_gam.get<float>(cap) : nullptr, n_parent.as<int>(),
+                                          quad && !(active && chunk > 0) ? merge_cap : 0);
     GF_CHECK_LAUNCH();
 }
 

@@ -286,6 +286,11 @@ int gf_sim_read(double* pos, double* vel, double* acc, double* dt_ind, double* t
  *                       the geometric criterion at the caller's theta is used. Set the option
  *                       again before evaluating an unrelated particle set of the same size. */
 #define GF_OPT_GRAVITY_REL 6
+/*   GF_OPT_WALK_MERGE   mixed form: walk items are runs of consecutive sibling walk groups
+ *                       (contiguous in tree order) holding <= this many particles, 0..128
+ *                       (0 = one item per group, default). Each item has the bounding sphere
+ *                       of its own particles and is walked once: fewer, larger walks. */
+#define GF_OPT_WALK_MERGE 7
 int gf_set_option(int key, double value);
 /* Current value of an option (-1 for an unknown key). */
 double gf_get_option(int key);

@@ -184,3 +184,38 @@ def test_relative_opening_active_subset(gpulib):
     on = act != 0
     assert np.array_equal(acc2[~on], acc[~on])
     assert np.percentile(rel_err(acc2[on], a_ref[on]), 99) < 2e-3
+
+
+def test_merged_walk_items(gpulib):
+    """GF_OPT_WALK_MERGE: runs of sibling groups walked as one item (up to 64 and up to 128
+    particles, the largest batch of one walk) keep the accuracy of the group walk against the
+    float64 direct sum."""
+    from galaxy_formation_gb300 import _lib, params, synthetic
+    from galaxy_formation_gb300.engine import Engine
+
+    lib = gpulib
+    d = synthetic.make_config(2, scale=0.05)
+    n = len(d["mass"])
+    tgt = np.random.default_rng(5).choice(n, 1000, replace=False)
+    exact = Engine().gravity_direct_targets(d["pos"], d["mass"], tgt, params.EPS)
+    dt = np.empty(n)
+    lib.gf_set_option(_lib.OPT_GRAVITY_QUAD, 1)
+    lib.gf_set_option(_lib.OPT_GRAVITY_REL, 3e-3)
+    errs = {}
+    try:
+        for merge in (0, 64, 128):
+            lib.gf_set_option(_lib.OPT_WALK_MERGE, merge)
+            acc = np.empty((n, 3))
+            for _ in range(2):
+                _lib.check(lib.gf_accelerations(n, d["pos"], d["vel"], d["mass"], d["kind"], d["u"], 0.55,
+                                                params.EPS, params.GAMMA, 1.0, 2.0, None, 1, 0, 1, acc, dt))
+            e = rel_err(acc[tgt], exact)
+            errs[merge] = (np.percentile(e, 99), e.max())
+    finally:
+        lib.gf_set_option(_lib.OPT_WALK_MERGE, 0)
+        lib.gf_set_option(_lib.OPT_GRAVITY_REL, 0)
+        lib.gf_set_option(_lib.OPT_GRAVITY_QUAD, 0)
+    # larger items have larger spheres: each particle's criterion only gets stricter
+    for merge in (64, 128):
+        assert errs[merge][0] < 1e-3 and errs[merge][0] <= 1.1 * errs[0][0], errs
+        assert errs[merge][1] < 5e-3, errs
