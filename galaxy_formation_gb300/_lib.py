@@ -57,6 +57,10 @@ SIGNATURES = {
     "gf_sim_step": ([_cd, ctypes.POINTER(_cd), ctypes.POINTER(_ci)], _ci),
     "gf_sim_read": ([_vp, _vp, _vp, _vp, ctypes.POINTER(_cd)], _ci),
     "gf_sim_diagnostics": ([_cd, _dbl], _ci),
+    "gf_sim_read_u": ([_dbl], _ci),
+    "gf_sim_thermo": ([_ci, _vp], _ci),
+    "gf_cooling_function": ([_ci, _dbl, _dbl], _ci),
+    "gf_cool": ([_ci, _dbl, _dbl, _dbl, _dbl, _vp, _cd, _dbl, _dbl], _ci),
     "gf_sim_blocks": ([_ci, _ci, ctypes.POINTER(_cd)], _ci),
     "gf_sim_updates": ([], _cd),
     "gf_sim_block_config": ([_vp, _ci, _ci], _ci),

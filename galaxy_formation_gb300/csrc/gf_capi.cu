@@ -4,11 +4,13 @@
 // via galaxy_formation/engine.py; galaxy_formation/sph.py): they copy inputs to the GPU,
 // run the kernels on the library stream, copy results back and synchronise. `_dev` entry
 // points take device pointers and only enqueue work.
+#include <cmath>
 #include <cstring>
 #include <vector>
 
 #include "gf_hydro.cuh"
 #include "gf_mlp.cuh"
+#include "gf_thermo.cuh"
 
 namespace gf {
 namespace {
@@ -658,6 +660,55 @@ int gf_sim_diagnostics(double theta, double* out) {
 
 int gf_sim_read(double* pos, double* vel, double* acc, double* dt_ind, double* t) {
     return guarded([&] { sim_read(pos, vel, acc, dt_ind, t); });
+}
+
+int gf_sim_read_u(double* u) {
+    return guarded([&] {
+        require(u != nullptr, "null array");
+        require(simulation_ready(), "no simulation (gf_sim_init)");
+        sim_read_u(u);
+    });
+}
+
+int gf_sim_thermo(int mode, const double* units) {
+    return guarded([&] {
+        require(mode >= 0 && mode <= 2, "thermal mode is 0, 1 or 2");
+        require(mode == 0 || units != nullptr, "null units");
+        if (mode) {
+            for (int i = 0; i < 8; ++i) require(std::isfinite(units[i]) && units[i] > 0, "units must be positive");
+        }
+        sim_thermo(mode, units);
+    });
+}
+
+int gf_cooling_function(int n, const double* T, double* lam) {
+    return guarded([&] {
+        require(n >= 0 && (n == 0 || (T && lam)), "bad arguments");
+        cudaStream_t s = ctx().stream;
+        const double* d_T = upload(g_st.r, T, size_t(n), s);
+        double* d_l = g_st.w.get<double>(size_t(n));
+        cooling_function(n, d_T, d_l, s);
+        download(lam, d_l, size_t(n), s);
+        collect_status(s);
+    });
+}
+
+int gf_cool(int n, const double* u, const double* T, const double* rho, const double* dt, const uint8_t* blocked,
+            double u_floor, const double* units, double* out) {
+    return guarded([&] {
+        require(n >= 0 && (n == 0 || (u && T && rho && dt && out)) && units, "bad arguments");
+        cudaStream_t s = ctx().stream;
+        const ThermoUnits U{units[0], units[1], units[2], units[3], units[4], units[5], units[6], units[7]};
+        const double* d_u = upload(g_st.u, u, size_t(n), s);
+        const double* d_T = upload(g_st.r, T, size_t(n), s);
+        const double* d_rho = upload(g_st.rho, rho, size_t(n), s);
+        const double* d_dt = upload(g_st.dt, dt, size_t(n), s);
+        const uint8_t* d_b = blocked ? upload(g_st.flags, blocked, size_t(n), s) : nullptr;
+        double* d_o = g_st.w.get<double>(size_t(n));
+        cool(n, d_u, d_T, d_rho, d_dt, d_b, u_floor, U, d_o, s);
+        download(out, d_o, size_t(n), s);
+        collect_status(s);
+    });
 }
 
 int gf_mlp_tensor_cores(void) { return mlp().tensor_cores; }

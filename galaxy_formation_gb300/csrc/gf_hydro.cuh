@@ -118,6 +118,10 @@ void block_config(const int* chunk, int nbins, int rebuild_every);
 void block_autotune(int nlev, int* chunk, int* rebuild_every, double* graph_ms);
 double sim_updates();
 void sim_read(double* pos, double* vel, double* acc, double* dt_ind, double* t);
+void sim_read_u(double* u);
+// thermal update of the step loop: mode 0 off, 1 heating/compression, 2 also cooling;
+// units: the 8 constants of ThermoUnits (gf_thermo.cuh), in its order
+void sim_thermo(int mode, const double* units);
 void sim_diagnostics(double theta, double* out);
 // Block time steps (the batched form): advances nblocks blocks of 2^(nlev-1) sub-steps;
 // returns the particle-updates done.

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "gf_hydro.cuh"
+#include "gf_thermo.cuh"
 
 namespace gf {
 
@@ -80,8 +81,21 @@ struct Simulation {
     double updates = 0;  // particle-updates of the last step (forces computed)
     DevBuf pos, vel, acc, mass, kind, u, dt_ind, fast, slow, keys, keys_alt, vals, vals_alt, scal;
     unsigned long long* h_scal = nullptr;
+    // thermal update at the start of every (sub-)step (simulation.py:97-104): 0 off, 1 the
+    // compression / shock-heating update of u, 2 also radiative cooling (cooling.py)
+    int thermo_mode = 0;
+    ThermoUnits thermo_units{};
 
     cudaStream_t s() const { return ctx().stream; }
+
+    // _thermodynamics(dt): on the gas of the last SPH evaluation, with its du/dt and density
+    void thermo(double dt) {
+        if (!thermo_mode) return;
+        ForceEngine& F = force_engine();
+        if (F.ng_valid <= 0) return;  // rho_gas.size == 0 (simulation.py:99)
+        thermo_gas(F.ng_valid, F.gidx.as<int>(), F.rho.as<double>(), F.dudt.as<double>(), u.as<double>(), dt,
+                   thermo_mode, thermo_units, s());
+    }
 
     void accelerations(const uint8_t* active, int rebuild, int sph, int fresh) {
         if (active) {  // particles receiving new forces: the active ones, plus the gas under SPH
@@ -151,6 +165,7 @@ struct Simulation {
         const double D = std::min(dt_max, percentile(10.0));
         last_substeps = 0;
         if (D <= 1.5 * dt_min) {  // global step (simulation.py:118-127)
+            thermo(dt_min);
             kick(nullptr, 0.5 * dt_min);
             drift(dt_min);
             accelerations(nullptr, 1, 1, 1);
@@ -168,6 +183,7 @@ struct Simulation {
         bool first = true;
         while (tau < D * (1 - 1e-9)) {
             const double dt = std::min(masked_min(f), D - tau);
+            thermo(dt);
             kick(f, 0.5 * dt);
             drift(dt);
             accelerations(f, 0, 1, first ? 1 : 0);
@@ -284,6 +300,18 @@ struct BlockIntegrator {
         GF_CHECK_LAUNCH();
     }
 
+    // thermal update of the gas due at sub-step `sub` (every gas particle at sub = nsub)
+    void thermo_at(Simulation& S, int sub) {
+        ForceEngine& F = force_engine();
+        if (!S.thermo_mode || F.ng_valid <= 0) return;
+        thermo_gas_levels(F.ng_valid, F.gidx.as<int>(), level.as<int8_t>(), sub, scal.as<unsigned long long>(),
+                          F.rho.as<double>(), F.dudt.as<double>(), S.u.as<double>(), S.thermo_mode, S.thermo_units,
+                          S.s());
+    }
+    unsigned long long capture_key(const Simulation& S) const {
+        return force_engine().option_key() * 31u + unsigned(S.thermo_mode);
+    }
+
     // nosync: inside the captured graph (rebuild = captured tree rebuild, else refit);
     // otherwise a regular evaluation of everybody on a rebuilt tree with fresh neighbours
     void force(Simulation& S, const uint8_t* active, bool nosync, bool rebuild = false, int chunk = 0, int npl = 2) {
@@ -318,6 +346,7 @@ struct BlockIntegrator {
                 k_active_at<<<div_up(S.n, 256), 256, 0, s>>>(S.n, level.as<int8_t>(), sub, ac, d + 1);
                 GF_CHECK_LAUNCH();
                 const bool rb = tune.rebuild_every > 0 && sub % tune.rebuild_every == 0;
+                thermo_at(S, sub);
                 force(S, ac, true, rb, tune.chunk[bin_of(sub)], tune.npl[bin_of(sub)]);
                 k_kick_levels<<<div_up(S.n, 256), 256, 0, s>>>(S.n, S.vel.as<double>(), S.acc.as<double>(),
                                                                level.as<int8_t>(), d, 1, sub);
@@ -342,7 +371,7 @@ struct BlockIntegrator {
         gen = g_alloc_generation;
         cap_n = S.n;
         cap_nlev = nlev;
-        cap_key = force_engine().option_key();
+        cap_key = capture_key(S);
         tune_changed = false;
         ++captures;
     }
@@ -368,7 +397,7 @@ struct BlockIntegrator {
         Event e0, e1;
         for (int b = 0; b < nblocks; ++b) {
             if (!exec || gen != g_alloc_generation || cap_n != S.n || cap_nlev != nlev || tune_changed ||
-                cap_key != force_engine().option_key())
+                cap_key != capture_key(S))
                 capture(S);
             unsigned long long* d = scal.as<unsigned long long>();
             GF_CUDA(cudaMemsetAsync(d + 1, 0, sizeof(unsigned long long), s));
@@ -376,6 +405,7 @@ struct BlockIntegrator {
             GF_CUDA(cudaGraphLaunch(exec, s));
             e1.record(s);
             GF_CUDA(cudaMemcpyAsync(h_cnt, d, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+            thermo_at(S, nsub());      // every gas particle is due at the block end
             force(S, nullptr, false);  // block end: synchronised, rebuilt tree, fresh neighbours
             GF_CUDA(cudaStreamSynchronize(s));
             last_graph_ms = e1.since(e0);
@@ -654,6 +684,22 @@ void sim_diagnostics(double theta, double* out) {
     out[5] = q[4];
     out[6] = q[5];
     out[7] = S.t;
+}
+
+void sim_thermo(int mode, const double* units) {
+    Simulation& S = g_sim;
+    S.thermo_mode = mode;
+    if (mode) {
+        ThermoUnits& U = S.thermo_units;
+        U = ThermoUnits{units[0], units[1], units[2], units[3], units[4], units[5], units[6], units[7]};
+    }
+}
+
+void sim_read_u(double* u) {
+    Simulation& S = g_sim;
+    cudaStream_t s = ctx().stream;
+    GF_CUDA(cudaMemcpyAsync(u, S.u.p, sizeof(double) * size_t(S.n), cudaMemcpyDeviceToHost, s));
+    GF_CUDA(cudaStreamSynchronize(s));
 }
 
 void sim_read(double* pos, double* vel, double* acc, double* dt_ind, double* t) {

@@ -20,6 +20,7 @@ KPC_CM = 3.086e21
 YR_S = 3.156e7
 RHO_CGS = MSUN * MSUN_G / (KPC * KPC_CM) ** 3
 U_CGS = (KMS * 1e5) ** 2
+SEC_PER_MYR = 1e6 * YR_S
 X_H = 0.76
 MU_IONISED = 0.6
 
@@ -35,3 +36,8 @@ N_CANDIDATES = 48
 ALPHA, BETA = 1.0, 2.0
 GAMMA = 5.0 / 3.0
 U_PER_K = K_B / ((GAMMA - 1) * MU_IONISED * M_H) / U_CGS
+T_FLOOR = 1e4                            # cooling.py:21
+U_FLOOR = T_FLOOR * U_PER_K              # simulation.py:42
+
+# constants of the thermal update of the step loop, in the order gf_sim_thermo takes them
+THERMO_UNITS = (U_PER_K, U_FLOOR, RHO_CGS, X_H, M_H, MYR, SEC_PER_MYR, U_CGS)

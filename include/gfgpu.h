@@ -243,6 +243,26 @@ int gf_sim_diagnostics(double theta, double* out);
 /* Copies the state out (host pointers; any may be NULL): pos, vel, acc (n,3), dt_ind (n),
  * and the simulated time t. */
 int gf_sim_read(double* pos, double* vel, double* acc, double* dt_ind, double* t);
+/* Copies the specific internal energies u (n) of the simulation state out. */
+int gf_sim_read_u(double* u);
+/* Thermal update at the start of every step and sub-step of gf_sim_step, as
+ * GalaxyFormation._thermodynamics (simulation.py:97-104) on the gas of the last SPH
+ * evaluation: mode 0 = off (default), 1 = u += dt du/dt floored at u_floor (compression and
+ * shock heating), 2 = 1 then radiative cooling of a primordial gas (cooling.py:34-43). No
+ * particle is blocked from cooling (supernova bubbles belong to star formation, which this
+ * library does not run). gf_sim_blocks applies the same update to each gas particle over its
+ * own step, at the sub-steps where it is due, before its evaluation there.
+ * units (mode > 0): 8 positive constants in this order: u_per_K, u_floor, RHO_CGS, X_H,
+ * M_H, MYR, SEC_PER_MYR, U_CGS (galaxy_formation/units.py, simulation.py:40-42). */
+int gf_sim_thermo(int mode, const double* units);
+/* cooling.py:24-31 (host pointers): lam[i] = Lambda(T[i]) in erg cm^3 / s, 0 at or below
+ * 1e4 K. */
+int gf_cooling_function(int n, const double* T, double* lam);
+/* cooling.py:34-43 elementwise (host pointers), with a step dt[i] per particle and blocked
+ * (may be NULL) as the reference's bubble mask; units as for gf_sim_thermo (the first two are
+ * not used: u_floor is passed explicitly). */
+int gf_cool(int n, const double* u, const double* T, const double* rho, const double* dt,
+            const uint8_t* blocked, double u_floor, const double* units, double* out);
 
 /* Options of the fused force evaluation (no reference counterpart):
  *   GF_OPT_SPH_FLOAT32  0 = float64 SPH arithmetic (the reference's, default);

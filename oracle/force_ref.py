@@ -14,6 +14,7 @@ Used as the checker of the fused GPU force evaluation and as the timed CPU basel
 import numpy as np
 from scipy.spatial import cKDTree
 
+import cooling_ref
 import oracle
 
 GAS = 0
@@ -58,6 +59,7 @@ class ForceOracle:
         self.acc_sph[:] = 0.0
         self.dt_courant[:] = np.inf
         self.dt_gas = np.inf
+        self.rho = np.zeros(0)  # simulation.py:78
         g = np.flatnonzero(kind == GAS)
         self.n_gas = g.size
         if g.size <= 40:
@@ -72,7 +74,7 @@ class ForceOracle:
         self.acc_sph[g] = a
         self.dt_courant[g] = dt_i
         self.dt_gas = dt_i.min()
-        self.h, self.rho, self.dudt, self.nb = h, rho, dudt, nb
+        self.h, self.rho, self.dudt, self.nb, self.gas_idx = h, rho, dudt, nb, g
 
     def accelerations(self, pos, vel, mass, kind, u, active=None, rebuild=True, sph=True,
                       fresh_nb=True):
@@ -88,16 +90,30 @@ class ForceOracle:
 
 class StepOracle:
     """GalaxyFormation.step (galaxy_formation/simulation.py:114-149) restated on ForceOracle,
-    without the sub-grid physics hooks (_thermodynamics, _stars) that sit outside the force
-    path. State: pos, vel, mass, kind, u (float64, updated in place)."""
+    without star formation (_stars). thermo = 0 also leaves out _thermodynamics; 1 applies its
+    compression / shock-heating update, 2 also cooling (oracle/cooling_ref.py), with
+    thermo_units = (u_per_K, u_floor, RHO_CGS, X_H, M_H, MYR, SEC_PER_MYR, U_CGS).
+    State: pos, vel, mass, kind, u (float64; u is copied)."""
 
-    def __init__(self, pos, vel, mass, kind, u, theta, eps, **kw):
+    def __init__(self, pos, vel, mass, kind, u, theta, eps, thermo=0, thermo_units=None, **kw):
         self.pos, self.vel = pos.copy(), vel.copy()
-        self.mass, self.kind, self.u = mass, kind, u
+        self.mass, self.kind, self.u = mass, kind, u.copy()
         self.eps = eps
+        self.thermo = thermo
+        if thermo:
+            u_per_K, u_floor, rho_cgs, x_h, m_h, myr, sec_per_myr, u_cgs = thermo_units
+            self.u_per_K, self.u_floor = u_per_K, u_floor
+            self.units = {"RHO_CGS": rho_cgs, "X_H": x_h, "M_H": m_h, "MYR": myr,
+                          "SEC_PER_MYR": sec_per_myr, "U_CGS": u_cgs}
         self.f = ForceOracle(len(mass), theta, eps, **kw)
         self.t = 0.0
         self.acc = self.accelerations()
+
+    def _thermodynamics(self, dt):
+        """simulation.py:97-104 on the gas of the last SPH evaluation."""
+        if self.thermo:
+            cooling_ref.thermodynamics(self.u, self.f.gas_idx, self.f.dudt, self.f.rho, dt, self.u_per_K,
+                                       self.u_floor, self.units, self.thermo)
 
     def accelerations(self, active=None, rebuild=True, sph=True, fresh_nb=True):
         acc = self.f.accelerations(self.pos, self.vel, self.mass, self.kind, self.u, active, rebuild,
@@ -111,6 +127,7 @@ class StepOracle:
         D = min(dt_max, np.percentile(self.dt_ind, 10))
         self.substeps = 0
         if D <= 1.5 * dt_min:
+            self._thermodynamics(dt_min)
             self.vel += 0.5 * dt_min * self.acc
             self.pos += dt_min * self.vel
             self.acc = self.accelerations()
@@ -125,6 +142,7 @@ class StepOracle:
         first = True
         while tau < D * (1 - 1e-9):
             dt = min(self.dt_ind[fast].min(), D - tau)
+            self._thermodynamics(dt)
             self.vel[fast] += 0.5 * dt * self.acc[fast]
             self.pos += dt * self.vel
             self.acc = self.accelerations(active=fast, rebuild=False, fresh_nb=first)

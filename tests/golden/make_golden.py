@@ -20,6 +20,11 @@ Fixtures (npz):
                    particles active.
   sph2k.npz        a 2k + 2k cloud: the 48-candidate neighbour search, h, sph_forces
                    outputs, and a Verlet reselection after a drift.
+  cooling.npz      the reference's cooling_function on a temperature grid spanning the floor,
+                   and cool() on random (u, rho, dt, blocked) with the simulator's floor
+                   (cooling.py:24-43, simulation.py:38-42).
+
+Pass fixture names (bh_gauss cloud sph cooling) to regenerate only those.
 """
 
 import os
@@ -39,7 +44,8 @@ import oracle  # noqa: E402
 from galaxy_formation.config import Config  # noqa: E402
 from galaxy_formation.initial_conditions import make_cloud  # noqa: E402
 from galaxy_formation import sph as ref_sph  # noqa: E402
-from galaxy_formation.units import KPC  # noqa: E402
+from galaxy_formation.units import K_B, KPC, M_H, MU_IONISED, U_CGS  # noqa: E402
+from galaxy_formation import cooling as ref_cooling  # noqa: E402
 
 
 def bh_gauss():
@@ -108,11 +114,28 @@ def sph():
                                            for r in np.linspace(0, 1.5, 61)]))
 
 
+def cooling():
+    T = np.concatenate([np.logspace(3, 9, 241), [5e3, 1e4, np.nextafter(1e4, 2e4), 2e4, 1e5, 1e6, 1e8]])
+    lam = ref_cooling.cooling_function(T)
+    gamma = 5.0 / 3.0
+    u_per_K = K_B / ((gamma - 1) * MU_IONISED * M_H) / U_CGS
+    u_floor = ref_cooling.T_FLOOR * u_per_K
+    rng = np.random.default_rng(11)
+    n = 4000
+    u = np.exp(rng.uniform(np.log(0.5e4), np.log(1e8), n)) * u_per_K
+    rho = np.exp(rng.uniform(np.log(1e-7), np.log(1e1), n))
+    dt = np.exp(rng.uniform(np.log(1e-6), np.log(1e-2), n))
+    blocked = rng.uniform(size=n) < 0.1
+    u_new = ref_cooling.cool(u, u / u_per_K, rho, dt, blocked, u_floor)
+    np.savez_compressed(os.path.join(OUT, "cooling.npz"), T=T, lam=lam, u_per_K=u_per_K, u_floor=u_floor,
+                        u=u, rho=rho, dt=dt, blocked=blocked, u_new=u_new)
+
+
 if __name__ == "__main__":
     oracle.build()
-    bh_gauss()
-    cloud()
-    sph()
+    names = sys.argv[1:] or ["bh_gauss", "cloud", "sph", "cooling"]
+    for name in names:
+        globals()[name]()
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)))

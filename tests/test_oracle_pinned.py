@@ -85,3 +85,21 @@ def test_kernel_matches_reference(oracle, golden):
     g = np.array([oracle.sph_kernel_grad(r, 0.7) for r in s["kernel_r"]])
     assert np.allclose(w, s["kernel_w"], rtol=1e-14, atol=0)
     assert np.allclose(g, s["kernel_g"], rtol=1e-14, atol=0)
+
+
+def test_cooling_matches_reference(golden):
+    """The restated cooling function and explicit cooling step against the reference's own
+    cooling.py outputs (tests/golden/cooling.npz), bit for bit; the unit constants of
+    galaxy_formation_gb300.params are the reference's."""
+    import cooling_ref
+
+    from galaxy_formation_gb300 import params
+
+    c = golden("cooling.npz")
+    lam = cooling_ref.cooling_function(c["T"])
+    assert np.array_equal(lam, c["lam"])
+    assert lam[c["T"] <= 1e4].max() == 0 and np.all(lam[c["T"] > 1e4] > 0)  # tests/test_physics.py:41-45
+    assert c["u_per_K"] == params.U_PER_K and c["u_floor"] == params.U_FLOOR
+    u_new = cooling_ref.cool(c["u"], c["u"] / c["u_per_K"], c["rho"], c["dt"], c["blocked"], c["u_floor"],
+                             cooling_ref.units_of(params))
+    assert np.array_equal(u_new, c["u_new"])
