@@ -644,9 +644,14 @@ def run_drift(args, world, rank, local):
                 "dL_over_L": float(np.linalg.norm(q1[4:7] - q0[4:7]) / np.linalg.norm(q0[4:7])),
                 "E0": q0[3], "E1": q1[3]}
 
+    # both forms integrate u with the explicit compression / shock-heating update of
+    # _thermodynamics (no cooling, which would radiate energy away), so the total energy
+    # kinetic + potential + thermal is the conserved quantity
+    units = np.array(p.THERMO_UNITS)
     theta = G.set_form("plain")
     L.check(lib.gf_sim_init(n, d["pos"], d["vel"], d["mass"], d["kind"], d["u"], theta, p.EPS, p.GAMMA, p.ALPHA,
                             p.BETA))
+    L.check(lib.gf_sim_thermo(1, units.ctypes.data))
     q0 = diag()
     tk, sub = ctypes.c_double(), ctypes.c_int()
     upd, subs = 0.0, 0
@@ -669,6 +674,7 @@ def run_drift(args, world, rank, local):
     theta = G.set_form("mixed_learned")
     L.check(lib.gf_sim_init(n, d["pos"], d["vel"], d["mass"], d["kind"], d["u"], theta, p.EPS, p.GAMMA, p.ALPHA,
                             p.BETA))
+    L.check(lib.gf_sim_thermo(1, units.ctypes.data))
     nlev = 7
     chunk = np.zeros(nlev - 1, np.int32)
     every, gms = ctypes.c_int(), ctypes.c_double()
@@ -704,7 +710,9 @@ def run_drift(args, world, rank, local):
         "forms": out,
         "simulated_time_per_wall_second_ratio": r / r0,
         "diagnostics": "gf_sim_diagnostics: float64 sums; potential from a monopole walk at theta 0.5",
+        "thermal_update": "u += dt du/dt at every (sub-)step, floored at 1e4 K (simulation.py:97-102); no cooling",
     }), flush=True)
+    lib.gf_sim_thermo(0, None)
 
 
 def main():

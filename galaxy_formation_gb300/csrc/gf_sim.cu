@@ -272,7 +272,7 @@ struct BlockIntegrator {
     int nlev = 7;
     bool started = false;
     DevBuf level, act, scal;  // scal: [0] delta bits, [1] active-count accumulator
-    DevBuf save_pos, save_vel, tune_acc;
+    DevBuf save_pos, save_vel, save_u, tune_acc;
     unsigned long long* h_cnt = nullptr;
     cudaGraphExec_t exec = nullptr;
     unsigned long long gen = ~0ull;
@@ -423,7 +423,7 @@ struct BlockIntegrator {
         return updates;
     }
 
-    // Autotuner. The state (positions, velocities, time) is saved first and restored at the
+    // Autotuner. The state (positions, velocities, energies, time) is saved first and restored at the
     // end; the next block then starts with a full evaluation, so tuning leaves no trace in the
     // trajectory. Two knobs:
     //   * walk items per bin: for the particles due at the first sub-step of each bin, the
@@ -437,6 +437,8 @@ struct BlockIntegrator {
         double* sv = save_vel.get<double>(n3);
         GF_CUDA(cudaMemcpyAsync(sp, S.pos.as<double>(), sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
         GF_CUDA(cudaMemcpyAsync(sv, S.vel.as<double>(), sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
+        double* su = save_u.get<double>(size_t(S.n));  // the thermal update changes u
+        GF_CUDA(cudaMemcpyAsync(su, S.u.as<double>(), sizeof(double) * size_t(S.n), cudaMemcpyDeviceToDevice, s));
         const double t0 = S.t;
         ForceEngine& F = force_engine();
         const long long collect = F.collect_cap;
@@ -492,6 +494,8 @@ struct BlockIntegrator {
                 if (r >= nsub()) continue;
                 GF_CUDA(cudaMemcpyAsync(S.pos.as<double>(), sp, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
                 GF_CUDA(cudaMemcpyAsync(S.vel.as<double>(), sv, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
+                GF_CUDA(cudaMemcpyAsync(S.u.as<double>(), su, sizeof(double) * size_t(S.n), cudaMemcpyDeviceToDevice,
+                                        s));
                 tune.rebuild_every = r;
                 tune_changed = true;
                 started = false;
@@ -513,6 +517,7 @@ struct BlockIntegrator {
         C.prof.on = prof;
         GF_CUDA(cudaMemcpyAsync(S.pos.as<double>(), sp, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
         GF_CUDA(cudaMemcpyAsync(S.vel.as<double>(), sv, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
+        GF_CUDA(cudaMemcpyAsync(S.u.as<double>(), su, sizeof(double) * size_t(S.n), cudaMemcpyDeviceToDevice, s));
         GF_CUDA(cudaStreamSynchronize(s));
         S.t = t0;
         started = false;

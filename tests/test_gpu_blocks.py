@@ -125,6 +125,8 @@ def test_chunked_walk_accuracy(gpulib, oracle):
 
 
 def test_block_autotune_restores_state(gpulib):
+    """The autotuner's trial blocks (with the thermal update on) leave positions, velocities,
+    energies and time as they were."""
     from galaxy_formation_gb300 import _lib, params, synthetic
 
     lib = gpulib
@@ -133,21 +135,30 @@ def test_block_autotune_restores_state(gpulib):
     n = len(d["mass"])
     _lib.check(lib.gf_sim_init(n, d["pos"], d["vel"], d["mass"], d["kind"], d["u"], params.THETA, params.EPS,
                                params.GAMMA, params.ALPHA, params.BETA))
-    upd = ctypes.c_double()
-    _lib.check(lib.gf_sim_blocks(1, 4, ctypes.byref(upd)))
-    p0, v0, t0 = _state(lib, n)
-    chunk = np.zeros(3, np.int32)
-    every = ctypes.c_int()
-    ms = ctypes.c_double()
-    _lib.check(lib.gf_sim_block_autotune(4, chunk.ctypes.data, ctypes.byref(every), ctypes.byref(ms)))
-    assert {c % 100 for c in chunk.tolist()} <= {0, 2, 4, 8, 16, 32, 64}
-    assert every.value in (0, 4) and ms.value > 0
-    p1, v1, t1 = _state(lib, n)
-    assert t1 == t0
-    assert np.array_equal(p1, p0) and np.array_equal(v1, v0)
-    _lib.check(lib.gf_sim_blocks(2, 4, ctypes.byref(upd)))
-    p2, v2, t2 = _state(lib, n)
-    assert t2 > t1 and np.all(np.isfinite(p2)) and np.all(np.isfinite(v2))
+    units = np.array(params.THERMO_UNITS)
+    _lib.check(lib.gf_sim_thermo(2, units.ctypes.data))
+    try:
+        upd = ctypes.c_double()
+        _lib.check(lib.gf_sim_blocks(1, 4, ctypes.byref(upd)))
+        p0, v0, t0 = _state(lib, n)
+        u0 = np.empty(n)
+        _lib.check(lib.gf_sim_read_u(u0))
+        chunk = np.zeros(3, np.int32)
+        every = ctypes.c_int()
+        ms = ctypes.c_double()
+        _lib.check(lib.gf_sim_block_autotune(4, chunk.ctypes.data, ctypes.byref(every), ctypes.byref(ms)))
+        assert {c % 100 for c in chunk.tolist()} <= {0, 2, 4, 8, 16, 32, 64}
+        assert every.value in (0, 4) and ms.value > 0
+        p1, v1, t1 = _state(lib, n)
+        u1 = np.empty(n)
+        _lib.check(lib.gf_sim_read_u(u1))
+        assert t1 == t0
+        assert np.array_equal(p1, p0) and np.array_equal(v1, v0) and np.array_equal(u1, u0)
+        _lib.check(lib.gf_sim_blocks(2, 4, ctypes.byref(upd)))
+        p2, v2, t2 = _state(lib, n)
+        assert t2 > t1 and np.all(np.isfinite(p2)) and np.all(np.isfinite(v2))
+    finally:
+        lib.gf_sim_thermo(0, None)
 
 
 def test_wide_rounds_walk_matches(gpulib):
