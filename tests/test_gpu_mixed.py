@@ -219,3 +219,4 @@ def test_merged_walk_items(gpulib):
     for merge in (64, 128):
         assert errs[merge][0] < 1e-3 and errs[merge][0] <= 1.1 * errs[0][0], errs
         assert errs[merge][1] < 5e-3, errs
+
