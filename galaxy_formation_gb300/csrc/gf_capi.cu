@@ -457,18 +457,29 @@ int gf_accelerations(int n, const double* pos, const double* vel, const double* 
         force_args_check(n, pos, vel, mass, kind, u, acc, dt_ind);
         if (n == 0) return;
         cudaStream_t s = ctx().stream;
-        ForceArgs a{n,
-                    upload(g_st.pos, pos, 3 * size_t(n), s),
-                    upload(g_st.vel, vel, 3 * size_t(n), s),
-                    upload(g_st.mass, mass, size_t(n), s),
-                    upload(g_st.kind, kind, size_t(n), s),
-                    upload(g_st.u, u, size_t(n), s),
-                    theta, eps, gamma, alpha, beta,
-                    active ? upload(g_st.active, active, size_t(n), s) : nullptr,
-                    rebuild, sph, fresh_nb,
-                    g_st.acc.get<double>(3 * size_t(n)),
-                    g_st.dt_ind.get<double>(size_t(n))};
+        // the gravity chain needs pos and mass (and kind for the gas flags) first; vel and u,
+        // read only by the hydro chain, are copied on a second stream meanwhile
+        static cudaStream_t s_late = nullptr;
+        static cudaEvent_t ev_start = nullptr, ev_late = nullptr;
+        if (!s_late) {
+            GF_CUDA(cudaStreamCreateWithFlags(&s_late, cudaStreamNonBlocking));
+            GF_CUDA(cudaEventCreateWithFlags(&ev_start, cudaEventDisableTiming));
+            GF_CUDA(cudaEventCreateWithFlags(&ev_late, cudaEventDisableTiming));
+        }
+        GF_CUDA(cudaEventRecord(ev_start, s));  // after the previous call's work on s
+        GF_CUDA(cudaStreamWaitEvent(s_late, ev_start, 0));
+        double* d_pos = upload(g_st.pos, pos, 3 * size_t(n), s);
+        double* d_mass = upload(g_st.mass, mass, size_t(n), s);
+        int8_t* d_kind = upload(g_st.kind, kind, size_t(n), s);
+        const uint8_t* d_act = active ? upload(g_st.active, active, size_t(n), s) : nullptr;
+        double* d_vel = upload(g_st.vel, vel, 3 * size_t(n), s_late);
+        double* d_u = upload(g_st.u, u, size_t(n), s_late);
+        GF_CUDA(cudaEventRecord(ev_late, s_late));
+        ForceArgs a{n, d_pos, d_vel, d_mass, d_kind, d_u, theta, eps, gamma, alpha, beta, d_act, rebuild, sph,
+                    fresh_nb, g_st.acc.get<double>(3 * size_t(n)), g_st.dt_ind.get<double>(size_t(n))};
+        a.late_inputs = ev_late;
         force_engine().evaluate(a, s);
+        GF_CUDA(cudaStreamWaitEvent(s, ev_late, 0));  // the copies are done before the call returns
         download(acc, a.acc, 3 * size_t(n), s);
         download(dt_ind, a.dt_ind, size_t(n), s);
         collect_status(s);

@@ -402,6 +402,7 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
     double* gv = gvel.get<double>(3 * size_t(ng));
     double* gm = gmass.get<double>(ng);
     double* gu = gu_.get<double>(ng);
+    if (a.late_inputs) GF_CUDA(cudaStreamWaitEvent(s, a.late_inputs, 0));
     k_gas_gather<<<grid, kThreads, 0, s>>>(n, fl, sc_, a.pos, a.vel, a.mass, a.u, gi, gp, gv, gm, gu);
     GF_CHECK_LAUNCH();
 

@@ -40,6 +40,9 @@ struct ForceArgs {
     // reference's groups); used with an active set
     int walk_chunk = 0;
     int walk_npl = 2;  // mixed walk: nodes per lane and round (2, or 8 for walks of a few items)
+    // vel and u may still be arriving (copies on another stream): the hydro chain waits for
+    // this event before it reads them; the gravity chain does not need them
+    cudaEvent_t late_inputs = nullptr;
 };
 
 struct ForceEngine {
