@@ -304,7 +304,12 @@ void ForceEngine::evaluate(const ForceArgs& a, cudaStream_t s) {
     const bool fork = a.sph != 0;
     if (fork) {
         if (!s2) {
-            GF_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+            // the hydro chain at the highest priority: its small kernels (neighbour-tree build,
+            // SPH passes) then get SMs ahead of the walk's blocks (measured 0.8 % faster; the
+            // reverse order is 3 % slower)
+            int lowest = 0, greatest = 0;
+            GF_CUDA(cudaDeviceGetStreamPriorityRange(&lowest, &greatest));
+            GF_CUDA(cudaStreamCreateWithPriority(&s2, cudaStreamNonBlocking, greatest));
             GF_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
             GF_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
         }
