@@ -402,10 +402,12 @@ class Gpu:
         s = torch.cuda.ExternalStream(lib.gf_stream())
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         launches0 = lib.gf_launch_count()
+        torch.cuda.nvtx.range_push("blocks")  # for profilers: the timed blocks only
         e0.record(s)
         L.check(lib.gf_sim_blocks(blocks, nlev, ctypes.byref(upd)))
         e1.record(s)
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         ms = e0.elapsed_time(e1)
         return {"value": upd.value / (ms * 1e-3), "unit": UNIT, "blocks": blocks, "substeps_per_block": 1 << (nlev - 1),
                 "levels": nlev, "level_fractions": [round(float(x), 5) for x in frac],
