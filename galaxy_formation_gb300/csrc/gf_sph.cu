@@ -370,6 +370,7 @@ __device__ int knn_collect(const KnnArgs& A, KnnSmem& S, float4 xh, float4 xl, f
         // particles of the opened leaves, concatenated in lane order (a lane's two leaves in
         // turn) and tested 32 at a time: lane l takes offset o = base + l
         const int lc = lcs[0] + lcs[1];
+        if (__any_sync(0xffffffffu, lc > 0)) {  // some leaf opened in this round
         const int lincl = warp_incl_scan(lc);
         const int lexcl = lincl - lc;
         const int ltot = __shfl_sync(0xffffffffu, lincl, 31);
@@ -406,6 +407,7 @@ __device__ int knn_collect(const KnnArgs& A, KnnSmem& S, float4 xh, float4 xl, f
             }
             cnt += __popc(hm);
         }
+        }  // any leaf
         __syncwarp();
     }
     return cnt;

@@ -544,7 +544,8 @@ __global__ void __launch_bounds__(kWalkWarps * 32, QUAD ? (NPL > 2 ? 1 : 4) : 5)
                 fill += na;
             }
 
-            // opened leaves: their particles
+            // opened leaves: their particles (the scan only in rounds that open one)
+            if (__any_sync(0xffffffffu, leaf)) {
             const int lc = leaf ? -code : 0;
             const int lincl = warp_incl_scan(lc);
             const int lexcl = lincl - lc;
@@ -570,6 +571,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32, QUAD ? (NPL > 2 ? 1 : 4) : 5)
                 fill += chunk;
                 done += chunk;
             }
+            }  // any leaf
             __syncwarp();
             }  // nodes of the lane
             if (overflow) break;
