@@ -58,6 +58,8 @@ SIGNATURES = {
     "gf_sim_read": ([_vp, _vp, _vp, _vp, ctypes.POINTER(_cd)], _ci),
     "gf_sim_diagnostics": ([_cd, _dbl], _ci),
     "gf_sim_read_u": ([_dbl], _ci),
+    "gf_sim_stars": ([_ci, _vp, _vp], _ci),
+    "gf_sim_read_stars": ([_vp, _vp, _vp, _vp], ctypes.c_longlong),
     "gf_sim_thermo": ([_ci, _vp], _ci),
     "gf_cooling_function": ([_ci, _dbl, _dbl], _ci),
     "gf_cool": ([_ci, _dbl, _dbl, _dbl, _dbl, _vp, _cd, _dbl, _dbl], _ci),

@@ -673,6 +673,28 @@ int gf_sim_read(double* pos, double* vel, double* acc, double* dt_ind, double* t
     return guarded([&] { sim_read(pos, vel, acc, dt_ind, t); });
 }
 
+int gf_sim_stars(int on, const double* params, const uint64_t* rng_state) {
+    return guarded([&] {
+        require(simulation_ready(), "no simulation (gf_sim_init)");
+        if (on) {
+            require(params != nullptr && rng_state != nullptr, "null argument");
+            for (int i = 0; i < 10; ++i) require(std::isfinite(params[i]) && params[i] >= 0, "bad star parameter");
+            require(params[3] >= 1 && params[3] <= 64, "fb_ngb is 1..64");
+            require((rng_state[3] & 1) == 1, "a PCG64 increment is odd");
+        }
+        sim_stars(on, params, reinterpret_cast<const unsigned long long*>(rng_state));
+    });
+}
+
+long long gf_sim_read_stars(int8_t* kind, double* birth, double* no_cool_until, uint64_t* rng_state) {
+    long long formed = -1;
+    const int st = guarded([&] {
+        require(simulation_ready(), "no simulation (gf_sim_init)");
+        formed = sim_read_stars(kind, birth, no_cool_until, reinterpret_cast<unsigned long long*>(rng_state));
+    });
+    return st ? -st : formed;
+}
+
 int gf_sim_read_u(double* u) {
     return guarded([&] {
         require(u != nullptr, "null array");

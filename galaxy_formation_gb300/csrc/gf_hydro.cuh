@@ -125,6 +125,13 @@ void sim_read_u(double* u);
 // thermal update of the step loop: mode 0 off, 1 heating/compression, 2 also cooling;
 // units: the 8 constants of ThermoUnits (gf_thermo.cuh), in its order
 void sim_thermo(int mode, const double* units);
+// star formation + supernova feedback after every step and sub-step of sim_step: params = the
+// 10 values of StarParams (gf_stars.cuh) in its order; rng_words = NumPy PCG64 state
+// (state high, state low, increment high, increment low)
+void sim_stars(int on, const double* params, const unsigned long long* rng_words);
+// copies kind, birth, no_cool (n each) and the PCG64 words out (any may be null); returns the
+// number of stars formed since sim_init
+long long sim_read_stars(int8_t* kind, double* birth, double* no_cool, unsigned long long* rng_words);
 void sim_diagnostics(double theta, double* out);
 // Block time steps (the batched form): advances nblocks blocks of 2^(nlev-1) sub-steps;
 // returns the particle-updates done.

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "gf_hydro.cuh"
+#include "gf_stars.cuh"
 #include "gf_thermo.cuh"
 
 namespace gf {
@@ -28,6 +29,11 @@ __global__ void k_kick(int n, double* __restrict__ vel, const double* __restrict
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || (mask && !mask[i])) return;
     for (int c = 0; c < 3; ++c) vel[3 * size_t(i) + c] += h * acc[3 * size_t(i) + c];
+}
+
+__global__ void k_set(int n, double* __restrict__ a, double v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = v;
 }
 
 __global__ void k_drift(int n, double* __restrict__ pos, const double* __restrict__ vel, double dt) {
@@ -85,6 +91,11 @@ struct Simulation {
     // compression / shock-heating update of u, 2 also radiative cooling (cooling.py)
     int thermo_mode = 0;
     ThermoUnits thermo_units{};
+    // star formation and supernova feedback after every (sub-)step (simulation.py:106-110)
+    bool stars_on = false;
+    StarParams star_params{};
+    DevBuf birth, no_cool, rng;   // per particle: birth time, end of the bubble; Pcg64
+    long long stars_formed = 0;
 
     cudaStream_t s() const { return ctx().stream; }
 
@@ -94,7 +105,18 @@ struct Simulation {
         ForceEngine& F = force_engine();
         if (F.ng_valid <= 0) return;  // rho_gas.size == 0 (simulation.py:99)
         thermo_gas(F.ng_valid, F.gidx.as<int>(), F.rho.as<double>(), F.dudt.as<double>(), u.as<double>(), dt,
-                   thermo_mode, thermo_units, s());
+                   thermo_mode, no_cool.as<double>(), t, thermo_units, s());
+    }
+
+    // _stars(dt) at the current time
+    void stars(double dt) {
+        if (!stars_on) return;
+        ForceEngine& F = force_engine();
+        if (F.ng_valid <= 0) return;  // rho_gas.size == 0 (simulation.py:107)
+        stars_formed += form_stars_and_feedback(n, F.ng_valid, F.gidx.as<int>(), F.rho.as<double>(),
+                                                pos.as<double>(), mass.as<double>(), kind.as<int8_t>(),
+                                                u.as<double>(), birth.as<double>(), no_cool.as<double>(), dt, t,
+                                                star_params, rng.as<Pcg64>(), s());
     }
 
     void accelerations(const uint8_t* active, int rebuild, int sph, int fresh) {
@@ -171,6 +193,7 @@ struct Simulation {
             accelerations(nullptr, 1, 1, 1);
             kick(nullptr, 0.5 * dt_min);
             t += dt_min;
+            stars(dt_min);
             last_substeps = 1;
             return dt_min;
         }
@@ -191,6 +214,7 @@ struct Simulation {
             kick(f, 0.5 * dt);
             tau += dt;
             t += dt;
+            stars(dt);
             ++last_substeps;
         }
         accelerations(sl, 1, 0, 1);
@@ -272,7 +296,8 @@ struct BlockIntegrator {
     int nlev = 7;
     bool started = false;
     DevBuf level, act, scal;  // scal: [0] delta bits, [1] active-count accumulator
-    DevBuf save_pos, save_vel, save_u, tune_acc;
+    DevBuf save_pos, save_vel, save_u, tune_acc, t_block;
+    double* h_tblock = nullptr;  // pinned
     unsigned long long* h_cnt = nullptr;
     cudaGraphExec_t exec = nullptr;
     unsigned long long gen = ~0ull;
@@ -305,11 +330,19 @@ struct BlockIntegrator {
         ForceEngine& F = force_engine();
         if (!S.thermo_mode || F.ng_valid <= 0) return;
         thermo_gas_levels(F.ng_valid, F.gidx.as<int>(), level.as<int8_t>(), sub, scal.as<unsigned long long>(),
-                          F.rho.as<double>(), F.dudt.as<double>(), S.u.as<double>(), S.thermo_mode, S.thermo_units,
-                          S.s());
+                          F.rho.as<double>(), F.dudt.as<double>(), S.u.as<double>(), S.thermo_mode,
+                          S.no_cool.as<double>(), t_block.get<double>(1), S.thermo_units, S.s());
     }
+    // options and gas set the graph bakes in
     unsigned long long capture_key(const Simulation& S) const {
-        return force_engine().option_key() * 31u + unsigned(S.thermo_mode);
+        const ForceEngine& F = force_engine();
+        return (F.option_key() * 31u + unsigned(S.thermo_mode)) * 1000003u + unsigned(F.ng_valid);
+    }
+    // the block's start time on the device (the thermal update's bubble test), before its replay
+    void set_block_time(Simulation& S) {
+        if (!h_tblock) GF_CUDA(cudaMallocHost(&h_tblock, sizeof(double)));
+        *h_tblock = S.t;
+        GF_CUDA(cudaMemcpyAsync(t_block.get<double>(1), h_tblock, sizeof(double), cudaMemcpyHostToDevice, S.s()));
     }
 
     // nosync: inside the captured graph (rebuild = captured tree rebuild, else refit);
@@ -333,6 +366,7 @@ struct BlockIntegrator {
         }
         Context& C = ctx();
         force_engine().reserve_nosync(S.n);  // nothing may allocate inside the capture
+        t_block.get<double>(1);
         const bool prof = C.prof.on;
         C.prof.on = false;
         unsigned long long* d = scal.as<unsigned long long>();
@@ -401,6 +435,7 @@ struct BlockIntegrator {
                 capture(S);
             unsigned long long* d = scal.as<unsigned long long>();
             GF_CUDA(cudaMemsetAsync(d + 1, 0, sizeof(unsigned long long), s));
+            set_block_time(S);
             e0.record(s);
             GF_CUDA(cudaGraphLaunch(exec, s));
             e1.record(s);
@@ -586,6 +621,11 @@ void sim_init(int n, const double* pos, const double* vel, const double* mass, c
     GF_CUDA(cudaMemcpyAsync(S.u.get<double>(n), u, sizeof(double) * n, cudaMemcpyHostToDevice, s));
     S.acc.get<double>(3 * size_t(n));
     S.dt_ind.get<double>(n);
+    k_set<<<div_up(n, kThreads), kThreads, 0, s>>>(n, S.birth.get<double>(n), INFINITY);       // simulation.py:36
+    GF_CHECK_LAUNCH();
+    k_set<<<div_up(n, kThreads), kThreads, 0, s>>>(n, S.no_cool.get<double>(n), -INFINITY);    // simulation.py:43
+    GF_CHECK_LAUNCH();
+    S.stars_formed = 0;
     force_engine().n_total = -1;  // fresh force state (simulation.py:51-54)
     g_block.started = false;
     S.dt_gas = INFINITY;
@@ -698,6 +738,31 @@ void sim_thermo(int mode, const double* units) {
         ThermoUnits& U = S.thermo_units;
         U = ThermoUnits{units[0], units[1], units[2], units[3], units[4], units[5], units[6], units[7]};
     }
+}
+
+void sim_stars(int on, const double* params, const unsigned long long* rng_words) {
+    Simulation& S = g_sim;
+    S.stars_on = on != 0;
+    if (!on) return;
+    StarParams& P = S.star_params;
+    P = StarParams{params[0], params[1], params[2], params[3], params[4],
+                   params[5], params[6], params[7], params[8], params[9]};
+    Pcg64 R;
+    for (int i = 0; i < 4; ++i) R.w[i] = rng_words[i];
+    GF_CUDA(cudaMemcpyAsync(S.rng.get<Pcg64>(1), &R, sizeof(Pcg64), cudaMemcpyHostToDevice, ctx().stream));
+    GF_CUDA(cudaStreamSynchronize(ctx().stream));
+}
+
+long long sim_read_stars(int8_t* kind, double* birth, double* no_cool, unsigned long long* rng_words) {
+    Simulation& S = g_sim;
+    cudaStream_t s = ctx().stream;
+    const size_t n = S.n;
+    if (kind) GF_CUDA(cudaMemcpyAsync(kind, S.kind.p, n, cudaMemcpyDeviceToHost, s));
+    if (birth) GF_CUDA(cudaMemcpyAsync(birth, S.birth.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    if (no_cool) GF_CUDA(cudaMemcpyAsync(no_cool, S.no_cool.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    if (rng_words && S.rng.p) GF_CUDA(cudaMemcpyAsync(rng_words, S.rng.p, sizeof(Pcg64), cudaMemcpyDeviceToHost, s));
+    GF_CUDA(cudaStreamSynchronize(s));
+    return S.stars_formed;
 }
 
 void sim_read_u(double* u) {

@@ -57,41 +57,50 @@ __global__ void k_cool(int n, const double* __restrict__ u, const double* __rest
 
 // simulation.py:97-104 for the ng gas particles of the last SPH evaluation (gas-local order,
 // gidx -> particle): heating/compression, then (mode 2) cooling at the updated temperature
+// no_cool (may be null): particles with no_cool > t sit in a supernova bubble and do not cool
 __global__ void k_thermo_gas(int ng, const int* __restrict__ gidx, const double* __restrict__ rho,
                              const double* __restrict__ dudt, double* __restrict__ u, double dt, int mode,
-                             ThermoUnits U) {
+                             const double* __restrict__ no_cool, double t, ThermoUnits U) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= ng) return;
     const int i = gidx[g];
     double ui = fmax(add(u[i], mul(dt, dudt[g])), U.u_floor);
-    if (mode == 2) ui = cool_one(ui, dvd(ui, U.u_per_k), rho[g], dt, false, U.u_floor, U);
+    if (mode == 2) ui = cool_one(ui, dvd(ui, U.u_per_k), rho[g], dt, no_cool && no_cool[i] > t, U.u_floor, U);
     u[i] = ui;
 }
 
 // Block time steps: the gas due at sub-step `sub` (level j with sub mod 2^j == 0) advances u
 // over its own step 2^j delta with the rate of its last evaluation, before its evaluation at
 // this sub-step (delta: float64 bits on the device)
+// t_block: time at the block start (device); the sub-step's time is t_block + sub delta
 __global__ void k_thermo_levels(int ng, const int* __restrict__ gidx, const int8_t* __restrict__ level, int sub,
                                 const unsigned long long* __restrict__ dbits, const double* __restrict__ rho,
-                                const double* __restrict__ dudt, double* __restrict__ u, int mode, ThermoUnits U) {
+                                const double* __restrict__ dudt, double* __restrict__ u, int mode,
+                                const double* __restrict__ no_cool, const double* __restrict__ t_block,
+                                ThermoUnits U) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= ng) return;
     const int i = gidx[g];
     const int j = level[i];
     if (sub & ((1 << j) - 1)) return;
-    const double dt = __longlong_as_double((long long)*dbits) * double(1 << j);
+    const double delta = __longlong_as_double((long long)*dbits);
+    const double dt = delta * double(1 << j);
     double ui = fmax(add(u[i], mul(dt, dudt[g])), U.u_floor);
-    if (mode == 2) ui = cool_one(ui, dvd(ui, U.u_per_k), rho[g], dt, false, U.u_floor, U);
+    if (mode == 2) {
+        const bool blocked = no_cool && no_cool[i] > *t_block + delta * double(sub);
+        ui = cool_one(ui, dvd(ui, U.u_per_k), rho[g], dt, blocked, U.u_floor, U);
+    }
     u[i] = ui;
 }
 
 }  // namespace
 
 void thermo_gas_levels(int ng, const int* gidx, const int8_t* level, int sub, const unsigned long long* dbits,
-                       const double* rho, const double* dudt, double* u, int mode, const ThermoUnits& U,
-                       cudaStream_t s) {
+                       const double* rho, const double* dudt, double* u, int mode, const double* no_cool,
+                       const double* t_block, const ThermoUnits& U, cudaStream_t s) {
     if (ng <= 0 || mode == 0) return;
-    k_thermo_levels<<<div_up(ng, kThreads), kThreads, 0, s>>>(ng, gidx, level, sub, dbits, rho, dudt, u, mode, U);
+    k_thermo_levels<<<div_up(ng, kThreads), kThreads, 0, s>>>(ng, gidx, level, sub, dbits, rho, dudt, u, mode,
+                                                              no_cool, t_block, U);
     GF_CHECK_LAUNCH();
 }
 
@@ -109,9 +118,9 @@ void cool(int n, const double* u, const double* T, const double* rho, const doub
 }
 
 void thermo_gas(int ng, const int* gidx, const double* rho, const double* dudt, double* u, double dt, int mode,
-                const ThermoUnits& U, cudaStream_t s) {
+                const double* no_cool, double t, const ThermoUnits& U, cudaStream_t s) {
     if (ng <= 0 || mode == 0) return;
-    k_thermo_gas<<<div_up(ng, kThreads), kThreads, 0, s>>>(ng, gidx, rho, dudt, u, dt, mode, U);
+    k_thermo_gas<<<div_up(ng, kThreads), kThreads, 0, s>>>(ng, gidx, rho, dudt, u, dt, mode, no_cool, t, U);
     GF_CHECK_LAUNCH();
 }
 

@@ -248,13 +248,31 @@ int gf_sim_read_u(double* u);
 /* Thermal update at the start of every step and sub-step of gf_sim_step, as
  * GalaxyFormation._thermodynamics (simulation.py:97-104) on the gas of the last SPH
  * evaluation: mode 0 = off (default), 1 = u += dt du/dt floored at u_floor (compression and
- * shock heating), 2 = 1 then radiative cooling of a primordial gas (cooling.py:34-43). No
- * particle is blocked from cooling (supernova bubbles belong to star formation, which this
- * library does not run). gf_sim_blocks applies the same update to each gas particle over its
- * own step, at the sub-steps where it is due, before its evaluation there.
+ * shock heating), 2 = 1 then radiative cooling of a primordial gas (cooling.py:34-43),
+ * except for particles inside a supernova bubble (no_cool_until > t, from gf_sim_stars).
+ * gf_sim_blocks applies the same update to each gas particle over its own step, at the
+ * sub-steps where it is due, before its evaluation there.
  * units (mode > 0): 8 positive constants in this order: u_per_K, u_floor, RHO_CGS, X_H,
  * M_H, MYR, SEC_PER_MYR, U_CGS (galaxy_formation/units.py, simulation.py:40-42). */
 int gf_sim_thermo(int mode, const double* units);
+/* Star formation and supernova feedback after every step and sub-step of gf_sim_step, as
+ * GalaxyFormation._stars (simulation.py:106-110, star_formation.py:35-65), on the device:
+ * gas of the last SPH evaluation with rho > rho_sf and T < 3e4 K becomes a star (kind 1,
+ * birth = t) when its uniform draw is below 1 - exp(-sf_eff dt / t_ff); each new star then
+ * heats its fb_ngb nearest gas particles and blocks their cooling for fb_myr. The draws are
+ * those of NumPy's Generator(PCG64): rng_state holds its bit generator's state and increment
+ * (128-bit each) as 4 words: state high, state low, inc high, inc low; the dense particle of
+ * rank r (ascending particle index) takes the stream's draw r + 1 and the stream advances by
+ * the number of dense particles per call, exactly as rng.uniform(size=p.size), so the same
+ * generator state gives the reference's stars. params (10, positive): rho_sf (code units),
+ * sf_eff, fb_eff, fb_ngb (1..64), fb_myr / MYR (code units), E_SN_PER_MSUN (erg), MSUN,
+ * MSUN_G, U_CGS, u_per_K. on = 0 turns it off (default). Block steps (gf_sim_blocks) form no
+ * stars; their thermal update honours the bubbles. */
+int gf_sim_stars(int on, const double* params, const uint64_t* rng_state);
+/* Copies kind (n, int8), birth and no_cool_until (n, float64; inf / -inf where unset) and the
+ * advanced PCG64 state (4 words) out; any may be NULL. Returns the number of stars formed
+ * since gf_sim_init, or -GF_ERR_* on failure. */
+long long gf_sim_read_stars(int8_t* kind, double* birth, double* no_cool_until, uint64_t* rng_state);
 /* cooling.py:24-31 (host pointers): lam[i] = Lambda(T[i]) in erg cm^3 / s, 0 at or below
  * 1e4 K. */
 int gf_cooling_function(int n, const double* T, double* lam);

@@ -40,12 +40,13 @@ def units_of(params):
             "SEC_PER_MYR": params.SEC_PER_MYR, "U_CGS": params.U_CGS}
 
 
-def thermodynamics(u, g, dudt, rho, dt, u_per_K, u_floor, units, mode=2):
+def thermodynamics(u, g, dudt, rho, dt, u_per_K, u_floor, units, mode=2, blocked=None):
     """simulation.py:97-104 on u (in place) for the gas g of the last SPH evaluation; mode 1
-    stops after the compression / shock-heating update, mode 2 also cools. No particle is
-    inside a supernova bubble (star formation is not part of this library)."""
+    stops after the compression / shock-heating update, mode 2 also cools, except where
+    blocked (inside a supernova bubble: no_cool_until[g] > t)."""
     if rho.size == 0 or mode == 0:
         return
     u[g] = np.maximum(u[g] + dt * dudt, u_floor)
     if mode == 2:
-        u[g] = cool(u[g], u[g] / u_per_K, rho, dt, np.zeros(g.size, bool), u_floor, units)
+        b = np.zeros(g.size, bool) if blocked is None else blocked
+        u[g] = cool(u[g], u[g] / u_per_K, rho, dt, b, u_floor, units)

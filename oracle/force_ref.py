@@ -16,6 +16,7 @@ from scipy.spatial import cKDTree
 
 import cooling_ref
 import oracle
+import star_ref
 
 GAS = 0
 N_NEIGHBOURS, N_CANDIDATES = 32, 48
@@ -89,17 +90,23 @@ class ForceOracle:
 
 
 class StepOracle:
-    """GalaxyFormation.step (galaxy_formation/simulation.py:114-149) restated on ForceOracle,
-    without star formation (_stars). thermo = 0 also leaves out _thermodynamics; 1 applies its
-    compression / shock-heating update, 2 also cooling (oracle/cooling_ref.py), with
-    thermo_units = (u_per_K, u_floor, RHO_CGS, X_H, M_H, MYR, SEC_PER_MYR, U_CGS).
-    State: pos, vel, mass, kind, u (float64; u is copied)."""
+    """GalaxyFormation.step (galaxy_formation/simulation.py:114-149) restated on ForceOracle.
+    thermo = 0 leaves out _thermodynamics; 1 applies its compression / shock-heating update, 2
+    also cooling (oracle/cooling_ref.py), with thermo_units = (u_per_K, u_floor, RHO_CGS, X_H,
+    M_H, MYR, SEC_PER_MYR, U_CGS). stars (the 10 values of subgrid.star_params) with rng (a
+    NumPy Generator) adds _stars (oracle/star_ref.py). State: pos, vel, mass, kind, u, birth,
+    no_cool_until (float64; mass is shared, the others are copies)."""
 
-    def __init__(self, pos, vel, mass, kind, u, theta, eps, thermo=0, thermo_units=None, **kw):
+    def __init__(self, pos, vel, mass, kind, u, theta, eps, thermo=0, thermo_units=None, stars=None, rng=None,
+                 **kw):
         self.pos, self.vel = pos.copy(), vel.copy()
-        self.mass, self.kind, self.u = mass, kind, u.copy()
+        self.mass, self.kind, self.u = mass, kind.copy(), u.copy()
+        self.birth = np.full(len(mass), np.inf)            # simulation.py:36
+        self.no_cool_until = np.full(len(mass), -np.inf)   # simulation.py:43
         self.eps = eps
         self.thermo = thermo
+        self.stars = None if stars is None else star_ref.param_dict(stars)
+        self.rng = rng
         if thermo:
             u_per_K, u_floor, rho_cgs, x_h, m_h, myr, sec_per_myr, u_cgs = thermo_units
             self.u_per_K, self.u_floor = u_per_K, u_floor
@@ -111,9 +118,19 @@ class StepOracle:
 
     def _thermodynamics(self, dt):
         """simulation.py:97-104 on the gas of the last SPH evaluation."""
-        if self.thermo:
-            cooling_ref.thermodynamics(self.u, self.f.gas_idx, self.f.dudt, self.f.rho, dt, self.u_per_K,
-                                       self.u_floor, self.units, self.thermo)
+        if self.thermo and self.f.rho.size:
+            g = self.f.gas_idx
+            cooling_ref.thermodynamics(self.u, g, self.f.dudt, self.f.rho, dt, self.u_per_K, self.u_floor,
+                                       self.units, self.thermo, blocked=self.no_cool_until[g] > self.t)
+
+    def _stars(self, dt):
+        """simulation.py:106-110."""
+        if self.stars is None or self.f.rho.size == 0:
+            return
+        st = {"pos": self.pos, "mass": self.mass, "kind": self.kind, "u": self.u, "birth": self.birth,
+              "no_cool_until": self.no_cool_until, "t": self.t}
+        new = star_ref.form_stars(st, self.f.gas_idx, self.f.rho, dt, self.stars, self.rng)
+        star_ref.supernova_feedback(st, new, self.stars)
 
     def accelerations(self, active=None, rebuild=True, sph=True, fresh_nb=True):
         acc = self.f.accelerations(self.pos, self.vel, self.mass, self.kind, self.u, active, rebuild,
@@ -133,6 +150,7 @@ class StepOracle:
             self.acc = self.accelerations()
             self.vel += 0.5 * dt_min * self.acc
             self.t += dt_min
+            self._stars(dt_min)
             self.substeps = 1
             return dt_min
         fast = (self.dt_ind < D) | (self.kind == GAS)
@@ -150,6 +168,7 @@ class StepOracle:
             self.vel[fast] += 0.5 * dt * self.acc[fast]
             tau += dt
             self.t += dt
+            self._stars(dt)
             self.substeps += 1
         self.acc = self.accelerations(active=slow, rebuild=True, sph=False)
         self.vel[slow] += 0.5 * D * self.acc[slow]

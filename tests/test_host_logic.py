@@ -82,3 +82,18 @@ def test_neighbour_finder_cache_logic(oracle, monkeypatch):
     # fresh=True always searches again
     f.find(g, d["pos"][g], True)
     assert calls["full"] == 2
+
+
+def test_pcg64_words_round_trip():
+    """The generator state handed to the device's star formation is NumPy's PCG64 state."""
+    import numpy as np
+
+    from galaxy_formation_gb300 import subgrid
+
+    g = np.random.default_rng(3)
+    g.uniform(size=5)
+    w = subgrid.pcg64_words(g)
+    h = np.random.default_rng(0)
+    subgrid.set_pcg64_words(h, w)
+    assert np.array_equal(g.uniform(size=9), h.uniform(size=9))
+    assert int(w[3]) & 1 == 1   # PCG increments are odd
