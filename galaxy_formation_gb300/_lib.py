@@ -58,6 +58,9 @@ SIGNATURES = {
     "gf_sim_read": ([_vp, _vp, _vp, _vp, ctypes.POINTER(_cd)], _ci),
     "gf_sim_diagnostics": ([_cd, _dbl], _ci),
     "gf_sim_read_u": ([_dbl], _ci),
+    "gf_sim_read_scalars": ([_dbl], _ci),
+    "gf_sim_read_hydro": ([_dbl, _dbl], _ci),
+    "gf_sim_restore": ([_dbl, _dbl, _vp, _vp, _vp, _vp, _cd, _cd, _cd], _ci),
     "gf_sim_stars": ([_ci, _vp, _vp], _ci),
     "gf_sim_read_stars": ([_vp, _vp, _vp, _vp], ctypes.c_longlong),
     "gf_sim_thermo": ([_ci, _vp], _ci),

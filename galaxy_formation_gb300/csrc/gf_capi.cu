@@ -695,6 +695,32 @@ long long gf_sim_read_stars(int8_t* kind, double* birth, double* no_cool_until, 
     return st ? -st : formed;
 }
 
+int gf_sim_read_scalars(double* out) {
+    return guarded([&] {
+        require(out != nullptr, "null array");
+        require(simulation_ready(), "no simulation (gf_sim_init)");
+        sim_scalars(out);
+    });
+}
+
+int gf_sim_read_hydro(double* rho, double* dudt) {
+    return guarded([&] {
+        require(rho != nullptr && dudt != nullptr, "null array");
+        require(simulation_ready(), "no simulation (gf_sim_init)");
+        sim_read_hydro(rho, dudt);
+    });
+}
+
+int gf_sim_restore(const double* acc, const double* dt_ind, const double* birth, const double* no_cool_until,
+                   const double* rho, const double* dudt, double t, double dt_grav, double dt_gas) {
+    return guarded([&] {
+        require(simulation_ready(), "no simulation (gf_sim_init)");
+        require(acc != nullptr && dt_ind != nullptr, "null array");
+        require(std::isfinite(t) && dt_grav > 0 && dt_gas > 0, "bad scalars");
+        sim_restore(acc, dt_ind, birth, no_cool_until, rho, dudt, t, dt_grav, dt_gas);
+    });
+}
+
 int gf_sim_read_u(double* u) {
     return guarded([&] {
         require(u != nullptr, "null array");

@@ -122,6 +122,14 @@ void block_autotune(int nlev, int* chunk, int* rebuild_every, double* graph_ms);
 double sim_updates();
 void sim_read(double* pos, double* vel, double* acc, double* dt_ind, double* t);
 void sim_read_u(double* u);
+// t, dt_grav, dt_gas of the step loop
+void sim_scalars(double* out);
+// overwrites the integrator state after sim_init of a saved particle set (exact resume):
+// accelerations and time-step limits of the last evaluations, times, bubble times
+void sim_restore(const double* acc, const double* dt_ind, const double* birth, const double* no_cool,
+                 const double* rho, const double* dudt, double t, double dt_grav, double dt_gas);
+// density and du/dt of the last SPH evaluation, per particle (NaN outside its gas set)
+void sim_read_hydro(double* rho, double* dudt);
 // thermal update of the step loop: mode 0 off, 1 heating/compression, 2 also cooling;
 // units: the 8 constants of ThermoUnits (gf_thermo.cuh), in its order
 void sim_thermo(int mode, const double* units);

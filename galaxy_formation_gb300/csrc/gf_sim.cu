@@ -765,6 +765,82 @@ long long sim_read_stars(int8_t* kind, double* birth, double* no_cool, unsigned 
     return S.stars_formed;
 }
 
+void sim_scalars(double* out) {
+    Simulation& S = g_sim;
+    out[0] = S.t;
+    out[1] = S.dt_grav;
+    out[2] = S.dt_gas;
+}
+
+namespace {
+__global__ void k_gas_to_particles(int ng, const int* __restrict__ gidx, const double* __restrict__ a,
+                                   const double* __restrict__ b, double* __restrict__ pa, double* __restrict__ pb) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < ng) {
+        pa[gidx[g]] = a[g];
+        pb[gidx[g]] = b[g];
+    }
+}
+__global__ void k_particles_to_gas(int ng, const int* __restrict__ gidx, const double* __restrict__ pa,
+                                   const double* __restrict__ pb, double* __restrict__ a, double* __restrict__ b) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < ng) {
+        a[g] = pa[gidx[g]];
+        b[g] = pb[gidx[g]];
+    }
+}
+}  // namespace
+
+// density and du/dt of the last SPH evaluation (the next thermal update's inputs), per particle
+// (NaN outside its gas set)
+void sim_read_hydro(double* rho, double* dudt) {
+    Simulation& S = g_sim;
+    ForceEngine& F = force_engine();
+    cudaStream_t s = ctx().stream;
+    const size_t n = S.n;
+    static DevBuf pr, pd;
+    double* a = pr.get<double>(n);
+    double* b = pd.get<double>(n);
+    GF_CUDA(cudaMemsetAsync(a, 0xff, sizeof(double) * n, s));  // NaN pattern
+    GF_CUDA(cudaMemsetAsync(b, 0xff, sizeof(double) * n, s));
+    if (F.ng_valid > 0) {
+        k_gas_to_particles<<<div_up(F.ng_valid, kThreads), kThreads, 0, s>>>(F.ng_valid, F.gidx.as<int>(),
+                                                                            F.rho.as<double>(), F.dudt.as<double>(),
+                                                                            a, b);
+        GF_CHECK_LAUNCH();
+    }
+    GF_CUDA(cudaMemcpyAsync(rho, a, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    GF_CUDA(cudaMemcpyAsync(dudt, b, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    GF_CUDA(cudaStreamSynchronize(s));
+}
+
+void sim_restore(const double* acc, const double* dt_ind, const double* birth, const double* no_cool,
+                 const double* rho, const double* dudt, double t, double dt_grav, double dt_gas) {
+    Simulation& S = g_sim;
+    cudaStream_t s = ctx().stream;
+    const size_t n = S.n;
+    ForceEngine& F = force_engine();
+    if (rho && dudt && F.ng_valid > 0) {  // the gas set of sim_init's evaluation: same kinds, same order
+        static DevBuf pr, pd;
+        double* a = pr.get<double>(n);
+        double* b = pd.get<double>(n);
+        GF_CUDA(cudaMemcpyAsync(a, rho, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+        GF_CUDA(cudaMemcpyAsync(b, dudt, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+        k_particles_to_gas<<<div_up(F.ng_valid, kThreads), kThreads, 0, s>>>(F.ng_valid, F.gidx.as<int>(), a, b,
+                                                                            F.rho.as<double>(), F.dudt.as<double>());
+        GF_CHECK_LAUNCH();
+    }
+    GF_CUDA(cudaMemcpyAsync(S.acc.p, acc, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+    GF_CUDA(cudaMemcpyAsync(S.dt_ind.p, dt_ind, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    if (birth) GF_CUDA(cudaMemcpyAsync(S.birth.p, birth, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    if (no_cool) GF_CUDA(cudaMemcpyAsync(S.no_cool.p, no_cool, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    GF_CUDA(cudaStreamSynchronize(s));
+    S.t = t;
+    S.dt_grav = dt_grav;
+    S.dt_gas = dt_gas;
+    g_block.started = false;  // block steps restart from a full evaluation
+}
+
 void sim_read_u(double* u) {
     Simulation& S = g_sim;
     cudaStream_t s = ctx().stream;

@@ -245,6 +245,21 @@ int gf_sim_diagnostics(double theta, double* out);
 int gf_sim_read(double* pos, double* vel, double* acc, double* dt_ind, double* t);
 /* Copies the specific internal energies u (n) of the simulation state out. */
 int gf_sim_read_u(double* u);
+/* out[3] = t, dt_grav, dt_gas of the step loop (the time and the global step limits that the
+ * next gf_sim_step starts from). */
+int gf_sim_read_scalars(double* out);
+/* Density and du/dt of the last SPH evaluation per particle (n each; NaN outside its gas
+ * set): the inputs of the next thermal update. */
+int gf_sim_read_hydro(double* rho, double* dudt);
+/* Exact resume of a checkpoint (no reference counterpart): after gf_sim_init of the saved
+ * particle set (pos, vel, mass, kind, u at the end of a step), overwrites the state that
+ * gf_sim_init recomputed with the saved one: accelerations acc (n,3) and dt_ind (n) of the
+ * last evaluations, birth and no_cool_until, the last SPH evaluation's rho and du/dt (as
+ * gf_sim_read_hydro gives them; these four may be NULL), t, dt_grav and dt_gas; the tree of
+ * the next sub-steps is the one gf_sim_init built at the same positions. The run then goes on
+ * as if it had not stopped. */
+int gf_sim_restore(const double* acc, const double* dt_ind, const double* birth, const double* no_cool_until,
+                   const double* rho, const double* dudt, double t, double dt_grav, double dt_gas);
 /* Thermal update at the start of every step and sub-step of gf_sim_step, as
  * GalaxyFormation._thermodynamics (simulation.py:97-104) on the gas of the last SPH
  * evaluation: mode 0 = off (default), 1 = u += dt du/dt floored at u_floor (compression and

@@ -97,3 +97,21 @@ def test_pcg64_words_round_trip():
     subgrid.set_pcg64_words(h, w)
     assert np.array_equal(g.uniform(size=9), h.uniform(size=9))
     assert int(w[3]) & 1 == 1   # PCG increments are odd
+
+
+def test_snapshot_round_trip(tmp_path):
+    """A particle set and extra arrays survive save / load bit for bit."""
+    import numpy as np
+
+    from galaxy_formation_gb300 import snapshot, synthetic
+
+    d = synthetic.rotating_cloud(300, 200, seed=2)
+    p = tmp_path / "snap.npz"
+    snapshot.save(p, d["pos"], d["vel"], d["mass"], d["kind"], d["u"], t=1.25, extra=np.arange(3))
+    s = snapshot.load(p)
+    for k in snapshot.PARTICLE_KEYS:
+        assert np.array_equal(s[k], d[k]) and s[k].dtype == np.asarray(d[k]).dtype
+    assert float(s["t"]) == 1.25 and np.array_equal(s["extra"], np.arange(3))
+    import pytest
+    with pytest.raises(ValueError):
+        snapshot.save(p, d["pos"][:10], d["vel"], d["mass"], d["kind"], d["u"])
