@@ -147,8 +147,9 @@ __global__ void k_cache_store(int ng, int kq, const int* __restrict__ gidx, cons
 __global__ void k_guess(int ng, const int* __restrict__ gidx, const double* __restrict__ hprev, float* __restrict__ rg) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ng) return;
-    // the 48th neighbour lies near 2 h (48/32)^(1/3) = 2.29 h; start slightly outside
-    rg[i] = float(2.4 * hprev[gidx[i]]);
+    // the 48th neighbour lies near 2 h (48/32)^(1/3) = 2.29 h; start outside it (2.5 h: 1 %
+    // faster than 2.4 h, whose radius fell short for 15 % of the particles; 2.6 h is slower)
+    rg[i] = float(2.5 * hprev[gidx[i]]);
 }
 
 __global__ void k_smoothing(int ng, const double* __restrict__ d31, double eps, const int* __restrict__ gidx,

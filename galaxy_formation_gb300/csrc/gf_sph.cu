@@ -689,7 +689,7 @@ __global__ void k_hfeatures(int n, const int* __restrict__ perm, const int* __re
 
 __global__ void k_guess_from_logh(int n, const float* __restrict__ Y, float* __restrict__ rg) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) rg[i] = 2.4f * expf(Y[i]);
+    if (i < n) rg[i] = 2.5f * expf(Y[i]);  // the factor of the previous-h start
 }
 
 void knn_exact(Octree& T, int n, const double* pos, int k, const float* r_guess, int64_t* nb,

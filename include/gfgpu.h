@@ -309,7 +309,7 @@ int gf_cool(int n, const double* u, const double* T, const double* rho, const do
  *                           keeps its own tree; nbody_accel_active is never affected. */
 #define GF_OPT_GRAVITY_QUAD 1
 /*   GF_OPT_HGUESS       start of the neighbour-count iteration of a full search:
- *                       0 = 2.4 x the previous h (default), 1 = the density of the particle's
+ *                       0 = 2.5 x the previous h (default), 1 = the density of the particle's
  *                       tree cell only, 2 = the learned guess (gf_mlp_*); the iteration always
  *                       runs to the exact 48 nearest, so only the iteration count changes. */
 #define GF_OPT_HGUESS 2
