@@ -595,6 +595,9 @@ def run_learned(args, world, rank, local):
     tr = G.train_hguess(collected=True)
     torch, lib, L = G.torch, G.lib, G._lib
     theta = G.set_form("mixed_learned")
+    # the geometric opening criterion here: the relative one takes its error scale from the
+    # previous evaluation, which differs between the three runs compared bit for bit below
+    lib.gf_set_option(L.OPT_GRAVITY_REL, 0)
     res = {}
     pos = G.T["pos"].clone()
     for mode, name in ((1, "cell_density"), (2, "learned"), (0, "previous_h")):
