@@ -53,11 +53,12 @@ PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # theta, quadrupole gravity, float32 SPH, h guess (0 previous h, 2 learned), relative opening
 # tolerance (0: geometric criterion at theta; > 0: the relative criterion once every particle
 # has a previous gravity, with theta used for the first evaluation), walk items merged from
-# sibling groups up to this many particles (0: the reference's groups)
+# sibling groups up to this many particles (0: the reference's groups), monopole tolerance of
+# accepted nodes (0: every accepted node to quadrupole order)
 FORMS = {
-    "plain": (0.7, 0, 0, 0, 0.0, 0),
-    "plain_matched": (0.15, 0, 0, 0, 0.0, 0),
-    "mixed_learned": (0.55, 1, 1, 2, 3.5e-3, 40),
+    "plain": (0.7, 0, 0, 0, 0.0, 0, 0.0),
+    "plain_matched": (0.15, 0, 0, 0, 0.0, 0, 0.0),
+    "mixed_learned": (0.55, 1, 1, 2, 3.5e-3, 40, 2e-4),
 }
 # flops per interaction (an FMA counting 2): monopole pair (cpp/nbody.cpp:398-402 in float32)
 # and the softened quadrupole node term of the mixed walk
@@ -261,13 +262,14 @@ class Gpu:
         self.flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=self.dev)  # 256 MB > L2
 
     def set_form(self, form):
-        theta, quad, sph32, hguess, rel, merge = FORMS[form]
+        theta, quad, sph32, hguess, rel, merge, relq = FORMS[form]
         L, lib = self._lib, self.lib
         lib.gf_set_option(L.OPT_GRAVITY_QUAD, quad)
         lib.gf_set_option(L.OPT_SPH_FLOAT32, sph32)
         lib.gf_set_option(L.OPT_HGUESS, hguess)
         lib.gf_set_option(L.OPT_GRAVITY_REL, rel)  # the next evaluation sets the error scale
         lib.gf_set_option(L.OPT_WALK_MERGE, merge)
+        lib.gf_set_option(L.OPT_GRAVITY_REL_MONO, relq)
         return theta
 
     def step(self, theta, pos=None, kind=None, sph=1):
@@ -539,11 +541,12 @@ def run_gpu(args, world, rank, local):
 
     def summary(f):
         r = res[f]
-        th, quad_f, sph32, hg, rel, merge = FORMS[f]
+        th, quad_f, sph32, hg, rel, merge, relq = FORMS[f]
         out = {"value": r["value"], "ms_per_step": r["ms_per_step"], "theta": th,
                "gravity": "quadrupole float32 + Kahan" if quad_f else "monopole float32 (reference)",
                "opening": (f"relative, alpha {rel:g} with a geometric floor at theta 1 (error scale: the "
-                           f"previous evaluation's gravity; theta {th} before it)") if rel else
+                           f"previous evaluation's gravity; theta {th} before it); accepted nodes with a "
+                           f"quadrupole term below {relq:g} a_min as monopoles") if rel else
                           f"geometric, theta {th} (cpp/nbody.cpp:104-106)",
                "walk_items": (f"runs of sibling groups of <= {merge} particles, own spheres" if merge else
                               "the reference's groups (cpp/nbody.cpp:235-243)"),
@@ -563,7 +566,7 @@ def run_gpu(args, world, rank, local):
         "data": "synthetic",
         "config": {"workload": workload_name(n_gas, n - n_gas), "particles": n, "gas": n_gas,
                    "form": head, "theta": FORMS[head][0], "relative_opening_alpha": FORMS[head][4],
-                   "walk_merge": FORMS[head][5],
+                   "walk_merge": FORMS[head][5], "monopole_alpha": FORMS[head][6],
                    "eps_kpc": params.EPS_KPC,
                    "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
         "roofline": roof,

@@ -100,6 +100,7 @@ OPT_WALK_CHUNK = 4
 OPT_WALK_GROUP = 5
 OPT_GRAVITY_REL = 6
 OPT_WALK_MERGE = 7
+OPT_GRAVITY_REL_MONO = 8
 MLP_PARAMS = 4545
 
 STAGES = ["tree_build", "tree_refit", "walk", "group_prep", "knn", "knn_tree", "sph_density",

@@ -576,6 +576,10 @@ int gf_set_option(int key, double value) {
                 require(value >= 0 && value <= 128, "walk merge is 0..128");
                 F.walk_merge = int(value);
                 break;
+            case GF_OPT_GRAVITY_REL_MONO:
+                require(value >= 0 && value < 1, "monopole tolerance is in [0, 1)");
+                F.grav_rel_mono = value;
+                break;
             case GF_OPT_GRAVITY_REL:
                 require(value >= 0 && value < 1, "relative opening tolerance is in [0, 1)");
                 F.grav_rel = value;
@@ -597,6 +601,7 @@ double gf_get_option(int key) {
         case GF_OPT_WALK_GROUP: return F.walk_group;
         case GF_OPT_GRAVITY_REL: return F.grav_rel;
         case GF_OPT_WALK_MERGE: return F.walk_merge;
+        case GF_OPT_GRAVITY_REL_MONO: return F.grav_rel_mono;
         default: return -1.0;
     }
 }

@@ -344,7 +344,7 @@ void ForceEngine::evaluate(const ForceArgs& a, cudaStream_t s) {
     }
     T.merge_cap = gravity_quad ? walk_merge : 0;
     T.prepare_walk(a.active, s, a.walk_chunk ? a.walk_chunk : walk_chunk, rel ? acc_grav.as<double>() : nullptr,
-                   rel ? float(grav_rel) : 0.f);
+                   rel ? float(grav_rel) : 0.f, rel ? float(grav_rel_mono) : 0.f);
     T.walk(a.eps, acc_grav.as<double>(), s, nullptr, a.walk_npl);
     if (!a.active) have_aold = true;  // every particle has a previous gravity now
 

@@ -59,6 +59,7 @@ struct ForceEngine {
     // evaluation of all particles) uses the geometric criterion; later ones a geometric floor
     // at theta = kRelFloorTheta combined with the relative test.
     double grav_rel = 0.0;
+    double grav_rel_mono = 0.0;  // accepted nodes with quadrupole term below this x a_min: monopoles
     bool have_aold = false;
     static constexpr double kRelFloorTheta = 1.0;
     int hguess = 0;          // start of the neighbour-count iteration: 0 previous h, 1 cell
@@ -92,7 +93,7 @@ struct ForceEngine {
         for (unsigned long long v : {(unsigned long long)sph_float32, (unsigned long long)gravity_quad,
                                      (unsigned long long)walk_chunk, (unsigned long long)walk_group,
                                      (unsigned long long)hguess, rel_bits, (unsigned long long)have_aold,
-                                     (unsigned long long)walk_merge})
+                                     (unsigned long long)walk_merge, (unsigned long long)(grav_rel_mono * 1e12)})
             k = (k ^ v) * 1099511628211ull;
         return k;
     }

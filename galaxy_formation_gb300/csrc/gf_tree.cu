@@ -508,11 +508,13 @@ __global__ void k_moments(MomentArgs A) {
 // the octupole-order estimate M b^3 / r^5 of the truncation error is at most alpha times the
 // group's smallest previous acceleration (the relative criterion of Springel 2005, GADGET-2,
 // to the next order). b bounds the distance of the node's mass from its centre of mass.
-// rho = M^(1/5) b^(3/5) in logarithms, so no intermediate overflows in float32.
-__device__ __forceinline__ float rel_radius(float m, float ox, float oy, float oz, float half) {
-    if (!(m > 0.f)) return 0.f;
-    const float b = sqrtf(ox * ox + oy * oy + oz * oz) + 1.7320508f * half;
-    return exp2f(0.2f * log2f(m) + 0.6f * log2f(b));
+// rho = M^(1/5) b^(3/5) in logarithms, so no intermediate overflows in float32. The second
+// radius, (M b^2)^(1/4), is the quadrupole-order one: beyond rho_q (alpha_q a_min)^(-1/4) the
+// node's quadrupole term itself is below alpha_q a_min and the walk takes its monopole alone.
+__device__ __forceinline__ float2 rel_radii(float m, float ox, float oy, float oz, float half) {
+    if (!(m > 0.f)) return make_float2(0.f, 0.f);
+    const float lm = log2f(m), lb = log2f(sqrtf(ox * ox + oy * oy + oz * oz) + 1.7320508f * half);
+    return make_float2(exp2f(0.2f * lm + 0.6f * lb), exp2f(0.25f * lm + 0.5f * lb));
 }
 
 // Mixed form: monopole and traceless quadrupole in one bottom-up pass, float32 with
@@ -647,6 +649,7 @@ struct RefitBfsArgs {
     float4* wb;   // open_r, first, code, rho
     float4* wq;   // Qxx, Qyy, Qxy, Qxz
     float2* wt;   // Qyz, T
+    float* wrq;   // quadrupole-order radius
     float* ndisp; // breadth-first
     const float4* p4;
     const float* pdisp;
@@ -660,7 +663,9 @@ __device__ __forceinline__ float4 finalize_bfs(const RefitBfsArgs& A, int b, con
     const float4 g = A.wgeo[b];
     const float ox = c.x - g.x, oy = c.y - g.y, oz = c.z - g.z;
     A.wb[b].x = 2.f * (g.w + dm) / A.theta + sqrtf(ox * ox + oy * oy + oz * oz);
-    A.wb[b].w = rel_radius(c.w, ox, oy, oz, g.w + dm);
+    const float2 rr = rel_radii(c.w, ox, oy, oz, g.w + dm);
+    A.wb[b].w = rr.x;
+    A.wrq[b] = rr.y;
     A.ndisp[b] = dm;
     return c;
 }
@@ -789,7 +794,7 @@ __global__ void k_walk_fill(int nn, const int4* __restrict__ n_i4, const int* __
                             float4* __restrict__ wgeo, int* __restrict__ leaf_of,
                             const float4* __restrict__ q4, const float2* __restrict__ qyz,
                             float4* __restrict__ wq, const int* __restrict__ parent, int* __restrict__ wparent,
-                            float2* __restrict__ wt, const int* __restrict__ nn_dev) {
+                            float2* __restrict__ wt, float* __restrict__ wrq, const int* __restrict__ nn_dev) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= live_nodes(nn, nn_dev)) return;
     const int4 q = n_i4[k];
@@ -806,12 +811,13 @@ __global__ void k_walk_fill(int nn, const int4* __restrict__ n_i4, const int* __
     }
     const float4 c = mom[k];
     wa[b] = c;
-    float rho = 0.f;
+    float2 rr = make_float2(0.f, 0.f);
     if (q4) {
         const float4 g = geo[k];
-        rho = rel_radius(c.w, c.x - g.x, c.y - g.y, c.z - g.z, g.w);
+        rr = rel_radii(c.w, c.x - g.x, c.y - g.y, c.z - g.z, g.w);
+        wrq[b] = rr.y;
     }
-    wb[b] = make_float4(open_r[k], __int_as_float(first), __int_as_float(code), rho);
+    wb[b] = make_float4(open_r[k], __int_as_float(first), __int_as_float(code), rr.x);
     if (wgeo) wgeo[b] = geo[k];
     if (q4) {
         wq[b] = q4[k];
@@ -929,7 +935,7 @@ void Octree::reserve_graph_build() {
     pdisp.get<float>(n);
     work.get<int4>(std::max(size_t(node_cap), size_t(n)) + 1);
     sphere.get<float4>(std::max(size_t(node_cap), size_t(n)) + 1);
-    if (quad) item_gam.get<float>(std::max(size_t(node_cap), size_t(n)) + 1);
+    if (quad) item_gam.get<float2>(std::max(size_t(node_cap), size_t(n)) + 1);
     reserve_scan_sort(std::max(n, node_cap), &scratch);
     deep_sort_attr();
 }
@@ -1104,7 +1110,8 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
                                            quad ? n_quad.as<float4>() : nullptr, quad ? n_qyz.as<float2>() : nullptr,
                                            quad ? w_q.get<float4>(cap) : nullptr, par,
                                            bfs_geo ? w_parent.get<int>(cap) : nullptr,
-                                           quad ? w_t.get<float2>(cap) : nullptr, nn_dev);
+                                           quad ? w_t.get<float2>(cap) : nullptr, quad ? w_rq.get<float>(cap) : nullptr,
+                                           nn_dev);
     GF_CHECK_LAUNCH();
     valid = true;
 }
@@ -1126,7 +1133,8 @@ void Octree::refit(const double* pos, const double* mass, cudaStream_t s) {
     GF_CUDA(cudaMemsetAsync(ctr, 0, sizeof(int) * size_t(span), s));
     if (quad) {  // mixed form: straight into the walk layout
         RefitBfsArgs A{span, nn_dev, theta_f, w_parent.as<int>(), w_geo.as<float4>(), ctr, w_a.as<float4>(),
-                       w_b.as<float4>(), w_q.as<float4>(), w_t.as<float2>(), n_disp.as<float>(), pp, pd};
+                       w_b.as<float4>(), w_q.as<float4>(), w_t.as<float2>(), w_rq.as<float>(), n_disp.as<float>(), pp,
+                       pd};
         k_refit_bfs_quad32<<<ngrid, kThreads, 0, s>>>(A);
         GF_CHECK_LAUNCH();
         return;
@@ -1158,7 +1166,7 @@ void Octree::refit(const double* pos, const double* mass, cudaStream_t s) {
                                            quad ? n_quad.as<float4>() : nullptr, quad ? n_qyz.as<float2>() : nullptr,
                                            quad ? w_q.as<float4>() : nullptr, n_parent.as<int>(),
                                            want_knn ? w_parent.as<int>() : nullptr,
-                                           quad ? w_t.as<float2>() : nullptr, nn_dev);
+                                           quad ? w_t.as<float2>() : nullptr, quad ? w_rq.as<float>() : nullptr, nn_dev);
     GF_CHECK_LAUNCH();
 }
 

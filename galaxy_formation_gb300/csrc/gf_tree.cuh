@@ -63,6 +63,7 @@ struct Octree {
     DevBuf w_geo;     // float4 {gx, gy, gz, half} of the cell, breadth-first order
     DevBuf w_q;       // float4 {Qxx, Qyy, Qxy, Qxz} (quadrupole trees)
     DevBuf w_t;       // float2 {Qyz, T = sum m |d|^2 about the centre of mass} (quadrupole trees)
+    DevBuf w_rq;      // float (M b^2)^(1/4): the quadrupole-order radius (quadrupole trees)
     DevBuf n_quad, n_qyz;  // traceless quadrupole about the centre of mass, preorder
     DevBuf bfs_key, bfs_key_alt, bfs_val, bfs_val_alt;
     // neighbour search extras (tree order): float32 remainders x - float(x) and the
@@ -77,7 +78,7 @@ struct Octree {
     bool kahan = false;          // walk: compensated accumulation of the tile sums
     // groups and walk work list
     DevBuf gflag, gscan, groups, work, sphere;
-    DevBuf item_gam;  // per work item: (alpha min |a_old|)^(-1/5), 0 = geometric criterion only
+    DevBuf item_gam;  // per work item: float2 {(alpha a_min)^(-1/5), (alpha_q a_min)^(-1/4)}, 0 = off
     DevBuf root, counts;
     ScanScratch scratch;  // this tree's scan / sort scratch (trees may build on different streams)
     TreeCounts* h_counts = nullptr;  // pinned
@@ -95,8 +96,10 @@ struct Octree {
     // cuts each group's active particles into items of <= chunk with their own spheres.
     // aold (quadrupole trees, may be null): the previous accelerations (n,3) in original order,
     // for the relative opening criterion with tolerance alpha.
+    // alpha_q > 0: accepted nodes whose quadrupole term is below alpha_q a_min are taken as
+    // monopoles.
     void prepare_walk(const uint8_t* active, cudaStream_t s, int chunk = 0, const double* aold = nullptr,
-                      float alpha = 0.f);
+                      float alpha = 0.f, float alpha_q = 0.f);
     // pot (monopole trees, may be null): softened potentials of the walked particles
     // npl: nodes per lane and round of the mixed walk (2, or 8 for walks of a few items)
     void walk(double eps, double* acc, cudaStream_t s, double* pot = nullptr, int npl = 2);

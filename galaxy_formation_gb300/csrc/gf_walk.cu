@@ -49,8 +49,10 @@ __device__ __forceinline__ float aold_mag(const double* aold, int k) {
     return float(sqrt(x * x + y * y + z * z));
 }
 
-__device__ __forceinline__ float rel_gamma(float alpha, float amin) {
-    return (alpha > 0.f && amin > 0.f && amin < 3e38f) ? exp2f(-0.2f * log2f(alpha * amin)) : 0.f;
+// (alpha a_min)^(-1/5) and (alpha_q a_min)^(-1/4) (0 where off or a_min is not positive)
+__device__ __forceinline__ float2 rel_gamma(float alpha, float alpha_q, float amin) {
+    if (!(alpha > 0.f && amin > 0.f && amin < 3e38f)) return make_float2(0.f, 0.f);
+    return make_float2(exp2f(-0.2f * log2f(alpha * amin)), alpha_q > 0.f ? exp2f(-0.25f * log2f(alpha_q * amin)) : 0.f);
 }
 
 // One work item over the particles [b, e) of the tree (a group, or a run of sibling groups):
@@ -59,7 +61,8 @@ __device__ __forceinline__ float rel_gamma(float alpha, float amin) {
 __device__ __forceinline__ void emit_item(int b, int e, const float4* __restrict__ p4, const int* __restrict__ perm,
                                           const uint8_t* __restrict__ active, TreeCounts* cnt,
                                           int4* __restrict__ work, float4* __restrict__ sphere,
-                                          const double* __restrict__ aold, float alpha, float* __restrict__ gam) {
+                                          const double* __restrict__ aold, float alpha, float alpha_q,
+                                          float2* __restrict__ gam) {
     const int lane = threadIdx.x & 31;
     int nact = 0;
     float x0 = 1e30f, y0 = 1e30f, z0 = 1e30f, x1 = -1e30f, y1 = -1e30f, z1 = -1e30f;
@@ -97,7 +100,7 @@ __device__ __forceinline__ void emit_item(int b, int e, const float4* __restrict
     if (lane == 0) {
         work[slot] = make_int4(b, e - b, nact, 0);
         sphere[slot] = make_float4(bx, by, bz, sqrtf(br2));
-        if (gam) gam[slot] = aold ? rel_gamma(alpha, amin) : 0.f;
+        if (gam) gam[slot] = aold ? rel_gamma(alpha, alpha_q, amin) : make_float2(0.f, 0.f);
     }
 }
 
@@ -105,8 +108,8 @@ __global__ void k_group_prep(const int* __restrict__ groups, const int4* __restr
                              const float4* __restrict__ p4, const int* __restrict__ perm,
                              const uint8_t* __restrict__ active, TreeCounts* cnt,
                              int4* __restrict__ work, float4* __restrict__ sphere, int chunk,
-                             const double* __restrict__ aold, float alpha, float* __restrict__ gam,
-                             const int* __restrict__ parent, int merge) {
+                             const double* __restrict__ aold, float alpha, float alpha_q,
+                             float2* __restrict__ gam, const int* __restrict__ parent, int merge) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = lanemask_lt();
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -167,7 +170,7 @@ __global__ void k_group_prep(const int* __restrict__ groups, const int4* __restr
                     work[slot] = make_int4(b, q.y, P, r0);
                     // float32 rounding of the centre: pad so every member stays inside
                     sphere[slot] = make_float4(bx, by, bz, sqrtf(br2) * (1.f + 1e-6f));
-                    if (gam) gam[slot] = aold ? rel_gamma(alpha, amin) : 0.f;
+                    if (gam) gam[slot] = aold ? rel_gamma(alpha, alpha_q, amin) : make_float2(0.f, 0.f);
                 }
                 if (P < chunk) break;
                 r0 += chunk;
@@ -189,13 +192,13 @@ __global__ void k_group_prep(const int* __restrict__ groups, const int4* __restr
                     if (rc + c2 > merge) break;
                     rc += c2;
                 }
-                emit_item(qj.x, qj.x + rc, p4, perm, active, cnt, work, sphere, aold, alpha, gam);
+                emit_item(qj.x, qj.x + rc, p4, perm, active, cnt, work, sphere, aold, alpha, alpha_q, gam);
                 j = j2;
                 if (j >= ng || parent[groups[j]] != par) break;
             }
             continue;
         }
-        emit_item(b, e, p4, perm, active, cnt, work, sphere, aold, alpha, gam);
+        emit_item(b, e, p4, perm, active, cnt, work, sphere, aold, alpha, alpha_q, gam);
     }
 }
 
@@ -337,9 +340,10 @@ __device__ __forceinline__ void eval_quad(const float4* tile, const float4* ntA,
 template <bool QUAD, bool POT = false, int NPL = (QUAD ? 2 : 1)>
 __global__ void __launch_bounds__(kWalkWarps * 32, QUAD ? (NPL > 2 ? 1 : 4) : 5) k_walk(
     const float4* __restrict__ wa, const float4* __restrict__ wb, const float4* __restrict__ wq,
-    const float2* __restrict__ wt, const float4* __restrict__ p4, const int* __restrict__ perm, const uint8_t* __restrict__ active,
-    const int4* __restrict__ work, const float4* __restrict__ sphere, const float* __restrict__ gam, TreeCounts* cnt,
-    int nn, float eps2, double* __restrict__ acc, uint32_t* status, double* __restrict__ pot = nullptr) {
+    const float2* __restrict__ wt, const float* __restrict__ wrq, const float4* __restrict__ p4,
+    const int* __restrict__ perm, const uint8_t* __restrict__ active, const int4* __restrict__ work,
+    const float4* __restrict__ sphere, const float2* __restrict__ gam, TreeCounts* cnt, int nn, float eps2,
+    double* __restrict__ acc, uint32_t* status, double* __restrict__ pot = nullptr) {
     static_assert(!(QUAD && POT), "potentials come from the monopole walk");
     using Smem = WarpSmem<QUAD, NPL>;
     constexpr int kNodesPerLane = NPL;
@@ -358,8 +362,10 @@ __global__ void __launch_bounds__(kWalkWarps * 32, QUAD ? (NPL > 2 ? 1 : 4) : 5)
         const int4 w = work[g];
         const float4 sph = sphere[g];
         // relative criterion: accept a node when its distance from the sphere exceeds both
-        // open_r (geometric) and rho * gm (rho = B.w: 0 outside quadrupole trees)
-        const float gm = QUAD ? gam[g] : 0.f;
+        // open_r (geometric) and rho * gm (rho = B.w: 0 outside quadrupole trees); take an
+        // accepted node as a monopole when that distance also exceeds rho_q * gq (gq > 0)
+        const float2 gg = QUAD ? gam[g] : make_float2(0.f, 0.f);
+        const float gm = gg.x, gq = gg.y;
         const int b = w.x, count = w.y, Pall = w.z, r0 = w.w;
         // Items hold <= kBatch particles except depth-48 leaves of coincident points; those
         // are evaluated in batches, each batch walking the tree again.
@@ -494,13 +500,16 @@ __global__ void __launch_bounds__(kWalkWarps * 32, QUAD ? (NPL > 2 ? 1 : 4) : 5)
                 __syncwarp();
             }
             float4 As[kNodesPerLane], Bs[kNodesPerLane];
+            float RQs[kNodesPerLane];
 #pragma unroll
             for (int i = 0; i < kNodesPerLane; ++i) {
                 As[i] = make_float4(0.f, 0.f, 0.f, 0.f);
                 Bs[i] = As[i];
+                RQs[i] = 0.f;
                 if (nodes[i] >= 0) {
                     As[i] = wa[nodes[i]];
                     Bs[i] = wb[nodes[i]];
+                    if (QUAD && gq > 0.f) RQs[i] = wrq[nodes[i]];
                 }
             }
 #pragma unroll
@@ -511,7 +520,10 @@ __global__ void __launch_bounds__(kWalkWarps * 32, QUAD ? (NPL > 2 ? 1 : 4) : 5)
             const float4 A = As[i], B = Bs[i];
             const float dx = A.x - sph.x, dy = A.y - sph.y, dz = A.z - sph.z;
             const float t = (QUAD ? fmaxf(B.x, B.w * gm) : B.x) + sph.w;
-            const bool accept = valid && (dx * dx + dy * dy + dz * dz > t * t);
+            const float dd2 = dx * dx + dy * dy + dz * dz;
+            const bool accept = valid && (dd2 > t * t);
+            const float tq = RQs[i] * gq + sph.w;
+            const bool mono = QUAD && accept && gq > 0.f && dd2 > tq * tq;  // quadrupole below alpha_q a_min
             const int first = __float_as_int(B.y), code = __float_as_int(B.z);
             const bool leaf = valid && !accept && code < 0;
             const bool open = valid && !accept && code > 0;
@@ -526,19 +538,29 @@ __global__ void __launch_bounds__(kWalkWarps * 32, QUAD ? (NPL > 2 ? 1 : 4) : 5)
             if (open) S.stack[sp + __popc(om & lt)] = (first << 4) | code;
             sp += npush;
 
-            // accepted nodes: monopole (reference) or monopole + quadrupole (mixed) entries
-            const unsigned am = __ballot_sync(0xffffffffu, accept);
-            const int na = __popc(am);
+            // accepted nodes: monopole (reference) or monopole + quadrupole (mixed) entries;
+            // the mixed form's far nodes (mono) join the monopole tile of the leaf particles
             if (QUAD) {
-                if (fillN + na > Smem::kNodeTile) GF_WALK_FLUSH();
-                if (accept) {
-                    const int slot_n = fillN + __popc(am & lt);
+                const unsigned qm = __ballot_sync(0xffffffffu, accept && !mono);
+                const int nq = __popc(qm);
+                if (fillN + nq > Smem::kNodeTile) GF_WALK_FLUSH();
+                if (accept && !mono) {
+                    const int slot_n = fillN + __popc(qm & lt);
                     S.ntA[slot_n] = A;
                     S.ntQ[slot_n] = wq[node];
                     S.ntYZ[slot_n] = wt[node];
                 }
-                fillN += na;
+                fillN += nq;
+                const unsigned mm = __ballot_sync(0xffffffffu, mono);
+                const int nm = __popc(mm);
+                if (nm) {
+                    if (fill + nm > Smem::kTile) GF_WALK_FLUSH();
+                    if (mono) S.tile[fill + __popc(mm & lt)] = A;
+                    fill += nm;
+                }
             } else {
+                const unsigned am = __ballot_sync(0xffffffffu, accept);
+                const int na = __popc(am);
                 if (fill + na > Smem::kTile) GF_WALK_FLUSH();
                 if (accept) S.tile[fill + __popc(am & lt)] = A;
                 fill += na;
@@ -644,7 +666,8 @@ __global__ void __launch_bounds__(kWalkWarps * 32, QUAD ? (NPL > 2 ? 1 : 4) : 5)
 
 }  // namespace
 
-void Octree::prepare_walk(const uint8_t* active, cudaStream_t s, int chunk, const double* aold, float alpha) {
+void Octree::prepare_walk(const uint8_t* active, cudaStream_t s, int chunk, const double* aold, float alpha,
+                          float alpha_q) {
     Context& C = ctx();
     TreeCounts* cnt = counts.as<TreeCounts>();
     GF_CUDA(cudaMemsetAsync(&cnt->num_work, 0, 2 * sizeof(int), s));  // num_work, walk_next
@@ -656,8 +679,8 @@ void Octree::prepare_walk(const uint8_t* active, cudaStream_t s, int chunk, cons
     k_group_prep<<<4 * C.sms, 256, 0, s>>>(groups.as<int>(), n_i4.as<int4>(), p4.as<float4>(),
                                           perm.as<int>(), active, cnt, work.get<int4>(cap),
                                           sphere.get<float4>(cap), active ? chunk : 0,
-                                          quad && alpha > 0.f ? aold : nullptr, alpha,
-                                          quad ? item_gam.get<float>(cap) : nullptr, n_parent.as<int>(),
+                                          quad && alpha > 0.f ? aold : nullptr, alpha, alpha_q,
+                                          quad ? item_gam.get<float2>(cap) : nullptr, n_parent.as<int>(),
                                           quad && !(active && chunk > 0) ? merge_cap : 0);
     GF_CHECK_LAUNCH();
 }
@@ -677,22 +700,22 @@ void Octree::walk(double eps, double* acc, cudaStream_t s, double* pot, int npl)
     if (pot) {
         if (quad) throw Error(GF_ERR_ARG, "potentials come from the monopole walk");
         k_walk<false, true><<<bps_mono * C.sms, kWalkWarps * 32, 0, s>>>(
-            w_a.as<float4>(), w_b.as<float4>(), nullptr, nullptr, p4.as<float4>(), perm.as<int>(), active_ptr,
+            w_a.as<float4>(), w_b.as<float4>(), nullptr, nullptr, nullptr, p4.as<float4>(), perm.as<int>(), active_ptr,
             work.as<int4>(), sphere.as<float4>(), nullptr, counts.as<TreeCounts>(), node_cap, eps2, acc, C.d_status,
             pot);
     } else if (quad && npl > 2) {
         k_walk<true, false, 8><<<bps_quad * C.sms, kWalkWarps * 32, 0, s>>>(
-            w_a.as<float4>(), w_b.as<float4>(), w_q.as<float4>(), w_t.as<float2>(), p4.as<float4>(), perm.as<int>(),
-            active_ptr, work.as<int4>(), sphere.as<float4>(), item_gam.as<float>(), counts.as<TreeCounts>(), node_cap,
-            eps2, acc, C.d_status);
+            w_a.as<float4>(), w_b.as<float4>(), w_q.as<float4>(), w_t.as<float2>(), w_rq.as<float>(), p4.as<float4>(),
+            perm.as<int>(), active_ptr, work.as<int4>(), sphere.as<float4>(), item_gam.as<float2>(),
+            counts.as<TreeCounts>(), node_cap, eps2, acc, C.d_status);
     } else if (quad) {
         k_walk<true><<<bps_quad * C.sms, kWalkWarps * 32, 0, s>>>(
-            w_a.as<float4>(), w_b.as<float4>(), w_q.as<float4>(), w_t.as<float2>(), p4.as<float4>(), perm.as<int>(),
-            active_ptr, work.as<int4>(), sphere.as<float4>(), item_gam.as<float>(), counts.as<TreeCounts>(), node_cap,
-            eps2, acc, C.d_status);
+            w_a.as<float4>(), w_b.as<float4>(), w_q.as<float4>(), w_t.as<float2>(), w_rq.as<float>(), p4.as<float4>(),
+            perm.as<int>(), active_ptr, work.as<int4>(), sphere.as<float4>(), item_gam.as<float2>(),
+            counts.as<TreeCounts>(), node_cap, eps2, acc, C.d_status);
     } else {
         k_walk<false><<<bps_mono * C.sms, kWalkWarps * 32, 0, s>>>(
-            w_a.as<float4>(), w_b.as<float4>(), nullptr, nullptr, p4.as<float4>(), perm.as<int>(), active_ptr,
+            w_a.as<float4>(), w_b.as<float4>(), nullptr, nullptr, nullptr, p4.as<float4>(), perm.as<int>(), active_ptr,
             work.as<int4>(), sphere.as<float4>(), nullptr, counts.as<TreeCounts>(), node_cap, eps2, acc, C.d_status);
     }
     GF_CHECK_LAUNCH();

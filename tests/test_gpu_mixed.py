@@ -220,3 +220,36 @@ def test_merged_walk_items(gpulib):
         assert errs[merge][0] < 1e-3 and errs[merge][0] <= 1.1 * errs[0][0], errs
         assert errs[merge][1] < 5e-3, errs
 
+
+
+def test_monopole_tolerance_for_far_nodes(gpulib):
+    """GF_OPT_GRAVITY_REL_MONO: accepted nodes whose quadrupole term is below alpha_q a_min are
+    taken as monopoles; fewer quadrupole interactions, the same interaction count, and the
+    accuracy bar against the float64 direct sum kept."""
+    from galaxy_formation_gb300 import _lib, params, synthetic
+    from galaxy_formation_gb300.engine import Engine
+
+    lib = gpulib
+    d = synthetic.make_config(2, scale=0.05)
+    n = len(d["mass"])
+    tgt = np.random.default_rng(6).choice(n, 1000, replace=False)
+    exact = Engine().gravity_direct_targets(d["pos"], d["mass"], tgt, params.EPS)
+    dt = np.empty(n)
+    res = {}
+    lib.gf_set_option(_lib.OPT_GRAVITY_QUAD, 1)
+    lib.gf_set_option(_lib.OPT_GRAVITY_REL, 3.5e-3)
+    lib.gf_set_option(_lib.OPT_WALK_MERGE, 40)
+    try:
+        for relq in (0.0, 2e-4):
+            lib.gf_set_option(_lib.OPT_GRAVITY_REL_MONO, relq)
+            acc = np.empty((n, 3))
+            for _ in range(2):
+                _lib.check(lib.gf_accelerations(n, d["pos"], d["vel"], d["mass"], d["kind"], d["u"], 0.55,
+                                                params.EPS, params.GAMMA, 1.0, 2.0, None, 1, 0, 1, acc, dt))
+            res[relq] = (np.percentile(rel_err(acc[tgt], exact), 99), lib.gf_walk_pairs(), lib.gf_walk_quad_pairs())
+    finally:
+        for key in (_lib.OPT_GRAVITY_REL_MONO, _lib.OPT_WALK_MERGE, _lib.OPT_GRAVITY_REL, _lib.OPT_GRAVITY_QUAD):
+            lib.gf_set_option(key, 0)
+    (e0, p0, q0), (e1, p1, q1) = res[0.0], res[2e-4]
+    assert p1 == p0 and q1 < 0.85 * q0, res
+    assert e1 < 1e-3 and e1 < 1.2 * e0, res
