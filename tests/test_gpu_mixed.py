@@ -251,5 +251,7 @@ def test_monopole_tolerance_for_far_nodes(gpulib):
         for key in (_lib.OPT_GRAVITY_REL_MONO, _lib.OPT_WALK_MERGE, _lib.OPT_GRAVITY_REL, _lib.OPT_GRAVITY_QUAD):
             lib.gf_set_option(key, 0)
     (e0, p0, q0), (e1, p1, q1) = res[0.0], res[2e-4]
-    assert p1 == p0 and q1 < 0.85 * q0, res
+    # the same acceptance (to the rounding of the error scale, which each run takes from the
+    # one before), fewer quadrupoles
+    assert abs(p1 - p0) <= 1e-3 * p0 and q1 < 0.85 * q0, res
     assert e1 < 1e-3 and e1 < 1.2 * e0, res
