@@ -9,13 +9,15 @@
 //                              bitonic sort of the (<= 64) candidates in registers.
 //   exact k nearest .......... replaces cKDTree(p).query(p, k) (sph.py:165-166):
 //                              octree of the points (same builder as gravity); one warp per
-//                              query walks it with a radius R, collecting points within R
-//                              (float32 distances from hi/lo split coordinates) until the
-//                              count lies in [k, 128] — the radius iteration, Newton steps
-//                              on count ~ R^3 from a guess (previous h, or the leaf's cell
-//                              density). The collected points are sorted, the k nearest plus
-//                              near-ties at the boundary are re-measured in float64 and
-//                              sorted again, so the result is the exact float64 kNN.
+//                              two consecutive queries walks it with a radius per query,
+//                              collecting the points within each radius (float32 distances
+//                              from hi/lo split coordinates) until the count lies in
+//                              [k, 128] — the radius iteration, Newton steps on
+//                              count ~ R^3 from a guess (previous h, the learned guess, or
+//                              the leaf's cell density). The collected points are sorted,
+//                              the k nearest plus near-ties at the boundary are re-measured
+//                              in float64 and sorted again, so the result is the exact
+//                              float64 kNN.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>

@@ -15,6 +15,11 @@
 //     the group owns 1..32 lanes (lanes split the tile when the group is small, two
 //     particles per lane when it has more than 32 active particles);
 //   * pair term as cpp/nbody.cpp:398-402 in float32: a += m d / (|d|^2 + eps^2)^(3/2).
+// The mixed form (QUAD) walks work items (groups, runs of sibling groups, or chunks of a
+// group's active particles), accepts nodes by the geometric or the relative criterion,
+// keeps a second tile of quadrupole nodes (far accepted nodes may join the monopole tile),
+// evaluates both tiles with 4 particles per lane and adds each tile's partial sums to Kahan
+// totals.
 // Accelerations are written as float64 into acc[3*k] for original index k (active only).
 #include <algorithm>
 
