@@ -228,14 +228,45 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_upsweep(const uint64_t* __res
     hist[threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
 }
 
+// Block d scans digit d's per-tile counts (row d of the digit-major histogram) in place,
+// exclusively, and writes the digit's total to tot[d]: one launch instead of a device-wide
+// scan of the whole histogram (three launches), since the digit bases come from the 256 totals.
+__global__ void __launch_bounds__(kRsThreads) k_rs_rows(int* __restrict__ hist, int tiles, int* __restrict__ tot) {
+    __shared__ int s_warp[33];
+    int* row = hist + size_t(blockIdx.x) * tiles;
+    int carry = 0;
+    for (int base = 0; base < tiles; base += kRsThreads * kScanItems) {
+        int v[kScanItems];
+        int acc = 0;
+        const int b0 = base + threadIdx.x * kScanItems;
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            v[k] = (b0 + k < tiles) ? row[b0 + k] : 0;
+            acc += v[k];
+        }
+        int t;
+        int ex = block_excl_scan(acc, s_warp, &t) + carry;
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            if (b0 + k < tiles) row[b0 + k] = ex;
+            ex += v[k];
+        }
+        carry += t;
+    }
+    if (threadIdx.x == 0) tot[blockIdx.x] = carry;
+}
+
 __global__ void __launch_bounds__(kRsThreads) k_rs_downsweep(
     const uint64_t* __restrict__ kin, const int* __restrict__ vin, uint64_t* __restrict__ kout,
-    int* __restrict__ vout, int n, int shift, const int* __restrict__ offs, int tiles) {
+    int* __restrict__ vout, int n, int shift, const int* __restrict__ offs, const int* __restrict__ tot,
+    int tiles) {
     __shared__ int s_cnt[kRsWarps][256];
     __shared__ int s_off[256];
+    __shared__ int s_warp[33];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int w = 0; w < kRsWarps; ++w) s_cnt[w][threadIdx.x] = 0;
-    s_off[threadIdx.x] = offs[threadIdx.x * tiles + blockIdx.x];
+    // output base of this tile's digit t: keys of smaller digits + digit t in earlier tiles
+    s_off[threadIdx.x] = block_excl_scan(tot[threadIdx.x], s_warp, nullptr) + offs[threadIdx.x * tiles + blockIdx.x];
     __syncthreads();
     const int base = blockIdx.x * kRsTile + warp * kRsWarpItems;
     uint64_t k[kRsItems];
@@ -282,7 +313,7 @@ void reserve_scan_sort(int n, ScanScratch* sc) {
     DevBuf& sort_tmp = sc ? sc->sort_tmp : g_ctx.sort_tmp;
     DevBuf& scan_tmp = sc ? sc->scan_tmp : g_ctx.scan_tmp;
     const int rs_tiles = div_up(std::max(n, 1), kRsTile);
-    sort_tmp.get<int>(size_t(256) * rs_tiles * 2);
+    sort_tmp.get<int>(size_t(256) * rs_tiles + 256);
     const int scan_n = std::max(n, 256 * rs_tiles);
     scan_tmp.get<int>(size_t(div_up(scan_n, kScanTile)) + 1);
 }
@@ -291,16 +322,17 @@ void radix_sort_pairs(uint64_t* keys, int* vals, uint64_t* keys_alt, int* vals_a
                       int bit_lo, int bit_hi, cudaStream_t s, ScanScratch* sc) {
     if (n <= 1) return;
     const int tiles = div_up(n, kRsTile);
-    int* hist = (sc ? sc->sort_tmp : g_ctx.sort_tmp).get<int>(size_t(256) * tiles * 2);
-    int* offs = hist + size_t(256) * tiles;
+    int* hist = (sc ? sc->sort_tmp : g_ctx.sort_tmp).get<int>(size_t(256) * tiles + 256);
+    int* tot = hist + size_t(256) * tiles;
     uint64_t *ka = keys, *kb = keys_alt;
     int *va = vals, *vb = vals_alt;
     int passes = 0;
     for (int shift = bit_lo; shift < bit_hi; shift += 8) {
         k_rs_upsweep<<<tiles, kRsThreads, 0, s>>>(ka, n, shift, hist, tiles);
         GF_CHECK_LAUNCH();
-        exclusive_scan(hist, offs, 256 * tiles, nullptr, s, sc);
-        k_rs_downsweep<<<tiles, kRsThreads, 0, s>>>(ka, va, kb, vb, n, shift, offs, tiles);
+        k_rs_rows<<<256, kRsThreads, 0, s>>>(hist, tiles, tot);
+        GF_CHECK_LAUNCH();
+        k_rs_downsweep<<<tiles, kRsThreads, 0, s>>>(ka, va, kb, vb, n, shift, hist, tot, tiles);
         GF_CHECK_LAUNCH();
         std::swap(ka, kb);
         std::swap(va, vb);
