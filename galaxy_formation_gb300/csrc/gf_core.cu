@@ -184,6 +184,36 @@ __global__ void k_scan_tiles(const int* __restrict__ in, int* __restrict__ out, 
     }
 }
 
+// Second launch of the two-launch scan: each block adds up the tile sums before its own tile
+// (at most kScanDirectTiles of them: a few KB of L2 reads per block) and scans its tile; the
+// last block writes the total.
+constexpr int kScanDirectTiles = 2048;
+
+__global__ void k_scan_tiles_direct(const int* __restrict__ in, int* __restrict__ out, int n,
+                                    const int* __restrict__ sums, int* __restrict__ total) {
+    __shared__ int s_warp[33];
+    int before = 0;
+    for (int t = threadIdx.x; t < int(blockIdx.x); t += kScanThreads) before += sums[t];
+    int prefix;
+    block_excl_scan(before, s_warp, &prefix);
+    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    int v[kScanItems];
+    int acc = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        v[k] = (base + k < n) ? in[base + k] : 0;
+        acc += v[k];
+    }
+    int tile_total;
+    int ex = block_excl_scan(acc, s_warp, &tile_total) + prefix;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        if (base + k < n) out[base + k] = ex;
+        ex += v[k];
+    }
+    if (total && threadIdx.x == 0 && blockIdx.x == gridDim.x - 1) *total = prefix + tile_total;
+}
+
 void exclusive_scan(const int* in, int* out, int n, int* total, cudaStream_t s, ScanScratch* sc) {
     if (n <= 0) {
         if (total) GF_CUDA(cudaMemsetAsync(total, 0, sizeof(int), s));
@@ -193,6 +223,11 @@ void exclusive_scan(const int* in, int* out, int n, int* total, cudaStream_t s, 
     int* sums = (sc ? sc->scan_tmp : g_ctx.scan_tmp).get<int>(size_t(tiles) + 1);
     k_scan_tile_sums<<<tiles, kScanThreads, 0, s>>>(in, n, sums);
     GF_CHECK_LAUNCH();
+    if (tiles <= kScanDirectTiles) {
+        k_scan_tiles_direct<<<tiles, kScanThreads, 0, s>>>(in, out, n, sums, total);
+        GF_CHECK_LAUNCH();
+        return;
+    }
     k_scan_sums<<<1, 1024, 0, s>>>(sums, tiles, total);
     GF_CHECK_LAUNCH();
     k_scan_tiles<<<tiles, kScanThreads, 0, s>>>(in, out, n, sums);

@@ -131,17 +131,16 @@ __global__ void __launch_bounds__(kSelWarps * 32) k_verlet_select(
 
 // one thread per cache entry (coalesced rows of 48 local indices; cgidx keeps the local ->
 // global map of the caching call)
-__global__ void k_cache_store(int ng, int kq, const int* __restrict__ gidx, const int* __restrict__ nb,
-                              int* __restrict__ row, int* __restrict__ cache, int* __restrict__ cgidx) {
-    const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (t >= size_t(ng) * kCand) return;
-    const int i = int(t / kCand), jj = int(t % kCand);
-    if (jj == 0) {
-        const int g = gidx[i];
-        row[g] = i;
-        cgidx[i] = g;
-    }
-    cache[t] = jj < kq ? nb[t] : -1;
+// The full search wrote its candidates straight into the cache (kq columns of kCand); this
+// records whose rows they are and marks the columns a search of fewer than kCand left empty.
+__global__ void k_cache_rows(int ng, int kq, const int* __restrict__ gidx, int* __restrict__ row,
+                             int* __restrict__ cache, int* __restrict__ cgidx) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ng) return;
+    const int g = gidx[i];
+    row[g] = i;
+    cgidx[i] = g;
+    for (int jj = kq; jj < kCand; ++jj) cache[size_t(i) * kCand + jj] = -1;
 }
 
 __global__ void k_guess(int ng, const int* __restrict__ gidx, const double* __restrict__ hprev, float* __restrict__ rg) {
@@ -457,8 +456,9 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
         verlet_hits += have_nb ? 1 : 0;
     }
     if (!have_nb && a.nosync) throw Error(GF_ERR_ARG, "a synchronisation-free evaluation needs a neighbour cache");
-    if (!have_nb) {  // full search, 48 candidates (sph.py:165-169)
+    if (!have_nb) {  // full search, 48 candidates (sph.py:165-169), written into the cache
         const int kq = std::min(kCand, ng);
+        nb = cache.get<int>(size_t(ng) * kCand);
         float* rg = nullptr;
         if (have_hprev && hguess == 0) {  // previous h
             rg = rguess.get<float>(ng);
@@ -480,11 +480,9 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
             GF_CHECK_LAUNCH();
             collect_n += take;
         }
-        int* ca = cache.get<int>(size_t(ng) * kCand);
         int* rw = row.as<int>();
         GF_CUDA(cudaMemsetAsync(rw, 0xff, sizeof(int) * size_t(n), s));
-        k_cache_store<<<div_up(size_t(ng) * kCand, kThreads), kThreads, 0, s>>>(ng, kq, gi, nb, rw, ca,
-                                                                                cgidx.get<int>(ng));
+        k_cache_rows<<<ggrid, kThreads, 0, s>>>(ng, kq, gi, rw, nb, cgidx.get<int>(ng));
         GF_CHECK_LAUNCH();
         cache_valid = true;
         full_searches += 1;
