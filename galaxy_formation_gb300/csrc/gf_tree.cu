@@ -260,6 +260,20 @@ __device__ int run_end(const KeyView& K, int n, int i, int d) {
     return lo;
 }
 
+// run_end for a node inside an enclosing node that ends at hi (> i): binary search of (i, hi]
+// (cpl(i, j) does not grow with j, so cpl(i, j) < d holds from some j on)
+__device__ int run_end_within(const KeyView& K, int i, int d, int hi) {
+    int lo = i + 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (cpl(K, i, mid) < d)
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    return lo;
+}
+
 // first j <= i with cpl(j, i) >= lev
 __device__ int run_begin(const KeyView& K, int i, int lev) {
     int hi = i, step = 1, lo;
@@ -306,6 +320,7 @@ __global__ void k_emit(KeyView K, int n, const RootBox* __restrict__ rootp,
         c[1] = __dadd_rn(c[1], (o & 2) ? h : -h);
         c[2] = __dadd_rn(c[2], (o & 4) ? h : -h);
     }
+    int end = n;
     for (int d = ds; d <= ld; ++d) {
         if (d > ds) {
             h = 0.5 * h;
@@ -316,7 +331,8 @@ __global__ void k_emit(KeyView K, int n, const RootBox* __restrict__ rootp,
         }
         const int id = base + (d - ds);
         if (id >= cap) return;  // reported by k_node_cap_check
-        const int end = run_end(K, n, i, d);
+        // the first node of the chain searches from i; each deeper one within its parent
+        end = d == ds ? run_end(K, n, i, d) : run_end_within(K, i, d, end);
         const int next = end < n ? nbase[end] : total;
         int parent;
         if (d == 0) {
