@@ -49,7 +49,6 @@ UNIT = "particle-updates/s"
 CONFIG_IDX = 2
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
-# (theta, quadrupole walk, float32 SPH, h guess mode)
 # theta, quadrupole gravity, float32 SPH, h guess (0 previous h, 2 learned), relative opening
 # tolerance (0: geometric criterion at theta; > 0: the relative criterion once every particle
 # has a previous gravity, with theta used for the first evaluation), walk items merged from
@@ -58,7 +57,7 @@ PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FORMS = {
     "plain": (0.7, 0, 0, 0, 0.0, 0, 0.0),
     "plain_matched": (0.15, 0, 0, 0, 0.0, 0, 0.0),
-    "mixed_learned": (0.55, 1, 1, 2, 3.5e-3, 40, 2e-4),
+    "mixed_learned": (0.55, 1, 1, 2, 4e-3, 40, 2e-4),
 }
 # flops per interaction (an FMA counting 2): monopole pair (cpp/nbody.cpp:398-402 in float32)
 # and the softened quadrupole node term of the mixed walk

@@ -2,10 +2,11 @@
 //
 // Radix sort: stable LSD sort of (uint64 key, int32 value) pairs, 8-bit digits. Per digit:
 //   upsweep   per-tile digit histograms (warp-aggregated shared-memory atomics),
-//   scan      one exclusive scan over the digit-major histogram table [256][tiles],
+//   rows      one block per digit scans that digit's row of the table [256][tiles] in place
+//             and writes the digit's total,
 //   downsweep stable in-tile ranks (__match_any_sync per warp, warp-ordered tiles) and
-//             scatter to the scanned offsets.
-// Tiles are 4096 keys (256 threads x 16). Traffic per pass: 8 B read (upsweep) + 12 B read
+//             scatter to (exclusive scan of the 256 totals) + the tile's row entry.
+// Tiles are 1024 keys (256 threads x 4). Traffic per pass: 8 B read (upsweep) + 12 B read
 // + 12 B write (downsweep) per pair.
 #include <cstdarg>
 #include <algorithm>
@@ -97,7 +98,8 @@ int collect_status(cudaStream_t s) {
 }
 
 // ---------------------------------------------------------------------------------------
-// exclusive scan (int32): tile sums -> scan of tile sums -> per-tile scan + offset
+// exclusive scan (int32): tile sums -> scan of tile sums -> per-tile scan + offset (up to
+// kScanDirectTiles tiles the last two steps are one launch)
 
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 8;

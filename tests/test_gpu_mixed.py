@@ -237,7 +237,7 @@ def test_monopole_tolerance_for_far_nodes(gpulib):
     dt = np.empty(n)
     res = {}
     lib.gf_set_option(_lib.OPT_GRAVITY_QUAD, 1)
-    lib.gf_set_option(_lib.OPT_GRAVITY_REL, 3.5e-3)
+    lib.gf_set_option(_lib.OPT_GRAVITY_REL, 4e-3)
     lib.gf_set_option(_lib.OPT_WALK_MERGE, 40)
     try:
         for relq in (0.0, 2e-4):
