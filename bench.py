@@ -330,7 +330,7 @@ class Gpu:
         return float(np.percentile(e, 99)), float(np.median(e))
 
     def collect_pairs(self, rows, collect_steps=4, start=True):
-        """(features, converged log h) pairs from the plain method's own evaluations of drifting
+        """(features, log distance of the 48th nearest) pairs from the plain method's own evaluations of drifting
         copies of the snapshot (the collection buffer is cleared when start)."""
         torch, lib, L = self.torch, self.lib, self._lib
         theta = self.set_form("plain")

@@ -161,13 +161,15 @@ __global__ void k_smoothing(int ng, const double* __restrict__ d31, double eps, 
 }
 
 // appends (features, log of the unfloored h = d_32 / 2) rows to the training set
-__global__ void k_collect(int ng, long long base, const float* __restrict__ X, const double* __restrict__ d31,
+// training pair: the features and the log distance of the 48th nearest (the radius the
+// search has to reach)
+__global__ void k_collect(int ng, long long base, const float* __restrict__ X, const float* __restrict__ dk,
                           float* __restrict__ colX, float* __restrict__ colT) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ng) return;
     const size_t r = size_t(base) + i;
     for (int c = 0; c < 4; ++c) colX[4 * r + c] = X[4 * size_t(i) + c];
-    colT[r] = float(log(0.5 * d31[i]));
+    colT[r] = logf(fmaxf(dk[i], 1e-30f));
 }
 
 __global__ void k_scatter_f(int ng, const int* __restrict__ gidx, const float* __restrict__ v, float* __restrict__ out,
@@ -468,14 +470,14 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
         const bool collect = collect_cap > collect_n && have_hprev;
         HGuess hg{gi, have_hprev ? h_prev.as<double>() : nullptr, have_divv ? divv_prev.as<float>() : nullptr,
                   hX.get<float>(4 * size_t(ng)), hY.get<float>(ng), hrg.get<float>(ng),
-                  hguess == 2 && have_hprev && mlp().ready};
+                  hguess == 2 && have_hprev && mlp().ready, collect ? hdk.get<float>(ng) : nullptr};
         const bool features = collect || hg.use_mlp;
         GF_CUDA(cudaMemsetAsync(&sc->knn_iters, 0, sizeof(unsigned long long), s));
         knn_exact(knn_tree, ng, gp, kq, rg, nullptr, nullptr, &sc->knn_iters, s, nb, kCand, d31, kNgb - 1,
                   features ? &hg : nullptr);
         if (collect) {
             const long long take = std::min<long long>(ng, collect_cap - collect_n);
-            k_collect<<<div_up(take, kThreads), kThreads, 0, s>>>(int(take), collect_n, hg.X, d31,
+            k_collect<<<div_up(take, kThreads), kThreads, 0, s>>>(int(take), collect_n, hg.X, hg.dk,
                                                                   colX.as<float>(), colT.as<float>());
             GF_CHECK_LAUNCH();
             collect_n += take;

@@ -64,7 +64,7 @@ struct ForceEngine {
     static constexpr double kRelFloorTheta = 1.0;
     int hguess = 0;          // start of the neighbour-count iteration: 0 previous h, 1 cell
                              // density only, 2 the learned guess (MLP)
-    long long collect_cap = 0, collect_n = 0;  // (features, log h) training pairs kept
+    long long collect_cap = 0, collect_n = 0;  // (features, log d48) training pairs kept
     bool have_divv = false;
     int n_total = -1;
     int order_ng = -1;       // gas count of the last full neighbour search
@@ -78,7 +78,7 @@ struct ForceEngine {
     DevBuf acc_grav, acc_sph, dt_courant, h_prev, row, loc, cache, cgidx;
     DevBuf flag, scan, gidx, gpos, gvel, gmass, gu_, nb48, dsel, rguess, h, rho, gacc, dudt, dt_i;
     DevBuf scalars;
-    DevBuf divv_prev, gdivv, hX, hY, hrg, colX, colT, gact, aflag, ascan, alist;
+    DevBuf divv_prev, gdivv, hX, hY, hrg, hdk, colX, colT, gact, aflag, ascan, alist;
     ScanScratch hscratch;    // scans of the hydro stream
     cudaStream_t s2 = nullptr;               // the hydro chain's stream
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;

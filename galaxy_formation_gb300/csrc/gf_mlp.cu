@@ -1,7 +1,8 @@
-// gf_mlp.cu — the smoothing-length guess: a 4 -> 64 -> 64 -> 1 ReLU MLP predicting log h of
-// a gas particle from (log cell density, log previous h, leaf count, velocity divergence).
-// Its output starts the neighbour-count iteration of the kNN search; the iteration stays
-// the judge, so the converged h does not depend on the guess, only the iteration count.
+// gf_mlp.cu — the smoothing-length guess: a 4 -> 64 -> 64 -> 1 ReLU MLP predicting the log
+// distance of a gas particle's 48th nearest neighbour (the radius a full search has to reach)
+// from (log cell density, log previous h, leaf count, velocity divergence). Its output starts
+// the neighbour-count iteration of the kNN search; the iteration stays the judge, so the
+// converged h does not depend on the guess, only the iteration count.
 //
 // Weights live as float32 masters (for Adam) and bfloat16 copies; every forward and backward
 // pass reads the bfloat16 weights and accumulates in float32. Layout of the flat parameter
@@ -96,7 +97,7 @@ __global__ void __launch_bounds__(kFwdThreads) k_mlp_forward(int n, const float*
         float y = w.b3;
 #pragma unroll
         for (int j = 0; j < H; ++j) y = fmaf(w.w3[j], fmaxf(z[j], 0.f), y);
-        Y[i] = y * nm.t_std + nm.t_mean;  // log h
+        Y[i] = y * nm.t_std + nm.t_mean;  // log d48
     }
 }
 

@@ -16,7 +16,7 @@ constexpr int kOffW3 = kOffB2 + kMlpHidden;
 constexpr int kOffB3 = kOffW3 + kMlpHidden;
 constexpr int kMlpParams = kOffB3 + 1;  // 4545
 
-// Standardisation of the 4 inputs and of the target (log h).
+// Standardisation of the 4 inputs and of the target (log distance of the 48th nearest).
 struct MlpNorm {
     float mean[4] = {0.f, 0.f, 0.f, 0.f};
     float inv_std[4] = {1.f, 1.f, 1.f, 1.f};
@@ -36,7 +36,7 @@ struct Mlp {
     void init(unsigned seed, cudaStream_t s);
     void set_params(const float* host, cudaStream_t s);
     void get_params(float* host, cudaStream_t s);
-    // log h predictions of n samples (X: n x 4 float, device)
+    // predictions (log distance of the 48th nearest) of n samples (X: n x 4 float, device)
     void predict(int n, const float* X, float* Y, cudaStream_t s);
     // gradient of 0.5 mean (y - t)^2 (standardised) over samples idx[0..n) (or 0..n) into grad
     double gradient(int n, const int* idx, const float* X, const float* T, float* grad, cudaStream_t s);

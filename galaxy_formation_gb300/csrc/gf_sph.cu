@@ -309,6 +309,7 @@ struct KnnArgs {
     int ld32;
     double* dsel;           // distance of neighbour `dsel_col` (n,), or null
     int dsel_col;
+    float* dfar;            // distance of the k-th nearest in float32 (n,), or null
     uint32_t* status;
     unsigned long long* iters;
     const int* wparent;     // breadth-first parent of each node (-1 for the root)
@@ -501,6 +502,7 @@ __device__ void knn_finish(const KnnArgs& A, unsigned long long* key, unsigned l
             if (A.nb) A.nb[size_t(oq) * k + t] = pj;
         }
         if (A.dsel && lane == 0) A.dsel[oq] = __dsqrt_rn(best);
+        if (A.dfar && lane == 0) A.dfar[oq] = sqrtf(key_d2(key[k - 1]));
         __syncwarp();
         return;
     }
@@ -528,6 +530,7 @@ __device__ void knn_finish(const KnnArgs& A, unsigned long long* key, unsigned l
         if (A.dist) A.dist[size_t(oq) * k + t] = __dsqrt_rn(dt);
         if (A.nb32) A.nb32[size_t(oq) * A.ld32 + t] = di[t];
         if (A.dsel && t == A.dsel_col) A.dsel[oq] = __dsqrt_rn(dt);
+        if (A.dfar && t == k - 1) A.dfar[oq] = sqrtf(float(dt));
     }
     __syncwarp();
 }
@@ -689,9 +692,14 @@ __global__ void k_hfeatures(int n, const int* __restrict__ perm, const int* __re
     X[4 * size_t(i) + 3] = divv ? divv[g] : 0.f;
 }
 
-__global__ void k_guess_from_logh(int n, const float* __restrict__ Y, float* __restrict__ rg) {
+// The learned guess predicts the log distance of the k-th nearest; the search starts a little
+// outside it, so that nearly every first sphere holds the k nearest and rarely more than 64
+// points (one sort of 64 keys instead of 128).
+constexpr float kFarMargin = 1.06f;
+
+__global__ void k_guess_from_logdk(int n, const float* __restrict__ Y, float* __restrict__ rg) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) rg[i] = 2.5f * expf(Y[i]);  // the factor of the previous-h start
+    if (i < n) rg[i] = kFarMargin * expf(Y[i]);
 }
 
 void knn_exact(Octree& T, int n, const double* pos, int k, const float* r_guess, int64_t* nb,
@@ -708,7 +716,7 @@ void knn_exact(Octree& T, int n, const double* pos, int k, const float* r_guess,
         GF_CHECK_LAUNCH();
         if (hg->use_mlp) {
             mlp().predict(n, hg->X, hg->Y, s);
-            k_guess_from_logh<<<div_up(n, kThreads), kThreads, 0, s>>>(n, hg->Y, hg->rg);
+            k_guess_from_logdk<<<div_up(n, kThreads), kThreads, 0, s>>>(n, hg->Y, hg->rg);
             GF_CHECK_LAUNCH();
             r_guess = hg->rg;
         }
@@ -731,6 +739,7 @@ void knn_exact(Octree& T, int n, const double* pos, int k, const float* r_guess,
     A.ld32 = ld32;
     A.dsel = dsel;
     A.dsel_col = dsel_col;
+    A.dfar = hg ? hg->dk : nullptr;
     A.exact_order = (nb != nullptr || dist != nullptr || dsel_col < 0) ? 1 : 0;
     A.status = ctx().d_status;
     A.iters = d_iters;

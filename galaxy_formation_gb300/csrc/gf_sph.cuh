@@ -19,7 +19,9 @@ void sph_forces(SphScratch& S, int n, int k, int ld, const double* pos, const do
                 float* divv = nullptr, Subset sub = Subset());
 
 // Inputs of the learned smoothing-length guess inside a neighbour search: X (n x 4) receives
-// the features; with use_mlp the network's log h gives the starting radius 2.4 h.
+// the features; with use_mlp the network's predicted distance of the k-th nearest, times a
+// small margin, gives the starting radius; dk (if set) receives the converged distances of
+// the k-th nearest, the training targets.
 struct HGuess {
     const int* gidx;      // caller index -> global particle index (null: identity)
     const double* hprev;  // previous h per global index (null: none)
@@ -28,6 +30,7 @@ struct HGuess {
     float* Y;             // n predictions (scratch)
     float* rg;            // n starting radii (scratch)
     bool use_mlp;
+    float* dk;            // n distances of the k-th nearest (out, training targets), or null
 };
 
 struct Sph32Scratch {

@@ -314,7 +314,7 @@ int gf_cool(int n, const double* u, const double* T, const double* rho, const do
  *                       runs to the exact 48 nearest, so only the iteration count changes. */
 #define GF_OPT_HGUESS 2
 /*   GF_OPT_COLLECT      capacity (rows) of a device buffer that every later full search
- *                       fills with (features, log of the converged h) pairs for training;
+ *                       fills with (features, log distance of the 48th nearest) pairs for training;
  *                       setting it clears the buffer; gf_get_option returns the rows kept. */
 #define GF_OPT_COLLECT 3
 /*   GF_OPT_WALK_CHUNK   walks of an active subset (gf_accel_active*, gf_accelerations with an
@@ -353,7 +353,8 @@ int gf_set_option(int key, double value);
 /* Current value of an option (-1 for an unknown key). */
 double gf_get_option(int key);
 /* ---- learned smoothing-length guess (no reference counterpart) ----------------------- */
-/* A 4 -> 64 -> 64 -> 1 ReLU MLP with bfloat16 weights and float32 accumulation predicting log h
+/* A 4 -> 64 -> 64 -> 1 ReLU MLP with bfloat16 weights and float32 accumulation predicting the log
+ * distance of the 48th nearest gas neighbour (a full search starts at 1.06 times it)
  * from (log cell density, log previous h, leaf count, velocity divergence), standardised by
  * gf_mlp_set_norm. Parameters: flat float32 vector of 4545 values, W1 (64x4), b1, W2 (64x64),
  * b2, w3 (64), b3. */
@@ -361,7 +362,7 @@ int gf_mlp_init(int seed);
 int gf_mlp_set_params(const float* params);
 int gf_mlp_get_params(float* params);
 int gf_mlp_set_norm(const float* mean4, const float* std4, double t_mean, double t_std);
-/* log h of n samples (X: n x 4), host pointers. Inference rounds the layer-2 inputs to
+/* Predictions of n samples (X: n x 4), host pointers. Inference rounds the layer-2 inputs to
  * bfloat16 and runs layer 2 on the tensor cores (tcgen05) once the first call has checked
  * them against the CUDA-core kernel. */
 int gf_mlp_predict(int n, const float* X, float* Y);

@@ -1,10 +1,11 @@
 """Float64 oracle of the smoothing-length MLP (TEST INFRASTRUCTURE ONLY).
 
-The network: 4 -> 64 -> 64 -> 1, ReLU hidden layers, predicting log h from
-(log cell density, log previous h, leaf count, velocity divergence), standardised by a
+The network: 4 -> 64 -> 64 -> 1, ReLU hidden layers, predicting the log distance of the
+48th nearest neighbour from (log cell density, log previous h, leaf count, velocity
+divergence), standardised by a
 per-feature affine map. The GPU kernels store weights in bfloat16 and accumulate in
 float32; this oracle takes the same (bfloat16-rounded) weights and evaluates the forward
-pass, the mean-squared-error loss on log h and its gradients in float64, so that the
+pass, the mean-squared-error loss on the standardised target and its gradients in float64, so that the
 GPU gradients can be checked against it.
 """
 

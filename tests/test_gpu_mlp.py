@@ -3,7 +3,7 @@
 * forward and gradient kernels against the float64 oracle (oracle/mlp_ref.py) evaluated
   with the same bfloat16-rounded weights;
 * training on the GPU lowers the loss;
-* end to end: trained on (features, converged h) pairs collected from the simulator's own
+* end to end: trained on (features, log distance of the 48th nearest) pairs collected from the simulator's own
   force evaluations, the guess needs fewer radius iterations than the start from the cell
   density alone, and the converged neighbours / h (hence accelerations) do not change.
 """
