@@ -57,7 +57,7 @@ PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FORMS = {
     "plain": (0.7, 0, 0, 0, 0.0, 0, 0.0),
     "plain_matched": (0.15, 0, 0, 0, 0.0, 0, 0.0),
-    "mixed_learned": (0.55, 1, 1, 2, 4e-3, 40, 2e-4),
+    "mixed_learned": (0.55, 1, 1, 2, 4e-3, 40, 1.5e-4),
 }
 # flops per interaction (an FMA counting 2): monopole pair (cpp/nbody.cpp:398-402 in float32)
 # and the softened quadrupole node term of the mixed walk

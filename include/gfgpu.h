@@ -347,7 +347,7 @@ int gf_cool(int n, const double* u, const double* T, const double* rho, const do
 /*   GF_OPT_GRAVITY_REL_MONO  with the relative criterion on: an accepted node whose quadrupole
  *                       term, estimated as M b^2 / r^4, is below this tolerance times the
  *                       group's a_min is evaluated as a monopole alone (0 = off, default;
- *                       e.g. 2e-4). Far nodes then cost a monopole's arithmetic. */
+ *                       e.g. 1.5e-4). Far nodes then cost a monopole's arithmetic. */
 #define GF_OPT_GRAVITY_REL_MONO 8
 int gf_set_option(int key, double value);
 /* Current value of an option (-1 for an unknown key). */
