@@ -6,15 +6,16 @@
 //                              (pressure, Monaghan-Gingold viscosity on approaching pairs,
 //                              du/dt, Courant step); one thread per particle, float64.
 //   knn_from_candidates ...... sph.py:109-135: one warp per particle, float64 distances,
-//                              bitonic sort of the (<= 64) candidates in registers.
+//                              bitonic sort of the (<= 64) candidates in shared memory.
 //   exact k nearest .......... replaces cKDTree(p).query(p, k) (sph.py:165-166):
 //                              octree of the points (same builder as gravity); one warp per
 //                              two consecutive queries walks it with a radius per query,
 //                              collecting the points within each radius (float32 distances
 //                              from hi/lo split coordinates) until the count lies in
 //                              [k, 128] — the radius iteration, Newton steps on
-//                              count ~ R^3 from a guess (previous h, the learned guess, or
-//                              the leaf's cell density). The collected points are sorted,
+//                              count ~ R^3 from a guess (2.5 x the previous h, 1.06 x the
+//                              learned guess of the k-th-neighbour distance, or the leaf's
+//                              cell density). The collected points are sorted,
 //                              the k nearest plus near-ties at the boundary are re-measured
 //                              in float64 and sorted again, so the result is the exact
 //                              float64 kNN.
