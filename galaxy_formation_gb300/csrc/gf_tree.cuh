@@ -79,6 +79,7 @@ struct Octree {
     // groups and walk work list
     DevBuf gflag, gscan, groups, work, sphere;
     DevBuf item_gam;  // per work item: float2 {(alpha a_min)^(-1/5), (alpha_q a_min)^(-1/4)}, 0 = off
+    int walk_stride = 1;  // regions of the work list the walk takes at a time (prepare_walk sets it)
     DevBuf root, counts;
     ScanScratch scratch;  // this tree's scan / sort scratch (trees may build on different streams)
     TreeCounts* h_counts = nullptr;  // pinned

@@ -45,7 +45,8 @@ constexpr int kTileCap = 256;     // interaction entries per warp
 //               each with the bounding sphere of its own particles. Sparse active sets
 //               (block time steps) then spread over many warps with tight spheres instead of
 //               one warp walking a whole group for a few particles.
-//   merge  > 0 (chunk == 0): consecutive sibling groups merged into items of <= merge particles;
+//   merged items (mixed form, chunk == 0): consecutive sibling groups merged into items of
+//               <= merge_cap particles, written in tree order by k_item_flag / k_item_fill;
 //   aold != null: per item, gam = (alpha * a_min)^(-1/5) with a_min the smallest previous
 //               |acceleration| among the item's particles (relative opening criterion; 0, i.e.
 //               geometric only, when that minimum is not positive).
@@ -62,13 +63,20 @@ __device__ __forceinline__ float2 rel_gamma(float alpha, float alpha_q, float am
 
 // One work item over the particles [b, e) of the tree (a group, or a run of sibling groups):
 // its active count, the bounding sphere of its massive particles and, with aold, its scale of
-// the relative criterion; items without active or massive particles are dropped.
-__device__ __forceinline__ void emit_item(int b, int e, const float4* __restrict__ p4, const int* __restrict__ perm,
-                                          const uint8_t* __restrict__ active, TreeCounts* cnt,
-                                          int4* __restrict__ work, float4* __restrict__ sphere,
-                                          const double* __restrict__ aold, float alpha, float alpha_q,
-                                          float2* __restrict__ gam) {
+// the relative criterion; an item without active or massive particles is not valid.
+struct ItemStats {
+    int nact;
+    float4 sph;
+    float2 gam;
+    bool valid;
+};
+
+__device__ __forceinline__ ItemStats item_stats(int b, int e, const float4* __restrict__ p4,
+                                                const int* __restrict__ perm, const uint8_t* __restrict__ active,
+                                                const double* __restrict__ aold, float alpha, float alpha_q) {
     const int lane = threadIdx.x & 31;
+    ItemStats st;
+    st.valid = false;
     int nact = 0;
     float x0 = 1e30f, y0 = 1e30f, z0 = 1e30f, x1 = -1e30f, y1 = -1e30f, z1 = -1e30f;
     float amin = INFINITY;
@@ -83,11 +91,11 @@ __device__ __forceinline__ void emit_item(int b, int e, const float4* __restrict
             z0 = fminf(z0, p.z); z1 = fmaxf(z1, p.z);
         }
     }
-    nact = __shfl_sync(0xffffffffu, nact, 0);
-    if (nact == 0) return;
+    st.nact = __shfl_sync(0xffffffffu, nact, 0);
+    if (st.nact == 0) return st;
     x0 = warp_min(x0); y0 = warp_min(y0); z0 = warp_min(z0);
     x1 = warp_max(x1); y1 = warp_max(y1); z1 = warp_max(z1);
-    if (x0 > x1) return;  // massless
+    if (x0 > x1) return st;  // massless
     const float bx = 0.5f * (x0 + x1), by = 0.5f * (y0 + y1), bz = 0.5f * (z0 + z1);
     float br2 = 0.f;
     for (int i = b + lane; i < e; i += 32) {
@@ -99,13 +107,114 @@ __device__ __forceinline__ void emit_item(int b, int e, const float4* __restrict
     }
     br2 = warp_max(br2);
     amin = warp_min(amin);
+    st.sph = make_float4(bx, by, bz, sqrtf(br2));
+    st.gam = aold ? rel_gamma(alpha, alpha_q, amin) : make_float2(0.f, 0.f);
+    st.valid = true;
+    return st;
+}
+
+// Appends a valid item to the work list (in the order the warps get there).
+__device__ __forceinline__ void emit_item(int b, int e, const float4* __restrict__ p4, const int* __restrict__ perm,
+                                          const uint8_t* __restrict__ active, TreeCounts* cnt,
+                                          int4* __restrict__ work, float4* __restrict__ sphere,
+                                          const double* __restrict__ aold, float alpha, float alpha_q,
+                                          float2* __restrict__ gam) {
+    const int lane = threadIdx.x & 31;
+    const ItemStats st = item_stats(b, e, p4, perm, active, aold, alpha, alpha_q);
+    if (!st.valid) return;
     int slot = 0;
     if (lane == 0) slot = atomicAdd(&cnt->num_work, 1);
     slot = __shfl_sync(0xffffffffu, slot, 0);
     if (lane == 0) {
-        work[slot] = make_int4(b, e - b, nact, 0);
-        sphere[slot] = make_float4(bx, by, bz, sqrtf(br2));
-        if (gam) gam[slot] = aold ? rel_gamma(alpha, alpha_q, amin) : make_float2(0.f, 0.f);
+        work[slot] = make_int4(b, e - b, st.nact, 0);
+        sphere[slot] = st.sph;
+        if (gam) gam[slot] = st.gam;
+    }
+}
+
+// Mixed form, merged items: each run of consecutive sibling groups (contiguous in tree order)
+// is cut greedily into items of at most `merge` particles (a larger group alone). A run holds
+// at most 8 groups, so lanes 0..15 load groups g-8 .. g+7; the warp finds the run around group
+// g and replays the cut from the run's first group. Returns the particle count of the item
+// that g starts (-1 if g starts none) and, in b, g's first particle.
+__device__ __forceinline__ int cut_at(const int* __restrict__ groups, const int4* __restrict__ n_i4,
+                                      const int* __restrict__ parent, int ng, int merge, int g, int& b) {
+    const int lane = threadIdx.x & 31;
+    const int idx = g - 8 + lane;
+    int pg = -2, cg = 0, bg = 0;
+    if (lane < 16 && idx >= 0 && idx < ng) {
+        const int nd = groups[idx];
+        const int4 q = n_i4[nd];
+        pg = parent[nd];
+        cg = q.y;
+        bg = q.x;
+    }
+    const int par = __shfl_sync(0xffffffffu, pg, 8);
+    b = __shfl_sync(0xffffffffu, bg, 8);
+    const unsigned same = __ballot_sync(0xffffffffu, pg == par);
+    const unsigned below = ~same & 0xffu;     // lanes 0..7 outside the run
+    const unsigned above = ~same & 0xfe00u;   // lanes 9..15 outside the run
+    const int first = below ? 32 - __clz(below) : 0;
+    const int last = above ? __ffs(above) - 1 : 16;
+    int start = first, rc = 0, mine = -1;
+    for (int l = first; l < last; ++l) {
+        const int c = __shfl_sync(0xffffffffu, cg, l);
+        if (l > start && rc + c <= merge) {
+            rc += c;
+            continue;
+        }
+        if (l > start) {  // the item [start, l) closes
+            if (start == 8) mine = rc;
+            start = l;
+        }
+        rc = c;
+    }
+    if (start == 8) mine = rc;  // the run's last item
+    return mine;
+}
+
+// flag[g] = 1 when group g starts a merged item (g < span; 0 past the live group count)
+__global__ void k_item_flag(const int* __restrict__ groups, const int4* __restrict__ n_i4,
+                            const int* __restrict__ parent, const TreeCounts* cnt, int merge, int span,
+                            int* __restrict__ flag) {
+    const int lane = threadIdx.x & 31;
+    const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const int ng = cnt->num_groups;
+    for (int g = wid; g < span; g += nw) {
+        int f = 0;
+        if (g < ng) {
+            int b;
+            f = cut_at(groups, n_i4, parent, ng, merge, g, b) > 0 ? 1 : 0;
+        }
+        if (lane == 0) flag[g] = f;
+    }
+}
+
+// The merged items in tree order: item of group g at slot[g] (the scan of the flags). An item
+// without active or massive particles keeps its slot with no particles to evaluate.
+__global__ void k_item_fill(const int* __restrict__ groups, const int4* __restrict__ n_i4,
+                            const int* __restrict__ parent, const TreeCounts* cnt, int merge,
+                            const int* __restrict__ flag, const int* __restrict__ slot,
+                            const float4* __restrict__ p4, const int* __restrict__ perm,
+                            const uint8_t* __restrict__ active, const double* __restrict__ aold,
+                            float alpha, float alpha_q, int4* __restrict__ work, float4* __restrict__ sphere,
+                            float2* __restrict__ gam) {
+    const int lane = threadIdx.x & 31;
+    const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const int ng = cnt->num_groups;
+    for (int g = wid; g < ng; g += nw) {
+        if (!flag[g]) continue;
+        int b;
+        const int count = cut_at(groups, n_i4, parent, ng, merge, g, b);
+        const ItemStats st = item_stats(b, b + count, p4, perm, active, aold, alpha, alpha_q);
+        if (lane == 0) {
+            const int k = slot[g];
+            work[k] = make_int4(b, count, st.valid ? st.nact : 0, 0);
+            sphere[k] = st.valid ? st.sph : make_float4(0.f, 0.f, 0.f, 0.f);
+            if (gam) gam[k] = st.valid ? st.gam : make_float2(0.f, 0.f);
+        }
     }
 }
 
@@ -114,7 +223,7 @@ __global__ void k_group_prep(const int* __restrict__ groups, const int4* __restr
                              const uint8_t* __restrict__ active, TreeCounts* cnt,
                              int4* __restrict__ work, float4* __restrict__ sphere, int chunk,
                              const double* __restrict__ aold, float alpha, float alpha_q,
-                             float2* __restrict__ gam, const int* __restrict__ parent, int merge) {
+                             float2* __restrict__ gam) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = lanemask_lt();
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -179,27 +288,6 @@ __global__ void k_group_prep(const int* __restrict__ groups, const int4* __restr
                 }
                 if (P < chunk) break;
                 r0 += chunk;
-            }
-            continue;
-        }
-        if (merge > 0) {
-            // mixed form: runs of consecutive sibling groups (contiguous in tree order) of at
-            // most `merge` particles, one item each, started by the first group of its siblings
-            const int par = parent[node];
-            if (g > 0 && parent[groups[g - 1]] == par) continue;
-            int j = g;
-            while (j < ng) {
-                const int4 qj = n_i4[groups[j]];
-                int rc = qj.y;
-                int j2 = j + 1;
-                for (; j2 < ng && parent[groups[j2]] == par; ++j2) {
-                    const int c2 = n_i4[groups[j2]].y;
-                    if (rc + c2 > merge) break;
-                    rc += c2;
-                }
-                emit_item(qj.x, qj.x + rc, p4, perm, active, cnt, work, sphere, aold, alpha, alpha_q, gam);
-                j = j2;
-                if (j >= ng || parent[groups[j]] != par) break;
             }
             continue;
         }
@@ -348,7 +436,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32, QUAD ? (NPL > 2 ? 1 : 4) : 5)
     const float2* __restrict__ wt, const float* __restrict__ wrq, const float4* __restrict__ p4,
     const int* __restrict__ perm, const uint8_t* __restrict__ active, const int4* __restrict__ work,
     const float4* __restrict__ sphere, const float2* __restrict__ gam, TreeCounts* cnt, int nn, float eps2,
-    double* __restrict__ acc, uint32_t* status, double* __restrict__ pot = nullptr) {
+    double* __restrict__ acc, uint32_t* status, int stride, double* __restrict__ pot = nullptr) {
     static_assert(!(QUAD && POT), "potentials come from the monopole walk");
     using Smem = WarpSmem<QUAD, NPL>;
     constexpr int kNodesPerLane = NPL;
@@ -357,13 +445,20 @@ __global__ void __launch_bounds__(kWalkWarps * 32, QUAD ? (NPL > 2 ? 1 : 4) : 5)
     Smem& S = smem_all[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     const unsigned lt = lanemask_lt();
+    // Tickets go to items through a stride permutation: ticket t -> item (t mod stride) *
+    // ceil(nwork / stride) + t / stride, so the warps at work at one time spread over `stride`
+    // regions of a work list in tree order, each taken in order (1: the list's own order).
     const int nwork = cnt->num_work;
+    const int per = (nwork + stride - 1) / stride;
+    const int ntick = per * stride;
 
     for (;;) {
-        int g = 0;
-        if (lane == 0) g = atomicAdd(&cnt->walk_next, 1);
-        g = __shfl_sync(0xffffffffu, g, 0);
-        if (g >= nwork) break;
+        int t = 0;
+        if (lane == 0) t = atomicAdd(&cnt->walk_next, 1);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= ntick) break;
+        const int g = (t % stride) * per + t / stride;
+        if (g >= nwork) continue;
         const int4 w = work[g];
         const float4 sph = sphere[g];
         // relative criterion: accept a node when its distance from the sphere exceeds both
@@ -681,15 +776,34 @@ void Octree::prepare_walk(const uint8_t* active, cudaStream_t s, int chunk, cons
     // items: one per group (<= nodes), or at most one per active particle with chunks
     const size_t cap = std::max(size_t(node_cap), size_t(n)) + 1;
     active_ptr = active;
+    if (quad && merge_cap > 0 && !(active && chunk > 0)) {
+        // merged items in tree order (flag, scan, fill), walked 4 regions at a time: 2 % faster
+        // per evaluation than the order of appending warps, 6 % faster than 1 region, 9 % than 8
+        const int span = std::max(node_cap, 1);
+        int* fl = gflag.get<int>(span);
+        int* sl = gscan.get<int>(span);
+        const int blocks = std::min(div_up(span, 8), 16 * C.sms);
+        k_item_flag<<<blocks, 256, 0, s>>>(groups.as<int>(), n_i4.as<int4>(), n_parent.as<int>(), cnt, merge_cap,
+                                           span, fl);
+        GF_CHECK_LAUNCH();
+        exclusive_scan(fl, sl, span, &cnt->num_work, s, &scratch);
+        k_item_fill<<<blocks, 256, 0, s>>>(groups.as<int>(), n_i4.as<int4>(), n_parent.as<int>(), cnt, merge_cap, fl,
+                                           sl, p4.as<float4>(), perm.as<int>(), active,
+                                           alpha > 0.f ? aold : nullptr, alpha, alpha_q, work.get<int4>(cap),
+                                           sphere.get<float4>(cap), item_gam.get<float2>(cap));
+        GF_CHECK_LAUNCH();
+        walk_stride = 4;
+        return;
+    }
+    walk_stride = 1;
     // The grid also fixes the order of the work list (each warp appends its groups' items as it
     // goes), and the walk takes items in that order: 4 blocks per SM measured 6 % faster per
-    // evaluation than 2 or 8, or than items in tree order.
+    // evaluation than 2 or 8.
     k_group_prep<<<4 * C.sms, 256, 0, s>>>(groups.as<int>(), n_i4.as<int4>(), p4.as<float4>(),
                                           perm.as<int>(), active, cnt, work.get<int4>(cap),
                                           sphere.get<float4>(cap), active ? chunk : 0,
                                           quad && alpha > 0.f ? aold : nullptr, alpha, alpha_q,
-                                          quad ? item_gam.get<float2>(cap) : nullptr, n_parent.as<int>(),
-                                          quad && !(active && chunk > 0) ? merge_cap : 0);
+                                          quad ? item_gam.get<float2>(cap) : nullptr);
     GF_CHECK_LAUNCH();
 }
 
@@ -710,21 +824,22 @@ void Octree::walk(double eps, double* acc, cudaStream_t s, double* pot, int npl)
         k_walk<false, true><<<bps_mono * C.sms, kWalkWarps * 32, 0, s>>>(
             w_a.as<float4>(), w_b.as<float4>(), nullptr, nullptr, nullptr, p4.as<float4>(), perm.as<int>(), active_ptr,
             work.as<int4>(), sphere.as<float4>(), nullptr, counts.as<TreeCounts>(), node_cap, eps2, acc, C.d_status,
-            pot);
+            walk_stride, pot);
     } else if (quad && npl > 2) {
         k_walk<true, false, 8><<<bps_quad * C.sms, kWalkWarps * 32, 0, s>>>(
             w_a.as<float4>(), w_b.as<float4>(), w_q.as<float4>(), w_t.as<float2>(), w_rq.as<float>(), p4.as<float4>(),
             perm.as<int>(), active_ptr, work.as<int4>(), sphere.as<float4>(), item_gam.as<float2>(),
-            counts.as<TreeCounts>(), node_cap, eps2, acc, C.d_status);
+            counts.as<TreeCounts>(), node_cap, eps2, acc, C.d_status, walk_stride);
     } else if (quad) {
         k_walk<true><<<bps_quad * C.sms, kWalkWarps * 32, 0, s>>>(
             w_a.as<float4>(), w_b.as<float4>(), w_q.as<float4>(), w_t.as<float2>(), w_rq.as<float>(), p4.as<float4>(),
             perm.as<int>(), active_ptr, work.as<int4>(), sphere.as<float4>(), item_gam.as<float2>(),
-            counts.as<TreeCounts>(), node_cap, eps2, acc, C.d_status);
+            counts.as<TreeCounts>(), node_cap, eps2, acc, C.d_status, walk_stride);
     } else {
         k_walk<false><<<bps_mono * C.sms, kWalkWarps * 32, 0, s>>>(
             w_a.as<float4>(), w_b.as<float4>(), nullptr, nullptr, nullptr, p4.as<float4>(), perm.as<int>(), active_ptr,
-            work.as<int4>(), sphere.as<float4>(), nullptr, counts.as<TreeCounts>(), node_cap, eps2, acc, C.d_status);
+            work.as<int4>(), sphere.as<float4>(), nullptr, counts.as<TreeCounts>(), node_cap, eps2, acc, C.d_status,
+            walk_stride);
     }
     GF_CHECK_LAUNCH();
 }
