@@ -13,15 +13,22 @@ Forms measured (same snapshot, same evaluation):
                  default), float64 SPH, search radius from the previous h;
   plain_matched  the same arithmetic at the opening angle whose gravity error against the
                  float64 direct sum meets p99 <= 1e-3 (theta 0.15);
-  mixed_learned  the headline: quadrupole walk in float32 with Kahan tile sums at theta 0.55
-                 (p99 <= 1e-3), float32 + Kahan SPH, search radius from the learned MLP guess
+  mixed_prevh    the headline's method with the search radius from the previous h instead of
+                 the learned guess (what the guess gains, in the headline setting);
+  mixed_learned  the headline: float32 walk with Kahan tile sums and quadrupole nodes under the
+                 relative opening criterion (alpha 4e-3, a geometric floor at theta 1; accepted
+                 nodes whose quadrupole term is below 1.5e-4 a_min taken as monopoles; walk items
+                 merged from sibling groups up to 40 particles), p99 <= 1e-3 against the float64
+                 direct sum; float32 + Kahan SPH; search radius from the learned MLP guess
                  (trained first on pairs the simulator produced, on the GPU);
 plus the batched form (block time steps, CUDA-graph replay, autotuned) as particle-updates/s
 over a 64-sub-step block.
 
 `value` = mixed_learned, timed on the device with CUDA events on the launching stream around
 each step, inputs resident in HBM, L2 flushed (256 MB write) between steps; `e2e` = the same
-form through the C ABI with pinned host buffers (copies in and out included). `--impl reference`
+form through the C ABI with pinned host buffers (copies in and out included); `parity` = the
+GPU forms against the oracle's evaluation of the same snapshot (computed by the cpu_baseline
+leg, which runs the oracle anyway). `--impl reference`
 times the reference's CPU algorithm on this host's cores (the oracle restatement of
 cpp/nbody.cpp + scipy cKDTree + the restated sph_forces) on the same workload.
 Multi-GPU (torchrun): independent replicas, one per GPU, no collective on the data path.
@@ -57,6 +64,7 @@ PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FORMS = {
     "plain": (0.7, 0, 0, 0, 0.0, 0, 0.0),
     "plain_matched": (0.15, 0, 0, 0, 0.0, 0, 0.0),
+    "mixed_prevh": (0.55, 1, 1, 0, 4e-3, 40, 1.5e-4),
     "mixed_learned": (0.55, 1, 1, 2, 4e-3, 40, 1.5e-4),
 }
 # flops per interaction (an FMA counting 2): monopole pair (cpp/nbody.cpp:398-402 in float32)
@@ -71,7 +79,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--scale", type=float, default=1.0, help="shrink the workload (testing only)")
-    ap.add_argument("--forms", default="plain,plain_matched,mixed_learned",
+    ap.add_argument("--forms", default="plain,plain_matched,mixed_prevh,mixed_learned",
                     help="comma list of forms to time (the last one given is the headline)")
     ap.add_argument("--blocks", type=int, default=3, help="64-sub-step blocks of the batched form (0: skip)")
     ap.add_argument("--workload", default="force", choices=["force", "drift", "learned"],
@@ -183,7 +191,8 @@ def cpu_force_step(fo, d):
 
 
 def time_cpu(d, reps, warm):
-    """The reference's algorithm on this host's CPU cores; returns seconds per step."""
+    """The reference's algorithm on this host's CPU cores; returns seconds per step, the
+    threads used and the oracle holding the last evaluation (the checker of the GPU forms)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     from force_ref import ForceOracle
@@ -199,7 +208,59 @@ def time_cpu(d, reps, warm):
         t0 = time.perf_counter()
         cpu_force_step(fo, d)
         ts.append(time.perf_counter() - t0)
-    return statistics.median(ts), oracle.num_threads()
+    return statistics.median(ts), oracle.num_threads(), fo
+
+
+def parity_vs_oracle(G, fo, head):
+    """The GPU forms against the oracle's evaluation of the same snapshot (the CPU leg's last
+    step): the plain form's gravity against the oracle's Barnes-Hut at theta 0.7 (per-particle
+    relative error), and the headline form's SPH against the oracle's float64 SPH — neighbour
+    sets, h, density, Courant step, SPH acceleration and du/dt (the last two also relative to
+    the sum of |pair terms|, the scale that bounds the rounding of a cancelling sum)."""
+    import sph_ref
+
+    torch, lib, L, params = G.torch, G.lib, G._lib, G.params
+    out = {"oracle": "ForceOracle: restated cpp/nbody.cpp Barnes-Hut at theta 0.7 + scipy cKDTree 48-candidate "
+                     "search + restated sph_forces (float64), same snapshot"}
+    theta = G.set_form("plain")
+    G.step(theta, kind=torch_full_like(torch, G.T["kind"], 2))
+    e = np.linalg.norm(G.acc.cpu().numpy() - fo.acc_grav, axis=1) / np.linalg.norm(fo.acc_grav, axis=1)
+    out["plain_gravity_vs_oracle_bh"] = {"p99_rel_err": float(np.percentile(e, 99)), "max_rel_err": float(e.max()),
+                                         "median_rel_err": float(np.median(e)), "bar_p99": 1e-4}
+    theta = G.set_form(head)
+    G.step(theta)
+    G.step(theta)  # the relative criterion's error scale is the previous evaluation's gravity
+    torch.cuda.synchronize()
+    gs = L.read_gas(lib)
+    g = fo.gas_idx
+    p, v, m, u = (np.ascontiguousarray(G.d[k][g]) for k in ("pos", "vel", "mass", "u"))
+    sa, sd = np.empty(g.size), np.empty(g.size)
+    for s0 in range(0, g.size, 100_000):
+        rows = np.arange(s0, min(g.size, s0 + 100_000))
+        _, _, _, sa[rows], sd[rows] = sph_ref.forces(p, v, m, fo.nb, fo.h, u, fo.rho, rows, params.GAMMA,
+                                                     params.ALPHA, params.BETA)
+    a, b = np.sort(gs["nb"].astype(np.int64), axis=1), np.sort(fo.nb, axis=1)
+    bad = np.flatnonzero(np.any(a != b, axis=1))
+    edge = 0
+    for i in bad:
+        diff = np.setxor1d(a[i], b[i])
+        r = np.linalg.norm(p[diff] - p[i], axis=1)
+        edge += int(np.all(np.abs(r - 2 * fo.h[i]) <= 1e-6 * fo.h[i]))
+    dti = fo.dt_courant[g]
+    a_sph = fo.acc_sph[g]
+    err = np.linalg.norm(gs["acc_sph"] - a_sph, axis=1)
+    out["headline_sph_vs_oracle_f64"] = {
+        "form": head, "gas": int(g.size),
+        "gas_index_identical": bool(np.array_equal(gs["gidx"], g)),
+        "neighbour_rows_differing": int(bad.size), "of_which_at_support_edge": edge,
+        "h_max_rel_diff": float(np.max(np.abs(gs["h"] - fo.h) / fo.h)),
+        "rho_max_rel_err": float(np.max(np.abs(gs["rho"] - fo.rho) / fo.rho)),
+        "dt_max_rel_err": float(np.max(np.abs(gs["dt_i"] - dti) / dti)),
+        "acc_sph_p99_rel_err": float(np.percentile(err / np.linalg.norm(a_sph, axis=1), 99)),
+        "acc_sph_max_err_over_term_sum": float(np.max(err / sa)),
+        "dudt_max_err_over_term_sum": float(np.max(np.abs(gs["dudt"] - fo.dudt) / sd)),
+        "bar": 1e-5}
+    return out
 
 
 def run_reference(args, world, rank):
@@ -208,9 +269,9 @@ def run_reference(args, world, rank):
     d = workload(args.scale)
     n = len(d["mass"])
     n_gas = int((d["kind"] == 0).sum())
-    steps = max(1, min(args.steps, 5))
-    warm = min(args.warmup, 1)
-    sec, cores = time_cpu(d, steps, warm)
+    steps = max(1, args.steps)
+    warm = args.warmup
+    sec, cores, _ = time_cpu(d, steps, warm)
     v = n / sec
     sample = (f"{steps} full force evaluations of the {n:,}-particle workload (median), "
               f"{warm} warm-up; oracle restatement of cpp/nbody.cpp (OpenMP) + scipy cKDTree "
@@ -220,7 +281,11 @@ def run_reference(args, world, rank):
         "steps": steps, "warmup": warm, "ms_per_step": sec * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
         "config": {"workload": workload_name(n_gas, n - n_gas), "particles": n, "gas": n_gas,
-                   "theta": 0.7, "eps_kpc": 0.4, "host_cores": os.cpu_count()},
+                   "theta": 0.7, "eps_kpc": 0.4, "host_cores": os.cpu_count(),
+                   "note": "the reference's method: geometric opening at theta 0.7 (float32 monopole walk) and "
+                           "float64 SPH; the GPU headline runs the relative opening criterion with quadrupoles "
+                           "(p99 <= 1e-3 against the float64 direct sum, which theta 0.7 misses) and float32 + "
+                           "Kahan SPH, so the two arms compute the same evaluation by different methods"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
@@ -237,17 +302,22 @@ def load_traffic():
 class Gpu:
     """The workload resident on one GPU and the library's entry points around it."""
 
-    def __init__(self, args, local, config_idx=CONFIG_IDX):
+    def __init__(self, args, local, config_idx=CONFIG_IDX, ic="host"):
         import torch
 
-        from galaxy_formation_gb300 import _lib, build, params
+        from galaxy_formation_gb300 import _lib, build, params, synthetic
 
         build.build()
         self.torch, self._lib, self.params = torch, _lib, params
         self.lib = _lib.load()
         torch.cuda.set_device(local)
         self.dev = torch.device("cuda", local)
-        self.d = workload(args.scale, config_idx)
+        t0 = time.perf_counter()
+        if ic == "device":  # drawn on the GPU (gf_ic_generate), copied to the host once
+            self.d = synthetic.make_config_device(config_idx, seed=3, scale=args.scale, lib=self.lib)
+        else:
+            self.d = workload(args.scale, config_idx)
+        self.ic = {"generator": ic, "seconds": time.perf_counter() - t0}
         self.n = len(self.d["mass"])
         self.n_gas = int((self.d["kind"] == 0).sum())
         self.T = {k: torch.from_numpy(np.ascontiguousarray(self.d[k])).to(self.dev)
@@ -263,6 +333,10 @@ class Gpu:
     def set_form(self, form):
         theta, quad, sph32, hguess, rel, merge, relq = FORMS[form]
         L, lib = self._lib, self.lib
+        tuned = getattr(self, "tuned", {}).get(form)
+        if tuned:  # the walk autotuner's choice for this form (time_form)
+            merge = tuned["walk_merge"]
+        lib.gf_set_option(L.OPT_WALK_SHAPE, tuned["walk_shape"] if tuned else 0)
         lib.gf_set_option(L.OPT_GRAVITY_QUAD, quad)
         lib.gf_set_option(L.OPT_SPH_FLOAT32, sph32)
         lib.gf_set_option(L.OPT_HGUESS, hguess)
@@ -294,6 +368,16 @@ class Gpu:
             self.step(theta)
             self.flush.zero_()
         torch.cuda.synchronize()
+        tuned = None
+        if FORMS[form][1]:  # mixed walk: item size and launch shape chosen by the autotuner
+            mg, sh, wms = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+            L.check(lib.gf_force_autotune(self.params.EPS, ctypes.byref(mg), ctypes.byref(sh), ctypes.byref(wms)))
+            tuned = {"walk_merge": mg.value, "walk_shape": sh.value, "walk_ms": wms.value}
+            if not hasattr(self, "tuned"):
+                self.tuned = {}
+            self.tuned[form] = tuned
+            self.step(theta)
+            torch.cuda.synchronize()
         lib.gf_profile(1)
         launches0 = lib.gf_launch_count()
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
@@ -313,8 +397,11 @@ class Gpu:
             if cnt.value:
                 stages[name] = {"ms_per_launch": ms.value / cnt.value, "launches": cnt.value}
         lib.gf_profile(0)
+        st = np.zeros(9)
+        lib.gf_force_stats(st, 9)
         return {"theta": theta, "times_ms": times, "launches": launches, "stages": stages,
-                "pairs": lib.gf_walk_pairs(), "qpairs": lib.gf_walk_quad_pairs(), "knn_iters": self.knn_iters()}
+                "pairs": lib.gf_walk_pairs(), "qpairs": lib.gf_walk_quad_pairs(), "knn_iters": self.knn_iters(),
+                "nodes": int(st[8]), "autotune": tuned}
 
     def gravity_error(self, form, targets, exact):
         """p99 / median relative error of the form's gravity against the float64 direct sum:
@@ -365,29 +452,44 @@ class Gpu:
         train_s = time.perf_counter() - t0
         lib.gf_set_option(L.OPT_COLLECT, 0)  # stop collecting (clears the pairs)
         # iterations of the count-to-48 search on a drifted snapshot: previous h, cell density
-        # alone, learned guess (the converged neighbours are the same in all three)
-        its = {}
-        for mode, name in ((0, "previous_h"), (1, "cell_density"), (2, "learned")):
-            lib.gf_set_option(L.OPT_HGUESS, 0)
-            self.step(theta, pos=pos)
-            nxt = pos + 0.5 * self.dt[:, None] * self.T["vel"]
-            lib.gf_set_option(L.OPT_HGUESS, mode)
-            lib.gf_profile(1)
-            self.step(theta, pos=nxt)
-            torch.cuda.synchronize()
-            ms, cnt = ctypes.c_double(), ctypes.c_int()
-            lib.gf_profile_stage(L.STAGES.index("knn"), ctypes.byref(ms), ctypes.byref(cnt))
-            lib.gf_profile(0)
-            its[name] = {"iterations_per_gas": self.knn_iters(), "knn_ms": ms.value}
+        # alone, learned guess (the converged neighbours are the same in all three); the
+        # previous h is that of the snapshot before the drift, so longer drifts make it staler
+        its, by_drift = {}, {}
+        for halves in (1, 4, 16):
+            row = {}
+            for mode, name in ((0, "previous_h"), (1, "cell_density"), (2, "learned")):
+                if halves > 1 and mode == 1:
+                    continue
+                row[name] = self.search_after_drift(theta, pos, halves, mode)
+            by_drift[f"{halves}_half_steps"] = row
+        its = by_drift["1_half_steps"]
         lib.gf_set_option(L.OPT_HGUESS, 0)
         return {"training_rows": int(m), "loss_start": loss0.value, "loss_end": loss1.value,
-                "train_s": train_s, "adam_steps": 2000, "batch": 4096, "search_on_drifted_snapshot": its}
+                "train_s": train_s, "adam_steps": 2000, "batch": 4096, "search_on_drifted_snapshot": its,
+                "search_after_drift": by_drift}
 
-    def batched(self, blocks, nlev=7):
+    def search_after_drift(self, theta, pos, halves, mode):
+        """Radius iterations and neighbour-search time of a full search on the snapshot drifted by
+        `halves` half time steps (dt of each particle's last evaluation), starting from h guess
+        `mode`, with the previous h from an evaluation before the drift."""
+        torch, lib, L = self.torch, self.lib, self._lib
+        lib.gf_set_option(L.OPT_HGUESS, 0)
+        self.step(theta, pos=pos)
+        nxt = pos + (0.5 * halves) * self.dt[:, None] * self.T["vel"]
+        lib.gf_set_option(L.OPT_HGUESS, mode)
+        lib.gf_profile(1)
+        self.step(theta, pos=nxt)
+        torch.cuda.synchronize()
+        ms, cnt = ctypes.c_double(), ctypes.c_int()
+        lib.gf_profile_stage(L.STAGES.index("knn"), ctypes.byref(ms), ctypes.byref(cnt))
+        lib.gf_profile(0)
+        return {"iterations_per_gas": self.knn_iters(), "knn_ms": ms.value}
+
+    def batched(self, blocks, nlev=7, form="mixed_learned"):
         """Block time steps at the mixed + learned form: autotune, one warm block, then
         `blocks` blocks timed with CUDA events on the library's stream."""
         torch, lib, L, p = self.torch, self.lib, self._lib, self.params
-        theta = self.set_form("mixed_learned")
+        theta = self.set_form(form)
         d = self.d
         L.check(lib.gf_sim_init(self.n, d["pos"], d["vel"], d["mass"], d["kind"], d["u"], theta, p.EPS,
                                 p.GAMMA, p.ALPHA, p.BETA))
@@ -410,13 +512,71 @@ class Gpu:
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_pop()
         ms = e0.elapsed_time(e1)
+        launches = lib.gf_launch_count() - launches0
+        # the full neighbour search of a block end (the previous h of the coarse levels' gas is
+        # a block old there): one more block with the stage profiler on
+        lib.gf_profile(1)
+        L.check(lib.gf_sim_blocks(1, nlev, ctypes.byref(ctypes.c_double())))
+        torch.cuda.synchronize()
+        kms, kcnt = ctypes.c_double(), ctypes.c_int()
+        lib.gf_profile_stage(L.STAGES.index("knn"), ctypes.byref(kms), ctypes.byref(kcnt))
+        lib.gf_profile(0)
+        block_end = {"knn_ms": kms.value / max(1, kcnt.value), "iterations_per_gas": self.knn_iters(),
+                     "h_guess": ["previous h", "cell density", "learned MLP"][FORMS[form][3]]}
         return {"value": upd.value / (ms * 1e-3), "unit": UNIT, "blocks": blocks, "substeps_per_block": 1 << (nlev - 1),
                 "levels": nlev, "level_fractions": [round(float(x), 5) for x in frac],
                 "updates": upd.value, "ms": ms, "ms_per_block": ms / blocks,
                 "autotune": {"chunk_per_bin": chunk.tolist(), "rebuild_every": every.value, "seconds": tune_s},
-                "launches_outside_graphs": lib.gf_launch_count() - launches0,
+                "launches_outside_graphs": launches, "block_end_search": block_end, "form": form,
                 "note": "an update = a particle given a freshly computed force at one of its own steps; "
                         "each block = 63 sub-steps replayed as one CUDA graph + a full evaluation"}
+
+
+# Algorithmic bytes of the HBM-bound passes (the per-unit figures of the scope table's
+# measurement row): the radix sort moves 12 B (key + index) in and out per digit pass; node
+# emission reads the 8 B sorted key per particle and writes a 64 B node; the moments pass reads
+# a 16 B float32 particle record and reads + writes 64 B per node; the SPH passes per gas
+# particle with float32 storage (int32 neighbour rows): density 152 B, force 188 B, and with the
+# reference's float64 storage 176 B and 256 B.
+SORT_PASSES = 8
+
+
+def pass_bytes(stage, n, n_gas, nodes, sph32):
+    if stage == "tree_sort":
+        return 2 * 12 * SORT_PASSES * n
+    if stage == "tree_emit":
+        return 8 * n + 64 * nodes
+    if stage == "tree_moments":
+        return 16 * n + 64 * nodes
+    if stage == "sph_density":
+        return (152 if sph32 else 176) * n_gas
+    if stage == "sph_force":
+        return (188 if sph32 else 256) * n_gas
+    return None
+
+
+def hbm_passes(res, forms, head, n, n_gas, peak, peak_src, traffic_db):
+    """HBM roofline of the sort, build and SPH passes: algorithmic bytes per launch / the
+    pass's CUDA-event time per launch inside the timed steps, against the measured copy
+    bandwidth; ncu DRAM bytes of one launch where profiles/roofline_traffic.json has them."""
+    out = {}
+    for f in forms:
+        if f not in (head, "plain"):
+            continue
+        r = res[f]
+        sph32 = FORMS[f][2] == 1
+        for stage in ("tree_sort", "tree_emit", "tree_moments", "sph_density", "sph_force"):
+            st = r["stages"].get(stage)
+            b = pass_bytes(stage, n, n_gas, r["nodes"], sph32)
+            if not st or b is None:
+                continue
+            t = st["ms_per_launch"] * 1e-3
+            tkey = f"{f}:{stage}"
+            tr = traffic_db.get(tkey, {}).get("bytes_per_launch") if traffic_db.get("particles") == n else None
+            out[tkey] = {"bound": "hbm", "achieved": b / t / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": b / t / 1e9 / peak, "bytes_per_launch": b, "ms_per_launch": st["ms_per_launch"],
+                         "traffic": tr, "peak_source": peak_src}
+    return out
 
 
 def torch_full_like(torch, t, v):
@@ -465,6 +625,10 @@ def run_gpu(args, world, rank, local):
         res[f]["p99"], res[f]["median"] = G.gravity_error(f, tgt, exact)
 
     batched = G.batched(args.blocks) if args.blocks > 0 else None
+    if batched is not None and learned is not None:  # the same blocks with the previous-h start
+        b0 = G.batched(args.blocks, form="mixed_prevh")
+        batched["with_previous_h_start"] = {"value": b0["value"], "ms_per_block": b0["ms_per_block"],
+                                            "block_end_search": b0["block_end_search"]}
 
     H = res[head]
     # roofline of the dominant kernel of the headline form
@@ -500,6 +664,8 @@ def run_gpu(args, world, rank, local):
                 "frac": achieved / hbm, "traffic": traffic, "peak_source": hbm_src,
                 "work_per_launch": {"bytes": work, "bytes_per_gas_particle": bytes_per_gas[dom]}}
 
+    passes = hbm_passes(res, forms, head, n, n_gas, hbm, hbm_src, traffic_db)
+
     e2e = None
     if not args.no_e2e:
         theta = G.set_form(head)
@@ -531,12 +697,14 @@ def run_gpu(args, world, rank, local):
                "host_buffers": "pinned (page-locked); copies in and out inside each timed call"}
 
     cpu = None
+    parity = None
     if world == 1 and not args.no_cpu:
-        sec, cores = time_cpu(G.d, 3, 1)
+        sec, cores, fo = time_cpu(G.d, 3, 1)
         cpu = {"value": n / sec, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"3 full force evaluations of the {n:,}-particle workload (median) after 1 "
                          "warm-up: oracle restatement of cpp/nbody.cpp (OpenMP) + scipy cKDTree "
                          "(workers=-1) + restated sph_forces (OpenMP), theta 0.7"}
+        parity = parity_vs_oracle(G, fo, head)
 
     def summary(f):
         r = res[f]
@@ -555,6 +723,10 @@ def run_gpu(args, world, rank, local):
                "stages_ms": {k: round(v["ms_per_launch"], 4) for k, v in r["stages"].items()},
                "knn_iterations_per_gas": r["knn_iters"], "walk_interactions": r["pairs"],
                "walk_quadrupole_interactions": r["qpairs"], "steps": len(r["times_ms"])}
+        if r.get("autotune"):
+            out["walk_autotune"] = r["autotune"]
+            out["walk_items"] = (f"runs of sibling groups of <= {r['autotune']['walk_merge']} particles, own spheres"
+                                 if r["autotune"]["walk_merge"] else "the reference's groups")
         return out
 
     line = {
@@ -565,11 +737,15 @@ def run_gpu(args, world, rank, local):
         "data": "synthetic",
         "config": {"workload": workload_name(n_gas, n - n_gas), "particles": n, "gas": n_gas,
                    "form": head, "theta": FORMS[head][0], "relative_opening_alpha": FORMS[head][4],
-                   "walk_merge": FORMS[head][5], "monopole_alpha": FORMS[head][6],
+                   "walk_merge": (H.get("autotune") or {}).get("walk_merge", FORMS[head][5]),
+                   "walk_shape": (H.get("autotune") or {}).get("walk_shape", 0),
+                   "monopole_alpha": FORMS[head][6],
                    "eps_kpc": params.EPS_KPC,
                    "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
         "roofline": roof,
+        "hbm_passes": passes,
         "cpu_baseline": cpu,
+        "parity": parity,
         "e2e": e2e,
         "gpu_launches": H["launches"],
         "clocks": clk,
@@ -633,7 +809,7 @@ def run_drift(args, world, rank, local):
     float64 energy / angular-momentum drift of each."""
     if rank != 0:
         return
-    G = Gpu(args, local, 4)
+    G = Gpu(args, local, 4, ic="device")
     torch, lib, L, p = G.torch, G.lib, G._lib, G.params
     G.collect_pairs(2_000_000, collect_steps=2, start=True)
     G.train_hguess(collected=True)
@@ -718,6 +894,7 @@ def run_drift(args, world, rank, local):
         "simulated_time_per_wall_second_ratio": r / r0,
         "diagnostics": "gf_sim_diagnostics: float64 sums; potential from a monopole walk at theta 0.5",
         "thermal_update": "u += dt du/dt at every (sub-)step, floored at 1e4 K (simulation.py:97-102); no cooling",
+        "initial_conditions": G.ic,
     }), flush=True)
     lib.gf_sim_thermo(0, None)
 

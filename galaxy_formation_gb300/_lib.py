@@ -50,6 +50,11 @@ SIGNATURES = {
                               _ci, _vp, _vp, _vp], _ci),
     "gf_accelerations": ([_ci, _dbl, _dbl, _dbl, np.ctypeslib.ndpointer(np.int8, flags="C_CONTIGUOUS"),
                           _dbl, _cd, _cd, _cd, _cd, _cd, _vp, _ci, _ci, _ci, _dbl, _dbl], _ci),
+    "gf_ic_generate_dev": ([_ci, _ci, _ci, ctypes.c_ulonglong, _dbl, _ci, _vp, _vp, _vp, _vp, _vp, _vp], _ci),
+    "gf_ic_generate": ([_ci, _ci, _ci, ctypes.c_ulonglong, _dbl, _ci, _dbl, _dbl, _dbl,
+                        np.ctypeslib.ndpointer(np.int8, flags="C_CONTIGUOUS"), _dbl], _ci),
+    "gf_force_autotune": ([_cd, ctypes.POINTER(_ci), ctypes.POINTER(_ci), ctypes.POINTER(_cd)], _ci),
+    "gf_force_read_gas": ([_ci, ctypes.POINTER(_ci), _vp, _vp, _vp, _vp, _vp, _vp, _vp], _ci),
     "gf_force_info": ([ctypes.POINTER(_ci), ctypes.POINTER(_cd), ctypes.POINTER(_cd),
                        ctypes.POINTER(ctypes.c_longlong)], _ci),
     "gf_sim_init": ([_ci, _dbl, _dbl, _dbl, np.ctypeslib.ndpointer(np.int8, flags="C_CONTIGUOUS"), _dbl,
@@ -92,6 +97,10 @@ SIGNATURES = {
     "gf_fp32_peak": ([ctypes.POINTER(_cd)], _ci),
 }
 
+# status bits (include/gfgpu.h)
+GF_ERR_CUDA, GF_ERR_ARG, GF_ERR_NONFINITE, GF_ERR_WALK_STACK = 1, 2, 4, 8
+GF_ERR_DEEP_CELL, GF_ERR_KNN, GF_ERR_NO_DEVICE, GF_ERR_CAPACITY = 16, 32, 64, 128
+
 OPT_SPH_FLOAT32 = 0
 OPT_GRAVITY_QUAD = 1
 OPT_HGUESS = 2
@@ -101,10 +110,11 @@ OPT_WALK_GROUP = 5
 OPT_GRAVITY_REL = 6
 OPT_WALK_MERGE = 7
 OPT_GRAVITY_REL_MONO = 8
+OPT_WALK_SHAPE = 9
 MLP_PARAMS = 4545
 
 STAGES = ["tree_build", "tree_refit", "walk", "group_prep", "knn", "knn_tree", "sph_density",
-          "sph_force", "verlet", "force"]
+          "sph_force", "verlet", "force", "tree_sort", "tree_emit", "tree_moments"]
 
 LIB_PATH = _build.LIB
 _lib = None
@@ -134,6 +144,21 @@ def load(path=None):
     if path == LIB_PATH:
         _lib = lib
     return lib
+
+
+def read_gas(lib):
+    """The gas state of the last hydro step (gf_force_read_gas) as numpy arrays: dict of gidx,
+    h, rho, dudt, dt_i, acc_sph (ng,3), nb (ng,32); empty dict when it had no hydro."""
+    ng = ctypes.c_int()
+    check(lib.gf_force_read_gas(0, ctypes.byref(ng), None, None, None, None, None, None, None))
+    m = ng.value
+    if m <= 0:
+        return {}
+    out = {"gidx": np.empty(m, np.int32), "h": np.empty(m), "rho": np.empty(m), "dudt": np.empty(m),
+           "dt_i": np.empty(m), "acc_sph": np.empty((m, 3)), "nb": np.empty((m, 32), np.int32)}
+    check(lib.gf_force_read_gas(m, ctypes.byref(ng), *(out[k].ctypes.data for k in
+                                                       ("gidx", "h", "rho", "dudt", "dt_i", "acc_sph", "nb"))))
+    return out
 
 
 def check(status=None):

@@ -129,6 +129,7 @@ void nbody_render(int n, const double* pos, const uint8_t* group, int ngroups, c
     guarded([&] {
         require(n >= 0 && ngroups >= 0 && W >= 0 && H >= 0, "negative size");
         require(img && rot && center && (n == 0 || (pos && group)), "null array");
+        for (int i = 0; i < n; ++i) require(group[i] < ngroups, "group index >= ngroups");
         cudaStream_t s = ctx().stream;
         const double* d_pos = upload(g_st.pos, pos, 3 * size_t(n), s);
         const uint8_t* d_grp = upload(g_st.group, group, size_t(n), s);
@@ -154,6 +155,53 @@ void nbody_tonemap(int W, int H, int ngroups, const float* img, const float* glo
         uint8_t* d_out = g_st.out.get<uint8_t>(3 * size_t(W) * H);
         render_tonemap(W, H, ngroups, d_img, d_glow, gw, gh, d_col, inv_ref, K, exposure, d_out, s);
         download(out, d_out, 3 * size_t(W) * H, s);
+        collect_status(s);
+    });
+}
+
+namespace {
+void ic_args_check(int kind, int n_gas, int n_dm, const double* params, int nparams) {
+    require(kind == 0 || kind == 1, "kind must be 0 (cloud) or 1 (disk + halo)");
+    require(n_gas >= 1 && n_dm >= 0 && (long long)n_gas + n_dm < (1ll << 30), "bad particle counts");
+    require(params && nparams >= 13, "need 13 parameters");
+    for (int i = 0; i < 13; ++i) require(std::isfinite(params[i]), "non-finite parameter");
+    require(params[0] > 0 && params[1] > 0 && params[1] < 1 && params[2] > 0, "bad mass, baryon fraction or radius");
+    if (kind == 1) {
+        require(params[5] >= 0 && params[5] <= 1 && params[6] > 0 && params[7] > 0, "bad disk parameters");
+        require(params[8] >= 0 && params[9] >= 0 && params[10] > 0, "bad clump parameters");
+        require(params[11] > 0 && params[12] >= params[11], "bad energy range");
+    }
+}
+}  // namespace
+
+int gf_ic_generate_dev(int kind, int n_gas, int n_dm, unsigned long long seed, const double* params,
+                       int nparams, double* pos, double* vel, double* mass, int8_t* kind_out, double* u,
+                       void* stream) {
+    return guarded([&] {
+        ic_args_check(kind, n_gas, n_dm, params, nparams);
+        require(pos && vel && mass && kind_out && u, "null array");
+        ic_generate(kind, n_gas, n_dm, seed, params, pos, vel, mass, kind_out, u, pick(stream));
+    });
+}
+
+int gf_ic_generate(int kind, int n_gas, int n_dm, unsigned long long seed, const double* params, int nparams,
+                   double* pos, double* vel, double* mass, int8_t* kind_out, double* u) {
+    return guarded([&] {
+        ic_args_check(kind, n_gas, n_dm, params, nparams);
+        require(pos && vel && mass && kind_out && u, "null array");
+        const size_t n = size_t(n_gas) + size_t(n_dm);
+        cudaStream_t s = ctx().stream;
+        double* d_pos = g_st.pos.get<double>(3 * n);
+        double* d_vel = g_st.vel.get<double>(3 * n);
+        double* d_mass = g_st.mass.get<double>(n);
+        int8_t* d_kind = g_st.kind.get<int8_t>(n);
+        double* d_u = g_st.u.get<double>(n);
+        ic_generate(kind, n_gas, n_dm, seed, params, d_pos, d_vel, d_mass, d_kind, d_u, s);
+        download(pos, d_pos, 3 * n, s);
+        download(vel, d_vel, 3 * n, s);
+        download(mass, d_mass, n, s);
+        download(kind_out, d_kind, n, s);
+        download(u, d_u, n, s);
         collect_status(s);
     });
 }
@@ -580,6 +628,10 @@ int gf_set_option(int key, double value) {
                 require(value >= 0 && value < 1, "monopole tolerance is in [0, 1)");
                 F.grav_rel_mono = value;
                 break;
+            case GF_OPT_WALK_SHAPE:
+                require(value >= 0 && value < kNumWalkShapes && value == int(value), "walk shape is 0..3");
+                F.walk_shape = int(value);
+                break;
             case GF_OPT_GRAVITY_REL:
                 require(value >= 0 && value < 1, "relative opening tolerance is in [0, 1)");
                 F.grav_rel = value;
@@ -602,6 +654,7 @@ double gf_get_option(int key) {
         case GF_OPT_GRAVITY_REL: return F.grav_rel;
         case GF_OPT_WALK_MERGE: return F.walk_merge;
         case GF_OPT_GRAVITY_REL_MONO: return F.grav_rel_mono;
+        case GF_OPT_WALK_SHAPE: return F.walk_shape;
         default: return -1.0;
     }
 }
@@ -869,13 +922,50 @@ int gf_force_stats(double* out, int nout) {
         ForceEngine& F = force_engine();
         GF_CUDA(cudaDeviceSynchronize());
         const HydroScalars* h = F.scalars_h;
-        TreeCounts kc{};
+        TreeCounts kc{}, gc{};
         if (F.knn_tree.valid)
             GF_CUDA(cudaMemcpy(&kc, F.knn_tree.counts.p, sizeof kc, cudaMemcpyDeviceToHost));
-        const double v[8] = {h ? double(F.ng) : 0.0, h ? h->dt_grav : 0.0, h ? h->dt_gas : 0.0,
-                             h ? double(h->knn_iters) : 0.0, double(kc.pad[1]), double(F.full_searches),
-                             double(F.verlet_hits), double(F.knn_tree.nn)};
-        for (int i = 0; i < nout && i < 8; ++i) out[i] = v[i];
+        if (F.grav.valid)  // the device count: also right after a synchronisation-free rebuild
+            GF_CUDA(cudaMemcpy(&gc, F.grav.counts.p, sizeof gc, cudaMemcpyDeviceToHost));
+        const double v[9] = {h ? double(F.ng) : 0.0, h ? h->dt_grav : 0.0, h ? h->dt_gas : 0.0,
+                             h ? double(h->knn_iters) : 0.0, double(kc.reserved), double(F.full_searches),
+                             double(F.verlet_hits), double(F.knn_tree.nn), double(gc.total_nodes)};
+        for (int i = 0; i < nout && i < 9; ++i) out[i] = v[i];
+    });
+}
+
+int gf_force_autotune(double eps, int* walk_merge, int* walk_shape, double* walk_ms) {
+    return guarded([&] {
+        require(eps > 0 && std::isfinite(eps), "bad eps");
+        GF_CUDA(cudaDeviceSynchronize());
+        force_engine().autotune_walk(eps, ctx().stream, walk_merge, walk_shape, walk_ms);
+        collect_status(ctx().stream);
+    });
+}
+
+int gf_force_read_gas(int cap, int* n_gas, int32_t* gidx, double* h, double* rho, double* dudt, double* dt_i,
+                      double* acc_sph, int32_t* nb32) {
+    return guarded([&] {
+        ForceEngine& F = force_engine();
+        GF_CUDA(cudaDeviceSynchronize());
+        const int ng = F.ng_valid;
+        if (n_gas) *n_gas = ng;
+        if (ng <= 0) return;
+        require(cap >= ng || !(gidx || h || rho || dudt || dt_i || acc_sph || nb32),
+                "output rows fewer than the gas particles");
+        cudaStream_t s = ctx().stream;
+        download(gidx, F.gidx.as<int32_t>(), gidx ? size_t(ng) : 0, s);
+        download(h, F.h.as<double>(), h ? size_t(ng) : 0, s);
+        download(rho, F.rho.as<double>(), rho ? size_t(ng) : 0, s);
+        download(dudt, F.dudt.as<double>(), dudt ? size_t(ng) : 0, s);
+        download(dt_i, F.dt_i.as<double>(), dt_i ? size_t(ng) : 0, s);
+        download(acc_sph, F.gacc.as<double>(), acc_sph ? 3 * size_t(ng) : 0, s);
+        if (nb32) {
+            require(F.last_nb != nullptr, "no neighbour rows");
+            GF_CUDA(cudaMemcpy2DAsync(nb32, 32 * sizeof(int32_t), F.last_nb, 48 * sizeof(int32_t),
+                                      32 * sizeof(int32_t), size_t(ng), cudaMemcpyDeviceToHost, s));
+        }
+        GF_CUDA(cudaStreamSynchronize(s));
     });
 }
 

@@ -239,6 +239,9 @@ enum Stage {
     kStSphForce,       // force kernel alone
     kStVerlet,         // Verlet reselection
     kStForce,          // one whole force evaluation
+    kStTreeSort,       // radix sort of the gravity tree's Morton keys
+    kStTreeEmit,       // node emission of the gravity tree (k_emit)
+    kStTreeMoments,    // moments pass of the gravity tree build
     kStCount
 };
 

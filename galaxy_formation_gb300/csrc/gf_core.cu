@@ -67,7 +67,9 @@ void Profiler::clear() {
     }
 }
 
-ProfScope::ProfScope(int st, cudaStream_t st_s) : stage(st), s(st_s), on(g_ctx.prof.on) {
+// a stage id outside [0, kStCount) records nothing
+ProfScope::ProfScope(int st, cudaStream_t st_s)
+    : stage(st), s(st_s), on(g_ctx.prof.on && st >= 0 && st < kStCount) {
     if (!on) return;
     Profiler& P = g_ctx.prof;
     cudaEvent_t a = P.take(), b = P.take();

@@ -331,7 +331,8 @@ void ForceEngine::evaluate(const ForceArgs& a, cudaStream_t s) {
         else
             T.refit(a.pos, a.mass, s);
     } else if (a.rebuild || !T.valid || T.n != n || T.quad != (gravity_quad != 0) || T.group_max != gmax) {
-        const bool same_set = T.valid && T.n == n && T.quad == (gravity_quad != 0) && T.group_max == gmax;
+        const bool same_set = T.valid && T.n == n && T.quad == (gravity_quad != 0) && T.group_max == gmax &&
+                              !T.outgrowing();
         T.quad = gravity_quad != 0;
         T.group_max = gmax;
         if (same_set) {
@@ -346,7 +347,7 @@ void ForceEngine::evaluate(const ForceArgs& a, cudaStream_t s) {
     T.merge_cap = gravity_quad ? walk_merge : 0;
     T.prepare_walk(a.active, s, a.walk_chunk ? a.walk_chunk : walk_chunk, rel ? acc_grav.as<double>() : nullptr,
                    rel ? float(grav_rel) : 0.f, rel ? float(grav_rel_mono) : 0.f);
-    T.walk(a.eps, acc_grav.as<double>(), s, nullptr, a.walk_npl);
+    T.walk(a.eps, acc_grav.as<double>(), s, nullptr, a.walk_npl, a.walk_shape >= 0 ? a.walk_shape : walk_shape);
     if (!a.active) have_aold = true;  // every particle has a previous gravity now
 
     if (fork) {
@@ -369,6 +370,45 @@ void ForceEngine::evaluate(const ForceArgs& a, cudaStream_t s) {
     GF_CHECK_LAUNCH();
     GF_CUDA(cudaMemcpyAsync(scalars_h, sc, sizeof(HydroScalars), cudaMemcpyDeviceToHost, s));
     (void)C;
+}
+
+void ForceEngine::autotune_walk(double eps, cudaStream_t s, int* merge_out, int* shape_out, double* ms_out) {
+    Octree& T = grav;
+    if (!T.valid || !T.quad || !gravity_quad)
+        throw Error(GF_ERR_ARG, "the walk autotuner needs a mixed-form (quadrupole) evaluation first");
+    const bool rel = grav_rel > 0 && have_aold;
+    double* ta = tune_acc.get<double>(3 * size_t(T.n));
+    static const int merges[] = {0, 24, 32, 40, 48, 64};
+    Event e0, e1;
+    double best = INFINITY;
+    int best_m = walk_merge, best_s = walk_shape;
+    for (int m : merges) {
+        for (int shape = 0; shape < kNumWalkShapes; ++shape) {
+            double ms[3];
+            for (int r = 0; r < 3; ++r) {
+                T.merge_cap = m;
+                T.prepare_walk(nullptr, s, 0, rel ? acc_grav.as<double>() : nullptr, rel ? float(grav_rel) : 0.f,
+                               rel ? float(grav_rel_mono) : 0.f);
+                e0.record(s);
+                T.walk(eps, ta, s, nullptr, 2, shape);
+                e1.record(s);
+                GF_CUDA(cudaStreamSynchronize(s));
+                ms[r] = e1.since(e0);
+            }
+            std::sort(ms, ms + 3);
+            if (ms[1] < best) {
+                best = ms[1];
+                best_m = m;
+                best_s = shape;
+            }
+        }
+    }
+    walk_merge = best_m;
+    walk_shape = best_s;
+    T.merge_cap = best_m;
+    if (merge_out) *merge_out = best_m;
+    if (shape_out) *shape_out = best_s;
+    if (ms_out) *ms_out = best;
 }
 
 void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
@@ -473,8 +513,9 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
                   hguess == 2 && have_hprev && mlp().ready, collect ? hdk.get<float>(ng) : nullptr};
         const bool features = collect || hg.use_mlp;
         GF_CUDA(cudaMemsetAsync(&sc->knn_iters, 0, sizeof(unsigned long long), s));
+        // the gas of the last full search, moved (same count): rebuild without a host round trip
         knn_exact(knn_tree, ng, gp, kq, rg, nullptr, nullptr, &sc->knn_iters, s, nb, kCand, d31, kNgb - 1,
-                  features ? &hg : nullptr);
+                  features ? &hg : nullptr, order_ng == ng);
         if (collect) {
             const long long take = std::min<long long>(ng, collect_cap - collect_n);
             k_collect<<<div_up(take, kThreads), kThreads, 0, s>>>(int(take), collect_n, hg.X, hg.dk,
@@ -490,6 +531,7 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
         full_searches += 1;
         order_ng = ng;
     }
+    last_nb = nb;
     double* hh = h.get<double>(ng);
     k_smoothing<<<ggrid, kThreads, 0, s>>>(ng, d31, a.eps, gi, hh, h_prev.as<double>(), sub);
     GF_CHECK_LAUNCH();

@@ -40,6 +40,7 @@ struct ForceArgs {
     // reference's groups); used with an active set
     int walk_chunk = 0;
     int walk_npl = 2;  // mixed walk: nodes per lane and round (2, or 8 for walks of a few items)
+    int walk_shape = -1;  // mixed walk's launch shape (kNumWalkShapes); -1: the engine's option
     // vel and u may still be arriving (copies on another stream): the hydro chain waits for
     // this event before it reads them; the gravity chain does not need them
     cudaEvent_t late_inputs = nullptr;
@@ -53,6 +54,7 @@ struct ForceEngine {
     int walk_group = 64;     // mixed form: walk groups = shallowest nodes with <= this many particles
     int walk_merge = 0;      // mixed form: walk items = runs of consecutive sibling groups of <= this
                              // many particles (0: one item per group)
+    int walk_shape = 0;      // mixed form: launch shape of the walk (block warps x tile size)
     // mixed form: relative opening criterion with this tolerance (0 = the geometric criterion
     // at the caller's theta). It takes the gravity of the previous evaluation of the same
     // particle set as the error scale: the first evaluation (and every one before an
@@ -70,6 +72,7 @@ struct ForceEngine {
     int order_ng = -1;       // gas count of the last full neighbour search
     int ng = 0, ng_valid = 0;
     bool cache_valid = false, have_hprev = false;
+    const int* last_nb = nullptr;  // neighbour rows (48 columns, the 32 nearest first) of the last hydro call
     long long full_searches = 0, verlet_hits = 0;
     Octree grav;             // gravity tree of the fused path
     Octree knn_tree;
@@ -93,7 +96,8 @@ struct ForceEngine {
         for (unsigned long long v : {(unsigned long long)sph_float32, (unsigned long long)gravity_quad,
                                      (unsigned long long)walk_chunk, (unsigned long long)walk_group,
                                      (unsigned long long)hguess, rel_bits, (unsigned long long)have_aold,
-                                     (unsigned long long)walk_merge, (unsigned long long)(grav_rel_mono * 1e12)})
+                                     (unsigned long long)walk_merge, (unsigned long long)(grav_rel_mono * 1e12),
+                                     (unsigned long long)walk_shape})
             k = (k ^ v) * 1099511628211ull;
         return k;
     }
@@ -110,6 +114,11 @@ struct ForceEngine {
         }
     }
     void hydro(const ForceArgs& a, cudaStream_t s);
+    // Autotuner of the mixed walk of full evaluations: on the tree and error scale of the last
+    // evaluation, times the walk for each item size (merge cap) and launch shape and keeps the
+    // fastest as walk_merge / walk_shape.
+    void autotune_walk(double eps, cudaStream_t s, int* merge_out, int* shape_out, double* ms_out);
+    DevBuf tune_acc;
 };
 
 ForceEngine& force_engine();

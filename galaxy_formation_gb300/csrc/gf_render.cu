@@ -10,11 +10,15 @@ namespace gf {
 
 namespace {
 
-__global__ void k_splat(int n, const double* __restrict__ pos, const uint8_t* __restrict__ group,
+__global__ void k_splat(int n, const double* __restrict__ pos, const uint8_t* __restrict__ group, int ngroups,
                         const double* __restrict__ rot, const double* __restrict__ center, double scale,
-                        int W, int H, float* __restrict__ img) {
+                        int W, int H, float* __restrict__ img, uint32_t* status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (group[i] >= ngroups) {  // no image plane for this group: skipped, reported
+        raise_status(status, GF_ERR_ARG);
+        return;
+    }
     const size_t plane = size_t(W) * H;
     const double x = pos[3 * size_t(i)] - center[0], y = pos[3 * size_t(i) + 1] - center[1],
                  z = pos[3 * size_t(i) + 2] - center[2];
@@ -66,7 +70,7 @@ void render_splat(int n, const double* pos, const uint8_t* group, int ngroups, c
                   const double* center, double scale, int W, int H, float* img, cudaStream_t s) {
     GF_CUDA(cudaMemsetAsync(img, 0, sizeof(float) * size_t(ngroups) * W * H, s));
     if (n <= 0) return;
-    k_splat<<<div_up(n, 256), 256, 0, s>>>(n, pos, group, rot, center, scale, W, H, img);
+    k_splat<<<div_up(n, 256), 256, 0, s>>>(n, pos, group, ngroups, rot, center, scale, W, H, img, ctx().d_status);
     GF_CHECK_LAUNCH();
 }
 

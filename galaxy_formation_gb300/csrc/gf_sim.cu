@@ -289,6 +289,7 @@ __global__ void k_active_at(int n, const int8_t* __restrict__ level, int s, uint
 struct BlockTuning {
     int chunk[8] = {4, 8, 8, 16, 16, 32, 64, 64};  // walk items of <= chunk active particles (0: groups)
     int npl[8] = {8, 8, 8, 2, 2, 2, 2, 2};         // mixed walk: nodes per lane and round (2 or 8)
+    int shape[8] = {0, 0, 0, 0, 0, 0, 0, 0};       // mixed walk with 2 per lane: launch shape
     int rebuild_every = 8;  // captured tree rebuild every this many sub-steps (0: refit only)
 };
 
@@ -347,7 +348,8 @@ struct BlockIntegrator {
 
     // nosync: inside the captured graph (rebuild = captured tree rebuild, else refit);
     // otherwise a regular evaluation of everybody on a rebuilt tree with fresh neighbours
-    void force(Simulation& S, const uint8_t* active, bool nosync, bool rebuild = false, int chunk = 0, int npl = 2) {
+    void force(Simulation& S, const uint8_t* active, bool nosync, bool rebuild = false, int chunk = 0, int npl = 2,
+               int shape = -1) {
         ForceArgs a{S.n, S.pos.as<double>(), S.vel.as<double>(), S.mass.as<double>(), S.kind.as<int8_t>(),
                     S.u.as<double>(), S.theta, S.eps, S.gamma, S.alpha, S.beta, active,
                     nosync ? (rebuild ? 1 : 0) : 1, 1, nosync ? 0 : 1, S.acc.as<double>(), S.dt_ind.as<double>()};
@@ -355,6 +357,7 @@ struct BlockIntegrator {
         a.nosync = nosync ? 1 : 0;
         a.walk_chunk = chunk;
         a.walk_npl = npl;
+        a.walk_shape = shape;
         force_engine().evaluate(a, S.s());
     }
 
@@ -381,7 +384,7 @@ struct BlockIntegrator {
                 GF_CHECK_LAUNCH();
                 const bool rb = tune.rebuild_every > 0 && sub % tune.rebuild_every == 0;
                 thermo_at(S, sub);
-                force(S, ac, true, rb, tune.chunk[bin_of(sub)], tune.npl[bin_of(sub)]);
+                force(S, ac, true, rb, tune.chunk[bin_of(sub)], tune.npl[bin_of(sub)], tune.shape[bin_of(sub)]);
                 k_kick_levels<<<div_up(S.n, 256), 256, 0, s>>>(S.n, S.vel.as<double>(), S.acc.as<double>(),
                                                                level.as<int8_t>(), d, 1, sub);
                 GF_CHECK_LAUNCH();
@@ -493,33 +496,40 @@ struct BlockIntegrator {
                                                              d + 1);
                 GF_CHECK_LAUNCH();
                 double best = INFINITY;
-                int best_c = 0, best_p = 2;
+                int best_c = 0, best_p = 2, best_s = 0;
                 for (int npl : {2, 8}) {
                     if (npl != 2 && !T.quad) continue;  // the monopole walk has one width
-                    for (int c : cand) {
-                        double ms[3];
-                        for (int r = 0; r < 3; ++r) {
-                            e0.record(s);
-                            T.prepare_walk(act.as<uint8_t>(), s, c);
-                            T.walk(S.eps, ta, s, nullptr, npl);
-                            e1.record(s);
-                            GF_CUDA(cudaStreamSynchronize(s));
-                            ms[r] = e1.since(e0);
-                        }
-                        std::sort(ms, ms + 3);
-                        if (ms[1] < best * 0.97) {  // prefer the earlier candidate on near-ties
-                            best = ms[1];
-                            best_c = c;
-                            best_p = npl;
+                    // launch shapes (block warps x tile size) of the 2-per-lane mixed walk
+                    const int nshape = npl == 2 && T.quad ? kNumWalkShapes : 1;
+                    for (int shape = 0; shape < nshape; ++shape) {
+                        for (int c : cand) {
+                            double ms[3];
+                            for (int r = 0; r < 3; ++r) {
+                                e0.record(s);
+                                T.prepare_walk(act.as<uint8_t>(), s, c);
+                                T.walk(S.eps, ta, s, nullptr, npl, shape);
+                                e1.record(s);
+                                GF_CUDA(cudaStreamSynchronize(s));
+                                ms[r] = e1.since(e0);
+                            }
+                            std::sort(ms, ms + 3);
+                            if (ms[1] < best * 0.97) {  // prefer the earlier candidate on near-ties
+                                best = ms[1];
+                                best_c = c;
+                                best_p = npl;
+                                best_s = shape;
+                            }
                         }
                     }
                 }
                 tune.chunk[bin] = best_c;
                 tune.npl[bin] = best_p;
+                tune.shape[bin] = best_s;
             }
             for (int bin = nlev - 1; bin < 8; ++bin) {
                 tune.chunk[bin] = tune.chunk[std::max(0, nlev - 2)];
                 tune.npl[bin] = tune.npl[std::max(0, nlev - 2)];
+                tune.shape[bin] = tune.shape[std::max(0, nlev - 2)];
             }
             // rebuild cadence: whole blocks from the same start
             static const int every[] = {0, 32, 16, 8, 4};
@@ -556,8 +566,9 @@ struct BlockIntegrator {
         GF_CUDA(cudaStreamSynchronize(s));
         S.t = t0;
         started = false;
-        if (chunk_out)  // chunk, with 100 added where the 8-nodes-per-lane walk won
-            for (int b = 0; b < nlev - 1; ++b) chunk_out[b] = tune.chunk[b] + (tune.npl[b] > 2 ? 100 : 0);
+        if (chunk_out)  // chunk, + 100 where the 8-nodes-per-lane walk won, + 1000 x the launch shape
+            for (int b = 0; b < nlev - 1; ++b)
+                chunk_out[b] = tune.chunk[b] + (tune.npl[b] > 2 ? 100 : 0) + 1000 * tune.shape[b];
         if (rebuild_out) *rebuild_out = tune.rebuild_every;
     }
 };
@@ -577,7 +588,8 @@ void block_config(const int* chunk, int nbins, int rebuild_every) {
     for (int b = 0; b < 8; ++b) {
         const int c = chunk ? chunk[std::min(b, nbins - 1)] : 0;
         t.chunk[b] = c % 100;
-        t.npl[b] = c >= 100 ? 8 : 2;
+        t.npl[b] = (c % 1000) >= 100 ? 8 : 2;
+        t.shape[b] = std::min(kNumWalkShapes - 1, std::max(0, c / 1000));
     }
     t.rebuild_every = rebuild_every;
     g_block.tune_changed = true;

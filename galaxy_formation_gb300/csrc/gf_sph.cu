@@ -72,13 +72,30 @@ __global__ void k_sph_kernel(int n, const double* __restrict__ r, const double* 
     if (dw) dw[i] = dw_m4(r[i], h[i]);
 }
 
+// A neighbour row from the caller may hold an index outside [0, n): such a particle gets NaN
+// outputs and GF_ERR_ARG is raised (status may be null), instead of a read out of bounds.
+template <class Idx>
+__device__ __forceinline__ bool row_in_range(const Idx* __restrict__ row, int k, int n, uint32_t* status) {
+    bool ok = true;
+    for (int jj = 0; jj < k; ++jj) {
+        const int64_t j = row[jj];
+        ok &= j >= 0 && j < n;
+    }
+    if (!ok) raise_status(status, GF_ERR_ARG);
+    return ok;
+}
+
 // pass 1 (sph.py:63-71): rho_i = sum_j m_j W(r_ij, h_i), the particle itself included
 template <class Idx>
 __global__ void k_sph_density(int n, int k, int ld, const double* __restrict__ pos, const double* __restrict__ mass,
                               const Idx* __restrict__ nb, const double* __restrict__ h,
-                              double* __restrict__ rho, Subset sub) {
+                              double* __restrict__ rho, Subset sub, uint32_t* status) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (!subset_item(sub, i, n, nullptr, i)) return;
+    if (!row_in_range(nb + size_t(i) * ld, k, n, status)) {
+        rho[i] = __longlong_as_double(0x7ff8000000000000ll);
+        return;
+    }
     const double xi = pos[3 * size_t(i)], yi = pos[3 * size_t(i) + 1], zi = pos[3 * size_t(i) + 2];
     const double hi = h[i];
     double s = 0.0;
@@ -123,9 +140,16 @@ __global__ void k_sph_force(int n, int k, int ld, const double* __restrict__ pos
                             const double* __restrict__ h, const double* __restrict__ rho,
                             const double* __restrict__ pr2, const double* __restrict__ cs, double alpha,
                             double beta, double* __restrict__ acc, double* __restrict__ dudt,
-                            double* __restrict__ dt_i, float* __restrict__ divv, Subset sub) {
+                            double* __restrict__ dt_i, float* __restrict__ divv, Subset sub, uint32_t* status) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (!subset_item(sub, i, n, nullptr, i)) return;
+    if (!row_in_range(nb + size_t(i) * ld, k, n, status)) {
+        const double nan = __longlong_as_double(0x7ff8000000000000ll);
+        acc[3 * size_t(i)] = acc[3 * size_t(i) + 1] = acc[3 * size_t(i) + 2] = nan;
+        dudt[i] = dt_i[i] = nan;
+        if (divv) divv[i] = __int_as_float(0x7fc00000);
+        return;
+    }
     const double xi = pos[3 * size_t(i)], yi = pos[3 * size_t(i) + 1], zi = pos[3 * size_t(i) + 2];
     const double vxi = vel[3 * size_t(i)], vyi = vel[3 * size_t(i) + 1], vzi = vel[3 * size_t(i) + 2];
     const double hi = h[i], rhoi = rho[i], pri = pr2[i], ci = cs[i];
@@ -196,25 +220,57 @@ __device__ void warp_bitonic(K* key, int* tag, int P) {
     }
 }
 
-// Ascending bitonic sort of P (power of two <= 128) 64-bit keys in shared memory by the
-// calling warp (keys are unique when they carry an index in their low bits).
-__device__ void warp_sort_u64(unsigned long long* key, int P) {
+// Ascending bitonic sort of 32 R 64-bit keys held in registers, key e = 32 r + lane in v[r]:
+// strides below 32 exchange with lane ^ stride by shuffles, larger ones between a lane's own
+// registers. No shared memory (a shared-memory network of 64-bit keys takes 2-way bank
+// conflicts at every stride below 16).
+template <int R>
+__device__ __forceinline__ void reg_bitonic(unsigned long long (&v)[R]) {
     const int lane = threadIdx.x & 31;
-    for (int size = 2; size <= P; size <<= 1) {
+    constexpr int N = 32 * R;
+#pragma unroll
+    for (int size = 2; size <= N; size <<= 1) {
+#pragma unroll
         for (int stride = size >> 1; stride > 0; stride >>= 1) {
-            for (int t = lane; t < P / 2; t += 32) {
-                const int a = ((t & ~(stride - 1)) << 1) | (t & (stride - 1));
-                const int b = a + stride;
-                const bool up = (a & size) == 0;
-                const unsigned long long ka = key[a], kb = key[b];
-                if ((ka > kb) == up) {
-                    key[a] = kb;
-                    key[b] = ka;
+            if (stride >= 32) {
+                const int rs = stride >> 5;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const int p = r ^ rs;
+                    if (p > r) {
+                        const bool up = ((32 * r) & size) == 0;
+                        const unsigned long long a = v[r], b = v[p];
+                        const bool sw = (a > b) == up;
+                        v[r] = sw ? b : a;
+                        v[p] = sw ? a : b;
+                    }
+                }
+            } else {
+                const bool lower = (lane & stride) == 0;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const unsigned long long o = __shfl_xor_sync(0xffffffffu, v[r], stride);
+                    const bool up = ((32 * r + lane) & size) == 0;
+                    v[r] = (lower == up) ? (v[r] < o ? v[r] : o) : (v[r] < o ? o : v[r]);
                 }
             }
-            __syncwarp();
         }
     }
+}
+
+// Sorts key[0, cnt) ascending in place (cnt <= 128), padding to 64 or 128 with ~0: the keys
+// go through registers, and the sorted ones are stored back lane-contiguous.
+template <int R>
+__device__ __forceinline__ void sort_keys_reg(unsigned long long* key, int cnt) {
+    const int lane = threadIdx.x & 31;
+    unsigned long long v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = 32 * r + lane < cnt ? key[32 * r + lane] : ~0ull;
+    __syncwarp();
+    reg_bitonic<R>(v);
+#pragma unroll
+    for (int r = 0; r < R; ++r) key[32 * r + lane] = v[r];
+    __syncwarp();
 }
 
 // --------------------------------------------------------------- knn_from_candidates
@@ -455,11 +511,10 @@ __device__ void knn_finish(const KnnArgs& A, unsigned long long* key, unsigned l
     const int lane = threadIdx.x & 31;
     const int k = A.k;
     const int oq = A.perm[q];
-    int P = 64;
-    while (P < cnt) P <<= 1;
-    for (int t = cnt + lane; t < P; t += 32) key[t] = ~0ull;
-    __syncwarp();
-    warp_sort_u64(key, P);
+    if (cnt <= 64)
+        sort_keys_reg<2>(key, cnt);
+    else
+        sort_keys_reg<4>(key, cnt);
     const int pi = oq;
     if (!A.exact_order) {
         // Float32 order: the k nearest as a set (only pairs tied to float32 rounding can
@@ -477,6 +532,9 @@ __device__ void knn_finish(const KnnArgs& A, unsigned long long* key, unsigned l
         below = warp_sum(below);
         inband = warp_sum(inband);
         double best;
+        // with float32 near-ties around entry c, the float64 order of the tied entries decides
+        // which of them are among the first c + 1 (the set the smoothing length is taken from)
+        const bool reorder = inband > 1 && below + inband <= 64;
         if (inband == 1) {  // no float32 near-tie: entry c itself, measured in float64
             best = d2_f64(A, pi, A.perm[key_idx(key[c])]);
         } else {
@@ -498,7 +556,9 @@ __device__ void knn_finish(const KnnArgs& A, unsigned long long* key, unsigned l
             best = __longlong_as_double((long long)dd[max(0, rank_need)]);
         }
         for (int t = lane; t < k; t += 32) {
-            const int pj = A.perm[key_idx(key[t])];
+            // the tied band [below, below + inband) in float64 order (ties by index): di holds
+            // its entries sorted first
+            const int pj = reorder && t >= below && t < below + inband ? di[t - below] : A.perm[key_idx(key[t])];
             if (A.nb32) A.nb32[size_t(oq) * A.ld32 + t] = pj;
             if (A.nb) A.nb[size_t(oq) * k + t] = pj;
         }
@@ -647,7 +707,7 @@ void sph_forces(SphScratch& S, int n, int k, int ld, const double* pos, const do
     const int grid = div_up(n, kThreads);
     {
         ProfScope ps(kStSphDensity, s);
-        k_sph_density<Idx><<<grid, kThreads, 0, s>>>(n, k, ld, pos, mass, nb, h, rho, sub);
+        k_sph_density<Idx><<<grid, kThreads, 0, s>>>(n, k, ld, pos, mass, nb, h, rho, sub, ctx().d_status);
         GF_CHECK_LAUNCH();
     }
     double* pr2 = S.pr2.get<double>(n);
@@ -656,7 +716,7 @@ void sph_forces(SphScratch& S, int n, int k, int ld, const double* pos, const do
     GF_CHECK_LAUNCH();
     ProfScope ps(kStSphForce, s);
     k_sph_force<Idx><<<grid, kThreads, 0, s>>>(n, k, ld, pos, vel, mass, nb, h, rho, pr2, cs, alpha, beta,
-                                               acc, dudt, dt_i, divv, sub);
+                                               acc, dudt, dt_i, divv, sub, ctx().d_status);
     GF_CHECK_LAUNCH();
 }
 template void sph_forces<int64_t>(SphScratch&, int, int, int, const double*, const double*, const double*,
@@ -705,11 +765,20 @@ __global__ void k_guess_from_logdk(int n, const float* __restrict__ Y, float* __
 
 void knn_exact(Octree& T, int n, const double* pos, int k, const float* r_guess, int64_t* nb,
                double* dist, unsigned long long* d_iters, cudaStream_t s, int* nb32, int ld32,
-               double* dsel, int dsel_col, const HGuess* hg) {
+               double* dsel, int dsel_col, const HGuess* hg, bool same_set) {
     if (n <= 0) return;
+    // same_set (the caller's point set drifted since the last search): the synchronisation-free
+    // rebuild inside the node buffers of the last regular build (no host round trip in the middle
+    // of the hydro chain), unless the last tree came close to filling them
+    const bool same = same_set && T.valid && T.n == n && T.want_knn && T.leaf_max == kKnnLeaf && !T.outgrowing();
     T.want_knn = true;
     T.leaf_max = kKnnLeaf;
-    T.build(n, pos, nullptr, 0.7, s);
+    if (same) {
+        T.reserve_graph_build();
+        T.build(n, pos, nullptr, 0.7, s, true);
+    } else {
+        T.build(n, pos, nullptr, 0.7, s);
+    }
     if (hg && hg->X) {  // features for the learned guess (and for training pairs)
         k_hfeatures<<<div_up(n, kThreads), kThreads, 0, s>>>(n, T.perm.as<int>(), T.leaf_of.as<int>(),
                                                              T.w_b.as<float4>(), T.w_geo.as<float4>(), hg->gidx,
@@ -725,7 +794,7 @@ void knn_exact(Octree& T, int n, const double* pos, int k, const float* r_guess,
     KnnArgs A{};
     A.n = n;
     A.k = k;
-    A.nn = T.nn;
+    A.nn = std::max(T.nn, T.node_cap);  // bounds the walk rounds (the live count is on the device)
     A.wb = T.w_b.as<float4>();
     A.wgeo = T.w_geo.as<float4>();
     A.p4 = T.p4.as<float4>();
@@ -767,7 +836,10 @@ void knn_exact(Octree& T, int n, const double* pos, int k, const float* r_guess,
 //
 // In host code `g_sph_noalloc_scratch` names a host-side stand-in, not device memory: the
 // device address is fetched with cudaGetSymbolAddress once per device (with that device
-// current) by the first call on that device, and passed to the kernels.
+// current) by the first call on that device, and passed to the kernels. The cached address
+// belongs to the device's context of that moment: after cudaDeviceReset (or a reset of the
+// primary context) the array is loaded anew elsewhere and the cache is stale, so a process
+// that resets a device must not call this entry point on it afterwards.
 
 namespace gf {
 namespace {
@@ -837,10 +909,10 @@ extern "C" int gf_sph_forces_noalloc_dev(int n, int k, const double* pos, const 
     double* cs = scratch + kNoallocMaxN;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int grid = div_up(n, kThreads);
-    k_sph_density<int64_t><<<grid, kThreads, 0, s>>>(n, k, k, pos, mass, nb, h, rho, Subset());
+    k_sph_density<int64_t><<<grid, kThreads, 0, s>>>(n, k, k, pos, mass, nb, h, rho, Subset(), nullptr);
     k_sph_eos<<<grid, kThreads, 0, s>>>(n, rho, u, gamma, pr2, cs, Subset());
     k_sph_force<int64_t><<<grid, kThreads, 0, s>>>(n, k, k, pos, vel, mass, nb, h, rho, pr2, cs, alpha,
-                                                   beta, acc, dudt, dt_i, nullptr, Subset());
+                                                   beta, acc, dudt, dt_i, nullptr, Subset(), nullptr);
     e = cudaGetLastError();
     if (e != cudaSuccess) return noalloc_fail(GF_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
     c.launches += 3;

@@ -52,13 +52,20 @@ void knn_from_candidates(int n, int m, const double* pos, const int64_t* cand, i
 // Exact float64 k nearest neighbours of every point (itself included), ascending; builds
 // the point octree in T. r_guess (caller order, optional): starting search radius.
 // Outputs either nb/dist (n,k) int64/float64, or nb32 (n, ld32) int32 plus the distance of
-// neighbour `dsel_col` in dsel (n,).
+// neighbour `dsel_col` in dsel (n,). same_set: the points are those of the last search on T,
+// moved (the tree is rebuilt without a host synchronisation).
 void knn_exact(Octree& T, int n, const double* pos, int k, const float* r_guess, int64_t* nb,
                double* dist, unsigned long long* d_iters, cudaStream_t s, int* nb32 = nullptr,
-               int ld32 = 0, double* dsel = nullptr, int dsel_col = -1, const HGuess* hg = nullptr);
+               int ld32 = 0, double* dsel = nullptr, int dsel_col = -1, const HGuess* hg = nullptr,
+               bool same_set = false);
 
 void direct_sum(int n, const double* pos, const double* mass, int nt, const int64_t* targets,
                 double* acc, double eps, cudaStream_t s);
+
+// Seeded initial conditions on the device (gf_ic.cu): kind 0 the rotating 1/r cloud, 1 the
+// disk + 1/r halo (+ Plummer clumps); prm: the 13 values documented at gf_ic_generate_dev.
+void ic_generate(int kind, int n_gas, int n_dm, uint64_t seed, const double* prm, double* pos, double* vel,
+                 double* mass, int8_t* kind_out, double* u, cudaStream_t s);
 
 void render_splat(int n, const double* pos, const uint8_t* group, int ngroups, const double* rot,
                   const double* center, double scale, int W, int H, float* img, cudaStream_t s);

@@ -37,7 +37,12 @@ constexpr int kThreads = 256;
 
 // ---------------------------------------------------------------------------- bbox
 
-__global__ void k_bbox_partial(const double* __restrict__ pos, int n, double* __restrict__ part) {
+// float64 bounding box -> root cube (cpp/nbody.cpp:210-219) in one launch: every block reduces
+// its share of the positions and writes a partial; the last block to finish (arrival counter)
+// reduces the partials and writes the root cube. min / max are exact, so the result does not
+// depend on the order of the reductions.
+__global__ void k_bbox(const double* __restrict__ pos, int n, double* __restrict__ part, RootBox* __restrict__ root,
+                       uint32_t* status, int* __restrict__ done) {
     double lo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, hi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
     double bad = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -50,59 +55,63 @@ __global__ void k_bbox_partial(const double* __restrict__ pos, int n, double* __
         }
     }
     __shared__ double s[7][kThreads / 32];
+    __shared__ bool s_last;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    auto block_reduce = [&](double* out) {
 #pragma unroll
-    for (int o = 16; o; o >>= 1) {
+        for (int o = 16; o; o >>= 1) {
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            lo[a] = fmin(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
-            hi[a] = fmax(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = fmin(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+                hi[a] = fmax(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+            }
+            bad = fmax(bad, __shfl_xor_sync(0xffffffffu, bad, o));
         }
-        bad = fmax(bad, __shfl_xor_sync(0xffffffffu, bad, o));
-    }
-    if (lane == 0) {
-        for (int a = 0; a < 3; ++a) {
-            s[a][warp] = lo[a];
-            s[3 + a][warp] = hi[a];
+        if (lane == 0) {
+            for (int a = 0; a < 3; ++a) {
+                s[a][warp] = lo[a];
+                s[3 + a][warp] = hi[a];
+            }
+            s[6][warp] = bad;
         }
-        s[6][warp] = bad;
-    }
+        __syncthreads();
+        if (threadIdx.x < 7) {
+            double v = s[threadIdx.x][0];
+            for (int w = 1; w < kThreads / 32; ++w)
+                v = threadIdx.x < 3 ? fmin(v, s[threadIdx.x][w]) : fmax(v, s[threadIdx.x][w]);
+            out[threadIdx.x] = v;
+        }
+    };
+    block_reduce(part + 7 * size_t(blockIdx.x));
+    __threadfence();
     __syncthreads();
-    if (threadIdx.x < 7) {
-        double v = s[threadIdx.x][0];
-        for (int w = 1; w < kThreads / 32; ++w)
-            v = threadIdx.x < 3 ? fmin(v, s[threadIdx.x][w]) : fmax(v, s[threadIdx.x][w]);
-        part[7 * blockIdx.x + threadIdx.x] = v;
+    if (threadIdx.x == 0) s_last = atomicAdd(done, 1) == int(gridDim.x) - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = DBL_MAX;
+        hi[a] = -DBL_MAX;
     }
-}
-
-__global__ void k_bbox_final(const double* __restrict__ part, int nparts, RootBox* __restrict__ root,
-                             uint32_t* status) {
-    // one warp reduces the block partials
-    double lo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, hi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
-    double bad = 0;
-    for (int b = threadIdx.x; b < nparts; b += 32) {
+    bad = 0.0;
+    for (int b = threadIdx.x; b < int(gridDim.x); b += blockDim.x) {
         for (int a = 0; a < 3; ++a) {
-            lo[a] = fmin(lo[a], part[7 * b + a]);
-            hi[a] = fmax(hi[a], part[7 * b + 3 + a]);
+            lo[a] = fmin(lo[a], __ldcg(&part[7 * size_t(b) + a]));
+            hi[a] = fmax(hi[a], __ldcg(&part[7 * size_t(b) + 3 + a]));
         }
-        bad = fmax(bad, part[7 * b + 6]);
+        bad = fmax(bad, __ldcg(&part[7 * size_t(b) + 6]));
     }
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-        for (int a = 0; a < 3; ++a) {
-            lo[a] = fmin(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
-            hi[a] = fmax(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
-        }
-        bad = fmax(bad, __shfl_xor_sync(0xffffffffu, bad, o));
-    }
+    __shared__ double tot[7];
+    __syncthreads();
+    block_reduce(tot);
+    __syncthreads();
     if (threadIdx.x != 0) return;
-    if (bad > 0) raise_status(status, GF_ERR_NONFINITE);
+    if (tot[6] > 0) raise_status(status, GF_ERR_NONFINITE);
     RootBox R;
     double ext = 0;
     for (int a = 0; a < 3; ++a) {
-        R.c[a] = __dmul_rn(0.5, __dadd_rn(lo[a], hi[a]));
-        ext = fmax(ext, __dsub_rn(hi[a], lo[a]));
+        R.c[a] = __dmul_rn(0.5, __dadd_rn(tot[a], tot[3 + a]));
+        ext = fmax(ext, __dsub_rn(tot[3 + a], tot[a]));
     }
     // 0.5 * max extent * 1.0001 + 1e-12 (cpp/nbody.cpp:219), unfused
     R.half = __dadd_rn(__dmul_rn(__dmul_rn(0.5, ext), 1.0001), 1e-12);
@@ -845,12 +854,17 @@ __global__ void k_walk_fill(int nn, const int4* __restrict__ n_i4, const int* __
 // ---------------------------------------------------------------------------- deep cells
 
 // Positions of cells that still hold > 8 particles at level 21 get extension keys.
+// Extension keys are read (by cpl and digit) only at positions whose level-21 key equals a
+// neighbour's in sorted order, so the others are skipped: they hold stale words that nothing
+// reads. Shared positions outside deep runs get zeros.
 __global__ void k_deep_keys(int n, const uint64_t* __restrict__ k0, const int* __restrict__ perm,
                             const double* __restrict__ pos, const RootBox* __restrict__ rootp,
                             uint64_t* __restrict__ k1, uint64_t* __restrict__ k2,
                             int* __restrict__ starts, int* __restrict__ nstarts, int L) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const uint64_t ki = k0[i];
+    if (!((i > 0 && k0[i - 1] == ki) || (i + 1 < n && k0[i + 1] == ki))) return;
     bool deep = false;
     for (int j = max(0, i - L); j <= i && !deep; ++j)
         deep = j + L < n && k0[j] == k0[j + L];
@@ -982,16 +996,17 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
     const int nparts = std::min(4 * C.sms, std::max(1, grid));
     int* nb = nbase.get<int>(std::max(size_t(n) + 1, size_t(nparts) * 14 + 16));
     double* part = reinterpret_cast<double*>(nb);  // bbox partials, consumed before the scan
-    k_bbox_partial<<<nparts, kThreads, 0, s>>>(pos, n, part);
-    GF_CHECK_LAUNCH();
-    k_bbox_final<<<1, 32, 0, s>>>(part, nparts, R, C.d_status);
+    k_bbox<<<nparts, kThreads, 0, s>>>(pos, n, part, R, C.d_status, &cnt->bbox_done);
     GF_CHECK_LAUNCH();
 
     uint64_t* k0 = key.get<uint64_t>(n);
     int* pm = perm.get<int>(n);
     k_keys<<<grid, kThreads, 0, s>>>(pos, n, R, k0, pm);
     GF_CHECK_LAUNCH();
-    radix_sort_pairs(k0, pm, key_alt.get<uint64_t>(n), perm_alt.get<int>(n), n, 0, 63, s, &scratch);
+    {
+        ProfScope pso(want_knn ? kStCount : kStTreeSort, s);
+        radix_sort_pairs(k0, pm, key_alt.get<uint64_t>(n), perm_alt.get<int>(n), n, 0, 63, s, &scratch);
+    }
 
     int8_t* c9 = cpl9.get<int8_t>(n);
     int8_t* ld = ldepth.get<int8_t>(n);
@@ -1016,7 +1031,7 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
         uint64_t* e1 = key1.get<uint64_t>(n);
         uint64_t* e2 = key2.get<uint64_t>(n);
         int* starts = reinterpret_cast<int*>(key_alt.get<uint64_t>(n));  // scratch
-        int* nst = &cnt->pad[0];
+        int* nst = &cnt->deep_runs;
         k_deep_keys<<<grid, kThreads, 0, s>>>(n, k0, pm, pos, R, e1, e2, starts, nst, leaf_max);
         GF_CHECK_LAUNCH();
         deep_sort_attr();
@@ -1049,8 +1064,11 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
     double4* cd = n_cd.get<double4>(cap);
     float4* geo = n_geo.get<float4>(cap);
     int* par = n_parent.get<int>(cap);
-    k_emit<<<grid, kThreads, 0, s>>>(K, n, R, ld, ds, ns, nb, cnt, i4, cd, geo, par, cap);
-    GF_CHECK_LAUNCH();
+    {
+        ProfScope pse(want_knn ? kStCount : kStTreeEmit, s);
+        k_emit<<<grid, kThreads, 0, s>>>(K, n, R, ld, ds, ns, nb, cnt, i4, cd, geo, par, cap);
+        GF_CHECK_LAUNCH();
+    }
     if (graph_safe) {  // more nodes than the buffers hold: flag, and leave an empty tree
         k_node_cap_check<<<1, 1, 0, s>>>(cnt, cap, C.d_status);
         GF_CHECK_LAUNCH();
@@ -1078,6 +1096,7 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
     } else if (quad) {  // mixed form: float32 monopole + quadrupole in one pass
         Mom32Args A{span, nn_dev, false, theta_f, i4, par, nch, ctr, geo, mom, opr, ndp, pp, nullptr,
                     n_quad.get<float4>(cap), n_qyz.get<float2>(cap)};
+        ProfScope psm(kStTreeMoments, s);
         k_moments_quad32<<<ngrid, kThreads, 0, s>>>(A);
         GF_CHECK_LAUNCH();
     } else {
@@ -1098,6 +1117,7 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
         A.perm = pm;
         A.pos = pos;
         A.mass = mass;
+        ProfScope psm(kStTreeMoments, s);
         k_moments<<<ngrid, kThreads, 0, s>>>(A);
         GF_CHECK_LAUNCH();
     }
@@ -1130,6 +1150,25 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
                                            nn_dev);
     GF_CHECK_LAUNCH();
     valid = true;
+    if (!g_no_alloc) {  // outside a capture: the live node count, for outgrowing()
+        if (!h_live) GF_CUDA(cudaMallocHost(&h_live, sizeof(int)));
+        if (!live_ev) GF_CUDA(cudaEventCreateWithFlags(&live_ev, cudaEventDisableTiming));
+        GF_CUDA(cudaMemcpyAsync(h_live, &cnt->total_nodes, sizeof(int), cudaMemcpyDeviceToHost, s));
+        GF_CUDA(cudaEventRecord(live_ev, s));
+        live_pending = true;
+    }
+}
+
+bool Octree::outgrowing() {
+    if (!live_pending) return false;
+    const cudaError_t e = cudaEventQuery(live_ev);
+    if (e == cudaErrorNotReady) {
+        (void)cudaGetLastError();  // not an error: the copy is still on its way
+        return false;
+    }
+    GF_CUDA(e);
+    live_pending = false;
+    return *h_live > node_cap - node_cap / 8;
 }
 
 // Node kernels cover node_cap and read the live node count on the device, so a refit stays

@@ -11,6 +11,9 @@ constexpr int kGroupMax = 64;    // cpp/nbody.cpp:34
 constexpr int kDepthMax = 48;    // cpp/nbody.cpp:35
 constexpr int kKeyLevels = 21;   // levels held by one 63-bit Morton key word
 constexpr int kDeepRunMax = 4096;
+// launch shapes of the mixed walk: warps per block x interaction tiles (particle / node
+// entries per warp): 0 = 4 x 256/96, 1 = 2 x 256/96, 2 = 4 x 128/64, 3 = 2 x 128/64
+constexpr int kNumWalkShapes = 4;
 
 // Root cube and the fixed-point grid used by the fast key path.
 struct RootBox {
@@ -28,7 +31,9 @@ struct TreeCounts {
     int num_groups;
     int num_work;
     int walk_next;    // dynamic scheduler of the walk
-    int pad[3];
+    int deep_runs;    // level-21 cells holding more than the leaf capacity (their first positions)
+    int reserved;
+    int bbox_done;    // blocks of the bounding-box pass that have written their partials
     unsigned long long pairs;   // list interactions evaluated by the last walk (all kinds)
     unsigned long long qpairs;  // of which with quadrupole nodes (mixed form)
 };
@@ -83,6 +88,14 @@ struct Octree {
     DevBuf root, counts;
     ScanScratch scratch;  // this tree's scan / sort scratch (trees may build on different streams)
     TreeCounts* h_counts = nullptr;  // pinned
+    // node count of the last build outside a captured graph, copied to the host behind it
+    // (read once the copy is done): a synchronisation-free rebuild bounds the tree by node_cap,
+    // so the caller does a regular build (which re-sizes the node buffers) once the tree grows
+    // close to it
+    int* h_live = nullptr;           // pinned
+    cudaEvent_t live_ev = nullptr;
+    bool live_pending = false;
+    bool outgrowing();
 
     // graph_safe: no host synchronisation and no allocation (inside a captured CUDA graph):
     // needs a regular build of the same particle set first (node_cap from it; a tree that
@@ -103,7 +116,8 @@ struct Octree {
                       float alpha = 0.f, float alpha_q = 0.f);
     // pot (monopole trees, may be null): softened potentials of the walked particles
     // npl: nodes per lane and round of the mixed walk (2, or 8 for walks of a few items)
-    void walk(double eps, double* acc, cudaStream_t s, double* pot = nullptr, int npl = 2);
+    // shape: launch shape of the mixed walk with npl 2 (kNumWalkShapes)
+    void walk(double eps, double* acc, cudaStream_t s, double* pot = nullptr, int npl = 2, int shape = 0);
 };
 
 Octree& gravity_tree();

@@ -296,12 +296,14 @@ __global__ void k_group_prep(const int* __restrict__ groups, const int4* __restr
 }
 
 // Shared memory of one warp. QUAD (mixed form) adds a tile of accepted nodes with their
-// quadrupoles; particles of opened leaves always go to the monopole tile.
-template <bool QUAD, int NPL>
+// quadrupoles; particles of opened leaves always go to the monopole tile. SMALL: the mixed
+// form's interaction tiles at 128 particle and 64 node entries instead of 256 and 96 (fewer
+// entries per evaluation pass, 40 % less shared memory per warp).
+template <bool QUAD, int NPL, bool SMALL = false>
 struct WarpSmem {
     static constexpr int kStack = QUAD ? 768 : kStackCap;
-    static constexpr int kTile = (QUAD && NPL > 2) ? 128 : kTileCap;  // particle entries
-    static constexpr int kNodeTile = QUAD ? 96 : 1;
+    static constexpr int kTile = (QUAD && (NPL > 2 || SMALL)) ? 128 : kTileCap;  // particle entries
+    static constexpr int kNodeTile = QUAD ? (SMALL ? 64 : 96) : 1;
     static constexpr int kBatch = QUAD ? 128 : 64;  // active particles evaluated per walk
     int stack[kStack];
     float4 tile[kTile];
@@ -430,18 +432,20 @@ __device__ __forceinline__ void eval_quad(const float4* tile, const float4* ntA,
 // POT (monopole form only): also the softened potential of every walked particle, into pot.
 // Blocks per SM: shared memory allows 4 of the mixed form's and 6 of the reference form's;
 // 5 keeps the latter free of register spills; the wide-round variant needs more registers.
-template <bool QUAD, bool POT = false, int NPL = (QUAD ? 2 : 1)>
-__global__ void __launch_bounds__(kWalkWarps * 32, QUAD ? (NPL > 2 ? 1 : 4) : 5) k_walk(
+// WARPS (block shape) and SMALL (tile size) are the mixed walk's tunable launch shape: the
+// register bound keeps 16 warps per SM whatever the block shape.
+template <bool QUAD, bool POT = false, int NPL = (QUAD ? 2 : 1), int WARPS = kWalkWarps, bool SMALL = false>
+__global__ void __launch_bounds__(WARPS * 32, QUAD ? (NPL > 2 ? 1 : 16 / WARPS) : 5) k_walk(
     const float4* __restrict__ wa, const float4* __restrict__ wb, const float4* __restrict__ wq,
     const float2* __restrict__ wt, const float* __restrict__ wrq, const float4* __restrict__ p4,
     const int* __restrict__ perm, const uint8_t* __restrict__ active, const int4* __restrict__ work,
     const float4* __restrict__ sphere, const float2* __restrict__ gam, TreeCounts* cnt, int nn, float eps2,
     double* __restrict__ acc, uint32_t* status, int stride, double* __restrict__ pot = nullptr) {
     static_assert(!(QUAD && POT), "potentials come from the monopole walk");
-    using Smem = WarpSmem<QUAD, NPL>;
+    using Smem = WarpSmem<QUAD, NPL, SMALL>;
     constexpr int kNodesPerLane = NPL;
     constexpr int kRound = 32 * kNodesPerLane;
-    __shared__ Smem smem_all[kWalkWarps];
+    __shared__ Smem smem_all[WARPS];
     Smem& S = smem_all[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     const unsigned lt = lanemask_lt();
@@ -807,7 +811,29 @@ void Octree::prepare_walk(const uint8_t* active, cudaStream_t s, int chunk, cons
     GF_CHECK_LAUNCH();
 }
 
-void Octree::walk(double eps, double* acc, cudaStream_t s, double* pot, int npl) {
+namespace {
+
+// Launch shapes of the mixed walk (2 nodes per lane and round): warps per block and tile size.
+// Every shape keeps its static shared memory under 48 KB per block (8 warps of the large tiles
+// would not).
+
+template <int WARPS, bool SMALL>
+void launch_quad_walk(const Octree& T, const uint8_t* active, float eps2, double* acc, cudaStream_t s) {
+    static int bps = 0;
+    if (!bps) {
+        GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_walk<true, false, 2, WARPS, SMALL>, WARPS * 32,
+                                                              0));
+        bps = std::max(1, bps);
+    }
+    k_walk<true, false, 2, WARPS, SMALL><<<bps * ctx().sms, WARPS * 32, 0, s>>>(
+        T.w_a.as<float4>(), T.w_b.as<float4>(), T.w_q.as<float4>(), T.w_t.as<float2>(), T.w_rq.as<float>(),
+        T.p4.as<float4>(), T.perm.as<int>(), active, T.work.as<int4>(), T.sphere.as<float4>(),
+        T.item_gam.as<float2>(), T.counts.as<TreeCounts>(), T.node_cap, eps2, acc, ctx().d_status, T.walk_stride);
+}
+
+}  // namespace
+
+void Octree::walk(double eps, double* acc, cudaStream_t s, double* pot, int npl, int shape) {
     Context& C = ctx();
     const float eps2 = float(eps * eps);
     static int bps_mono = 0, bps_quad = 0;
@@ -831,10 +857,12 @@ void Octree::walk(double eps, double* acc, cudaStream_t s, double* pot, int npl)
             perm.as<int>(), active_ptr, work.as<int4>(), sphere.as<float4>(), item_gam.as<float2>(),
             counts.as<TreeCounts>(), node_cap, eps2, acc, C.d_status, walk_stride);
     } else if (quad) {
-        k_walk<true><<<bps_quad * C.sms, kWalkWarps * 32, 0, s>>>(
-            w_a.as<float4>(), w_b.as<float4>(), w_q.as<float4>(), w_t.as<float2>(), w_rq.as<float>(), p4.as<float4>(),
-            perm.as<int>(), active_ptr, work.as<int4>(), sphere.as<float4>(), item_gam.as<float2>(),
-            counts.as<TreeCounts>(), node_cap, eps2, acc, C.d_status, walk_stride);
+        switch (shape) {
+            case 1: launch_quad_walk<2, false>(*this, active_ptr, eps2, acc, s); break;
+            case 2: launch_quad_walk<4, true>(*this, active_ptr, eps2, acc, s); break;
+            case 3: launch_quad_walk<2, true>(*this, active_ptr, eps2, acc, s); break;
+            default: launch_quad_walk<4, false>(*this, active_ptr, eps2, acc, s); break;
+        }
     } else {
         k_walk<false><<<bps_mono * C.sms, kWalkWarps * 32, 0, s>>>(
             w_a.as<float4>(), w_b.as<float4>(), nullptr, nullptr, nullptr, p4.as<float4>(), perm.as<int>(), active_ptr,

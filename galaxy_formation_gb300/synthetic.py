@@ -16,6 +16,10 @@
 
 Each generator returns a dict with pos (n,3), vel (n,3), mass (n,), kind (n,) int8 and
 u (n,) specific internal energy; gas comes first, then dark matter.
+
+`make_config_device` draws the same workloads on the GPU (gf_ic_generate: counter-based
+random numbers, the same distributions, not the same streams), for sizes where the host
+generators take long (4M particles and up).
 """
 
 import numpy as np
@@ -151,6 +155,42 @@ CONFIGS = {
     3: dict(gen="disk", n_gas=1_000_000, n_dm=0, n_clumps=200),
     4: dict(gen="cloud", n_gas=2_000_000, n_dm=2_000_000),
 }
+
+
+# defaults of the two generators above, in their units
+CLOUD_DEFAULTS = dict(mass=2.8e11, f_baryon=0.16, r0=100.0, spin=0.05, t_gas=1e4)
+DISK_DEFAULTS = dict(mass=2.8e11, f_baryon=0.16, r0=100.0, disk_frac=0.6, rd_kpc=3.0, z0_kpc=0.3,
+                     n_clumps=0, clump_frac=1e-3, clump_kpc=0.2, t_lo=1e4, t_hi=1e6)
+
+
+def device_params(gen, **kw):
+    """(kind, the 13 code-unit parameters of gf_ic_generate) of a generator and overrides."""
+    if gen == "cloud":
+        c = dict(CLOUD_DEFAULTS, **kw)
+        return 0, np.array([c["mass"] / MSUN, c["f_baryon"], c["r0"] / KPC, c["spin"], c["t_gas"] * U_PER_K,
+                            0, 1, 1, 0, 0, 1, 1, 1], np.float64)
+    c = dict(DISK_DEFAULTS, **kw)
+    return 1, np.array([c["mass"] / MSUN, c["f_baryon"], c["r0"] / KPC, 0.05, 0.0, c["disk_frac"],
+                        c["rd_kpc"] / KPC, c["z0_kpc"] / KPC, c["n_clumps"], c["clump_frac"],
+                        c["clump_kpc"] / KPC, c["t_lo"] * U_PER_K, c["t_hi"] * U_PER_K], np.float64)
+
+
+def make_config_device(idx, seed=3, scale=1.0, lib=None):
+    """Workload `idx` drawn on the GPU (gf_ic_generate), returned in host arrays."""
+    from . import _lib
+
+    lib = lib or _lib.load()
+    c = dict(CONFIGS[idx])
+    gen = c.pop("gen")
+    n_gas = max(1, int(c.pop("n_gas") * scale))
+    n_dm = int(c.pop("n_dm") * scale)
+    kind, prm = device_params(gen, **c)
+    n = n_gas + n_dm
+    out = {"pos": np.empty((n, 3)), "vel": np.empty((n, 3)), "mass": np.empty(n), "kind": np.empty(n, np.int8),
+           "u": np.empty(n)}
+    _lib.check(lib.gf_ic_generate(kind, n_gas, n_dm, seed, prm, len(prm), out["pos"], out["vel"], out["mass"],
+                                  out["kind"], out["u"]))
+    return out
 
 
 def make_config(idx, seed=3, scale=1.0):

@@ -133,7 +133,10 @@ int gf_sph_forces_mixed(int n, int k, const double* pos, const double* vel, cons
 /* Particles accepted by gf_sph_forces_noalloc_dev (its fixed scratch: 16 bytes each). */
 #define GF_SPH_NOALLOC_MAX_N 262144
 
-/* sph_forces on device pointers. */
+/* sph_forces on device pointers. Every neighbour row is checked on the device before it is
+ * read through: a particle whose row holds an index outside [0, n) gets NaN outputs (and so
+ * do the particles that have it as a neighbour), and GF_ERR_ARG is reported by the next
+ * synchronising call (e.g. gf_last_status). */
 int gf_sph_forces_dev(int n, int k, const double* pos, const double* vel, const double* mass,
                       const int64_t* nb, const double* h, const double* u, double gamma,
                       double alpha, double beta, double* rho, double* acc, double* dudt,
@@ -149,7 +152,12 @@ int gf_sph_forces_dev(int n, int k, const double* pos, const double* vel, const 
  * that first call before any stream capture. All calls share the one array: calls that
  * overlap on the GPU (different streams, or different host threads) race and must be
  * serialised by the caller. stream: cudaStream_t as void*, NULL = the legacy default
- * stream. Returns GF_OK or GF_ERR_* bits; enqueues work without synchronising. */
+ * stream. Returns GF_OK or GF_ERR_* bits; enqueues work without synchronising. Neighbour
+ * rows are checked on the device as in gf_sph_forces_dev; with no status word to write, a
+ * row holding an index outside [0, n) shows only as NaN outputs of its particle (and of the
+ * particles that have it as a neighbour). The fixed array's device address is looked up
+ * once per device and kept for the life of the process: it does not survive
+ * cudaDeviceReset or a reset of the device's primary context. */
 int gf_sph_forces_noalloc_dev(int n, int k, const double* pos, const double* vel,
                               const double* mass, const int64_t* nb, const double* h,
                               const double* u, double gamma, double alpha, double beta,
@@ -192,6 +200,30 @@ int gf_accelerations(int n, const double* pos, const double* vel, const double* 
                      const int8_t* kind, const double* u, double theta, double eps, double gamma,
                      double alpha, double beta, const uint8_t* active, int rebuild, int sph,
                      int fresh_nb, double* acc, double* dt_ind);
+/* ---- initial conditions on the device ------------------------------------------------ */
+
+/* Seeded particle sets generated on the GPU (the reference builds its initial cloud on the
+ * host, galaxy_formation/initial_conditions.py:25-68; the disk + halo snapshot has no
+ * reference counterpart). kind 0: the rotating cloud of initial_conditions.py:33-68 (both
+ * species in a 1/r sphere of radius R0, rotation from the spin parameter, 10 % velocity
+ * dispersion, no bulk motion, gas at u_gas); kind 1: a 1/r dark-matter halo, an exponential
+ * gas disk (scale length rd truncated at 12 rd, sech^2 height z0) holding disk_frac of the
+ * gas, of which n_clumps Plummer spheres (each clump_frac of the gas, radius a_clump, centres
+ * in the disk) are carved out, the rest of the gas in the 1/r sphere; circular velocities
+ * from the enclosed mass plus 10 % dispersion; gas energies log-uniform in [u_lo, u_hi].
+ * params (code units, 13 values): M_tot, f_baryon, R0, spin, u_gas, disk_frac, rd, z0,
+ * n_clumps, clump_frac, a_clump, u_lo, u_hi. Outputs: pos (n,3), vel (n,3), mass (n),
+ * kind (n) (0 gas first, then 2 dark matter), u (n), n = n_gas + n_dm. Every draw is a
+ * function of (seed, particle index, draw number), so a set depends only on its arguments.
+ * The sets match the host generators (galaxy_formation_gb300/synthetic.py) in distribution,
+ * not bit for bit. _dev: device pointers, enqueued on stream. */
+int gf_ic_generate_dev(int kind, int n_gas, int n_dm, unsigned long long seed, const double* params,
+                       int nparams, double* pos, double* vel, double* mass, int8_t* kind_out, double* u,
+                       void* stream);
+/* gf_ic_generate_dev into host arrays (copies out, synchronises). */
+int gf_ic_generate(int kind, int n_gas, int n_dm, unsigned long long seed, const double* params, int nparams,
+                   double* pos, double* vel, double* mass, int8_t* kind_out, double* u);
+
 /* ---- the step loop (galaxy_formation/simulation.py:114-149) ----------------------------- */
 
 /* Loads a particle set onto the GPU (host pointers, copied) and computes its initial
@@ -218,12 +250,14 @@ int gf_sim_blocks(int nblocks, int nlev, double* updates);
  * (0: the reference's walk groups with their spheres; 1..64: items of <= chunk[b] active
  * particles in tree order, each with its own bounding sphere), plus 100 to walk with 8 nodes
  * per lane and round instead of 2 (mixed form; for bins of a few items, whose walks are bound
- * by the latency of their rounds); bins past nbins reuse chunk[nbins-1]; chunk NULL =
+ * by the latency of their rounds), plus 1000 x s to walk with launch shape s
+ * (GF_OPT_WALK_SHAPE, 2 per lane only); bins past nbins reuse chunk[nbins-1]; chunk NULL =
  * groups everywhere. rebuild_every > 0 rebuilds the tree inside the captured block every
  * that many sub-steps (0: refit only). */
 int gf_sim_block_config(const int* chunk, int nbins, int rebuild_every);
 /* Autotuner of that launch shape on the current state: times the gravity walk of each bin's
- * active set per chunk candidate and walk width, then one block per rebuild cadence; keeps
+ * active set per chunk candidate, walk width and launch shape, then one block per rebuild
+ * cadence; keeps
  * the fastest and writes them to chunk (nlev-1 entries, in gf_sim_block_config's encoding) /
  * rebuild_every; graph_ms = the best block's graph time. Positions, velocities and time are restored afterwards (the next block starts with
  * a full evaluation). */
@@ -349,6 +383,11 @@ int gf_cool(int n, const double* u, const double* T, const double* rho, const do
  *                       group's a_min is evaluated as a monopole alone (0 = off, default;
  *                       e.g. 1.5e-4). Far nodes then cost a monopole's arithmetic. */
 #define GF_OPT_GRAVITY_REL_MONO 8
+/*   GF_OPT_WALK_SHAPE   mixed form: launch shape of the walk (2 nodes per lane and round),
+ *                       warps per block x interaction tiles (particle / node entries per
+ *                       warp): 0 = 4 x 256/96 (default), 1 = 2 x 256/96, 2 = 4 x 128/64,
+ *                       3 = 2 x 128/64. gf_force_autotune and gf_sim_block_autotune choose it. */
+#define GF_OPT_WALK_SHAPE 9
 int gf_set_option(int key, double value);
 /* Current value of an option (-1 for an unknown key). */
 double gf_get_option(int key);
@@ -383,9 +422,27 @@ int gf_mlp_train(int steps, int batch, double lr, double* loss);
  * dt_gas = min Courant step (inf without hydro), search-radius iterations of the last full
  * neighbour search. Any pointer may be NULL. Synchronises the device. */
 int gf_force_info(int* n_gas, double* dt_grav, double* dt_gas, long long* knn_iters);
+/* Autotuner of the mixed form's walk (no reference counterpart): on the tree, work items and
+ * error scale of the last fused evaluation (which must have used GF_OPT_GRAVITY_QUAD), times the
+ * gravity walk for each item size (GF_OPT_WALK_MERGE in {0, 24, 32, 40, 48, 64}) and launch
+ * shape (GF_OPT_WALK_SHAPE 0..3), three times each, and sets both options to the fastest
+ * (median time). Outputs (any may be NULL): the chosen merge cap and shape and that walk's
+ * time in ms. Synchronises the device. */
+int gf_force_autotune(double eps, int* walk_merge, int* walk_shape, double* walk_ms);
+/* The gas state of the last hydro step of the fused evaluation (simulation.py:74-95: the
+ * arrays _hydro builds for sph_forces), in gas-local order = np.flatnonzero(kind == 0):
+ * global index, smoothing length h, density, du/dt, Courant step dt_i, SPH acceleration
+ * (ng,3), and the 32 neighbours of each row (local indices, the set of the 32 nearest, in no
+ * particular order). After a block sub-step only the gas due was recomputed; the other rows
+ * hold their last values. *n_gas receives ng (0 when the last call had <= 40 gas); cap is the
+ * row capacity of the arrays; any pointer may be NULL. Synchronises the device. No reference
+ * counterpart (a read-out for checks against a CPU restatement). */
+int gf_force_read_gas(int cap, int* n_gas, int32_t* gidx, double* h, double* rho, double* dudt,
+                      double* dt_i, double* acc_sph, int32_t* nb32);
 /* Up to nout statistics of the fused evaluation, in this order: gas count, dt_grav, dt_gas,
  * search-radius iterations of the last full search, 0 (reserved), full searches so far,
- * Verlet reselections so far, nodes of the gas octree. Synchronises the device. */
+ * Verlet reselections so far, nodes of the gas octree, nodes of the gravity octree.
+ * Synchronises the device. */
 int gf_force_stats(double* out, int nout);
 
 /* ---- measurement hooks (no reference counterpart) ----------------------------------- */
@@ -395,7 +452,8 @@ int gf_force_stats(double* out, int nout);
 int gf_profile(int on);
 /* Stage ids: 0 gravity tree build, 1 refit, 2 walk kernel, 3 walk work list, 4 neighbour
  * search kernel, 5 gas octree build, 6 SPH density kernel, 7 SPH force kernel, 8 Verlet
- * reselection, 9 whole force evaluation. Total milliseconds and number of launches
+ * reselection, 9 whole force evaluation, 10 radix sort of the gravity tree's keys, 11 node
+ * emission of the gravity tree, 12 moments pass of the gravity tree build. Total milliseconds and number of launches
  * recorded in the session; synchronises the device. */
 int gf_profile_stage(int stage, double* total_ms, int* launches);
 /* Kernels launched by the library since it was loaded. */

@@ -178,10 +178,18 @@ class StepOracle:
 class BlockOracle:
     """CPU restatement of the block time-step scheme of the library's batched form (power-of-two
     levels, gravity of the particles due at each sub-step on a refitted tree — or a rebuilt one
-    every `rebuild_every` sub-steps — opening /
-    full / closing kicks). Gravity only: for particle sets without gas."""
+    every `rebuild_every` sub-steps — opening / full / closing kicks).
 
-    def __init__(self, pos, vel, mass, theta, eps, nlev, rebuild_every=0, chunk=None):
+    With gas (kind given, more than 40 gas particles) each evaluation also runs the hydro step:
+    the block-start and block-end evaluations are full ones (cKDTree search of 48 candidates,
+    h, sph_forces of every gas particle: simulation.py:74-95); at a sub-step only the gas due
+    gets its 32 neighbours re-selected among its cached candidates (sph.py:155-164), a new h,
+    density, pressure and viscous forces (oracle/sph_ref.py), its neighbours that are not due
+    entering with their density and h of their own last evaluation; the others keep their SPH
+    acceleration and Courant step. u stays fixed (no thermal update)."""
+
+    def __init__(self, pos, vel, mass, theta, eps, nlev, rebuild_every=0, chunk=None, kind=None, u=None,
+                 gamma=5.0 / 3.0, alpha=1.0, beta=2.0):
         self.pos, self.vel, self.mass = pos.copy(), vel.copy(), mass
         self.theta, self.eps, self.nlev = theta, eps, nlev
         self.rebuild_every = rebuild_every  # tree rebuilt at sub-steps s % rebuild_every == 0
@@ -189,13 +197,55 @@ class BlockOracle:
         self.chunk = chunk
         self.acc = np.zeros_like(pos)
         self.t = 0.0
+        self.gas = np.zeros(0, np.int64) if kind is None else np.flatnonzero(kind == GAS)
+        self.hydro = self.gas.size > 40
+        if self.hydro:
+            ng = self.gas.size
+            self.u = u
+            self.gamma, self.alpha, self.beta = gamma, alpha, beta
+            self.acc_grav = np.zeros_like(pos)
+            self.acc_sph = np.zeros_like(pos)
+            self.dt_courant = np.full(len(mass), np.inf)
+            self.h, self.rho = np.zeros(ng), np.zeros(ng)
+            self.nb = np.zeros((ng, N_NEIGHBOURS), np.int64)
         self._force(None, True)
         self._levels_and_open()
 
+    def _hydro(self, active):
+        import sph_ref
+
+        g = self.gas
+        p, v = np.ascontiguousarray(self.pos[g]), np.ascontiguousarray(self.vel[g])
+        m, u = self.mass[g], self.u[g]
+        if active is None:  # full search (sph.py:165-169)
+            d, nb = cKDTree(p).query(p, k=min(N_CANDIDATES, g.size), workers=-1)
+            self.cand = nb
+            rows = np.arange(g.size)
+            self.nb[:] = nb[:, :N_NEIGHBOURS]
+            self.h[:] = np.maximum(0.5 * d[:, N_NEIGHBOURS - 1], 0.5 * self.eps)
+        else:  # the gas due: Verlet reselection among the cached candidates
+            rows = np.flatnonzero(active[g])
+            sel = sph_ref.reselect(p, self.cand, rows, N_NEIGHBOURS)
+            assert sel is not None, "a gas particle lost its candidates"
+            self.nb[rows] = sel[0]
+            self.h[rows] = np.maximum(0.5 * sel[1], 0.5 * self.eps)
+        self.rho[rows] = sph_ref.density(p, m, self.nb, self.h, rows)
+        a, _, dt_i, _, _ = sph_ref.forces(p, v, m, self.nb, self.h, u, self.rho, rows, self.gamma, self.alpha,
+                                       self.beta)
+        self.acc_sph[g[rows]] = a
+        self.dt_courant[g[rows]] = dt_i
+
     def _force(self, active, rebuild):
-        oracle.accel_active(self.pos, self.mass, self.acc, self.theta, self.eps, active, rebuild)
+        if not self.hydro:
+            oracle.accel_active(self.pos, self.mass, self.acc, self.theta, self.eps, active, rebuild)
+            a = np.sqrt(np.einsum("ij,ij->i", self.acc, self.acc))
+            self.dt_ind = 0.3 * np.sqrt(self.eps / np.maximum(a, 1e-30))
+            return
+        oracle.accel_active(self.pos, self.mass, self.acc_grav, self.theta, self.eps, active, rebuild)
+        self._hydro(active)
+        self.acc = self.acc_grav + self.acc_sph
         a = np.sqrt(np.einsum("ij,ij->i", self.acc, self.acc))
-        self.dt_ind = 0.3 * np.sqrt(self.eps / np.maximum(a, 1e-30))
+        self.dt_ind = np.minimum(0.3 * np.sqrt(self.eps / np.maximum(a, 1e-30)), self.dt_courant)
 
     def _levels_and_open(self):
         self.delta = self.dt_ind.min()

@@ -673,4 +673,58 @@ void orc_knn_brute(int n, const double* pos, int k, double* dist, int64_t* nb) {
     }
 }
 
+// Orthographic projection with a bilinear deposit of four weights per particle into
+// img (ngroups, H, W), as cpp/nbody.cpp:445-469; serial, so the float sums of a pixel come
+// in particle order.
+void orc_render(int n, const double* pos, const uint8_t* group, int ngroups, const double* rot,
+                const double* center, double scale, int W, int H, float* img) {
+    const size_t plane = size_t(W) * H;
+    for (size_t t = 0; t < size_t(ngroups) * plane; ++t) img[t] = 0.0f;
+    for (int i = 0; i < n; ++i) {
+        const double x = pos[3 * size_t(i)] - center[0];
+        const double y = pos[3 * size_t(i) + 1] - center[1];
+        const double z = pos[3 * size_t(i) + 2] - center[2];
+        const double sx = rot[0] * x + rot[1] * y + rot[2] * z;
+        const double sy = rot[3] * x + rot[4] * y + rot[5] * z;
+        const double u = 0.5 * W + scale * sx - 0.5, v = 0.5 * H - scale * sy - 0.5;
+        if (!(u >= 0 && v >= 0 && u < W - 1 && v < H - 1)) continue;
+        const int iu = int(u), iv = int(v);
+        const float fu = float(u - iu), fv = float(v - iv);
+        float* p = img + size_t(group[i]) * plane + size_t(iv) * W + iu;
+        p[0] += (1 - fu) * (1 - fv);
+        p[1] += fu * (1 - fv);
+        p[W] += (1 - fu) * fv;
+        p[W + 1] += fu * fv;
+    }
+}
+
+// 8-bit RGB from the group images (cpp/nbody.cpp:474-503): per group a log-compressed
+// brightness plus a bilinearly upsampled glow, weighted by the group colour, then the soft
+// saturation 255 (1 - exp(-exposure s)), rounded.
+void orc_tonemap(int W, int H, int ngroups, const float* img, const float* glow, int gw, int gh,
+                 const float* colors, float inv_ref, float K, float exposure, uint8_t* out) {
+    const size_t plane = size_t(W) * H, gplane = size_t(gw) * gh;
+    const float norm = 1.0f / std::log1p(K);
+    const float ax = float(gw) / W, ay = float(gh) / H;
+    for (int y = 0; y < H; ++y) {
+        const float gyf = std::min(std::max((y + 0.5f) * ay - 0.5f, 0.0f), gh - 1.001f);
+        const int gy = int(gyf);
+        const float fy = gyf - gy;
+        for (int x = 0; x < W; ++x) {
+            const float gxf = std::min(std::max((x + 0.5f) * ax - 0.5f, 0.0f), gw - 1.001f);
+            const int gx = int(gxf);
+            const float fx = gxf - gx;
+            float c[3] = {0, 0, 0};
+            for (int g = 0; g < ngroups; ++g) {
+                const float* q = glow + g * gplane + size_t(gy) * gw + gx;
+                const float glow_v = (1 - fy) * ((1 - fx) * q[0] + fx * q[1]) + fy * ((1 - fx) * q[gw] + fx * q[gw + 1]);
+                const float l = std::log1p(K * inv_ref * img[g * plane + size_t(y) * W + x]) * norm + glow_v;
+                for (int a = 0; a < 3; ++a) c[a] += l * colors[3 * g + a];
+            }
+            for (int a = 0; a < 3; ++a)
+                out[3 * (size_t(y) * W + x) + a] = uint8_t(255.0f * (1 - std::exp(-exposure * c[a])) + 0.5f);
+        }
+    }
+}
+
 }  // extern "C"

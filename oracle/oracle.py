@@ -20,6 +20,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liborc.so")
 REF_LIB = os.path.join(HERE, "_ref", "libnbody.so")
 SRC = os.path.join(HERE, "gf_oracle.cpp")
+# Where the reference's sources live (only in the container that builds the pinned copy);
+# override with the GALAXY_FORMATION_REFERENCE environment variable.
+REFERENCE_ROOT = os.environ.get("GALAXY_FORMATION_REFERENCE", "/root/reference")
 
 _dbl = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 _f32 = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
@@ -34,9 +37,9 @@ def build(force=False):
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
         subprocess.run(["make", "-C", HERE, "liborc.so"], check=True,
                        stdout=subprocess.DEVNULL)
-    ref_src = "/root/reference/cpp/nbody.cpp"
+    ref_src = os.path.join(REFERENCE_ROOT, "cpp", "nbody.cpp")
     if os.path.exists(ref_src) and not os.path.exists(REF_LIB):
-        subprocess.run(["make", "-C", HERE, "ref"], check=True, stdout=subprocess.DEVNULL)
+        subprocess.run(["make", "-C", HERE, "ref", f"REF_SRC={ref_src}"], check=True, stdout=subprocess.DEVNULL)
 
 
 _lib = None
@@ -66,6 +69,9 @@ def lib():
         L.orc_knn_from_candidates.argtypes = [_ci, _ci, _dbl, _i64, _ci, _i64, _dbl]
         L.orc_knn_from_candidates.restype = _ci
         L.orc_knn_brute.argtypes = [_ci, _dbl, _ci, _dbl, _i64]
+        L.orc_render.argtypes = [_ci, _dbl, _u8, _ci, _dbl, _dbl, _cd, _ci, _ci, _f32]
+        L.orc_tonemap.argtypes = [_ci, _ci, _ci, _f32, _f32, _ci, _ci, _f32, ctypes.c_float, ctypes.c_float,
+                                  ctypes.c_float, _u8]
         _lib = L
     return _lib
 
@@ -172,6 +178,24 @@ def knn_brute(pos, k):
     return dist, nb
 
 
+def render(pos, group, ngroups, rot, center, scale, W, H):
+    """Restatement of nbody_render (cpp/nbody.cpp:445-469); returns img (ngroups, H, W)."""
+    img = np.zeros((ngroups, H, W), np.float32)
+    lib().orc_render(len(pos), np.ascontiguousarray(pos), np.ascontiguousarray(group, np.uint8), ngroups,
+                     np.ascontiguousarray(rot, np.float64), np.ascontiguousarray(center, np.float64), scale, W, H, img)
+    return img
+
+
+def tonemap(img, glow, colors, inv_ref, K, exposure):
+    """Restatement of nbody_tonemap (cpp/nbody.cpp:474-503); returns (H, W, 3) uint8."""
+    ng, H, W = img.shape
+    gh, gw = glow.shape[1:]
+    out = np.zeros((H, W, 3), np.uint8)
+    lib().orc_tonemap(W, H, ng, np.ascontiguousarray(img, np.float32), np.ascontiguousarray(glow, np.float32), gw, gh,
+                      np.ascontiguousarray(colors, np.float32), inv_ref, K, exposure, out)
+    return out
+
+
 class RefNbody:
     """The reference's cpp/nbody.cpp built from its own sources (oracle/_ref/)."""
 
@@ -179,6 +203,9 @@ class RefNbody:
         if not os.path.exists(REF_LIB):
             raise FileNotFoundError(REF_LIB)
         L = ctypes.CDLL(REF_LIB)
+        L.nbody_render.argtypes = [_ci, _dbl, _u8, _ci, _dbl, _dbl, _cd, _ci, _ci, _f32]
+        L.nbody_tonemap.argtypes = [_ci, _ci, _ci, _f32, _f32, _ci, _ci, _f32, ctypes.c_float, ctypes.c_float,
+                                    ctypes.c_float, _u8]
         L.nbody_accel_active.argtypes = [_ci, _dbl, _dbl, _dbl, _cd, _cd, _u8, _ci]
         L.nbody_accel_direct.argtypes = [_ci, _dbl, _dbl, _dbl, _cd]
         L.nbody_num_threads.restype = _ci

@@ -1,6 +1,7 @@
 """Generates the golden fixtures under tests/golden/ from the reference itself.
 
-Run once in a container that has the reference sources at /root/reference:
+Run once in a container that has the reference sources (at $GALAXY_FORMATION_REFERENCE,
+by default /root/reference):
 
     make -C oracle ref          # compiles the reference's cpp/nbody.cpp into oracle/_ref/
     python tests/golden/make_golden.py
@@ -23,8 +24,12 @@ Fixtures (npz):
   cooling.npz      the reference's cooling_function on a temperature grid spanning the floor,
                    and cool() on random (u, rho, dt, blocked) with the simulator's floor
                    (cooling.py:24-43, simulation.py:38-42).
+  render.npz       the default cloud splatted by the reference's nbody_render into three
+                   colour groups of a 160 x 120 image (cpp/nbody.cpp:445-469), and its
+                   nbody_tonemap of that image with a glow derived from it as
+                   rendering.py:115-124 does (cpp/nbody.cpp:474-503).
 
-Pass fixture names (bh_gauss cloud sph cooling) to regenerate only those.
+Pass fixture names (bh_gauss cloud sph cooling render) to regenerate only those.
 """
 
 import os
@@ -33,7 +38,7 @@ import sys
 import numpy as np
 
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
-REF = "/root/reference"
+REF = os.environ.get("GALAXY_FORMATION_REFERENCE", "/root/reference")
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 sys.path.insert(0, os.path.join(ROOT, "oracle", "numba_shim"))
@@ -131,9 +136,39 @@ def cooling():
                         u=u, rho=rho, dt=dt, blocked=blocked, u_new=u_new)
 
 
+def render():
+    from scipy.ndimage import gaussian_filter
+
+    ref = oracle.RefNbody()
+    cfg = Config()
+    rng = np.random.default_rng(cfg.seed)
+    pos, _, _, kind = make_cloud(cfg, rng)
+    group = np.ascontiguousarray(np.random.default_rng(13).integers(0, 3, len(kind)), np.uint8)
+    a, e = np.radians(30.0), np.radians(25.0)  # the screen axes of an azimuth / elevation view
+    d = np.array([np.cos(e) * np.cos(a), np.cos(e) * np.sin(a), np.sin(e)])
+    right = np.array([-np.sin(a), np.cos(a), 0.0])
+    rot = np.ascontiguousarray(np.stack([right, np.cross(d, right), d]))
+    center = np.zeros(3)
+    W, H, K, exposure, glow_gain = 160, 120, 40.0, 1.6, 0.5
+    scale = W / (2 * 1.2 * np.abs(pos).max())
+    img = np.zeros((3, H, W), np.float32)
+    ref.lib.nbody_render(len(kind), np.ascontiguousarray(pos), group, 3, rot, center, scale, W, H, img)
+    small = img.reshape(3, H // 4, 4, W // 4, 4).mean(axis=(2, 4))
+    level = max(np.percentile(small.sum(axis=0), 99.9), 1e-3)
+    glow = gaussian_filter(small / level, sigma=(0, 3, 3))
+    glow = np.ascontiguousarray(glow_gain * np.log1p(K * glow) / np.log1p(K), np.float32)
+    colors = np.array([[1.0, 0.55, 0.25], [0.35, 0.6, 1.0], [0.9, 0.9, 0.85]], np.float32)
+    rgb = np.zeros((H, W, 3), np.uint8)
+    ref.lib.nbody_tonemap(W, H, 3, img, glow, W // 4, H // 4, colors, np.float32(1 / level), np.float32(K),
+                          np.float32(exposure), rgb)
+    np.savez_compressed(os.path.join(OUT, "render.npz"), pos=pos, group=group, rot=rot, center=center,
+                        scale=scale, img=img, glow=glow, colors=colors, inv_ref=np.float32(1 / level), K=K,
+                        exposure=exposure, rgb=rgb)
+
+
 if __name__ == "__main__":
     oracle.build()
-    names = sys.argv[1:] or ["bh_gauss", "cloud", "sph", "cooling"]
+    names = sys.argv[1:] or ["bh_gauss", "cloud", "sph", "cooling", "render"]
     for name in names:
         globals()[name]()
     for f in sorted(os.listdir(OUT)):

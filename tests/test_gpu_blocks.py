@@ -1,7 +1,7 @@
 """Block time steps (gf_sim_blocks, the batched form; its inner sub-steps replay a captured
 CUDA graph) against the CPU restatement of the same scheme (oracle/force_ref.py
-BlockOracle) on a gas-free particle set, and a run with gas for sanity (finite state,
-update counts, level populations)."""
+BlockOracle): gravity alone on a gas-free particle set, and with gas (partial SPH of the gas
+due at each sub-step, Verlet reselection inside the graph)."""
 
 import ctypes
 
@@ -23,7 +23,8 @@ def _state(lib, n):
 def _plain(lib):
     from galaxy_formation_gb300 import _lib
 
-    for key in (_lib.OPT_SPH_FLOAT32, _lib.OPT_GRAVITY_QUAD, _lib.OPT_HGUESS, _lib.OPT_WALK_CHUNK):
+    for key in (_lib.OPT_SPH_FLOAT32, _lib.OPT_GRAVITY_QUAD, _lib.OPT_HGUESS, _lib.OPT_WALK_CHUNK,
+                _lib.OPT_GRAVITY_REL, _lib.OPT_WALK_MERGE, _lib.OPT_GRAVITY_REL_MONO):
         lib.gf_set_option(key, 0)
 
 
@@ -63,27 +64,60 @@ def test_blocks_match_cpu_gravity_only(gpulib, oracle, rebuild_every, chunk):
     assert np.percentile(np.linalg.norm(vel - ref.vel, axis=1), 99) < 1e-4 * vs
 
 
-def test_blocks_with_gas(gpulib):
+@pytest.mark.parametrize("rebuild_every,sph32", [(0, 0), (4, 0), (4, 1)])
+def test_blocks_with_gas_match_cpu(gpulib, oracle, rebuild_every, sph32):
+    """Block steps with gas against the CPU restatement (BlockOracle with its hydro path):
+    at every sub-step the gas due is compacted, re-selects its 32 neighbours among its cached
+    candidates, and gets a new h, density and SPH forces, its neighbours that are not due
+    entering with their last density and h; the block ends with a full evaluation (new tree,
+    fresh search). Positions, velocities, time, level populations and the final gas state
+    (h, neighbour sets, densities) match; also with the float32 + Kahan SPH of the mixed form
+    (sph32) against the float64 restatement."""
+    from force_ref import BlockOracle
+
     from galaxy_formation_gb300 import _lib, params, synthetic
 
-    d = synthetic.make_config(1, scale=0.05)
+    d = synthetic.make_config(1, scale=0.05)  # 5k gas + 5k DM disk + halo
     n = len(d["mass"])
     lib = gpulib
     _plain(lib)
-    chunk = np.array([4, 8, 16, 64], np.int32)
-    _lib.check(lib.gf_sim_block_config(chunk.ctypes.data, 4, 4))
+    lib.gf_set_option(_lib.OPT_SPH_FLOAT32, sph32)
+    chunk = [4, 8, 16, 64]
+    ch = np.array(chunk, np.int32)
+    _lib.check(lib.gf_sim_block_config(ch.ctypes.data, len(ch), rebuild_every))
     _lib.check(lib.gf_sim_init(n, d["pos"], d["vel"], d["mass"], d["kind"], d["u"], params.THETA, params.EPS,
                                params.GAMMA, params.ALPHA, params.BETA))
+    ref = BlockOracle(d["pos"], d["vel"], d["mass"], params.THETA, params.EPS, nlev=4, rebuild_every=rebuild_every,
+                      chunk=chunk, kind=d["kind"], u=d["u"], gamma=params.GAMMA, alpha=params.ALPHA,
+                      beta=params.BETA)
+    assert ref.hydro
     upd = ctypes.c_double()
     total = 0.0
-    for _ in range(3):
-        _lib.check(lib.gf_sim_blocks(1, 4, ctypes.byref(upd)))
-        total += upd.value
+    try:
+        for _ in range(3):
+            _lib.check(lib.gf_sim_blocks(1, 4, ctypes.byref(upd)))
+            ref.block()
+            total += upd.value
+    finally:
+        lib.gf_set_option(_lib.OPT_SPH_FLOAT32, 0)
     frac = np.zeros(4)
     _lib.check(lib.gf_sim_levels(4, frac))
-    assert abs(frac.sum() - 1) < 1e-9
+    ref_frac = np.bincount(ref.level, minlength=4) / n
+    assert np.abs(frac - ref_frac).max() <= 2e-3, (frac, ref_frac)
     pos, vel, t = _state(lib, n)
-    assert np.all(np.isfinite(pos)) and np.all(np.isfinite(vel)) and t > 0
+    assert abs(t - ref.t) <= 1e-5 * ref.t
+    scale = np.linalg.norm(ref.pos, axis=1).mean()
+    assert np.percentile(np.linalg.norm(pos - ref.pos, axis=1), 99) < 1e-5 * scale
+    vs = np.linalg.norm(ref.vel, axis=1).mean()
+    assert np.percentile(np.linalg.norm(vel - ref.vel, axis=1), 99) < 1e-4 * vs
+    # the block-end evaluation's gas state against the restatement's (same positions up to the
+    # trajectories' float32-gravity differences)
+    gs = _lib.read_gas(lib)
+    assert np.array_equal(gs["gidx"], ref.gas)
+    assert np.percentile(np.abs(gs["h"] - ref.h) / ref.h, 99) < 1e-4
+    assert np.percentile(np.abs(gs["rho"] - ref.rho) / ref.rho, 99) < 1e-4
+    same = np.all(np.sort(gs["nb"], axis=1) == np.sort(ref.nb, axis=1), axis=1)
+    assert same.mean() > 0.98, same.mean()
     # at least one evaluation of everybody per block, at most one per sub-step
     assert 3 * n <= total <= 3 * n * 8 + n
 

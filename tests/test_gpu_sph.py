@@ -134,3 +134,31 @@ def test_sph_forces_match_oracle_disk(sph, oracle):
     an = np.linalg.norm(acc - r_acc, axis=1) / np.linalg.norm(r_acc, axis=1)
     assert np.max(an) < TOL
     assert np.max(np.abs(dudt - r_dudt)) <= TOL * np.abs(r_dudt).max()
+
+
+def test_sph_forces_dev_checks_neighbour_rows(gpulib, golden):
+    """gf_sph_forces_dev on device buffers with a neighbour index outside [0, n): no read out of
+    bounds; that particle's outputs are NaN and the call's status reports GF_ERR_ARG."""
+    import ctypes
+
+    torch = pytest.importorskip("torch")
+    from galaxy_formation_gb300 import _lib, params
+
+    s = golden("sph2k.npz")
+    nb = s["nb"].astype(np.int64)
+    n = len(nb)
+    nb[11, 7] = -3
+    dev = torch.device("cuda")
+    t = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in
+         dict(pos=s["pos"], vel=s["vel"], mass=s["mass"], nb=nb, h=s["h"], u=s["u"]).items()}
+    out = [torch.zeros(n, dtype=torch.float64, device=dev), torch.zeros((n, 3), dtype=torch.float64, device=dev),
+           torch.zeros(n, dtype=torch.float64, device=dev), torch.zeros(n, dtype=torch.float64, device=dev)]
+    st = gpulib.gf_sph_forces_dev(n, 32, t["pos"].data_ptr(), t["vel"].data_ptr(), t["mass"].data_ptr(),
+                                  t["nb"].data_ptr(), t["h"].data_ptr(), t["u"].data_ptr(), params.GAMMA, params.ALPHA,
+                                  params.BETA, *(o.data_ptr() for o in out),
+                                  ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert st == 0  # enqueued; the kernels report through the device status word
+    torch.cuda.synchronize()
+    assert gpulib.gf_last_status() & _lib.GF_ERR_ARG
+    rho = out[0].cpu().numpy()
+    assert np.isnan(rho[11]) and np.isfinite(np.delete(rho, 11)).all()
