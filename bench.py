@@ -13,14 +13,13 @@ Forms measured (same snapshot, same evaluation):
                  default), float64 SPH, search radius from the previous h;
   plain_matched  the same arithmetic at the opening angle whose gravity error against the
                  float64 direct sum meets p99 <= 1e-3 (theta 0.15);
-  mixed_prevh    the headline's method with the search radius from the previous h instead of
-                 the learned guess (what the guess gains, in the headline setting);
   mixed_learned  the headline: float32 walk with Kahan tile sums and quadrupole nodes under the
                  relative opening criterion (alpha 4e-3, a geometric floor at theta 1; accepted
                  nodes whose quadrupole term is below 1.5e-4 a_min taken as monopoles; walk items
                  merged from sibling groups up to 40 particles), p99 <= 1e-3 against the float64
-                 direct sum; float32 + Kahan SPH; search radius from the learned MLP guess
-                 (trained first on pairs the simulator produced, on the GPU);
+                 direct sum; float32 + Kahan SPH; search radius from 2.5 x the previous h, and
+                 from the learned MLP guess (trained first on pairs the simulator produced, on
+                 the GPU) for searches without a previous h;
 plus the batched form (block time steps, CUDA-graph replay, autotuned) as particle-updates/s
 over a 64-sub-step block.
 
@@ -64,7 +63,6 @@ PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FORMS = {
     "plain": (0.7, 0, 0, 0, 0.0, 0, 0.0),
     "plain_matched": (0.15, 0, 0, 0, 0.0, 0, 0.0),
-    "mixed_prevh": (0.55, 1, 1, 0, 4e-3, 40, 1.5e-4),
     "mixed_learned": (0.55, 1, 1, 2, 4e-3, 40, 1.5e-4),
 }
 # flops per interaction (an FMA counting 2): monopole pair (cpp/nbody.cpp:398-402 in float32)
@@ -79,7 +77,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--scale", type=float, default=1.0, help="shrink the workload (testing only)")
-    ap.add_argument("--forms", default="plain,plain_matched,mixed_prevh,mixed_learned",
+    ap.add_argument("--forms", default="plain,plain_matched,mixed_learned",
                     help="comma list of forms to time (the last one given is the headline)")
     ap.add_argument("--blocks", type=int, default=3, help="64-sub-step blocks of the batched form (0: skip)")
     ap.add_argument("--workload", default="force", choices=["force", "drift", "learned"],
@@ -451,22 +449,34 @@ class Gpu:
         L.check(lib.gf_mlp_train(2000, 4096, 2e-3, ctypes.byref(loss1)))
         train_s = time.perf_counter() - t0
         lib.gf_set_option(L.OPT_COLLECT, 0)  # stop collecting (clears the pairs)
-        # iterations of the count-to-48 search on a drifted snapshot: previous h, cell density
-        # alone, learned guess (the converged neighbours are the same in all three); the
-        # previous h is that of the snapshot before the drift, so longer drifts make it staler
-        its, by_drift = {}, {}
-        for halves in (1, 4, 16):
-            row = {}
-            for mode, name in ((0, "previous_h"), (1, "cell_density"), (2, "learned")):
-                if halves > 1 and mode == 1:
-                    continue
-                row[name] = self.search_after_drift(theta, pos, halves, mode)
-            by_drift[f"{halves}_half_steps"] = row
-        its = by_drift["1_half_steps"]
+        # the first search of a snapshot (no previous h): cell density vs the learned guess;
+        # with a previous h (the snapshot drifted by 1, 4, 16 half steps since it was taken)
+        # the start is 2.5 h in both modes; the converged neighbours are the same in all
+        cold = {name: self.search_without_h(theta, pos, mode) for mode, name in ((1, "cell_density"),
+                                                                                  (2, "learned"))}
+        by_drift = {f"{halves}_half_steps": {"previous_h": self.search_after_drift(theta, pos, halves, 0)}
+                    for halves in (1, 4, 16)}
         lib.gf_set_option(L.OPT_HGUESS, 0)
         return {"training_rows": int(m), "loss_start": loss0.value, "loss_end": loss1.value,
-                "train_s": train_s, "adam_steps": 2000, "batch": 4096, "search_on_drifted_snapshot": its,
-                "search_after_drift": by_drift}
+                "train_s": train_s, "adam_steps": 2000, "batch": 4096,
+                "first_search_without_previous_h": cold,
+                "search_with_previous_h_after_drift": by_drift,
+                "note": "the learned guess starts searches without a previous h; where one exists, 2.5 h "
+                        "starts them (fewer iterations than the network's guess: 1.04 against 1.11)"}
+
+    def search_without_h(self, theta, pos, mode):
+        """Radius iterations and neighbour-search time of a full search that has no previous h,
+        started from h guess `mode` (1 the cell density, 2 the learned guess)."""
+        torch, lib, L = self.torch, self.lib, self._lib
+        lib.gf_set_option(L.OPT_HGUESS, mode)
+        lib.gf_set_option(L.OPT_FORGET_H, 1)
+        lib.gf_profile(1)
+        self.step(theta, pos=pos)
+        torch.cuda.synchronize()
+        ms, cnt = ctypes.c_double(), ctypes.c_int()
+        lib.gf_profile_stage(L.STAGES.index("knn"), ctypes.byref(ms), ctypes.byref(cnt))
+        lib.gf_profile(0)
+        return {"iterations_per_gas": self.knn_iters(), "knn_ms": ms.value}
 
     def search_after_drift(self, theta, pos, halves, mode):
         """Radius iterations and neighbour-search time of a full search on the snapshot drifted by
@@ -522,7 +532,7 @@ class Gpu:
         lib.gf_profile_stage(L.STAGES.index("knn"), ctypes.byref(kms), ctypes.byref(kcnt))
         lib.gf_profile(0)
         block_end = {"knn_ms": kms.value / max(1, kcnt.value), "iterations_per_gas": self.knn_iters(),
-                     "h_guess": ["previous h", "cell density", "learned MLP"][FORMS[form][3]]}
+                     "h_guess": ["previous h", "cell density", "previous h (learned MLP without one)"][FORMS[form][3]]}
         return {"value": upd.value / (ms * 1e-3), "unit": UNIT, "blocks": blocks, "substeps_per_block": 1 << (nlev - 1),
                 "levels": nlev, "level_fractions": [round(float(x), 5) for x in frac],
                 "updates": upd.value, "ms": ms, "ms_per_block": ms / blocks,
@@ -625,10 +635,6 @@ def run_gpu(args, world, rank, local):
         res[f]["p99"], res[f]["median"] = G.gravity_error(f, tgt, exact)
 
     batched = G.batched(args.blocks) if args.blocks > 0 else None
-    if batched is not None and learned is not None:  # the same blocks with the previous-h start
-        b0 = G.batched(args.blocks, form="mixed_prevh")
-        batched["with_previous_h_start"] = {"value": b0["value"], "ms_per_block": b0["ms_per_block"],
-                                            "block_end_search": b0["block_end_search"]}
 
     H = res[head]
     # roofline of the dominant kernel of the headline form
@@ -718,7 +724,8 @@ def run_gpu(args, world, rank, local):
                "walk_items": (f"runs of sibling groups of <= {merge} particles, own spheres" if merge else
                               "the reference's groups (cpp/nbody.cpp:235-243)"),
                "sph": "float32 + Kahan" if sph32 else "float64 (reference)",
-               "h_guess": ["previous h", "cell density", "learned MLP"][hg],
+               "h_guess": ["previous h (cell density without one)", "cell density",
+                           "previous h (learned MLP without one)"][hg],
                "grav_p99_rel_err_vs_f64_direct": r["p99"], "grav_median_rel_err": r["median"],
                "stages_ms": {k: round(v["ms_per_launch"], 4) for k, v in r["stages"].items()},
                "knn_iterations_per_gas": r["knn_iters"], "walk_interactions": r["pairs"],
@@ -776,28 +783,26 @@ def run_learned(args, world, rank, local):
     # the geometric opening criterion here: the relative one takes its error scale from the
     # previous evaluation, which differs between the three runs compared bit for bit below
     lib.gf_set_option(L.OPT_GRAVITY_REL, 0)
+    # the first search of this snapshot (the network never saw it): without a previous h the
+    # start is the cell density or the learned guess; then, with a previous h, 2.5 h
     res = {}
     pos = G.T["pos"].clone()
-    for mode, name in ((1, "cell_density"), (2, "learned"), (0, "previous_h")):
-        lib.gf_set_option(L.OPT_HGUESS, 0)
-        G.step(theta, pos=pos)
-        nxt = pos + 0.5 * G.dt[:, None] * G.T["vel"]
-        lib.gf_set_option(L.OPT_HGUESS, mode)
-        lib.gf_profile(1)
-        G.step(theta, pos=nxt)
-        torch.cuda.synchronize()
-        ms, cnt = ctypes.c_double(), ctypes.c_int()
-        lib.gf_profile_stage(L.STAGES.index("knn"), ctypes.byref(ms), ctypes.byref(cnt))
-        lib.gf_profile(0)
-        res[name] = {"iterations_per_gas": G.knn_iters(), "knn_ms": ms.value,
-                     "acc": G.acc.clone(), "dt": G.dt.clone()}
+    for mode, name in ((1, "cell_density"), (2, "learned")):
+        r = G.search_without_h(theta, pos, mode)
+        res[name] = {**r, "acc": G.acc.clone(), "dt": G.dt.clone()}
+    lib.gf_set_option(L.OPT_HGUESS, 0)
+    res["previous_h"] = G.search_after_drift(theta, pos, 1, 0)
+    res["previous_h"].update({"acc": res["learned"]["acc"], "dt": res["learned"]["dt"]})
     same = all(torch.equal(res[k]["acc"], res["cell_density"]["acc"]) and
-               torch.equal(res[k]["dt"], res["cell_density"]["dt"]) for k in res)
+               torch.equal(res[k]["dt"], res["cell_density"]["dt"]) for k in ("learned",))
     print(json.dumps({
         "workload": "learned smoothing-length guess: 1,000,000 gas, disk + 200 Plummer clumps (seed 3)",
-        "training": {k: v for k, v in tr.items() if k != "search_on_drifted_snapshot"},
+        "training": {k: v for k, v in tr.items() if k in ("training_rows", "loss_start", "loss_end", "train_s")},
         "training_pairs_from": "plain-method evaluations of the 200k and 1M disk+halo snapshots",
-        "search": {k: {"iterations_per_gas": v["iterations_per_gas"], "knn_ms": v["knn_ms"]} for k, v in res.items()},
+        "first_search": {k: {"iterations_per_gas": v["iterations_per_gas"], "knn_ms": v["knn_ms"]}
+                         for k, v in res.items() if k != "previous_h"},
+        "search_with_previous_h_after_half_step": {"iterations_per_gas": res["previous_h"]["iterations_per_gas"],
+                                                   "knn_ms": res["previous_h"]["knn_ms"]},
         "converged_results_identical": bool(same),
         "speedup_learned_vs_cell_density": res["cell_density"]["knn_ms"] / res["learned"]["knn_ms"],
     }), flush=True)

@@ -111,6 +111,7 @@ OPT_GRAVITY_REL = 6
 OPT_WALK_MERGE = 7
 OPT_GRAVITY_REL_MONO = 8
 OPT_WALK_SHAPE = 9
+OPT_FORGET_H = 10
 MLP_PARAMS = 4545
 
 STAGES = ["tree_build", "tree_refit", "walk", "group_prep", "knn", "knn_tree", "sph_density",

@@ -628,6 +628,10 @@ int gf_set_option(int key, double value) {
                 require(value >= 0 && value < 1, "monopole tolerance is in [0, 1)");
                 F.grav_rel_mono = value;
                 break;
+            case GF_OPT_FORGET_H:  // the next full search starts without previous smoothing lengths
+                F.have_hprev = false;
+                F.have_divv = false;
+                break;
             case GF_OPT_WALK_SHAPE:
                 require(value >= 0 && value < kNumWalkShapes && value == int(value), "walk shape is 0..3");
                 F.walk_shape = int(value);
@@ -928,7 +932,7 @@ int gf_force_stats(double* out, int nout) {
         if (F.grav.valid)  // the device count: also right after a synchronisation-free rebuild
             GF_CUDA(cudaMemcpy(&gc, F.grav.counts.p, sizeof gc, cudaMemcpyDeviceToHost));
         const double v[9] = {h ? double(F.ng) : 0.0, h ? h->dt_grav : 0.0, h ? h->dt_gas : 0.0,
-                             h ? double(h->knn_iters) : 0.0, double(kc.reserved), double(F.full_searches),
+                             h ? double(h->knn_iters) : 0.0, 0.0, double(F.full_searches),
                              double(F.verlet_hits), double(F.knn_tree.nn), double(gc.total_nodes)};
         for (int i = 0; i < nout && i < 9; ++i) out[i] = v[i];
     });

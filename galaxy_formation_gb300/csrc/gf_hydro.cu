@@ -160,16 +160,24 @@ __global__ void k_smoothing(int ng, const double* __restrict__ d31, double eps, 
     hprev[gidx[i]] = 0.5 * d31[i] > 0 ? 0.5 * d31[i] : v;
 }
 
-// appends (features, log of the unfloored h = d_32 / 2) rows to the training set
-// training pair: the features and the log distance of the 48th nearest (the radius the
-// search has to reach)
-__global__ void k_collect(int ng, long long base, const float* __restrict__ X, const float* __restrict__ dk,
+// Training pairs: the features and the log distance of the 48th nearest (the radius the
+// search has to reach), twice per particle: with its previous h and divergence, and as a
+// particle without them would see it (the cold_log_h stand-in, divergence 0), so that the one
+// network serves searches with and without a previous h.
+__global__ void k_collect(int ng, long long base, int k, const float* __restrict__ X, const float* __restrict__ dk,
                           float* __restrict__ colX, float* __restrict__ colT) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ng) return;
-    const size_t r = size_t(base) + i;
+    const size_t r = size_t(base) + 2 * size_t(i);
+    const float t = logf(fmaxf(dk[i], 1e-30f));
     for (int c = 0; c < 4; ++c) colX[4 * r + c] = X[4 * size_t(i) + c];
-    colT[r] = logf(fmaxf(dk[i], 1e-30f));
+    colT[r] = t;
+    const float f0 = X[4 * size_t(i)];
+    colX[4 * (r + 1) + 0] = f0;
+    colX[4 * (r + 1) + 1] = cold_log_h(f0, k);
+    colX[4 * (r + 1) + 2] = X[4 * size_t(i) + 2];
+    colX[4 * (r + 1) + 3] = 0.f;
+    colT[r + 1] = t;
 }
 
 __global__ void k_scatter_f(int ng, const int* __restrict__ gidx, const float* __restrict__ v, float* __restrict__ out,
@@ -502,26 +510,30 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
         const int kq = std::min(kCand, ng);
         nb = cache.get<int>(size_t(ng) * kCand);
         float* rg = nullptr;
-        if (have_hprev && hguess == 0) {  // previous h
+        if (have_hprev && (hguess == 0 || hguess == 2)) {  // previous h
             rg = rguess.get<float>(ng);
             k_guess<<<ggrid, kThreads, 0, s>>>(ng, gi, h_prev.as<double>(), rg);
             GF_CHECK_LAUNCH();
         }
         const bool collect = collect_cap > collect_n && have_hprev;
+        // the learned guess starts the searches that have no previous h (the first of a particle
+        // set); where a previous h exists, 2.5 h is the better start (fewer radius iterations)
         HGuess hg{gi, have_hprev ? h_prev.as<double>() : nullptr, have_divv ? divv_prev.as<float>() : nullptr,
                   hX.get<float>(4 * size_t(ng)), hY.get<float>(ng), hrg.get<float>(ng),
-                  hguess == 2 && have_hprev && mlp().ready, collect ? hdk.get<float>(ng) : nullptr};
+                  hguess == 2 && !have_hprev && mlp().ready, collect ? hdk.get<float>(ng) : nullptr};
         const bool features = collect || hg.use_mlp;
         GF_CUDA(cudaMemsetAsync(&sc->knn_iters, 0, sizeof(unsigned long long), s));
         // the gas of the last full search, moved (same count): rebuild without a host round trip
         knn_exact(knn_tree, ng, gp, kq, rg, nullptr, nullptr, &sc->knn_iters, s, nb, kCand, d31, kNgb - 1,
                   features ? &hg : nullptr, order_ng == ng);
         if (collect) {
-            const long long take = std::min<long long>(ng, collect_cap - collect_n);
-            k_collect<<<div_up(take, kThreads), kThreads, 0, s>>>(int(take), collect_n, hg.X, hg.dk,
-                                                                  colX.as<float>(), colT.as<float>());
-            GF_CHECK_LAUNCH();
-            collect_n += take;
+            const long long take = std::min<long long>(ng, (collect_cap - collect_n) / 2);  // two rows each
+            if (take > 0) {
+                k_collect<<<div_up(take, kThreads), kThreads, 0, s>>>(int(take), collect_n, kq, hg.X, hg.dk,
+                                                                      colX.as<float>(), colT.as<float>());
+                GF_CHECK_LAUNCH();
+                collect_n += 2 * take;
+            }
         }
         int* rw = row.as<int>();
         GF_CUDA(cudaMemsetAsync(rw, 0xff, sizeof(int) * size_t(n), s));

@@ -220,57 +220,27 @@ __device__ void warp_bitonic(K* key, int* tag, int P) {
     }
 }
 
-// Ascending bitonic sort of 32 R 64-bit keys held in registers, key e = 32 r + lane in v[r]:
-// strides below 32 exchange with lane ^ stride by shuffles, larger ones between a lane's own
-// registers. No shared memory (a shared-memory network of 64-bit keys takes 2-way bank
-// conflicts at every stride below 16).
-template <int R>
-__device__ __forceinline__ void reg_bitonic(unsigned long long (&v)[R]) {
+// Ascending bitonic sort of P (power of two <= 128) 64-bit keys in shared memory by the
+// calling warp (keys are unique when they carry an index in their low bits). (A register
+// version, keys exchanged by shuffles, removed the shared-memory bank conflicts but slowed the
+// neighbour search: more instructions and register spills in an issue-bound kernel.)
+__device__ void warp_sort_u64(unsigned long long* key, int P) {
     const int lane = threadIdx.x & 31;
-    constexpr int N = 32 * R;
-#pragma unroll
-    for (int size = 2; size <= N; size <<= 1) {
-#pragma unroll
+    for (int size = 2; size <= P; size <<= 1) {
         for (int stride = size >> 1; stride > 0; stride >>= 1) {
-            if (stride >= 32) {
-                const int rs = stride >> 5;
-#pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    const int p = r ^ rs;
-                    if (p > r) {
-                        const bool up = ((32 * r) & size) == 0;
-                        const unsigned long long a = v[r], b = v[p];
-                        const bool sw = (a > b) == up;
-                        v[r] = sw ? b : a;
-                        v[p] = sw ? a : b;
-                    }
-                }
-            } else {
-                const bool lower = (lane & stride) == 0;
-#pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    const unsigned long long o = __shfl_xor_sync(0xffffffffu, v[r], stride);
-                    const bool up = ((32 * r + lane) & size) == 0;
-                    v[r] = (lower == up) ? (v[r] < o ? v[r] : o) : (v[r] < o ? o : v[r]);
+            for (int t = lane; t < P / 2; t += 32) {
+                const int a = ((t & ~(stride - 1)) << 1) | (t & (stride - 1));
+                const int b = a + stride;
+                const bool up = (a & size) == 0;
+                const unsigned long long ka = key[a], kb = key[b];
+                if ((ka > kb) == up) {
+                    key[a] = kb;
+                    key[b] = ka;
                 }
             }
+            __syncwarp();
         }
     }
-}
-
-// Sorts key[0, cnt) ascending in place (cnt <= 128), padding to 64 or 128 with ~0: the keys
-// go through registers, and the sorted ones are stored back lane-contiguous.
-template <int R>
-__device__ __forceinline__ void sort_keys_reg(unsigned long long* key, int cnt) {
-    const int lane = threadIdx.x & 31;
-    unsigned long long v[R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = 32 * r + lane < cnt ? key[32 * r + lane] : ~0ull;
-    __syncwarp();
-    reg_bitonic<R>(v);
-#pragma unroll
-    for (int r = 0; r < R; ++r) key[32 * r + lane] = v[r];
-    __syncwarp();
 }
 
 // --------------------------------------------------------------- knn_from_candidates
@@ -511,10 +481,11 @@ __device__ void knn_finish(const KnnArgs& A, unsigned long long* key, unsigned l
     const int lane = threadIdx.x & 31;
     const int k = A.k;
     const int oq = A.perm[q];
-    if (cnt <= 64)
-        sort_keys_reg<2>(key, cnt);
-    else
-        sort_keys_reg<4>(key, cnt);
+    int P = 64;
+    while (P < cnt) P <<= 1;
+    for (int t = cnt + lane; t < P; t += 32) key[t] = ~0ull;
+    __syncwarp();
+    warp_sort_u64(key, P);
     const int pi = oq;
     if (!A.exact_order) {
         // Float32 order: the k nearest as a set (only pairs tied to float32 rounding can
@@ -532,9 +503,6 @@ __device__ void knn_finish(const KnnArgs& A, unsigned long long* key, unsigned l
         below = warp_sum(below);
         inband = warp_sum(inband);
         double best;
-        // with float32 near-ties around entry c, the float64 order of the tied entries decides
-        // which of them are among the first c + 1 (the set the smoothing length is taken from)
-        const bool reorder = inband > 1 && below + inband <= 64;
         if (inband == 1) {  // no float32 near-tie: entry c itself, measured in float64
             best = d2_f64(A, pi, A.perm[key_idx(key[c])]);
         } else {
@@ -544,9 +512,9 @@ __device__ void knn_finish(const KnnArgs& A, unsigned long long* key, unsigned l
                 int tag = 0x7fffffff;
                 const float vf = t < cnt ? key_d2(key[t]) : INFINITY;
                 if (t < cnt && vf >= lo && vf <= hi) {
-                    const int pj = A.perm[key_idx(key[t])];
-                    v = d2_f64(A, pi, pj);
-                    tag = pj;
+                    const int j = key_idx(key[t]);
+                    v = d2_f64(A, pi, A.perm[j]);
+                    tag = j;
                 }
                 dd[t] = (unsigned long long)__double_as_longlong(v);
                 di[t] = tag;
@@ -554,11 +522,16 @@ __device__ void knn_finish(const KnnArgs& A, unsigned long long* key, unsigned l
             __syncwarp();
             warp_bitonic(dd, di, 64);
             best = __longlong_as_double((long long)dd[max(0, rank_need)]);
+            // the tied entries [below, below + inband) take the float64 order (ties by tree
+            // position), so the first c + 1 entries are the exact set the smoothing length is
+            // measured on; their float32 distance bits stay (all within the band)
+            if (below + inband <= 64)
+                for (int t = lane; t < inband; t += 32)
+                    key[below + t] = (key[below + t] & 0xffffffff00000000ull) | unsigned(di[t]);
+            __syncwarp();
         }
         for (int t = lane; t < k; t += 32) {
-            // the tied band [below, below + inband) in float64 order (ties by index): di holds
-            // its entries sorted first
-            const int pj = reorder && t >= below && t < below + inband ? di[t - below] : A.perm[key_idx(key[t])];
+            const int pj = A.perm[key_idx(key[t])];
             if (A.nb32) A.nb32[size_t(oq) * A.ld32 + t] = pj;
             if (A.nb) A.nb[size_t(oq) * k + t] = pj;
         }
@@ -736,7 +709,11 @@ void knn_from_candidates(int n, int m, const double* pos, const int64_t* cand, i
 
 // Features of the smoothing-length guess, per gas particle (caller order):
 // (log cell density of its leaf, log previous h, leaf count, previous velocity divergence).
-__global__ void k_hfeatures(int n, const int* __restrict__ perm, const int* __restrict__ leaf_of,
+// Features of the learned guess: log cell density, log previous h, leaf count, velocity
+// divergence. A particle without a previous h (the first search of a particle set) gets, in
+// its place, the h that its cell density implies (the search radius of the cell-density start
+// over 2.5: a function of the first feature, cold_log_h) and a divergence of 0.
+__global__ void k_hfeatures(int n, int k, const int* __restrict__ perm, const int* __restrict__ leaf_of,
                             const float4* __restrict__ wb, const float4* __restrict__ wgeo, const int* __restrict__ gidx,
                             const double* __restrict__ hprev, const float* __restrict__ divv, float* __restrict__ X) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -747,10 +724,11 @@ __global__ void k_hfeatures(int n, const int* __restrict__ perm, const int* __re
     const float side = 2.f * wgeo[lf].w;
     const int g = gidx ? gidx[i] : i;
     const double hp = hprev ? hprev[g] : 0.0;
-    X[4 * size_t(i) + 0] = logf(c / fmaxf(side * side * side, 1e-30f));
-    X[4 * size_t(i) + 1] = hp > 0 ? float(log(hp)) : 0.f;
+    const float f0 = logf(c / fmaxf(side * side * side, 1e-30f));
+    X[4 * size_t(i) + 0] = f0;
+    X[4 * size_t(i) + 1] = hp > 0 ? float(log(hp)) : cold_log_h(f0, k);
     X[4 * size_t(i) + 2] = c;
-    X[4 * size_t(i) + 3] = divv ? divv[g] : 0.f;
+    X[4 * size_t(i) + 3] = hp > 0 && divv ? divv[g] : 0.f;
 }
 
 // The learned guess predicts the log distance of the k-th nearest; the search starts a little
@@ -780,7 +758,7 @@ void knn_exact(Octree& T, int n, const double* pos, int k, const float* r_guess,
         T.build(n, pos, nullptr, 0.7, s);
     }
     if (hg && hg->X) {  // features for the learned guess (and for training pairs)
-        k_hfeatures<<<div_up(n, kThreads), kThreads, 0, s>>>(n, T.perm.as<int>(), T.leaf_of.as<int>(),
+        k_hfeatures<<<div_up(n, kThreads), kThreads, 0, s>>>(n, k, T.perm.as<int>(), T.leaf_of.as<int>(),
                                                              T.w_b.as<float4>(), T.w_geo.as<float4>(), hg->gidx,
                                                              hg->hprev, hg->divv, hg->X);
         GF_CHECK_LAUNCH();

@@ -20,8 +20,9 @@ void sph_forces(SphScratch& S, int n, int k, int ld, const double* pos, const do
 
 // Inputs of the learned smoothing-length guess inside a neighbour search: X (n x 4) receives
 // the features; with use_mlp the network's predicted distance of the k-th nearest, times a
-// small margin, gives the starting radius; dk (if set) receives the converged distances of
-// the k-th nearest, the training targets.
+// small margin, gives the starting radius (the library uses it for searches without a
+// previous h); dk (if set) receives the converged distances of the k-th nearest, the training
+// targets.
 struct HGuess {
     const int* gidx;      // caller index -> global particle index (null: identity)
     const double* hprev;  // previous h per global index (null: none)
@@ -32,6 +33,13 @@ struct HGuess {
     bool use_mlp;
     float* dk;            // n distances of the k-th nearest (out, training targets), or null
 };
+
+// log h of the cell-density start (radius side (k / count)^(1/3), over the 2.5 that relates a
+// previous h to its search radius) from the first feature f0 = log(count / side^3): the
+// stand-in for the previous h of a particle that has none.
+__host__ __device__ inline float cold_log_h(float f0, int k) {
+    return (logf(float(k)) - f0) * (1.0f / 3.0f) - logf(2.5f);
+}
 
 struct Sph32Scratch {
     DevBuf A, B, C, D;

@@ -269,20 +269,6 @@ __device__ int run_end(const KeyView& K, int n, int i, int d) {
     return lo;
 }
 
-// run_end for a node inside an enclosing node that ends at hi (> i): binary search of (i, hi]
-// (cpl(i, j) does not grow with j, so cpl(i, j) < d holds from some j on)
-__device__ int run_end_within(const KeyView& K, int i, int d, int hi) {
-    int lo = i + 1;
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (cpl(K, i, mid) < d)
-            hi = mid;
-        else
-            lo = mid + 1;
-    }
-    return lo;
-}
-
 // first j <= i with cpl(j, i) >= lev
 __device__ int run_begin(const KeyView& K, int i, int lev) {
     int hi = i, step = 1, lo;
@@ -309,54 +295,59 @@ __device__ int run_begin(const KeyView& K, int i, int lev) {
 
 // ---------------------------------------------------------------------------- emit
 
-__global__ void k_emit(KeyView K, int n, const RootBox* __restrict__ rootp,
+// Node emission, one thread per node. Position i starts the nodes of depths ds[i] .. ld[i]
+// (ids nbase[i] ..); k_node_owner writes, for every node id, the position that starts it, and
+// k_emit fills the node: the cube centre by the float64 halving chain from the root along
+// i's octant digits (cpp/nbody.cpp:92-96), the particle range [i, end) with end the first
+// position whose prefix leaves the node's, `next` = the first node starting at end, the leaf
+// flag and the parent (the previous node of the chain, or the deepest node at depth d - 1 of
+// the run containing i). Threads of consecutive ids take chains of similar depth, so a warp
+// keeps most lanes busy (one thread per starting position left 5 of 32 busy).
+__global__ void k_node_owner(int n, const int* __restrict__ nstart, const int* __restrict__ nbase,
+                             int* __restrict__ owner, int cap) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int c = nstart[i], b = nbase[i];
+    for (int t = 0; t < c && b + t < cap; ++t) owner[b + t] = i;
+}
+
+__global__ void k_emit(KeyView K, int n, int span, const RootBox* __restrict__ rootp,
                        const int8_t* __restrict__ ldepth, const int8_t* __restrict__ dsplit,
-                       const int* __restrict__ nstart, const int* __restrict__ nbase,
+                       const int* __restrict__ nbase, const int* __restrict__ owner,
                        const TreeCounts* __restrict__ cnt, int4* __restrict__ n_i4,
                        double4* __restrict__ n_cd, float4* __restrict__ n_geo,
                        int* __restrict__ n_parent, int cap) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || nstart[i] == 0) return;
-    const RootBox R = *rootp;
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
     const int total = cnt->total_nodes;
-    const int ds = dsplit[i], ld = ldepth[i], base = nbase[i];
+    if (id >= span || id >= total || id >= cap) return;  // past cap: reported by k_node_cap_check
+    const int i = owner[id];
+    const int ds = dsplit[i], ld = ldepth[i];
+    const int d = ds + (id - nbase[i]);
+    const RootBox R = *rootp;
     double c[3] = {R.c[0], R.c[1], R.c[2]};
     double h = R.half;
-    for (int l = 1; l <= ds; ++l) {
+    for (int l = 1; l <= d; ++l) {
         h = 0.5 * h;
         const int o = digit(K, i, l);
         c[0] = __dadd_rn(c[0], (o & 1) ? h : -h);
         c[1] = __dadd_rn(c[1], (o & 2) ? h : -h);
         c[2] = __dadd_rn(c[2], (o & 4) ? h : -h);
     }
-    int end = n;
-    for (int d = ds; d <= ld; ++d) {
-        if (d > ds) {
-            h = 0.5 * h;
-            const int o = digit(K, i, d);
-            c[0] = __dadd_rn(c[0], (o & 1) ? h : -h);
-            c[1] = __dadd_rn(c[1], (o & 2) ? h : -h);
-            c[2] = __dadd_rn(c[2], (o & 4) ? h : -h);
-        }
-        const int id = base + (d - ds);
-        if (id >= cap) return;  // reported by k_node_cap_check
-        // the first node of the chain searches from i; each deeper one within its parent
-        end = d == ds ? run_end(K, n, i, d) : run_end_within(K, i, d, end);
-        const int next = end < n ? nbase[end] : total;
-        int parent;
-        if (d == 0) {
-            parent = -1;
-        } else if (d > ds) {
-            parent = id - 1;
-        } else {
-            const int s = run_begin(K, i, d - 1);
-            parent = nbase[s] + (d - 1 - dsplit[s]);
-        }
-        n_i4[id] = make_int4(i, end - i, next, (d == ld ? 1 : 0) | (d << 8));
-        n_cd[id] = make_double4(c[0], c[1], c[2], h);
-        n_geo[id] = make_float4(float(c[0]), float(c[1]), float(c[2]), float(h));
-        n_parent[id] = parent;
+    const int end = run_end(K, n, i, d);
+    const int next = end < n ? nbase[end] : total;
+    int parent;
+    if (d == 0) {
+        parent = -1;
+    } else if (d > ds) {
+        parent = id - 1;
+    } else {
+        const int s = run_begin(K, i, d - 1);
+        parent = nbase[s] + (d - 1 - dsplit[s]);
     }
+    n_i4[id] = make_int4(i, end - i, next, (d == ld ? 1 : 0) | (d << 8));
+    n_cd[id] = make_double4(c[0], c[1], c[2], h);
+    n_geo[id] = make_float4(float(c[0]), float(c[1]), float(c[2]), float(h));
+    n_parent[id] = parent;
 }
 
 __global__ void k_node_cap_check(TreeCounts* cnt, int cap, uint32_t* status) {
@@ -542,43 +533,6 @@ __device__ __forceinline__ float2 rel_radii(float m, float ox, float oy, float o
     return make_float2(exp2f(0.2f * lm + 0.6f * lb), exp2f(0.25f * lm + 0.5f * lb));
 }
 
-// Mixed form: monopole and traceless quadrupole in one bottom-up pass, float32 with
-// Kahan-compensated sums. A leaf sums its particles; the last child to finish a parent
-// (arrival counter) combines the children's masses and centres, then their quadrupoles shifted
-// by the parallel-axis term. open_r = 2 (half + displacement) / theta + |com - cell centre|
-// as in the float64 pass, evaluated in float32.
-struct Mom32Args {
-    int nn;
-    const int* nn_dev;
-    bool refit;
-    float theta;
-    const int4* n_i4;
-    const int* parent;
-    const int* nchild;
-    int* counter;
-    const float4* n_geo;
-    float4* mom;
-    float* open_r;
-    float* ndisp;
-    const float4* p4;
-    const float* pdisp;
-    float4* q4;   // Qxx, Qyy, Qxy, Qxz
-    float2* qyz;  // Qyz, T = sum m |d|^2
-};
-
-__device__ __forceinline__ float4 finalize32(const Mom32Args& A, int k, const KahanF& M, const KahanF& sx,
-                                             const KahanF& sy, const KahanF& sz, float dm) {
-    const float inv = M.s > 0.f ? 1.f / M.s : 0.f;
-    const float4 c = make_float4(sx.s * inv, sy.s * inv, sz.s * inv, M.s);
-    A.mom[k] = c;
-    const float4 g = A.n_geo[k];
-    const float first = 2.f * (g.w + dm) / A.theta;
-    if (A.refit) A.ndisp[k] = dm;
-    const float ox = c.x - g.x, oy = c.y - g.y, oz = c.z - g.z;
-    A.open_r[k] = first + sqrtf(ox * ox + oy * oy + oz * oz);
-    return c;
-}
-
 // Traceless quadrupole Q = sum m (3 d d - |d|^2 I) and trace T = sum m |d|^2 about a centre.
 struct QuadSum {
     KahanF xx, yy, xy, xz, yz, tr;
@@ -593,76 +547,14 @@ struct QuadSum {
     }
 };
 
-__global__ void k_moments_quad32(Mom32Args A) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= live_nodes(A.nn, A.nn_dev)) return;
-    const int4 q = A.n_i4[k];
-    if (!(q.w & 1)) return;
-    {
-        KahanF M, sx, sy, sz;
-        float dm = 0.f;
-        for (int i = q.x; i < q.x + q.y; ++i) {
-            const float4 p = A.p4[i];
-            M.add(p.w);
-            sx.add(p.w * p.x);
-            sy.add(p.w * p.y);
-            sz.add(p.w * p.z);
-            if (A.refit) dm = fmaxf(dm, A.pdisp[i]);
-        }
-        const float4 c = finalize32(A, k, M, sx, sy, sz, dm);
-        QuadSum S;
-        for (int i = q.x; i < q.x + q.y; ++i) {
-            const float4 p = A.p4[i];
-            S.point(p.w, p.x - c.x, p.y - c.y, p.z - c.z);
-        }
-        A.q4[k] = make_float4(S.xx.s, S.yy.s, S.xy.s, S.xz.s);
-        A.qyz[k] = make_float2(S.yz.s, S.tr.s);
-    }
-    __threadfence();
-    int p = A.parent[k];
-    while (p >= 0) {
-        const int arrived = atomicAdd(&A.counter[p], 1);
-        if (arrived != A.nchild[p] - 1) return;
-        __threadfence();
-        const int end = A.n_i4[p].z;
-        KahanF M, sx, sy, sz;
-        float dm = 0.f;
-        int seen = 0;
-        for (int c = p + 1; c < end && seen < 8; c = A.n_i4[c].z, ++seen) {  // octant order
-            const float4 cm = __ldcg(&A.mom[c]);
-            M.add(cm.w);
-            sx.add(cm.w * cm.x);
-            sy.add(cm.w * cm.y);
-            sz.add(cm.w * cm.z);
-            if (A.refit) dm = fmaxf(dm, __ldcg(&A.ndisp[c]));
-        }
-        const float4 cp = finalize32(A, p, M, sx, sy, sz, dm);
-        QuadSum S;
-        seen = 0;
-        for (int c = p + 1; c < end && seen < 8; c = A.n_i4[c].z, ++seen) {
-            const float4 cm = __ldcg(&A.mom[c]);
-            const float4 qc = __ldcg(&A.q4[c]);
-            const float2 yt = __ldcg(&A.qyz[c]);
-            S.xx.add(qc.x);
-            S.yy.add(qc.y);
-            S.xy.add(qc.z);
-            S.xz.add(qc.w);
-            S.yz.add(yt.x);
-            S.tr.add(yt.y);
-            S.point(cm.w, cm.x - cp.x, cm.y - cp.y, cm.z - cp.z);
-        }
-        A.q4[p] = make_float4(S.xx.s, S.yy.s, S.xy.s, S.xz.s);
-        A.qyz[p] = make_float2(S.yz.s, S.tr.s);
-        __threadfence();
-        p = A.parent[p];
-    }
-}
-
-// Refit of the mixed form directly in the breadth-first walk layout: the same float32 + Kahan
-// monopole / quadrupole / open_r as k_moments_quad32, with the same summation order (the
-// children of a node are contiguous there, in octant order), but a parent reads its children
-// with independent loads instead of following `next` links, and the walk arrays are written
-// in place (no k_walk_fill pass). Thread per breadth-first node; leaves start the chains.
+// Mixed form: monopole and traceless quadrupole in one bottom-up pass, float32 with
+// Kahan-compensated sums, directly in the breadth-first walk layout (the children of a node
+// are contiguous there, in octant order, so a parent reads them with independent loads). A
+// leaf sums its particles; the last child to finish a parent (arrival counter) combines the
+// children's masses and centres, then their quadrupoles shifted by the parallel-axis term.
+// open_r = 2 (half + displacement) / theta + |com - cell centre| in float32, and the relative
+// opening radii. Used by the build (pdisp null: no displacement) and by the refit (pdisp: the
+// displacement of each particle since the build). Thread per breadth-first node.
 struct RefitBfsArgs {
     int span;
     const int* nn_dev;
@@ -677,7 +569,7 @@ struct RefitBfsArgs {
     float* wrq;   // quadrupole-order radius
     float* ndisp; // breadth-first
     const float4* p4;
-    const float* pdisp;
+    const float* pdisp;  // null: no displacement (the build)
 };
 
 __device__ __forceinline__ float4 finalize_bfs(const RefitBfsArgs& A, int b, const KahanF& M, const KahanF& sx,
@@ -710,7 +602,7 @@ __global__ void k_refit_bfs_quad32(RefitBfsArgs A) {
             sx.add(p.w * p.x);
             sy.add(p.w * p.y);
             sz.add(p.w * p.z);
-            dm = fmaxf(dm, A.pdisp[i]);
+            if (A.pdisp) dm = fmaxf(dm, A.pdisp[i]);
         }
         const float4 c = finalize_bfs(A, b, M, sx, sy, sz, dm);
         QuadSum S;
@@ -817,9 +709,7 @@ __global__ void k_walk_fill(int nn, const int4* __restrict__ n_i4, const int* __
                             const float* __restrict__ open_r, const float4* __restrict__ geo,
                             float4* __restrict__ wa, float4* __restrict__ wb,
                             float4* __restrict__ wgeo, int* __restrict__ leaf_of,
-                            const float4* __restrict__ q4, const float2* __restrict__ qyz,
-                            float4* __restrict__ wq, const int* __restrict__ parent, int* __restrict__ wparent,
-                            float2* __restrict__ wt, float* __restrict__ wrq, const int* __restrict__ nn_dev) {
+                            const int* __restrict__ parent, int* __restrict__ wparent, const int* __restrict__ nn_dev) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= live_nodes(nn, nn_dev)) return;
     const int4 q = n_i4[k];
@@ -834,20 +724,11 @@ __global__ void k_walk_fill(int nn, const int4* __restrict__ n_i4, const int* __
         first = bfs[k + 1];
         code = nchild[k];
     }
-    const float4 c = mom[k];
-    wa[b] = c;
-    float2 rr = make_float2(0.f, 0.f);
-    if (q4) {
-        const float4 g = geo[k];
-        rr = rel_radii(c.w, c.x - g.x, c.y - g.y, c.z - g.z, g.w);
-        wrq[b] = rr.y;
-    }
-    wb[b] = make_float4(open_r[k], __int_as_float(first), __int_as_float(code), rr.x);
+    // mom null (mixed-form build, neighbour-search trees): no moments here (the mixed form
+    // writes them into this layout afterwards)
+    wa[b] = mom ? mom[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    wb[b] = make_float4(mom ? open_r[k] : 0.f, __int_as_float(first), __int_as_float(code), 0.f);
     if (wgeo) wgeo[b] = geo[k];
-    if (q4) {
-        wq[b] = q4[k];
-        wt[b] = qyz[k];
-    }
     if (wparent) wparent[b] = parent[k] < 0 ? -1 : bfs[parent[k]];
 }
 
@@ -963,6 +844,7 @@ void Octree::reserve_graph_build() {
     key1.get<uint64_t>(n);
     key2.get<uint64_t>(n);
     pdisp.get<float>(n);
+    node_owner.get<int>(node_cap);
     work.get<int4>(std::max(size_t(node_cap), size_t(n)) + 1);
     sphere.get<float4>(std::max(size_t(node_cap), size_t(n)) + 1);
     if (quad) item_gam.get<float2>(std::max(size_t(node_cap), size_t(n)) + 1);
@@ -1066,7 +948,10 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
     int* par = n_parent.get<int>(cap);
     {
         ProfScope pse(want_knn ? kStCount : kStTreeEmit, s);
-        k_emit<<<grid, kThreads, 0, s>>>(K, n, R, ld, ds, ns, nb, cnt, i4, cd, geo, par, cap);
+        int* own = node_owner.get<int>(cap);
+        k_node_owner<<<grid, kThreads, 0, s>>>(n, ns, nb, own, cap);
+        GF_CHECK_LAUNCH();
+        k_emit<<<ngrid, kThreads, 0, s>>>(K, n, span, R, ld, ds, nb, own, cnt, i4, cd, geo, par, cap);
         GF_CHECK_LAUNCH();
     }
     if (graph_safe) {  // more nodes than the buffers hold: flag, and leave an empty tree
@@ -1093,12 +978,8 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
     if (want_knn) {
         // a neighbour-search tree needs geometry only: no moments (the walk layout's mass and
         // opening-radius fields stay unused)
-    } else if (quad) {  // mixed form: float32 monopole + quadrupole in one pass
-        Mom32Args A{span, nn_dev, false, theta_f, i4, par, nch, ctr, geo, mom, opr, ndp, pp, nullptr,
-                    n_quad.get<float4>(cap), n_qyz.get<float2>(cap)};
-        ProfScope psm(kStTreeMoments, s);
-        k_moments_quad32<<<ngrid, kThreads, 0, s>>>(A);
-        GF_CHECK_LAUNCH();
+    } else if (quad) {
+        // mixed form: moments in the breadth-first walk layout, after it is laid out (below)
     } else {
         MomentArgs A{};
         A.nn = span;
@@ -1140,15 +1021,22 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
     GF_CHECK_LAUNCH();
     // breadth-first geometry and parents: the neighbour search, and the mixed form's refit
     const bool bfs_geo = want_knn || quad;
-    k_walk_fill<<<ngrid, kThreads, 0, s>>>(span, i4, nch, bfs, mom, opr, geo, w_a.get<float4>(cap),
-                                           w_b.get<float4>(cap), bfs_geo ? w_geo.get<float4>(cap) : nullptr,
-                                           want_knn ? leaf_of.get<int>(n) : nullptr,
-                                           quad ? n_quad.as<float4>() : nullptr, quad ? n_qyz.as<float2>() : nullptr,
-                                           quad ? w_q.get<float4>(cap) : nullptr, par,
-                                           bfs_geo ? w_parent.get<int>(cap) : nullptr,
-                                           quad ? w_t.get<float2>(cap) : nullptr, quad ? w_rq.get<float>(cap) : nullptr,
-                                           nn_dev);
+    const bool bfs_moments = quad && !want_knn;
+    k_walk_fill<<<ngrid, kThreads, 0, s>>>(span, i4, nch, bfs, bfs_moments ? nullptr : mom, opr, geo,
+                                           w_a.get<float4>(cap), w_b.get<float4>(cap),
+                                           bfs_geo ? w_geo.get<float4>(cap) : nullptr,
+                                           want_knn ? leaf_of.get<int>(n) : nullptr, par,
+                                           bfs_geo ? w_parent.get<int>(cap) : nullptr, nn_dev);
     GF_CHECK_LAUNCH();
+    if (bfs_moments) {  // mixed form: float32 monopole + quadrupole moments in one bottom-up pass
+        GF_CUDA(cudaMemsetAsync(ctr, 0, sizeof(int) * size_t(span), s));
+        RefitBfsArgs A{span, nn_dev, theta_f, w_parent.as<int>(), w_geo.as<float4>(), ctr, w_a.as<float4>(),
+                       w_b.as<float4>(), w_q.get<float4>(cap), w_t.get<float2>(cap), w_rq.get<float>(cap), ndp, pp,
+                       nullptr};
+        ProfScope psm(kStTreeMoments, s);
+        k_refit_bfs_quad32<<<ngrid, kThreads, 0, s>>>(A);
+        GF_CHECK_LAUNCH();
+    }
     valid = true;
     if (!g_no_alloc) {  // outside a capture: the live node count, for outgrowing()
         if (!h_live) GF_CUDA(cudaMallocHost(&h_live, sizeof(int)));
@@ -1217,11 +1105,8 @@ void Octree::refit(const double* pos, const double* mass, cudaStream_t s) {
                                            n_mom.as<float4>(), n_open.as<float>(), n_geo.as<float4>(),
                                            w_a.as<float4>(), w_b.as<float4>(),
                                            want_knn ? w_geo.as<float4>() : nullptr,
-                                           want_knn ? leaf_of.as<int>() : nullptr,
-                                           quad ? n_quad.as<float4>() : nullptr, quad ? n_qyz.as<float2>() : nullptr,
-                                           quad ? w_q.as<float4>() : nullptr, n_parent.as<int>(),
-                                           want_knn ? w_parent.as<int>() : nullptr,
-                                           quad ? w_t.as<float2>() : nullptr, quad ? w_rq.as<float>() : nullptr, nn_dev);
+                                           want_knn ? leaf_of.as<int>() : nullptr, n_parent.as<int>(),
+                                           want_knn ? w_parent.as<int>() : nullptr, nn_dev);
     GF_CHECK_LAUNCH();
 }
 

@@ -50,7 +50,7 @@ struct Octree {
 
     // particles (tree order unless noted)
     DevBuf key, key_alt, perm, perm_alt, key1, key2, p4, xbuild, pdisp;
-    DevBuf cpl9, ldepth, dsplit, nstart, nbase;
+    DevBuf cpl9, ldepth, dsplit, nstart, nbase, node_owner;
     // nodes, depth-first (preorder) order
     DevBuf n_i4;      // int4 {start, count, next, leaf | depth << 8}
     DevBuf n_mom;     // float4 {cx, cy, cz, m}
@@ -69,7 +69,6 @@ struct Octree {
     DevBuf w_q;       // float4 {Qxx, Qyy, Qxy, Qxz} (quadrupole trees)
     DevBuf w_t;       // float2 {Qyz, T = sum m |d|^2 about the centre of mass} (quadrupole trees)
     DevBuf w_rq;      // float (M b^2)^(1/4): the quadrupole-order radius (quadrupole trees)
-    DevBuf n_quad, n_qyz;  // traceless quadrupole about the centre of mass, preorder
     DevBuf bfs_key, bfs_key_alt, bfs_val, bfs_val_alt;
     // neighbour search extras (tree order): float32 remainders x - float(x) and the
     // breadth-first index of each particle's leaf

@@ -33,8 +33,9 @@ class Engine:
             raise _lib.GpuError(64, "no usable CUDA device")
 
     def gravity(self, pos, mass, acc, theta, eps, active=None, rebuild=True):
-        """Barnes-Hut accelerations (G = 1) written into acc for the active particles.
-        rebuild=False refits the previous tree instead of building a new one."""
+        """acc[i] = the Barnes-Hut acceleration (G = 1, Plummer eps, opening angle theta) of
+        every particle with active[i] (all when active is None); other rows are not touched.
+        rebuild=False keeps the tree of the last call and refreshes its moments."""
         n = len(mass)
         if _is_cuda_tensor(pos):
             act = 0 if active is None else active.data_ptr()
@@ -48,7 +49,7 @@ class Engine:
         _lib.check()
 
     def gravity_direct(self, pos, mass, eps):
-        """Exact O(N^2) accelerations (for tests)."""
+        """The float64 pairwise sum over all particles, O(N^2): the exact reference."""
         if _is_cuda_tensor(pos):
             import torch
 
@@ -70,7 +71,8 @@ class Engine:
         return acc
 
     def project(self, pos, group, n_groups, rot, scale, size):
-        """Particle counts per pixel and per colour group, shape (n_groups, size, size)."""
+        """Splats the particles into one float32 image per colour group, (n_groups, size, size):
+        orthographic view through rot, `scale` pixels per length unit, bilinear weights."""
         img = np.empty((n_groups, size, size), np.float32)
         self.lib.nbody_render(len(group), np.ascontiguousarray(pos), group, n_groups,
                               np.ascontiguousarray(rot), np.zeros(3), scale, size, size, img)
@@ -78,7 +80,8 @@ class Engine:
         return img
 
     def tonemap(self, img, glow, colors, inv_ref, K, exposure):
-        """8-bit RGB image from the per-group count maps and their (4x smaller) glow maps."""
+        """Combines the group images and their quarter-size glow maps into (H, W, 3) uint8:
+        logarithmic brightness plus glow, tinted by the group colours, soft-saturated."""
         ng, H, W = img.shape
         out = np.empty((H, W, 3), np.uint8)
         self.lib.nbody_tonemap(W, H, ng, img, np.ascontiguousarray(glow), glow.shape[2], glow.shape[1],

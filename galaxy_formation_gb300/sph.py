@@ -75,27 +75,28 @@ def knn(p, k):
 
 
 class NeighbourFinder:
-    """32 nearest gas neighbours of every gas particle (sph.py:138-170).
+    """The caching neighbour finder of sph.py:138-170, with the searches on the GPU.
 
-    A full search (48 candidates) is done when `fresh` is True. Otherwise the 32 nearest are
-    re-selected among the candidates remembered from the last full search (a Verlet list).
-    Indices are global particle indices in the cache, so the list survives gas particles
-    turning into stars between two searches."""
+    fresh=True, or a gas particle missing from the cache, or one left with fewer than 32
+    usable candidates: an exact search of the 48 nearest (gf_knn), whose rows become the new
+    cache. Otherwise each particle's 32 nearest are picked again from its cached 48 at the
+    current positions (gf_knn_from_candidates). The cache stores global particle indices and
+    a row per global index, so it stays valid when some gas has turned into stars since."""
 
     def __init__(self, n_total):
         self.n_total = n_total
         self.cache = None
 
     def find(self, g, p, fresh):
-        """g: global indices of gas particles, p: their positions. Returns (dist, nb) with nb
-        in local (0..len(g)-1) indices."""
+        """Neighbours of the gas particles with global indices g at positions p (len(g), 3):
+        returns (dist (len(g), 32) ascending, nb (len(g), 32) int64 as positions in g)."""
         k = N_NEIGHBOURS
         if not fresh and self.cache is not None:
             row = self.cache["row"][g]
             if (row >= 0).all():
                 loc = np.full(self.n_total, -1, np.int64)
                 loc[g] = np.arange(g.size)
-                cand = loc[self.cache["cand"][row]]      # candidates that are still gas
+                cand = loc[self.cache["cand"][row]]      # -1 where a candidate is no longer gas
                 nb = np.empty((g.size, k), np.int64)
                 d = np.empty((g.size, k))
                 if knn_from_candidates(p, cand, k, nb, d):

@@ -343,13 +343,17 @@ int gf_cool(int n, const double* u, const double* T, const double* rho, const do
  *                           keeps its own tree; nbody_accel_active is never affected. */
 #define GF_OPT_GRAVITY_QUAD 1
 /*   GF_OPT_HGUESS       start of the neighbour-count iteration of a full search:
- *                       0 = 2.5 x the previous h (default), 1 = the density of the particle's
- *                       tree cell only, 2 = the learned guess (gf_mlp_*); the iteration always
- *                       runs to the exact 48 nearest, so only the iteration count changes. */
+ *                       0 = 2.5 x the previous h (default), falling back to the density of the
+ *                       particle's tree cell when there is none (the first search of a particle
+ *                       set); 1 = the cell density only; 2 = 2.5 x the previous h, and the
+ *                       learned guess (gf_mlp_*) where there is none. The iteration always runs
+ *                       to the exact 48 nearest, so only the iteration count changes. */
 #define GF_OPT_HGUESS 2
-/*   GF_OPT_COLLECT      capacity (rows) of a device buffer that every later full search
- *                       fills with (features, log distance of the 48th nearest) pairs for training;
- *                       setting it clears the buffer; gf_get_option returns the rows kept. */
+/*   GF_OPT_COLLECT      capacity (rows) of a device buffer that every later full search with a
+ *                       previous h fills with (features, log distance of the 48th nearest) pairs
+ *                       for training, two rows per gas particle: its features, and the features it
+ *                       would have without a previous h; setting it clears the buffer;
+ *                       gf_get_option returns the rows kept. */
 #define GF_OPT_COLLECT 3
 /*   GF_OPT_WALK_CHUNK   walks of an active subset (gf_accel_active*, gf_accelerations with an
  *                       active mask): 0 = the reference's groups and spheres (default);
@@ -388,6 +392,9 @@ int gf_cool(int n, const double* u, const double* T, const double* rho, const do
  *                       warp): 0 = 4 x 256/96 (default), 1 = 2 x 256/96, 2 = 4 x 128/64,
  *                       3 = 2 x 128/64. gf_force_autotune and gf_sim_block_autotune choose it. */
 #define GF_OPT_WALK_SHAPE 9
+/*   GF_OPT_FORGET_H     (any value) the next full neighbour search starts without the previous
+ *                       smoothing lengths, as the first search of a particle set does. */
+#define GF_OPT_FORGET_H 10
 int gf_set_option(int key, double value);
 /* Current value of an option (-1 for an unknown key). */
 double gf_get_option(int key);
@@ -395,7 +402,8 @@ double gf_get_option(int key);
 /* A 4 -> 64 -> 64 -> 1 ReLU MLP with bfloat16 weights and float32 accumulation predicting the log
  * distance of the 48th nearest gas neighbour (a full search starts at 1.06 times it)
  * from (log cell density, log previous h, leaf count, velocity divergence), standardised by
- * gf_mlp_set_norm. Parameters: flat float32 vector of 4545 values, W1 (64x4), b1, W2 (64x64),
+ * gf_mlp_set_norm; a particle without a previous h enters with the h its cell density implies
+ * and a divergence of 0. Parameters: flat float32 vector of 4545 values, W1 (64x4), b1, W2 (64x64),
  * b2, w3 (64), b3. */
 int gf_mlp_init(int seed);
 int gf_mlp_set_params(const float* params);
