@@ -543,7 +543,8 @@ class Gpu:
 
 
 # Algorithmic bytes of the HBM-bound passes (the per-unit figures of the scope table's
-# measurement row): the radix sort moves 12 B (key + index) in and out per digit pass; node
+# measurement row): the radix sort reads the 8 B keys once for its digit counts and moves 12 B
+# (key + index) in and out per digit pass; node
 # emission reads the 8 B sorted key per particle and writes a 64 B node; the moments pass reads
 # a 16 B float32 particle record and reads + writes 64 B per node; the SPH passes per gas
 # particle with float32 storage (int32 neighbour rows): density 152 B, force 188 B, and with the
@@ -553,7 +554,7 @@ SORT_PASSES = 8
 
 def pass_bytes(stage, n, n_gas, nodes, sph32):
     if stage == "tree_sort":
-        return 2 * 12 * SORT_PASSES * n
+        return 8 * n + 2 * 12 * SORT_PASSES * n
     if stage == "tree_emit":
         return 8 * n + 64 * nodes
     if stage == "tree_moments":

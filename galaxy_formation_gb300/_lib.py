@@ -100,6 +100,7 @@ SIGNATURES = {
 # status bits (include/gfgpu.h)
 GF_ERR_CUDA, GF_ERR_ARG, GF_ERR_NONFINITE, GF_ERR_WALK_STACK = 1, 2, 4, 8
 GF_ERR_DEEP_CELL, GF_ERR_KNN, GF_ERR_NO_DEVICE, GF_ERR_CAPACITY = 16, 32, 64, 128
+GF_ERR_TIMEOUT = 256
 
 OPT_SPH_FLOAT32 = 0
 OPT_GRAVITY_QUAD = 1

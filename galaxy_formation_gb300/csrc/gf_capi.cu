@@ -612,7 +612,7 @@ int gf_set_option(int key, double value) {
                 break;
             }
             case GF_OPT_WALK_CHUNK:
-                require(value >= 0 && value <= 64, "walk chunk is 0..64");
+                require(value >= 0 && value <= kChunkCodeMax, "walk chunk is 0..96");
                 F.walk_chunk = int(value);
                 break;
             case GF_OPT_WALK_GROUP:
@@ -700,8 +700,9 @@ int gf_sim_block_config(const int* chunk, int nbins, int rebuild_every) {
         require(rebuild_every >= 0, "rebuild_every < 0");
         if (chunk)
             for (int b = 0; b < nbins; ++b)
-                require((chunk[b] >= 0 && chunk[b] <= 64) || (chunk[b] >= 100 && chunk[b] <= 164),
-                        "chunk out of [0, 64] (+100)");
+                require(chunk[b] >= 0 && chunk[b] % 100 <= kChunkCodeMax && chunk[b] % 1000 < 200 &&
+                            chunk[b] / 1000 < kNumWalkShapes,
+                        "chunk out of [0, 96] (+100, + 1000 x shape)");
         block_config(chunk, nbins, rebuild_every);
     });
 }

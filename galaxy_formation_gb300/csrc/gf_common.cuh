@@ -169,6 +169,14 @@ struct KahanF {
     }
 };
 
+// atomicAdd with acquire-release semantics at GPU scope (bottom-up tree passes: the last
+// arriving child sees its siblings' records without separate fences)
+__device__ __forceinline__ int atom_add_acq_rel(int* p, int v) {
+    int old;
+    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
 __device__ __forceinline__ void raise_status(uint32_t* st, uint32_t bit) {
     if (st) atomicOr(st, bit);
 }

@@ -1,13 +1,16 @@
 // gf_core.cu — library context, status handling, device-wide scan and radix sort.
 //
-// Radix sort: stable LSD sort of (uint64 key, int32 value) pairs, 8-bit digits. Per digit:
-//   upsweep   per-tile digit histograms (warp-aggregated shared-memory atomics),
-//   rows      one block per digit scans that digit's row of the table [256][tiles] in place
-//             and writes the digit's total,
-//   downsweep stable in-tile ranks (__match_any_sync per warp, warp-ordered tiles) and
-//             scatter to (exclusive scan of the 256 totals) + the tile's row entry.
-// Tiles are 1024 keys (256 threads x 4). Traffic per pass: 8 B read (upsweep) + 12 B read
-// + 12 B write (downsweep) per pair.
+// Radix sort: stable LSD sort of (uint64 key, int32 value) pairs, 8-bit digits, one sweep
+// per digit (the single-pass scheme of Adinets & Merrill, "Onesweep", 2022):
+//   histogram  one launch reads the keys once and counts the digits of every pass,
+//   pass       one launch per digit: each block takes the next tile by ticket, ranks its keys
+//              stably (__match_any_sync per warp, warps in key order), publishes its digit
+//              counts, adds up the counts of the tiles before it by decoupled look-back (a
+//              tile's flag says whether its value is its own count or the inclusive prefix;
+//              waits are bounded, GF_ERR_TIMEOUT past the bound) and scatters each key to
+//              (keys of smaller digits) + (its digit in earlier tiles) + its rank.
+// Tiles are 2048 keys (256 threads x 8). Traffic per pass: 12 B read + 12 B write per pair,
+// plus 8 B per pair once for the histogram.
 #include <cstdarg>
 #include <algorithm>
 #include <cstring>
@@ -243,81 +246,73 @@ void exclusive_scan(const int* in, int* out, int n, int* total, cudaStream_t s, 
 
 constexpr int kRsThreads = 256;
 constexpr int kRsWarps = kRsThreads / 32;
-constexpr int kRsItems = 4;                   // per thread (more blocks: 0.5 % faster evaluations than 16)
-constexpr int kRsWarpItems = 32 * kRsItems;   // 128 consecutive keys per warp
-constexpr int kRsTile = kRsThreads * kRsItems;
+// --- one sweep per digit --------------------------------------------------------------------
 
-__global__ void __launch_bounds__(kRsThreads) k_rs_upsweep(const uint64_t* __restrict__ keys, int n,
-                                                           int shift, int* __restrict__ hist,
-                                                           int tiles) {
-    __shared__ int h[256];
-    h[threadIdx.x] = 0;
-    __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int base = blockIdx.x * kRsTile + warp * kRsWarpItems;
-#pragma unroll 4
-    for (int s = 0; s < kRsItems; ++s) {
-        const int i = base + s * 32 + lane;
-        const bool ok = i < n;
-        const unsigned d = ok ? unsigned((keys[i] >> shift) & 255u) : 256u;
-        const unsigned peers = __match_any_sync(0xffffffffu, d);
-        if (ok && lane == __ffs(peers) - 1) atomicAdd(&h[d], __popc(peers));
-    }
-    __syncthreads();
-    hist[threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
+constexpr int kOsItems = 8;                   // keys per thread
+constexpr int kOsWarpItems = 32 * kOsItems;   // consecutive keys per warp
+constexpr int kOsTile = kRsThreads * kOsItems;
+constexpr int kOsMaxPasses = 8;
+constexpr unsigned kOsAgg = 1u << 30;         // look-back flags: the tile's own count,
+constexpr unsigned kOsInc = 2u << 30;         // or the inclusive prefix up to the tile
+constexpr unsigned kOsValue = (1u << 30) - 1;
+constexpr long kOsSpinMax = 1l << 20;         // bounded waits (a waited-on tile is always running)
+constexpr int kOsWindow = 16;                 // look-back statuses loaded at a time
+
+__device__ __forceinline__ unsigned ld_relaxed(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed(unsigned* p, unsigned v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Block d scans digit d's per-tile counts (row d of the digit-major histogram) in place,
-// exclusively, and writes the digit's total to tot[d]: one launch instead of a device-wide
-// scan of the whole histogram (three launches), since the digit bases come from the 256 totals.
-__global__ void __launch_bounds__(kRsThreads) k_rs_rows(int* __restrict__ hist, int tiles, int* __restrict__ tot) {
-    __shared__ int s_warp[33];
-    int* row = hist + size_t(blockIdx.x) * tiles;
-    int carry = 0;
-    for (int base = 0; base < tiles; base += kRsThreads * kScanItems) {
-        int v[kScanItems];
-        int acc = 0;
-        const int b0 = base + threadIdx.x * kScanItems;
-#pragma unroll
-        for (int k = 0; k < kScanItems; ++k) {
-            v[k] = (b0 + k < tiles) ? row[b0 + k] : 0;
-            acc += v[k];
-        }
-        int t;
-        int ex = block_excl_scan(acc, s_warp, &t) + carry;
-#pragma unroll
-        for (int k = 0; k < kScanItems; ++k) {
-            if (b0 + k < tiles) row[b0 + k] = ex;
-            ex += v[k];
-        }
-        carry += t;
+// Digit counts of every pass: hist[p * 256 + d] (hist zeroed by the caller).
+__global__ void __launch_bounds__(kRsThreads) k_os_hist(const uint64_t* __restrict__ keys, int n, int bit_lo,
+                                                        int npass, int* __restrict__ hist) {
+    __shared__ int h[kOsMaxPasses * 256];
+    for (int i = threadIdx.x; i < npass * 256; i += kRsThreads) h[i] = 0;
+    __syncthreads();
+    for (int i = blockIdx.x * kRsThreads + threadIdx.x; i < n; i += gridDim.x * kRsThreads) {
+        const uint64_t k = keys[i];
+        for (int p = 0; p < npass; ++p) atomicAdd(&h[p * 256 + int((k >> (bit_lo + 8 * p)) & 255u)], 1);
     }
-    if (threadIdx.x == 0) tot[blockIdx.x] = carry;
+    __syncthreads();
+    for (int i = threadIdx.x; i < npass * 256; i += kRsThreads)
+        if (h[i]) atomicAdd(&hist[i], h[i]);
 }
 
-__global__ void __launch_bounds__(kRsThreads) k_rs_downsweep(
+// One pass: tiles in ticket order; status[tile * 256 + d] holds the flag and value of digit d.
+__global__ void __launch_bounds__(kRsThreads) k_os_pass(
     const uint64_t* __restrict__ kin, const int* __restrict__ vin, uint64_t* __restrict__ kout,
-    int* __restrict__ vout, int n, int shift, const int* __restrict__ offs, const int* __restrict__ tot,
-    int tiles) {
+    int* __restrict__ vout, int n, int shift, const int* __restrict__ tot, unsigned* __restrict__ status,
+    int* __restrict__ ticket, uint32_t* __restrict__ err) {
     __shared__ int s_cnt[kRsWarps][256];
-    __shared__ int s_off[256];
+    __shared__ int s_base[256];
     __shared__ int s_warp[33];
+    __shared__ int s_tile;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1);
     for (int w = 0; w < kRsWarps; ++w) s_cnt[w][threadIdx.x] = 0;
-    // output base of this tile's digit t: keys of smaller digits + digit t in earlier tiles
-    s_off[threadIdx.x] = block_excl_scan(tot[threadIdx.x], s_warp, nullptr) + offs[threadIdx.x * tiles + blockIdx.x];
-    __syncthreads();
-    const int base = blockIdx.x * kRsTile + warp * kRsWarpItems;
-    uint64_t k[kRsItems];
-    int v[kRsItems];
-    int rank[kRsItems];
+    // keys of smaller digits (the pass's digit totals, scanned)
+    const int gbase = block_excl_scan(tot[threadIdx.x], s_warp, nullptr);  // synchronises
+    const int tile = s_tile;
+    const int base = tile * kOsTile + warp * kOsWarpItems;
+    uint64_t k[kOsItems];
+    int v[kOsItems];
+    int rank[kOsItems];
     const unsigned lt = lanemask_lt();
 #pragma unroll
-    for (int s = 0; s < kRsItems; ++s) {
+    for (int s = 0; s < kOsItems; ++s) {
         const int i = base + s * 32 + lane;
         const bool ok = i < n;
         k[s] = ok ? kin[i] : 0ull;
         v[s] = ok ? vin[i] : 0;
+    }
+#pragma unroll
+    for (int s = 0; s < kOsItems; ++s) {
+        const int i = base + s * 32 + lane;
+        const bool ok = i < n;
         const unsigned d = ok ? unsigned((k[s] >> shift) & 255u) : 256u;
         const unsigned peers = __match_any_sync(0xffffffffu, d);
         const int before = ok ? s_cnt[warp][d] : 0;
@@ -327,57 +322,101 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_downsweep(
         __syncwarp();
     }
     __syncthreads();
-    {   // exclusive prefix over warps, per digit (thread t owns digit t)
-        int run = 0;
-        for (int w = 0; w < kRsWarps; ++w) {
-            const int c = s_cnt[w][threadIdx.x];
-            s_cnt[w][threadIdx.x] = run;
-            run += c;
-        }
+    // thread d: the tile's count of digit d, and the exclusive prefix over warps
+    const int d = threadIdx.x;
+    int run = 0;
+    for (int w = 0; w < kRsWarps; ++w) {
+        const int c = s_cnt[w][d];
+        s_cnt[w][d] = run;
+        run += c;
     }
+    unsigned* my = status + size_t(tile) * 256 + d;
+    int excl = 0;
+    if (tile == 0) {
+        st_relaxed(my, kOsInc | unsigned(run));
+    } else {
+        st_relaxed(my, kOsAgg | unsigned(run));
+        // look back over the tiles before this one until an inclusive prefix, kOsWindow
+        // statuses loaded at a time (a tile before 0 counts as an inclusive 0); a tile not
+        // ready yet is polled again (bounded)
+        int j = tile - 1;
+        long polls = 0;
+        for (;;) {
+            unsigned w[kOsWindow];
+#pragma unroll
+            for (int u = 0; u < kOsWindow; ++u) w[u] = j - u >= 0 ? ld_relaxed(status + size_t(j - u) * 256 + d) : kOsInc;
+            int u = 0;
+            bool done = false;
+#pragma unroll
+            for (int t = 0; t < kOsWindow; ++t) {
+                if (done || u < t) continue;  // stopped at an inclusive or a tile not ready
+                if ((w[t] & ~kOsValue) == 0u) continue;
+                excl += int(w[t] & kOsValue);
+                if (w[t] & kOsInc) done = true;
+                u = t + 1;
+            }
+            if (done) break;
+            j -= u;
+            if (u == 0 && ++polls >= kOsSpinMax) {  // gave up: flag it and stop (output invalid)
+                raise_status(err, GF_ERR_TIMEOUT);
+                break;
+            }
+        }
+        st_relaxed(my, kOsInc | unsigned(excl + run));
+    }
+    s_base[d] = gbase + excl;
     __syncthreads();
 #pragma unroll
-    for (int s = 0; s < kRsItems; ++s) {
+    for (int s = 0; s < kOsItems; ++s) {
         const int i = base + s * 32 + lane;
         if (i < n) {
-            const unsigned d = unsigned((k[s] >> shift) & 255u);
-            const int pos = s_off[d] + s_cnt[warp][d] + rank[s];
+            const unsigned dg = unsigned((k[s] >> shift) & 255u);
+            const int pos = s_base[dg] + s_cnt[warp][dg] + rank[s];
             kout[pos] = k[s];
             vout[pos] = v[s];
         }
     }
 }
 
+// Scratch of a one-sweep sort of n pairs: digit totals [8][256], tickets [8], tile status
+// [8][tiles][256].
+size_t os_scratch_ints(int n) {
+    const size_t tiles = size_t(div_up(std::max(n, 1), kOsTile));
+    return size_t(kOsMaxPasses) * 256 + 64 + size_t(kOsMaxPasses) * tiles * 256;
+}
+
 void reserve_scan_sort(int n, ScanScratch* sc) {
     DevBuf& sort_tmp = sc ? sc->sort_tmp : g_ctx.sort_tmp;
     DevBuf& scan_tmp = sc ? sc->scan_tmp : g_ctx.scan_tmp;
-    const int rs_tiles = div_up(std::max(n, 1), kRsTile);
-    sort_tmp.get<int>(size_t(256) * rs_tiles + 256);
-    const int scan_n = std::max(n, 256 * rs_tiles);
-    scan_tmp.get<int>(size_t(div_up(scan_n, kScanTile)) + 1);
+    sort_tmp.get<int>(os_scratch_ints(n));
+    scan_tmp.get<int>(size_t(div_up(std::max(n, 1), kScanTile)) + 1);
 }
 
 void radix_sort_pairs(uint64_t* keys, int* vals, uint64_t* keys_alt, int* vals_alt, int n,
                       int bit_lo, int bit_hi, cudaStream_t s, ScanScratch* sc) {
     if (n <= 1) return;
-    const int tiles = div_up(n, kRsTile);
-    int* hist = (sc ? sc->sort_tmp : g_ctx.sort_tmp).get<int>(size_t(256) * tiles + 256);
-    int* tot = hist + size_t(256) * tiles;
+    if (n > int(kOsValue)) throw Error(GF_ERR_CAPACITY, "radix sort of more than 2^30 - 1 keys");
+    const int npass = div_up(bit_hi - bit_lo, 8);
+    if (npass < 1 || npass > kOsMaxPasses) throw Error(GF_ERR_ARG, "radix sort bit range");
+    const int tiles = div_up(n, kOsTile);
+    int* hist = (sc ? sc->sort_tmp : g_ctx.sort_tmp).get<int>(os_scratch_ints(n));
+    int* tickets = hist + kOsMaxPasses * 256;
+    unsigned* status = reinterpret_cast<unsigned*>(tickets + 64);
+    const size_t zero = size_t(kOsMaxPasses) * 256 + 64 + size_t(npass) * tiles * 256;
+    GF_CUDA(cudaMemsetAsync(hist, 0, sizeof(int) * zero, s));
+    const int hblocks = std::min(div_up(n, kRsThreads * 8), 2 * g_ctx.sms);
+    k_os_hist<<<hblocks, kRsThreads, 0, s>>>(keys, n, bit_lo, npass, hist);
+    GF_CHECK_LAUNCH();
     uint64_t *ka = keys, *kb = keys_alt;
     int *va = vals, *vb = vals_alt;
-    int passes = 0;
-    for (int shift = bit_lo; shift < bit_hi; shift += 8) {
-        k_rs_upsweep<<<tiles, kRsThreads, 0, s>>>(ka, n, shift, hist, tiles);
-        GF_CHECK_LAUNCH();
-        k_rs_rows<<<256, kRsThreads, 0, s>>>(hist, tiles, tot);
-        GF_CHECK_LAUNCH();
-        k_rs_downsweep<<<tiles, kRsThreads, 0, s>>>(ka, va, kb, vb, n, shift, hist, tot, tiles);
+    for (int p = 0; p < npass; ++p) {
+        k_os_pass<<<tiles, kRsThreads, 0, s>>>(ka, va, kb, vb, n, bit_lo + 8 * p, hist + 256 * p,
+                                               status + size_t(p) * tiles * 256, tickets + p, g_ctx.d_status);
         GF_CHECK_LAUNCH();
         std::swap(ka, kb);
         std::swap(va, vb);
-        ++passes;
     }
-    if (passes & 1) {
+    if (npass & 1) {
         GF_CUDA(cudaMemcpyAsync(keys, ka, sizeof(uint64_t) * n, cudaMemcpyDeviceToDevice, s));
         GF_CUDA(cudaMemcpyAsync(vals, va, sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
     }

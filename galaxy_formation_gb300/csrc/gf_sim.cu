@@ -287,7 +287,7 @@ __global__ void k_active_at(int n, const int8_t* __restrict__ level, int s, uint
 // Launch shape of the batched step, per sub-step bin (bin = number of trailing zero bits of
 // the sub-step index: levels 0..bin are due). Chosen by BlockIntegrator::autotune.
 struct BlockTuning {
-    int chunk[8] = {4, 8, 8, 16, 16, 32, 64, 64};  // walk items of <= chunk active particles (0: groups)
+    int chunk[8] = {4, 8, 8, 16, 16, 32, 64, 64};  // walk item code per bin (Octree::prepare_walk)
     int npl[8] = {8, 8, 8, 2, 2, 2, 2, 2};         // mixed walk: nodes per lane and round (2 or 8)
     int shape[8] = {0, 0, 0, 0, 0, 0, 0, 0};       // mixed walk with 2 per lane: launch shape
     int rebuild_every = 8;  // captured tree rebuild every this many sub-steps (0: refit only)
@@ -489,7 +489,9 @@ struct BlockIntegrator {
             Octree& T = F.grav;
             double* ta = tune_acc.get<double>(n3);
             unsigned long long* d = scal.as<unsigned long long>();
-            static const int cand[] = {0, 2, 4, 8, 16, 32, 64};
+            // chunks of one group's active particles, then sibling-group runs merged by active
+            // count (codes 72, 80, 84, 96: <= 16, 32, 40, 64 active particles per item)
+            static const int cand[] = {0, 2, 4, 8, 16, 32, 64, 72, 80, 84, 96};
             Event e0, e1;
             for (int bin = 0; bin < nlev - 1; ++bin) {
                 k_active_at<<<div_up(S.n, 256), 256, 0, s>>>(S.n, level.as<int8_t>(), 1 << bin, act.as<uint8_t>(),

@@ -74,6 +74,9 @@ __global__ void k_sph32_density(int n, int k, int ld, const Idx* __restrict__ nb
     const float4 ai = A[i], bi = B[i];
     const float inv_h = 1.f / ai.w;
     Kahan s;
+    // unrolled: the neighbours' loads of several iterations are in flight together (the sums
+    // keep their order)
+#pragma unroll 8
     for (int jj = 0; jj < k; ++jj) {
         const int j = int(nb[size_t(i) * ld + jj]);
         const float4 aj = A[j], bj = B[j];
@@ -104,6 +107,7 @@ __global__ void k_sph32_force(int n, int k, int ld, const Idx* __restrict__ nb, 
     const float s4i = ih2 * ih2 * kInvPi;
     Kahan ax, ay, az, du, dv;
     float mu_max = 0.f;
+#pragma unroll 4
     for (int jj = 0; jj < k; ++jj) {
         const int j = int(nb[size_t(i) * ld + jj]);
         if (j == i) continue;

@@ -613,14 +613,16 @@ __global__ void k_refit_bfs_quad32(RefitBfsArgs A) {
         A.wq[b] = make_float4(S.xx.s, S.yy.s, S.xy.s, S.xz.s);
         A.wt[b] = make_float2(S.yz.s, S.tr.s);
     }
-    __threadfence();
+    // Climb: the arrival counter is an acquire-release atomic (it publishes this node's records
+    // and, for the last child, makes its siblings' records visible), issued together with the
+    // loads of the parent's child range and of the next parent.
     int p = A.wparent[b];
     while (p >= 0) {
-        const float4 pb = A.wb[p];
-        const int c0 = __float_as_int(pb.y), nc = __float_as_int(pb.z);
-        const int arrived = atomicAdd(&A.counter[p], 1);
+        const int* pbi = reinterpret_cast<const int*>(A.wb) + 4 * size_t(p);
+        const int c0 = __ldg(pbi + 1), nc = __ldg(pbi + 2);  // structure fields: constant here
+        const int pnext = A.wparent[p];
+        const int arrived = atom_add_acq_rel(&A.counter[p], 1);
         if (arrived != nc - 1) return;
-        __threadfence();
         float4 cm[8];
         float dmc[8];
 #pragma unroll
@@ -660,8 +662,7 @@ __global__ void k_refit_bfs_quad32(RefitBfsArgs A) {
         }
         A.wq[p] = make_float4(S.xx.s, S.yy.s, S.xy.s, S.xz.s);
         A.wt[p] = make_float2(S.yz.s, S.tr.s);
-        __threadfence();
-        p = A.wparent[p];
+        p = pnext;
     }
 }
 
@@ -848,6 +849,7 @@ void Octree::reserve_graph_build() {
     work.get<int4>(std::max(size_t(node_cap), size_t(n)) + 1);
     sphere.get<float4>(std::max(size_t(node_cap), size_t(n)) + 1);
     if (quad) item_gam.get<float2>(std::max(size_t(node_cap), size_t(n)) + 1);
+    gweight.get<int>(std::max(node_cap, 1));
     reserve_scan_sort(std::max(n, node_cap), &scratch);
     deep_sort_attr();
 }

@@ -80,8 +80,9 @@ struct Octree {
     int leaf_max = kLeafMax;     // leaf capacity (the reference's 8 for gravity trees)
     bool quad = false;           // also build quadrupole moments (mixed-precision form)
     bool kahan = false;          // walk: compensated accumulation of the tile sums
-    // groups and walk work list
-    DevBuf gflag, gscan, groups, work, sphere;
+    // groups and walk work list (gweight: active particles per group, for items merged by
+    // active count)
+    DevBuf gflag, gscan, groups, work, sphere, gweight;
     DevBuf item_gam;  // per work item: float2 {(alpha a_min)^(-1/5), (alpha_q a_min)^(-1/4)}, 0 = off
     int walk_stride = 1;  // regions of the work list the walk takes at a time (prepare_walk sets it)
     DevBuf root, counts;
@@ -105,8 +106,11 @@ struct Octree {
     void deep_sort_attr();
     // Node kernels read the live node count on the device (valid after captured rebuilds).
     void refit(const double* pos, const double* mass, cudaStream_t s);
-    // Work list of groups with at least one active particle (active may be null); chunk > 0
-    // cuts each group's active particles into items of <= chunk with their own spheres.
+    // Work list of groups with at least one active particle (active may be null); chunk in
+    // 1..kChunkMax cuts each group's active particles into items of <= chunk with their own
+    // spheres; chunk in kChunkMax+1..kChunkCodeMax (active sets) merges runs of sibling groups
+    // into items of <= merged_active_cap(chunk) active particles, each with the bounding
+    // sphere of its active particles.
     // aold (quadrupole trees, may be null): the previous accelerations (n,3) in original order,
     // for the relative opening criterion with tolerance alpha.
     // alpha_q > 0: accepted nodes whose quadrupole term is below alpha_q a_min are taken as
@@ -118,6 +122,12 @@ struct Octree {
     // shape: launch shape of the mixed walk with npl 2 (kNumWalkShapes)
     void walk(double eps, double* acc, cudaStream_t s, double* pot = nullptr, int npl = 2, int shape = 0);
 };
+
+// Walk item codes (prepare_walk's chunk): 1..kChunkMax chunks of one group's active particles,
+// kChunkMax+1..kChunkCodeMax sibling-group runs merged by active count.
+constexpr int kChunkMax = 64;
+constexpr int kChunkCodeMax = 96;
+__host__ __device__ inline int merged_active_cap(int chunk) { return 2 * (chunk - kChunkMax); }
 
 Octree& gravity_tree();
 // The tree walked most recently (for the pair counter).

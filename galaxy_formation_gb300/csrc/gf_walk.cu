@@ -71,9 +71,12 @@ struct ItemStats {
     bool valid;
 };
 
+// act_sphere: the sphere bounds the active particles (the item's targets) instead of the massive
+// ones (items merged by active count, whose inactive members are not evaluated).
 __device__ __forceinline__ ItemStats item_stats(int b, int e, const float4* __restrict__ p4,
                                                 const int* __restrict__ perm, const uint8_t* __restrict__ active,
-                                                const double* __restrict__ aold, float alpha, float alpha_q) {
+                                                const double* __restrict__ aold, float alpha, float alpha_q,
+                                                bool act_sphere = false) {
     const int lane = threadIdx.x & 31;
     ItemStats st;
     st.valid = false;
@@ -85,7 +88,7 @@ __device__ __forceinline__ ItemStats item_stats(int b, int e, const float4* __re
         nact += __popc(__ballot_sync(__activemask(), a));
         if (aold && a) amin = fminf(amin, aold_mag(aold, perm[i]));
         const float4 p = p4[i];
-        if (p.w > 0) {
+        if (act_sphere ? a : p.w > 0) {
             x0 = fminf(x0, p.x); x1 = fmaxf(x1, p.x);
             y0 = fminf(y0, p.y); y1 = fmaxf(y1, p.y);
             z0 = fminf(z0, p.z); z1 = fmaxf(z1, p.z);
@@ -100,14 +103,15 @@ __device__ __forceinline__ ItemStats item_stats(int b, int e, const float4* __re
     float br2 = 0.f;
     for (int i = b + lane; i < e; i += 32) {
         const float4 p = p4[i];
-        if (p.w > 0) {
+        if (act_sphere ? active[perm[i]] != 0 : p.w > 0) {
             const float dx = p.x - bx, dy = p.y - by, dz = p.z - bz;
             br2 = fmaxf(br2, dx * dx + dy * dy + dz * dz);
         }
     }
     br2 = warp_max(br2);
     amin = warp_min(amin);
-    st.sph = make_float4(bx, by, bz, sqrtf(br2));
+    // float32 rounding of the centre: pad so every target stays inside
+    st.sph = make_float4(bx, by, bz, act_sphere ? sqrtf(br2) * (1.f + 1e-6f) : sqrtf(br2));
     st.gam = aold ? rel_gamma(alpha, alpha_q, amin) : make_float2(0.f, 0.f);
     st.valid = true;
     return st;
@@ -132,22 +136,25 @@ __device__ __forceinline__ void emit_item(int b, int e, const float4* __restrict
     }
 }
 
-// Mixed form, merged items: each run of consecutive sibling groups (contiguous in tree order)
-// is cut greedily into items of at most `merge` particles (a larger group alone). A run holds
-// at most 8 groups, so lanes 0..15 load groups g-8 .. g+7; the warp finds the run around group
-// g and replays the cut from the run's first group. Returns the particle count of the item
-// that g starts (-1 if g starts none) and, in b, g's first particle.
+// Merged items: each run of consecutive sibling groups (contiguous in tree order) is cut
+// greedily into items of at most `merge` weight (a heavier group alone); the weight of a group
+// is its particle count, or gw[g] where given (its active particles). A run holds at most 8
+// groups (the octree fan-out), so lanes 0..15 load groups g-8 .. g+7; the warp finds the run
+// around group g and replays the cut from the run's first group. Returns the weight of the item
+// that g starts (-1 if g starts none) and, in b and len, its first particle and particle count.
 __device__ __forceinline__ int cut_at(const int* __restrict__ groups, const int4* __restrict__ n_i4,
-                                      const int* __restrict__ parent, int ng, int merge, int g, int& b) {
+                                      const int* __restrict__ parent, const int* __restrict__ gw, int ng,
+                                      int merge, int g, int& b, int& len) {
     const int lane = threadIdx.x & 31;
     const int idx = g - 8 + lane;
-    int pg = -2, cg = 0, bg = 0;
+    int pg = -2, cg = 0, bg = 0, wg = 0;
     if (lane < 16 && idx >= 0 && idx < ng) {
         const int nd = groups[idx];
         const int4 q = n_i4[nd];
         pg = parent[nd];
         cg = q.y;
         bg = q.x;
+        wg = gw ? gw[idx] : q.y;
     }
     const int par = __shfl_sync(0xffffffffu, pg, 8);
     b = __shfl_sync(0xffffffffu, bg, 8);
@@ -156,27 +163,55 @@ __device__ __forceinline__ int cut_at(const int* __restrict__ groups, const int4
     const unsigned above = ~same & 0xfe00u;   // lanes 9..15 outside the run
     const int first = below ? 32 - __clz(below) : 0;
     const int last = above ? __ffs(above) - 1 : 16;
-    int start = first, rc = 0, mine = -1;
+    int start = first, rw = 0, rl = 0, mine = -1;
+    len = 0;
     for (int l = first; l < last; ++l) {
+        const int w = __shfl_sync(0xffffffffu, wg, l);
         const int c = __shfl_sync(0xffffffffu, cg, l);
-        if (l > start && rc + c <= merge) {
-            rc += c;
+        if (l > start && rw + w <= merge) {
+            rw += w;
+            rl += c;
             continue;
         }
         if (l > start) {  // the item [start, l) closes
-            if (start == 8) mine = rc;
+            if (start == 8) {
+                mine = rw;
+                len = rl;
+            }
             start = l;
         }
-        rc = c;
+        rw = w;
+        rl = c;
     }
-    if (start == 8) mine = rc;  // the run's last item
+    if (start == 8) {  // the run's last item
+        mine = rw;
+        len = rl;
+    }
     return mine;
 }
 
-// flag[g] = 1 when group g starts a merged item (g < span; 0 past the live group count)
+// Active particles per group (items merged by active count).
+__global__ void k_group_nact(const int* __restrict__ groups, const int4* __restrict__ n_i4,
+                             const int* __restrict__ perm, const uint8_t* __restrict__ active,
+                             const TreeCounts* cnt, int* __restrict__ gw) {
+    const int lane = threadIdx.x & 31;
+    const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const int ng = cnt->num_groups;
+    for (int g = wid; g < ng; g += nw) {
+        const int4 q = n_i4[groups[g]];
+        int c = 0;
+        for (int i = q.x + lane; i < q.x + q.y; i += 32) c += active[perm[i]] != 0 ? 1 : 0;
+        c = warp_sum(c);
+        if (lane == 0) gw[g] = c;
+    }
+}
+
+// flag[g] = 1 when group g starts a merged item of positive weight (g < span; 0 past the live
+// group count)
 __global__ void k_item_flag(const int* __restrict__ groups, const int4* __restrict__ n_i4,
-                            const int* __restrict__ parent, const TreeCounts* cnt, int merge, int span,
-                            int* __restrict__ flag) {
+                            const int* __restrict__ parent, const int* __restrict__ gw, const TreeCounts* cnt,
+                            int merge, int span, int* __restrict__ flag) {
     const int lane = threadIdx.x & 31;
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -184,17 +219,19 @@ __global__ void k_item_flag(const int* __restrict__ groups, const int4* __restri
     for (int g = wid; g < span; g += nw) {
         int f = 0;
         if (g < ng) {
-            int b;
-            f = cut_at(groups, n_i4, parent, ng, merge, g, b) > 0 ? 1 : 0;
+            int b, len;
+            f = cut_at(groups, n_i4, parent, gw, ng, merge, g, b, len) > 0 ? 1 : 0;
         }
         if (lane == 0) flag[g] = f;
     }
 }
 
 // The merged items in tree order: item of group g at slot[g] (the scan of the flags). An item
-// without active or massive particles keeps its slot with no particles to evaluate.
+// without active or massive particles keeps its slot with no particles to evaluate. With gw
+// (merged by active count) the sphere bounds the item's active particles.
 __global__ void k_item_fill(const int* __restrict__ groups, const int4* __restrict__ n_i4,
-                            const int* __restrict__ parent, const TreeCounts* cnt, int merge,
+                            const int* __restrict__ parent, const int* __restrict__ gw, const TreeCounts* cnt,
+                            int merge,
                             const int* __restrict__ flag, const int* __restrict__ slot,
                             const float4* __restrict__ p4, const int* __restrict__ perm,
                             const uint8_t* __restrict__ active, const double* __restrict__ aold,
@@ -206,9 +243,9 @@ __global__ void k_item_fill(const int* __restrict__ groups, const int4* __restri
     const int ng = cnt->num_groups;
     for (int g = wid; g < ng; g += nw) {
         if (!flag[g]) continue;
-        int b;
-        const int count = cut_at(groups, n_i4, parent, ng, merge, g, b);
-        const ItemStats st = item_stats(b, b + count, p4, perm, active, aold, alpha, alpha_q);
+        int b, count;
+        cut_at(groups, n_i4, parent, gw, ng, merge, g, b, count);
+        const ItemStats st = item_stats(b, b + count, p4, perm, active, aold, alpha, alpha_q, gw != nullptr);
         if (lane == 0) {
             const int k = slot[g];
             work[k] = make_int4(b, count, st.valid ? st.nact : 0, 0);
@@ -780,21 +817,30 @@ void Octree::prepare_walk(const uint8_t* active, cudaStream_t s, int chunk, cons
     // items: one per group (<= nodes), or at most one per active particle with chunks
     const size_t cap = std::max(size_t(node_cap), size_t(n)) + 1;
     active_ptr = active;
-    if (quad && merge_cap > 0 && !(active && chunk > 0)) {
+    // chunk > kChunkMax (active sets): runs of sibling groups merged by active count
+    const bool by_active = active && chunk > kChunkMax;
+    if ((quad && merge_cap > 0 && !(active && chunk > 0)) || by_active) {
         // merged items in tree order (flag, scan, fill), walked 4 regions at a time: 2 % faster
         // per evaluation than the order of appending warps, 6 % faster than 1 region, 9 % than 8
         const int span = std::max(node_cap, 1);
         int* fl = gflag.get<int>(span);
         int* sl = gscan.get<int>(span);
         const int blocks = std::min(div_up(span, 8), 16 * C.sms);
-        k_item_flag<<<blocks, 256, 0, s>>>(groups.as<int>(), n_i4.as<int4>(), n_parent.as<int>(), cnt, merge_cap,
+        const int cap_w = by_active ? merged_active_cap(chunk) : merge_cap;
+        int* gw = nullptr;
+        if (by_active) {
+            gw = gweight.get<int>(span);
+            k_group_nact<<<blocks, 256, 0, s>>>(groups.as<int>(), n_i4.as<int4>(), perm.as<int>(), active, cnt, gw);
+            GF_CHECK_LAUNCH();
+        }
+        k_item_flag<<<blocks, 256, 0, s>>>(groups.as<int>(), n_i4.as<int4>(), n_parent.as<int>(), gw, cnt, cap_w,
                                            span, fl);
         GF_CHECK_LAUNCH();
         exclusive_scan(fl, sl, span, &cnt->num_work, s, &scratch);
-        k_item_fill<<<blocks, 256, 0, s>>>(groups.as<int>(), n_i4.as<int4>(), n_parent.as<int>(), cnt, merge_cap, fl,
+        k_item_fill<<<blocks, 256, 0, s>>>(groups.as<int>(), n_i4.as<int4>(), n_parent.as<int>(), gw, cnt, cap_w, fl,
                                            sl, p4.as<float4>(), perm.as<int>(), active,
                                            alpha > 0.f ? aold : nullptr, alpha, alpha_q, work.get<int4>(cap),
-                                           sphere.get<float4>(cap), item_gam.get<float2>(cap));
+                                           sphere.get<float4>(cap), quad ? item_gam.get<float2>(cap) : nullptr);
         GF_CHECK_LAUNCH();
         walk_stride = 4;
         return;

@@ -38,6 +38,7 @@ extern "C" {
 #define GF_ERR_KNN 32         /* neighbour search did not converge for some particles  */
 #define GF_ERR_NO_DEVICE 64   /* no CUDA device                                        */
 #define GF_ERR_CAPACITY 128   /* a fixed-capacity buffer was too small                 */
+#define GF_ERR_TIMEOUT 256    /* a bounded device-side wait gave up (results invalid)   */
 
 /* ---- drop-ins for cpp/nbody.cpp (signatures identical to the reference) ---------------- */
 
@@ -248,7 +249,9 @@ int gf_sim_blocks(int nblocks, int nlev, double* updates);
 /* Launch shape of gf_sim_blocks per sub-step bin (bin b = sub-steps whose index has b
  * trailing zero bits, i.e. levels 0..b due): chunk[b] = active particles per walk item
  * (0: the reference's walk groups with their spheres; 1..64: items of <= chunk[b] active
- * particles in tree order, each with its own bounding sphere), plus 100 to walk with 8 nodes
+ * particles of one group in tree order, each with its own bounding sphere; 65..96: runs of
+ * consecutive sibling groups merged into items of <= 2 (chunk[b] - 64) active particles, each
+ * with the bounding sphere of its active particles), plus 100 to walk with 8 nodes
  * per lane and round instead of 2 (mixed form; for bins of a few items, whose walks are bound
  * by the latency of their rounds), plus 1000 x s to walk with launch shape s
  * (GF_OPT_WALK_SHAPE, 2 per lane only); bins past nbins reuse chunk[nbins-1]; chunk NULL =
@@ -359,7 +362,9 @@ int gf_cool(int n, const double* u, const double* T, const double* rho, const do
  *                       active mask): 0 = the reference's groups and spheres (default);
  *                       1..64 = items of <= that many active particles in tree order, each
  *                       with the bounding sphere of its own particles (no reference
- *                       counterpart: same opening criterion per particle, tighter spheres). */
+ *                       counterpart: same opening criterion per particle, tighter spheres);
+ *                       65..96 = runs of sibling groups merged into items of <= 2 (value - 64)
+ *                       active particles, each with the sphere of its active particles. */
 #define GF_OPT_WALK_CHUNK 4
 /*   GF_OPT_WALK_GROUP   mixed form (GF_OPT_GRAVITY_QUAD = 1): walk groups are the shallowest
  *                       nodes holding <= this many particles, 8..128 (default 64, the

@@ -316,7 +316,51 @@ void walk_list(const Octree& T, float bx, float by, float bz, float br, Append&&
 // Walk items of <= chunk active particles (the library's GF_OPT_WALK_CHUNK; no reference
 // counterpart): a group's active particles in tree order are cut into items, each walked
 // with the bounding sphere (float32 box centre, radius padded by 1e-6) of its own particles.
+// Codes 65..96: runs of consecutive sibling groups (the same parent node) cut greedily into
+// items of <= 2 (code - 64) active particles (an item takes its first group whatever its
+// count), each walked with the sphere of its active particles; items without one are skipped.
 int g_walk_chunk = 0;
+constexpr int kChunkMax = 64;
+
+// [first, end) tree positions of the merged-by-active-count items of an active set.
+std::vector<std::pair<int, int>> merged_active_items(const Octree& T, const uint8_t* active, int cap) {
+    const Node* nd = T.nodes.data();
+    const int nn = int(T.nodes.size());
+    std::vector<int> par(nn, -1);
+    for (int k = 0; k < nn; ++k) {
+        if (nd[k].leaf) continue;
+        const int end = nd[k].next < 0 ? nn : nd[k].next;
+        for (int c = k + 1; c < end && c >= 0; c = nd[c].next) par[c] = k;
+    }
+    std::vector<std::pair<int, int>> items;
+    const int ng = int(T.groups.size());
+    for (int g = 0; g < ng;) {
+        int e = g + 1;  // the run of groups with g's parent
+        while (e < ng && par[T.groups[e]] == par[T.groups[g]]) ++e;
+        int start = g, w = 0;
+        auto close = [&](int from, int to, int weight) {
+            if (weight > 0) items.emplace_back(nd[T.groups[from]].start, nd[T.groups[to - 1]].start +
+                                                                              nd[T.groups[to - 1]].count);
+        };
+        for (int l = g; l < e; ++l) {
+            const Node& G = nd[T.groups[l]];
+            int c = 0;
+            for (int i = G.start; i < G.start + G.count; ++i) c += active[T.order[i]] ? 1 : 0;
+            if (l > start && w + c <= cap) {
+                w += c;
+                continue;
+            }
+            if (l > start) {
+                close(start, l, w);
+                start = l;
+            }
+            w = c;
+        }
+        close(start, e, w);
+        g = e;
+    }
+    return items;
+}
 
 // Group walk + list evaluation (cpp/nbody.cpp:323-411).
 void accel(Octree& T, double* acc, double eps, const uint8_t* active) {
@@ -327,6 +371,10 @@ void accel(Octree& T, double* acc, double eps, const uint8_t* active) {
     const float* py = T.fy.data();
     const float* pz = T.fz.data();
     const float* pm = T.fm.data();
+    const bool merged = active && g_walk_chunk > kChunkMax;
+    const std::vector<std::pair<int, int>> items =
+        merged ? merged_active_items(T, active, 2 * (g_walk_chunk - kChunkMax)) : std::vector<std::pair<int, int>>();
+    const int nitems = int(items.size());
 #pragma omp parallel
     {
         std::vector<float> lx(8192), ly(8192), lz(8192), lm(8192);
@@ -363,6 +411,30 @@ void accel(Octree& T, double* acc, double eps, const uint8_t* active) {
             acc[3 * k + 1] = sy;
             acc[3 * k + 2] = sz;
         };
+        if (merged) {
+#pragma omp for schedule(dynamic, 4)
+            for (int it = 0; it < nitems; ++it) {
+                const int b = items[it].first, e = items[it].second;
+                float x0 = 1e30f, y0 = 1e30f, z0 = 1e30f, x1 = -1e30f, y1 = -1e30f, z1 = -1e30f;
+                for (int i = b; i < e; ++i) {
+                    if (!active[T.order[i]]) continue;
+                    x0 = std::min(x0, px[i]); x1 = std::max(x1, px[i]);
+                    y0 = std::min(y0, py[i]); y1 = std::max(y1, py[i]);
+                    z0 = std::min(z0, pz[i]); z1 = std::max(z1, pz[i]);
+                }
+                const float bx = 0.5f * (x0 + x1), by = 0.5f * (y0 + y1), bz = 0.5f * (z0 + z1);
+                float br2 = 0;
+                for (int i = b; i < e; ++i) {
+                    if (!active[T.order[i]]) continue;
+                    const float dx = px[i] - bx, dy = py[i] - by, dz = pz[i] - bz;
+                    br2 = std::max(br2, dx * dx + dy * dy + dz * dz);
+                }
+                len = 0;
+                walk_list(T, bx, by, bz, std::sqrt(br2) * (1.f + 1e-6f), append);
+                for (int i = b; i < e; ++i)
+                    if (active[T.order[i]]) eval(i);
+            }
+        } else {
 #pragma omp for schedule(dynamic, 4)
         for (int g = 0; g < ng; ++g) {
             const Node& G = nd[T.groups[g]];
@@ -425,6 +497,7 @@ void accel(Octree& T, double* acc, double eps, const uint8_t* active) {
                 eval(p);
             }
         }
+        }  // groups
     }
 }
 
@@ -470,7 +543,7 @@ void orc_set_threads(int t) {
     if (t > 0) omp_set_num_threads(t);
 }
 
-void orc_set_walk_chunk(int c) { g_walk_chunk = c > 0 ? c : 0; }
+void orc_set_walk_chunk(int c) { g_walk_chunk = c > 0 ? c : 0; }  // codes as GF_OPT_WALK_CHUNK
 
 // Mirrors nbody_accel_active (cpp/nbody.cpp:422-425): a process-global tree, rebuilt when
 // asked or when n changes, refitted otherwise.

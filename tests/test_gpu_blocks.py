@@ -28,11 +28,12 @@ def _plain(lib):
         lib.gf_set_option(key, 0)
 
 
-@pytest.mark.parametrize("rebuild_every,chunk", [(0, None), (2, None), (2, [1, 4])])
+@pytest.mark.parametrize("rebuild_every,chunk", [(0, None), (2, None), (2, [1, 4]), (2, [4, 80])])
 def test_blocks_match_cpu_gravity_only(gpulib, oracle, rebuild_every, chunk):
     """Against the CPU restatement: the reference's walk groups with the tree refitted at
-    every sub-step; rebuilt inside the captured graph every other sub-step; and walk items of
-    a few active particles per bin."""
+    every sub-step; rebuilt inside the captured graph every other sub-step; walk items of a
+    few active particles per bin; and sibling groups merged into items of <= 32 active
+    particles (code 80) on the coarser bin."""
     from force_ref import BlockOracle
 
     from galaxy_formation_gb300 import _lib, params, synthetic
@@ -123,9 +124,11 @@ def test_blocks_with_gas_match_cpu(gpulib, oracle, rebuild_every, sph32):
 
 
 def test_chunked_walk_accuracy(gpulib, oracle):
-    """Walk items of a few active particles with their own spheres: the same interaction lists
-    as the CPU restatement of those items, and every particle still meets the opening
-    criterion, so the error against the float64 direct sum stays at the per-particle level."""
+    """Walk items of a few active particles with their own spheres (chunks of one group, or
+    sibling groups merged by active count: codes 72 and 96, <= 16 and <= 64 active particles):
+    the same interaction lists as the CPU restatement of those items, and every particle still
+    meets the opening criterion, so the error against the float64 direct sum stays at the
+    per-particle level."""
     from galaxy_formation_gb300 import _lib, params, synthetic
 
     lib = gpulib
@@ -137,7 +140,7 @@ def test_chunked_walk_accuracy(gpulib, oracle):
     idx = np.flatnonzero(active)
     ref = oracle.accel_direct_targets(d["pos"], d["mass"], idx, params.EPS)
     errs = {}
-    for chunk in (0, 1, 4, 16):
+    for chunk in (0, 1, 4, 16, 72, 96):
         lib.gf_set_option(_lib.OPT_WALK_CHUNK, chunk)
         acc = np.zeros((n, 3))
         lib.nbody_accel_active(n, d["pos"], d["mass"], acc, params.THETA, params.EPS, active, 1)
@@ -154,7 +157,7 @@ def test_chunked_walk_accuracy(gpulib, oracle):
         errs[chunk] = np.percentile(e, 99)
     lib.gf_set_option(_lib.OPT_WALK_CHUNK, 0)
     # items drop the group's extra margin: the error is the per-particle criterion's
-    for chunk in (1, 4, 16):
+    for chunk in (1, 4, 16, 72, 96):
         assert errs[chunk] <= 2.0 * errs[0], errs
 
 
