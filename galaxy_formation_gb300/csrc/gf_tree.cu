@@ -362,14 +362,16 @@ __device__ __forceinline__ int live_nodes(int span, const int* nn_dev) {
     return nn_dev ? min(span, *nn_dev) : span;
 }
 
+// Child count of every node and its children's ids in octant order (kids[8k .. 8k + nchild)),
+// so that the bottom-up passes load a node's children together.
 __global__ void k_nchild(int span, const int* __restrict__ nn_dev, const int4* __restrict__ n_i4,
-                         int* __restrict__ nchild, int* __restrict__ counter) {
+                         int* __restrict__ nchild, int* __restrict__ counter, int* __restrict__ kids) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= live_nodes(span, nn_dev)) return;
     const int4 q = n_i4[k];
     int c = 0;
     if (!(q.w & 1)) {
-        for (int ch = k + 1; ch < q.z && c <= 8; ch = n_i4[ch].z) ++c;  // <= 8 children
+        for (int ch = k + 1; ch < q.z && c < 8; ch = n_i4[ch].z) kids[8 * size_t(k) + c++] = ch;  // <= 8 children
     }
     nchild[k] = c;
     counter[k] = 0;
@@ -430,6 +432,7 @@ struct MomentArgs {
     const int4* n_i4;
     const int* parent;
     const int* nchild;
+    const int* kids;    // children in octant order, 8 slots per node
     int* counter;
     const double4* n_cd;  // build: float64 centre + half
     const float4* n_geo;  // refit: float32 centre + half
@@ -475,6 +478,38 @@ __global__ void k_moments(MomentArgs A) {
     if (!(q.w & 1)) return;
     double M = 0, sx = 0, sy = 0, sz = 0;
     float dm = 0.f;
+    if (q.y <= kLeafMax) {  // the leaf's particles loaded together, summed in order
+        double4 pm[kLeafMax];
+        float pd[kLeafMax];
+#pragma unroll
+        for (int t = 0; t < kLeafMax; ++t) {
+            pm[t] = make_double4(0.0, 0.0, 0.0, 0.0);
+            pd[t] = 0.f;
+            if (t < q.y) {
+                const int i = q.x + t;
+                if (!A.refit) {
+                    const int j = A.perm[i];
+                    pm[t] = make_double4(A.pos[3 * size_t(j)], A.pos[3 * size_t(j) + 1], A.pos[3 * size_t(j) + 2],
+                                         A.mass ? A.mass[j] : 1.0);
+                } else {
+                    const float4 p = A.p4[i];
+                    pm[t] = make_double4(double(p.x), double(p.y), double(p.z), double(p.w));
+                    pd[t] = A.pdisp[i];
+                }
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < kLeafMax; ++t) {
+            if (t < q.y) {  // cpp/nbody.cpp:124-131 (build), :285-289 (refit: float x float exact)
+                const double m = pm[t].w;
+                M = __dadd_rn(M, m);
+                sx = __dadd_rn(sx, __dmul_rn(m, pm[t].x));
+                sy = __dadd_rn(sy, __dmul_rn(m, pm[t].y));
+                sz = __dadd_rn(sz, __dmul_rn(m, pm[t].z));
+                dm = fmaxf(dm, pd[t]);
+            }
+        }
+    } else
     for (int i = q.x; i < q.x + q.y; ++i) {
         if (!A.refit) {  // cpp/nbody.cpp:124-131
             const int j = A.perm[i];
@@ -502,16 +537,29 @@ __global__ void k_moments(MomentArgs A) {
         __threadfence();
         double PM = 0, px = 0, py = 0, pz = 0;
         float pd = 0.f;
-        const int end = A.n_i4[p].z;
-        int seen = 0;
-        for (int c = p + 1; c < end && seen < 8; c = A.n_i4[c].z, ++seen) {  // octant order
-            const float4 cm = __ldcg(&A.mom[c]);
-            const double m = double(cm.w);
-            PM = __dadd_rn(PM, m);
-            px = __dadd_rn(px, m * double(cm.x));
-            py = __dadd_rn(py, m * double(cm.y));
-            pz = __dadd_rn(pz, m * double(cm.z));
-            if (A.refit) pd = fmaxf(pd, __ldcg(&A.ndisp[c]));
+        const int nc = A.nchild[p];
+        float4 cms[8];
+        float cds[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {  // the children's records in flight together
+            cms[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+            cds[c] = 0.f;
+            if (c < nc) {
+                const int ch = A.kids[8 * size_t(p) + c];
+                cms[c] = __ldcg(&A.mom[ch]);
+                if (A.refit) cds[c] = __ldcg(&A.ndisp[ch]);
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {  // octant order
+            if (c < nc) {
+                const double m = double(cms[c].w);
+                PM = __dadd_rn(PM, m);
+                px = __dadd_rn(px, m * double(cms[c].x));
+                py = __dadd_rn(py, m * double(cms[c].y));
+                pz = __dadd_rn(pz, m * double(cms[c].z));
+                pd = fmaxf(pd, cds[c]);
+            }
         }
         finalize(A, p, PM, px, py, pz, pd);
         __threadfence();
@@ -593,10 +641,38 @@ __global__ void k_refit_bfs_quad32(RefitBfsArgs A) {
     const float4 wb = A.wb[b];
     const int first = __float_as_int(wb.y), code = __float_as_int(wb.z);
     if (code >= 0) return;  // internal: reached by the last of its children
-    {
+    const int cnt = -code;
+    if (cnt <= kLeafMax) {  // the leaf's particles loaded once, together (one memory latency)
+        float4 pp[kLeafMax];
+        float pd[kLeafMax];
+#pragma unroll
+        for (int t = 0; t < kLeafMax; ++t) {
+            pp[t] = t < cnt ? A.p4[first + t] : make_float4(0.f, 0.f, 0.f, 0.f);
+            pd[t] = t < cnt && A.pdisp ? A.pdisp[first + t] : 0.f;
+        }
         KahanF M, sx, sy, sz;
         float dm = 0.f;
-        for (int i = first; i < first - code; ++i) {
+#pragma unroll
+        for (int t = 0; t < kLeafMax; ++t) {
+            if (t < cnt) {
+                M.add(pp[t].w);
+                sx.add(pp[t].w * pp[t].x);
+                sy.add(pp[t].w * pp[t].y);
+                sz.add(pp[t].w * pp[t].z);
+                dm = fmaxf(dm, pd[t]);
+            }
+        }
+        const float4 c = finalize_bfs(A, b, M, sx, sy, sz, dm);
+        QuadSum S;
+#pragma unroll
+        for (int t = 0; t < kLeafMax; ++t)
+            if (t < cnt) S.point(pp[t].w, pp[t].x - c.x, pp[t].y - c.y, pp[t].z - c.z);
+        A.wq[b] = make_float4(S.xx.s, S.yy.s, S.xy.s, S.xz.s);
+        A.wt[b] = make_float2(S.yz.s, S.tr.s);
+    } else {  // depth-48 leaves of coincident points
+        KahanF M, sx, sy, sz;
+        float dm = 0.f;
+        for (int i = first; i < first + cnt; ++i) {
             const float4 p = A.p4[i];
             M.add(p.w);
             sx.add(p.w * p.x);
@@ -606,7 +682,7 @@ __global__ void k_refit_bfs_quad32(RefitBfsArgs A) {
         }
         const float4 c = finalize_bfs(A, b, M, sx, sy, sz, dm);
         QuadSum S;
-        for (int i = first; i < first - code; ++i) {
+        for (int i = first; i < first + cnt; ++i) {
             const float4 p = A.p4[i];
             S.point(p.w, p.x - c.x, p.y - c.y, p.z - c.z);
         }
@@ -962,7 +1038,8 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
     }
     int* nch = n_nchild.get<int>(cap);
     int* ctr = n_counter.get<int>(cap);
-    k_nchild<<<ngrid, kThreads, 0, s>>>(span, nn_dev, i4, nch, ctr);
+    int* kid = n_kids.get<int>(8 * size_t(cap));
+    k_nchild<<<ngrid, kThreads, 0, s>>>(span, nn_dev, i4, nch, ctr, kid);
     GF_CHECK_LAUNCH();
     k_leaf_sort<<<ngrid, kThreads, 0, s>>>(span, nn_dev, i4, pm);
     GF_CHECK_LAUNCH();
@@ -991,6 +1068,7 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
         A.n_i4 = i4;
         A.parent = par;
         A.nchild = nch;
+        A.kids = kid;
         A.counter = ctr;
         A.n_cd = cd;
         A.n_geo = geo;
@@ -1092,6 +1170,7 @@ void Octree::refit(const double* pos, const double* mass, cudaStream_t s) {
         A.n_i4 = n_i4.as<int4>();
         A.parent = n_parent.as<int>();
         A.nchild = n_nchild.as<int>();
+        A.kids = n_kids.as<int>();
         A.counter = ctr;
         A.n_cd = n_cd.as<double4>();
         A.n_geo = n_geo.as<float4>();

@@ -58,6 +58,7 @@ struct Octree {
     DevBuf n_geo;     // float4 {gx, gy, gz, half}
     DevBuf n_cd;      // double4 {centre, half} (build only)
     DevBuf n_parent, n_nchild, n_counter, n_disp, n_bfs;
+    DevBuf n_kids;    // children of each node in octant order (8 slots per node)
     // walk layout, breadth-first order: children of a node are contiguous
     DevBuf w_a;       // float4 {cx, cy, cz, m}
     DevBuf w_b;       // float4 {open_r, first (int bits), code (int bits), rho};

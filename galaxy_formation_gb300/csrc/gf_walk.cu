@@ -227,11 +227,12 @@ __global__ void k_item_flag(const int* __restrict__ groups, const int4* __restri
 }
 
 // The merged items in tree order: item of group g at slot[g] (the scan of the flags). An item
-// without active or massive particles keeps its slot with no particles to evaluate. With gw
-// (merged by active count) the sphere bounds the item's active particles.
+// without active or massive particles keeps its slot with no particles to evaluate. act_sphere
+// (walks of an active set): the sphere bounds the item's active particles, the only ones it
+// evaluates.
 __global__ void k_item_fill(const int* __restrict__ groups, const int4* __restrict__ n_i4,
-                            const int* __restrict__ parent, const int* __restrict__ gw, const TreeCounts* cnt,
-                            int merge,
+                            const int* __restrict__ parent, const int* __restrict__ gw, bool act_sphere,
+                            const TreeCounts* cnt, int merge,
                             const int* __restrict__ flag, const int* __restrict__ slot,
                             const float4* __restrict__ p4, const int* __restrict__ perm,
                             const uint8_t* __restrict__ active, const double* __restrict__ aold,
@@ -245,7 +246,7 @@ __global__ void k_item_fill(const int* __restrict__ groups, const int4* __restri
         if (!flag[g]) continue;
         int b, count;
         cut_at(groups, n_i4, parent, gw, ng, merge, g, b, count);
-        const ItemStats st = item_stats(b, b + count, p4, perm, active, aold, alpha, alpha_q, gw != nullptr);
+        const ItemStats st = item_stats(b, b + count, p4, perm, active, aold, alpha, alpha_q, act_sphere);
         if (lane == 0) {
             const int k = slot[g];
             work[k] = make_int4(b, count, st.valid ? st.nact : 0, 0);
@@ -837,7 +838,8 @@ void Octree::prepare_walk(const uint8_t* active, cudaStream_t s, int chunk, cons
                                            span, fl);
         GF_CHECK_LAUNCH();
         exclusive_scan(fl, sl, span, &cnt->num_work, s, &scratch);
-        k_item_fill<<<blocks, 256, 0, s>>>(groups.as<int>(), n_i4.as<int4>(), n_parent.as<int>(), gw, cnt, cap_w, fl,
+        k_item_fill<<<blocks, 256, 0, s>>>(groups.as<int>(), n_i4.as<int4>(), n_parent.as<int>(), gw,
+                                           active != nullptr, cnt, cap_w, fl,
                                            sl, p4.as<float4>(), perm.as<int>(), active,
                                            alpha > 0.f ? aold : nullptr, alpha, alpha_q, work.get<int4>(cap),
                                            sphere.get<float4>(cap), quad ? item_gam.get<float2>(cap) : nullptr);

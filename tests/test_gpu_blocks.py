@@ -184,7 +184,8 @@ def test_block_autotune_restores_state(gpulib):
         every = ctypes.c_int()
         ms = ctypes.c_double()
         _lib.check(lib.gf_sim_block_autotune(4, chunk.ctypes.data, ctypes.byref(every), ctypes.byref(ms)))
-        assert {c % 100 for c in chunk.tolist()} <= {0, 2, 4, 8, 16, 32, 64}
+        # walk items: chunks of one group, or sibling runs merged by active count
+        assert {c % 100 for c in chunk.tolist()} <= {0, 2, 4, 8, 16, 32, 64, 72, 80, 84, 96}
         assert every.value in (0, 4) and ms.value > 0
         p1, v1, t1 = _state(lib, n)
         u1 = np.empty(n)
