@@ -26,6 +26,7 @@
 //      rounded to the same float32 node record.
 #include <algorithm>
 #include <cfloat>
+#include <climits>
 
 #include "gf_tree.cuh"
 
@@ -37,52 +38,74 @@ constexpr int kThreads = 256;
 
 // ---------------------------------------------------------------------------- bbox
 
+// Order-preserving map of float64 values to int64 (and back): min / max of the images is the
+// image of the min / max, so the reduction runs on the integer pipes instead of the narrow
+// float64 one. Non-finite values are flagged separately.
+__device__ __forceinline__ long long fkey(double v) {
+    const long long b = __double_as_longlong(v);
+    return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ double fkey_inv(long long k) { return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffLL)); }
+__device__ __forceinline__ bool finite_bits(double v) {
+    return ((__double_as_longlong(v) >> 52) & 0x7ff) != 0x7ff;
+}
+
 // float64 bounding box -> root cube (cpp/nbody.cpp:210-219) in one launch: every block reduces
 // its share of the positions and writes a partial; the last block to finish (arrival counter)
 // reduces the partials and writes the root cube. min / max are exact, so the result does not
 // depend on the order of the reductions.
 __global__ void k_bbox(const double* __restrict__ pos, int n, double* __restrict__ part, RootBox* __restrict__ root,
                        uint32_t* status, int* __restrict__ done) {
-    double lo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, hi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
-    double bad = 0.0;
+    long long lo[3] = {LLONG_MAX, LLONG_MAX, LLONG_MAX}, hi[3] = {LLONG_MIN, LLONG_MIN, LLONG_MIN};
+    int bad = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             const double v = pos[3 * size_t(i) + a];
-            if (!isfinite(v)) bad = 1.0;
-            lo[a] = fmin(lo[a], v);
-            hi[a] = fmax(hi[a], v);
+            bad |= finite_bits(v) ? 0 : 1;
+            const long long k = fkey(v);
+            lo[a] = min(lo[a], k);
+            hi[a] = max(hi[a], k);
         }
     }
-    __shared__ double s[7][kThreads / 32];
+    __shared__ long long s[6][kThreads / 32];
+    __shared__ int s_bad[kThreads / 32];
     __shared__ bool s_last;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    auto block_reduce = [&](double* out) {
+    auto block_reduce = [&](long long* out, int* out_bad) {
 #pragma unroll
         for (int o = 16; o; o >>= 1) {
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-                lo[a] = fmin(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
-                hi[a] = fmax(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+                lo[a] = min(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+                hi[a] = max(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
             }
-            bad = fmax(bad, __shfl_xor_sync(0xffffffffu, bad, o));
+            bad |= __shfl_xor_sync(0xffffffffu, bad, o);
         }
         if (lane == 0) {
             for (int a = 0; a < 3; ++a) {
                 s[a][warp] = lo[a];
                 s[3 + a][warp] = hi[a];
             }
-            s[6][warp] = bad;
+            s_bad[warp] = bad;
         }
         __syncthreads();
-        if (threadIdx.x < 7) {
-            double v = s[threadIdx.x][0];
+        if (threadIdx.x < 6) {
+            long long v = s[threadIdx.x][0];
             for (int w = 1; w < kThreads / 32; ++w)
-                v = threadIdx.x < 3 ? fmin(v, s[threadIdx.x][w]) : fmax(v, s[threadIdx.x][w]);
+                v = threadIdx.x < 3 ? min(v, s[threadIdx.x][w]) : max(v, s[threadIdx.x][w]);
             out[threadIdx.x] = v;
         }
+        if (threadIdx.x == 6) {
+            int v = 0;
+            for (int w = 0; w < kThreads / 32; ++w) v |= s_bad[w];
+            *out_bad = v;
+        }
     };
-    block_reduce(part + 7 * size_t(blockIdx.x));
+    long long* ipart = reinterpret_cast<long long*>(part);
+    int dummy;
+    block_reduce(ipart + 7 * size_t(blockIdx.x), &dummy);
+    if (threadIdx.x == 6) ipart[7 * size_t(blockIdx.x) + 6] = dummy;
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) s_last = atomicAdd(done, 1) == int(gridDim.x) - 1;
@@ -90,23 +113,26 @@ __global__ void k_bbox(const double* __restrict__ pos, int n, double* __restrict
     if (!s_last) return;
     __threadfence();
     for (int a = 0; a < 3; ++a) {
-        lo[a] = DBL_MAX;
-        hi[a] = -DBL_MAX;
+        lo[a] = LLONG_MAX;
+        hi[a] = LLONG_MIN;
     }
-    bad = 0.0;
+    bad = 0;
     for (int b = threadIdx.x; b < int(gridDim.x); b += blockDim.x) {
         for (int a = 0; a < 3; ++a) {
-            lo[a] = fmin(lo[a], __ldcg(&part[7 * size_t(b) + a]));
-            hi[a] = fmax(hi[a], __ldcg(&part[7 * size_t(b) + 3 + a]));
+            lo[a] = min(lo[a], __ldcg(&ipart[7 * size_t(b) + a]));
+            hi[a] = max(hi[a], __ldcg(&ipart[7 * size_t(b) + 3 + a]));
         }
-        bad = fmax(bad, __ldcg(&part[7 * size_t(b) + 6]));
+        bad |= int(__ldcg(&ipart[7 * size_t(b) + 6]));
     }
-    __shared__ double tot[7];
+    __shared__ long long itot[6];
+    __shared__ int tot_bad;
     __syncthreads();
-    block_reduce(tot);
+    block_reduce(itot, &tot_bad);
     __syncthreads();
     if (threadIdx.x != 0) return;
-    if (tot[6] > 0) raise_status(status, GF_ERR_NONFINITE);
+    double tot[6];
+    for (int a = 0; a < 6; ++a) tot[a] = fkey_inv(itot[a]);
+    if (tot_bad) raise_status(status, GF_ERR_NONFINITE);
     RootBox R;
     double ext = 0;
     for (int a = 0; a < 3; ++a) {
@@ -125,6 +151,12 @@ __global__ void k_bbox(const double* __restrict__ pos, int n, double* __restrict
     // that of the fixed-point position stays below 2^-27 (|c|/half + 2) grid units; the
     // margin keeps a factor 8 on top.
     R.margin = ldexp(1.0, -24) * (cmax / R.half + 2.0);
+    // the same test in 32.32 fixed point (scaling by 2^32 is exact): the fraction window
+    // [m_lo, m_hi] of the truncated fixed-point position lies inside [margin, 1 - margin]
+    R.inv_w32 = R.inv_w * 4294967296.0;
+    const double ml = fmin(ceil(R.margin * 4294967296.0), 2147483648.0);
+    R.m_lo = uint32_t(ml);
+    R.m_hi = uint32_t(4294967295.0 - ml);
     *root = R;
 }
 
@@ -162,13 +194,19 @@ __device__ void exact_keys(double x, double y, double z, const RootBox& R, int l
     if (levels < 21) k0 <<= 3 * (21 - levels);
 }
 
+// Grid cell of coordinate a on the 2^21 grid, when the position lies at least `margin` grid
+// units from every cell wall (else the exact path decides). 32.32 fixed point: u = (x - lo) *
+// inv_w * 2^32 (the same rounding as without the 2^32), truncated; the integer part is the
+// cell, the fraction is tested against a window no wider than [margin, 1 - margin]. One float64
+// subtract, multiply and conversion per coordinate; the tests are integer.
 __device__ __forceinline__ bool grid_coord(double x, int a, const RootBox& R, uint32_t& ic) {
-    const double u = __dmul_rn(__dsub_rn(x, R.lo[a]), R.inv_w);
-    const double f = floor(u);
-    const double fr = u - f;
-    if (!(f >= 0.0 && f < 2097152.0 && fr >= R.margin && fr <= 1.0 - R.margin)) return false;
-    ic = uint32_t(f);
-    return true;
+    const double u = __dmul_rn(__dsub_rn(x, R.lo[a]), R.inv_w32);
+    const long long ub = __double_as_longlong(u);
+    if (ub < 0 || ub >= 0x4340000000000000LL) return false;  // outside [0, 2^53) (or NaN)
+    const unsigned long long q = __double2ull_rz(u);
+    ic = uint32_t(q >> 32);
+    const uint32_t fr = uint32_t(q);
+    return ic < 2097152u && fr >= R.m_lo && fr <= R.m_hi;
 }
 
 __global__ void k_keys(const double* __restrict__ pos, int n, const RootBox* __restrict__ rootp,

@@ -22,6 +22,8 @@ struct RootBox {
     double lo[3];     // c - half
     double inv_w;     // 2^21 / (2 half): grid units per unit length
     double margin;    // grid units: closer than this to a cell wall -> exact path
+    double inv_w32;   // inv_w * 2^32: 32.32 fixed-point grid units per unit length
+    uint32_t m_lo, m_hi;  // fixed-point fraction window that is at least `margin` from a wall
 };
 
 // Small device-side counters read back once per build.
