@@ -631,6 +631,17 @@ struct QuadSum {
         yz.add(3.f * m * dy * dz);
         tr.add(m * r2);
     }
+    // a child cell: its own moments (q, yt) plus the parallel-axis term of its mass m at d, added
+    // to each compensated sum as one term
+    __device__ __forceinline__ void cell(const float4 q, const float2 yt, float m, float dx, float dy, float dz) {
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        xx.add(q.x + m * (3.f * dx * dx - r2));
+        yy.add(q.y + m * (3.f * dy * dy - r2));
+        xy.add(q.z + 3.f * m * dx * dy);
+        xz.add(q.w + 3.f * m * dx * dz);
+        yz.add(yt.x + 3.f * m * dy * dz);
+        tr.add(yt.y + m * r2);
+    }
 };
 
 // Mixed form: monopole and traceless quadrupole in one bottom-up pass, float32 with
@@ -765,13 +776,7 @@ __global__ void k_refit_bfs_quad32(RefitBfsArgs A) {
             if (c < nc) {
                 const float4 qc = __ldcg(&A.wq[c0 + c]);
                 const float2 yt = __ldcg(&A.wt[c0 + c]);
-                S.xx.add(qc.x);
-                S.yy.add(qc.y);
-                S.xy.add(qc.z);
-                S.xz.add(qc.w);
-                S.yz.add(yt.x);
-                S.tr.add(yt.y);
-                S.point(cm[c].w, cm[c].x - cp.x, cm[c].y - cp.y, cm[c].z - cp.z);
+                S.cell(qc, yt, cm[c].w, cm[c].x - cp.x, cm[c].y - cp.y, cm[c].z - cp.z);
             }
         }
         A.wq[p] = make_float4(S.xx.s, S.yy.s, S.xy.s, S.xz.s);

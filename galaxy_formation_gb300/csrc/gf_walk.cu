@@ -352,10 +352,15 @@ struct WarpSmem {
     int slot_pos[kBatch];
 };
 
+// |d|^2 + eps^2 as one fused chain seeded with eps^2 (three FMAs)
+__device__ __forceinline__ float soft_r2(float ex, float ey, float ez, float eps2) {
+    return fmaf(ex, ex, fmaf(ey, ey, fmaf(ez, ez, eps2)));
+}
+
 __device__ __forceinline__ void pair_acc(const float4 e, float x, float y, float z, float eps2,
                                          float& ax, float& ay, float& az) {
     const float ex = e.x - x, ey = e.y - y, ez = e.z - z;
-    const float r2 = ex * ex + ey * ey + ez * ez + eps2;
+    const float r2 = soft_r2(ex, ey, ez, eps2);
     const float inv = rsqrtf(r2);
     const float f = e.w * inv * inv * inv;
     ax += f * ex;
@@ -368,7 +373,7 @@ __device__ __forceinline__ void pair_acc(const float4 e, float x, float y, float
 __device__ __forceinline__ void pair_acc_pot(const float4 e, float x, float y, float z, float eps2,
                                              float& ax, float& ay, float& az, float& ph) {
     const float ex = e.x - x, ey = e.y - y, ez = e.z - z;
-    const float r2 = ex * ex + ey * ey + ez * ez + eps2;
+    const float r2 = soft_r2(ex, ey, ez, eps2);
     const float inv = rsqrtf(r2);
     const float mi = e.w * inv;
     const float f = mi * inv * inv;
@@ -383,21 +388,23 @@ __device__ __forceinline__ void pair_acc_pot(const float4 e, float x, float y, f
 //   a = M d / r^3 - Q d / r^5 + (5/2) (d.Q.d) d / r^7 - (5/2) T eps^2 d / r^7.
 // The last term comes from the trace of the second moment, which the softened potential
 // (unlike 1/r) does not annihilate; it matters for cells accepted within a few eps.
-__device__ __forceinline__ void quad_acc(const float4 e, const float4 q, float2 yt, float x, float y, float z,
-                                         float eps2, float& ax, float& ay, float& az) {
-    const float qyz = yt.x;
+// c_t = (5/2) T eps^2 is the node's constant of that term (the caller computes it once per node
+// for all the particles it serves).
+__device__ __forceinline__ void quad_acc(const float4 e, const float4 q, float qyz, float c_t, float x, float y,
+                                         float z, float eps2, float& ax, float& ay, float& az) {
     const float dx = e.x - x, dy = e.y - y, dz = e.z - z;
-    const float r2 = dx * dx + dy * dy + dz * dz + eps2;
+    const float r2 = soft_r2(dx, dy, dz, eps2);
     const float inv = rsqrtf(r2);
     const float inv2 = inv * inv;
     const float inv3 = inv2 * inv;
     const float inv5 = inv3 * inv2;
+    const float inv7 = inv5 * inv2;
     const float qzz = -(q.x + q.y);
     const float qdx = q.x * dx + q.z * dy + q.w * dz;
     const float qdy = q.z * dx + q.y * dy + qyz * dz;
     const float qdz = q.w * dx + qyz * dy + qzz * dz;
     const float dqd = dx * qdx + dy * qdy + dz * qdz;
-    const float f = e.w * inv3 + 2.5f * (dqd - yt.y * eps2) * inv5 * inv2;
+    const float f = fmaf(fmaf(2.5f, dqd, -c_t), inv7, e.w * inv3);
     ax += f * dx - inv5 * qdx;
     ay += f * dy - inv5 * qdy;
     az += f * dz - inv5 * qdz;
@@ -456,8 +463,9 @@ __device__ __forceinline__ void eval_quad(const float4* tile, const float4* ntA,
     for (int j = ksub; j < fillN; j += m) {
         const float4 e = ntA[j], q = ntQ[j];
         const float2 yt = ntYZ[j];
+        const float c_t = 2.5f * yt.y * eps2;
 #pragma unroll
-        for (int t = 0; t < PPL; ++t) quad_acc(e, q, yt, x[t], y[t], z[t], eps2, px[t], py[t], pz[t]);
+        for (int t = 0; t < PPL; ++t) quad_acc(e, q, yt.x, c_t, x[t], y[t], z[t], eps2, px[t], py[t], pz[t]);
     }
 #pragma unroll
     for (int t = 0; t < PPL; ++t) {
