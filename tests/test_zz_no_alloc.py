@@ -5,9 +5,10 @@ or a step loop that must not allocate because cudaMalloc/cudaFree synchronise th
 device). Here it is called through the C ABI on caller-owned device buffers and compared
 with gf_sph_forces_dev, the allocating entry point, on two calls in a row: first a larger
 particle set, then a smaller one written into output buffers with spare rows, which must
-stay untouched (the call writes rows 0..n-1 only). It must refuse a particle count above its
-fixed scratch size, and a neighbour index outside [0, n) gives that particle NaN outputs
-instead of a read out of bounds.
+stay untouched (the call writes rows 0..n-1 only); around the second call the device's free
+memory must not change. It must refuse a particle count above its fixed scratch size, and a
+neighbour index outside [0, n) gives that particle NaN outputs instead of a read out of
+bounds.
 """
 
 import ctypes
@@ -35,7 +36,7 @@ def _sets(golden, oracle):
     return a, b
 
 
-def _run(lib, torch, fn, data, spare=0, expect_finite=True):
+def _run(lib, torch, fn, data, spare=0, expect_finite=True, check_free=False):
     from galaxy_formation_gb300 import params
 
     dev = torch.device("cuda")
@@ -46,12 +47,16 @@ def _run(lib, torch, fn, data, spare=0, expect_finite=True):
            "acc": torch.full((m, 3), np.nan, dtype=torch.float64, device=dev),
            "dudt": torch.full((m,), np.nan, dtype=torch.float64, device=dev),
            "dt": torch.full((m,), np.nan, dtype=torch.float64, device=dev)}
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]  # every buffer of the call exists already
     st = fn(n, k, t["pos"].data_ptr(), t["vel"].data_ptr(), t["mass"].data_ptr(), t["nb"].data_ptr(),
             t["h"].data_ptr(), t["u"].data_ptr(), params.GAMMA, params.ALPHA, params.BETA,
             out["rho"].data_ptr(), out["acc"].data_ptr(), out["dudt"].data_ptr(), out["dt"].data_ptr(),
             ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
     torch.cuda.synchronize()
     assert st == 0, (st, lib.gf_last_error())
+    if check_free:  # the call took no device memory
+        assert torch.cuda.mem_get_info()[0] == free0
     res = {k: v.cpu().numpy() for k, v in out.items()}
     for v in res.values():
         assert np.all(np.isnan(v[n:]))
@@ -71,7 +76,8 @@ def test_noalloc_matches_allocating_entry_twice(gpulib, golden, oracle):
     small, large = _sets(golden, oracle)
     assert len(large["pos"]) > len(small["pos"])
     for data, spare in ((large, 0), (small, 1000)):
-        got = _run(lib, torch, lib.gf_sph_forces_noalloc_dev, data, spare)
+        # the second call on this device: its one-time set-up (the scratch address) is done
+        got = _run(lib, torch, lib.gf_sph_forces_noalloc_dev, data, spare, check_free=spare > 0)
         ref = _run(lib, torch, lib.gf_sph_forces_dev, data)
         for key in ("rho", "acc", "dudt", "dt"):
             assert _close(got[key], ref[key]), key
