@@ -678,6 +678,35 @@ __global__ void __launch_bounds__(WARPS * 32, QUAD ? (NPL > 2 ? 1 : 16 / WARPS) 
             const bool leaf = valid && !accept && code < 0;
             const bool open = valid && !accept && code > 0;
 
+            // The loads this slot needs are issued here, ahead of the pushes and appends that
+            // do not depend on them: an accepted quadrupole node's moments, and the first 32
+            // particles of the round's opened leaves (concatenated in lane order; entry o goes
+            // to lane o, which finds its leaf by a binary search over the inclusive sums).
+            float4 qv = make_float4(0.f, 0.f, 0.f, 0.f);
+            float2 yv = make_float2(0.f, 0.f);
+            if (QUAD && accept && !mono) {
+                qv = wq[node];
+                yv = wt[node];
+            }
+            const bool anyleaf = __any_sync(0xffffffffu, leaf);
+            int lincl = 0, lexcl = 0, ltot = 0;
+            float4 lp = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (anyleaf) {
+                const int lc = leaf ? -code : 0;
+                lincl = warp_incl_scan(lc);
+                lexcl = lincl - lc;
+                ltot = __shfl_sync(0xffffffffu, lincl, 31);
+                int src = 0;
+#pragma unroll
+                for (int step = 16; step; step >>= 1) {
+                    const int v = __shfl_sync(0xffffffffu, lincl, src + step - 1);
+                    if (v <= lane) src += step;
+                }
+                const int f = __shfl_sync(0xffffffffu, first, src);
+                const int x = __shfl_sync(0xffffffffu, lexcl, src);
+                if (lane < ltot) lp = p4[f + (lane - x)];
+            }
+
             // opened internal nodes: push their child ranges
             const unsigned om = __ballot_sync(0xffffffffu, open);
             const int npush = __popc(om);
@@ -697,8 +726,8 @@ __global__ void __launch_bounds__(WARPS * 32, QUAD ? (NPL > 2 ? 1 : 16 / WARPS) 
                 if (accept && !mono) {
                     const int slot_n = fillN + __popc(qm & lt);
                     S.ntA[slot_n] = A;
-                    S.ntQ[slot_n] = wq[node];
-                    S.ntYZ[slot_n] = wt[node];
+                    S.ntQ[slot_n] = qv;
+                    S.ntYZ[slot_n] = yv;
                 }
                 fillN += nq;
                 const unsigned mm = __ballot_sync(0xffffffffu, mono);
@@ -716,13 +745,13 @@ __global__ void __launch_bounds__(WARPS * 32, QUAD ? (NPL > 2 ? 1 : 16 / WARPS) 
                 fill += na;
             }
 
-            // opened leaves: their particles (the scan only in rounds that open one)
-            if (__any_sync(0xffffffffu, leaf)) {
-            const int lc = leaf ? -code : 0;
-            const int lincl = warp_incl_scan(lc);
-            const int lexcl = lincl - lc;
-            const int ltot = __shfl_sync(0xffffffffu, lincl, 31);
-            for (int done = 0; done < ltot;) {
+            // opened leaves: their particles, the first 32 from the loads above
+            if (anyleaf) {
+            const int n0 = min(32, ltot);
+            if (fill + n0 > Smem::kTile) GF_WALK_FLUSH();
+            if (lane < n0) S.tile[fill + lane] = lp;
+            fill += n0;
+            for (int done = n0; done < ltot;) {
                 if (fill == Smem::kTile) GF_WALK_FLUSH();
                 const int chunk = min(Smem::kTile - fill, ltot - done);
                 // warp-cooperative copy: entry o of the concatenated leaves goes to lane o % 32,
