@@ -85,6 +85,9 @@ def parse():
                          "plain step loop vs batched mixed+learned blocks over the same simulated time, "
                          "energy and angular-momentum drift; learned: 1M gas with clumps, search "
                          "iterations with and without the learned guess")
+    ap.add_argument("--no-configs", dest="configs", action="store_false",
+                    help="skip the shortened config 3 (clumped snapshot) and config 4 (4M drift) measurements")
+    ap.add_argument("--drift-steps", type=int, default=10, help="long steps of the plain loop in the 4M drift run")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
@@ -495,7 +498,39 @@ class Gpu:
         lib.gf_profile(0)
         return {"iterations_per_gas": self.knn_iters(), "knn_ms": ms.value}
 
-    def batched(self, blocks, nlev=7, form="mixed_learned"):
+    def step_loop(self, form, steps):
+        """The reference's step loop (gf_sim_step) in `form` for `steps` long steps from the
+        snapshot: particle-updates/s and the simulated time covered."""
+        torch, lib, L, p = self.torch, self.lib, self._lib, self.params
+        theta = self.set_form(form)
+        d = self.d
+        L.check(lib.gf_sim_init(self.n, d["pos"], d["vel"], d["mass"], d["kind"], d["u"], theta, p.EPS,
+                                p.GAMMA, p.ALPHA, p.BETA))
+        s = torch.cuda.ExternalStream(lib.gf_stream())
+        tk, sub = ctypes.c_double(), ctypes.c_int()
+        L.check(lib.gf_sim_step(1e30, ctypes.byref(tk), ctypes.byref(sub)))  # warm-up
+        t0 = ctypes.c_double()
+        L.check(lib.gf_sim_read(None, None, None, None, ctypes.byref(t0)))
+        tk0 = t0.value
+        upd, subs = 0.0, 0
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(steps):
+            L.check(lib.gf_sim_step(1e30, ctypes.byref(tk), ctypes.byref(sub)))
+            upd += lib.gf_sim_updates()
+            subs += sub.value
+        e1.record(s)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        t1 = ctypes.c_double()
+        L.check(lib.gf_sim_read(None, None, None, None, ctypes.byref(t1)))
+        return {"value": upd / (ms * 1e-3), "unit": UNIT, "form": form, "steps": steps, "substeps": subs,
+                "updates": upd, "ms": ms, "simulated_time": t1.value - tk0,
+                "simulated_time_per_wall_second": (t1.value - tk0) / (ms * 1e-3),
+                "note": "simulation.py:114-149 on the GPU: per sub-step the gravity of the fast particles on a "
+                        "refitted tree and the SPH of all the gas"}
+
+    def batched(self, blocks, nlev=7, form="mixed_learned", plain_steps=10):
         """Block time steps at the mixed + learned form: autotune, one warm block, then
         `blocks` blocks timed with CUDA events on the library's stream."""
         torch, lib, L, p = self.torch, self.lib, self._lib, self.params
@@ -515,6 +550,8 @@ class Gpu:
         s = torch.cuda.ExternalStream(lib.gf_stream())
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         launches0 = lib.gf_launch_count()
+        tb0 = ctypes.c_double()
+        L.check(lib.gf_sim_read(None, None, None, None, ctypes.byref(tb0)))
         torch.cuda.nvtx.range_push("blocks")  # for profilers: the timed blocks only
         e0.record(s)
         L.check(lib.gf_sim_blocks(blocks, nlev, ctypes.byref(upd)))
@@ -523,6 +560,9 @@ class Gpu:
         torch.cuda.nvtx.range_pop()
         ms = e0.elapsed_time(e1)
         launches = lib.gf_launch_count() - launches0
+        tb1 = ctypes.c_double()
+        L.check(lib.gf_sim_read(None, None, None, None, ctypes.byref(tb1)))
+        sim_rate = (tb1.value - tb0.value) / (ms * 1e-3)
         # the full neighbour search of a block end (the previous h of the coarse levels' gas is
         # a block old there): one more block with the stage profiler on
         lib.gf_profile(1)
@@ -533,11 +573,20 @@ class Gpu:
         lib.gf_profile(0)
         block_end = {"knn_ms": kms.value / max(1, kcnt.value), "iterations_per_gas": self.knn_iters(),
                      "h_guess": ["previous h", "cell density", "previous h (learned MLP without one)"][FORMS[form][3]]}
-        return {"value": upd.value / (ms * 1e-3), "unit": UNIT, "blocks": blocks, "substeps_per_block": 1 << (nlev - 1),
+        # the plain GPU form of the same hierarchical time stepping: the reference's step loop
+        # (simulation.py:114-149: gravity of the fast particles on a refitted tree and SPH of all
+        # the gas at every sub-step) with the reference's arithmetic, from the same snapshot
+        plain = self.step_loop("plain", plain_steps)
+        self.set_form(form)
+        value = upd.value / (ms * 1e-3)
+        return {"value": value, "unit": UNIT, "blocks": blocks, "substeps_per_block": 1 << (nlev - 1),
                 "levels": nlev, "level_fractions": [round(float(x), 5) for x in frac],
                 "updates": upd.value, "ms": ms, "ms_per_block": ms / blocks,
                 "autotune": {"chunk_per_bin": chunk.tolist(), "rebuild_every": every.value, "seconds": tune_s},
                 "launches_outside_graphs": launches, "block_end_search": block_end, "form": form,
+                "simulated_time_per_wall_second": sim_rate,
+                "plain_step_loop": plain, "ratio_vs_plain_step_loop": value / plain["value"],
+                "time_to_solution_ratio_vs_plain_step_loop": sim_rate / plain["simulated_time_per_wall_second"],
                 "note": "an update = a particle given a freshly computed force at one of its own steps; "
                         "each block = 63 sub-steps replayed as one CUDA graph + a full evaluation"}
 
@@ -713,6 +762,18 @@ def run_gpu(args, world, rank, local):
                          "(workers=-1) + restated sph_forces (OpenMP), theta 0.7"}
         parity = parity_vs_oracle(G, fo, head)
 
+    # configs 3 and 4 at bench time, after every measurement of the headline snapshot
+    # (shortened: the first search of the clumped snapshot, and 10 long steps of the 4M cloud
+    # against block steps over the same simulated time)
+    configs = {}
+    if args.configs and learned is not None:
+        configs["learned_clumps_1M"] = measure_learned_clumps(args, local)
+        D = Gpu(args, local, 4, ic="device")
+        configs["drift_4M"] = measure_drift(D, args.drift_steps)
+        del D
+        torch.cuda.set_stream(G.stream)
+        torch.cuda.empty_cache()
+
     def summary(f):
         r = res[f]
         th, quad_f, sph32, hg, rel, merge, relq = FORMS[f]
@@ -761,6 +822,7 @@ def run_gpu(args, world, rank, local):
         "speedup_vs_plain": {f"{head}/{f}": H["value"] / res[f]["value"] for f in forms if f != head},
         "batched": batched,
         "learned_h": learned,
+        "configs": configs or None,
     }
     print(json.dumps(line), flush=True)
 
@@ -809,16 +871,12 @@ def run_learned(args, world, rank, local):
     }), flush=True)
 
 
-def run_drift(args, world, rank, local):
-    """4M rotating cloud: the plain form with the reference's step loop against the mixed +
-    batched + learned form (block time steps), over the same simulated time; updates/s and the
-    float64 energy / angular-momentum drift of each."""
-    if rank != 0:
-        return
-    G = Gpu(args, local, 4, ic="device")
+def measure_drift(G, steps, nlev=7):
+    """Config 4: the plain form with the reference's step loop against the mixed + batched +
+    learned form (block time steps) over the same simulated time, on G's particle set (the
+    learned guess must be trained already); updates/s, time to solution and the float64 energy /
+    angular-momentum drift of each."""
     torch, lib, L, p = G.torch, G.lib, G._lib, G.params
-    G.collect_pairs(2_000_000, collect_steps=2, start=True)
-    G.train_hguess(collected=True)
     d, n = G.d, G.n
     s = torch.cuda.ExternalStream(lib.gf_stream())
     out = {}
@@ -846,7 +904,7 @@ def run_drift(args, world, rank, local):
     upd, subs = 0.0, 0
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(s)
-    for _ in range(args.steps):
+    for _ in range(steps):
         L.check(lib.gf_sim_step(1e30, ctypes.byref(tk), ctypes.byref(sub)))
         upd += lib.gf_sim_updates()
         subs += sub.value
@@ -855,7 +913,7 @@ def run_drift(args, world, rank, local):
     ms = e0.elapsed_time(e1)
     q1 = diag()
     t_end = q1[7]
-    out["plain_step_loop"] = {"value": upd / (ms * 1e-3), "unit": UNIT, "steps": args.steps, "substeps": subs,
+    out["plain_step_loop"] = {"value": upd / (ms * 1e-3), "unit": UNIT, "steps": steps, "substeps": subs,
                               "updates": upd, "ms": ms, "simulated_time": t_end, **drift(q0, q1),
                               "form": "plain: reference step loop (simulation.py:114-149), theta 0.7, "
                                       "float32 monopole walk, float64 SPH"}
@@ -864,7 +922,6 @@ def run_drift(args, world, rank, local):
     L.check(lib.gf_sim_init(n, d["pos"], d["vel"], d["mass"], d["kind"], d["u"], theta, p.EPS, p.GAMMA, p.ALPHA,
                             p.BETA))
     L.check(lib.gf_sim_thermo(1, units.ctypes.data))
-    nlev = 7
     chunk = np.zeros(nlev - 1, np.int32)
     every, gms = ctypes.c_int(), ctypes.c_double()
     L.check(lib.gf_sim_block_autotune(nlev, chunk.ctypes.data, ctypes.byref(every), ctypes.byref(gms)))
@@ -878,7 +935,7 @@ def run_drift(args, world, rank, local):
         blocks += 1
         t = ctypes.c_double()
         L.check(lib.gf_sim_read(None, None, None, None, ctypes.byref(t)))
-        if t.value >= t_end or blocks >= 10 * args.steps:
+        if t.value >= t_end or blocks >= 10 * steps:
             break
     e1.record(s)
     torch.cuda.synchronize()
@@ -891,18 +948,59 @@ def run_drift(args, world, rank, local):
                                     "form": "quadrupole float32 + Kahan walk (relative opening criterion, alpha "
                                             f"{FORMS['mixed_learned'][4]:g}; merged walk items), float32 + Kahan SPH, "
                                             "learned h guess, block time steps (7 levels) replayed as CUDA graphs"}
+    lib.gf_sim_thermo(0, None)
     r = out["mixed_batched_learned"]["simulated_time"] / out["mixed_batched_learned"]["ms"]
     r0 = out["plain_step_loop"]["simulated_time"] / out["plain_step_loop"]["ms"]
-    print(json.dumps({
+    return {
         "workload": f"rotating 1/r cloud, {int((d['kind'] == 0).sum()):,} gas + {int((d['kind'] != 0).sum()):,} DM "
-                    "(seed 3), the same simulated time for both forms",
+                    "(seed 3, drawn on the GPU), the same simulated time for both forms",
         "forms": out,
         "simulated_time_per_wall_second_ratio": r / r0,
         "diagnostics": "gf_sim_diagnostics: float64 sums; potential from a monopole walk at theta 0.5",
         "thermal_update": "u += dt du/dt at every (sub-)step, floored at 1e4 K (simulation.py:97-102); no cooling",
         "initial_conditions": G.ic,
-    }), flush=True)
-    lib.gf_sim_thermo(0, None)
+    }
+
+
+def run_drift(args, world, rank, local):
+    """4M rotating cloud: the plain form with the reference's step loop against the mixed +
+    batched + learned form (block time steps), over the same simulated time; updates/s and the
+    float64 energy / angular-momentum drift of each."""
+    if rank != 0:
+        return
+    G = Gpu(args, local, 4, ic="device")
+    G.collect_pairs(2_000_000, collect_steps=2, start=True)
+    G.train_hguess(collected=True)
+    print(json.dumps(measure_drift(G, args.steps)), flush=True)
+
+
+def measure_learned_clumps(args, local):
+    """Config 3: the first search (no previous h) of 1M gas in a disk with 200 Plummer clumps,
+    densities over 6 decades, with the trained network (this process trained it on pairs from
+    the disk+halo snapshots, which hold no clumps) against the cell-density start; the
+    converged neighbours, hence accelerations and time steps, must be identical."""
+    G = Gpu(args, local, 3)
+    torch, lib, L = G.torch, G.lib, G._lib
+    theta = G.set_form("mixed_learned")
+    # the geometric opening criterion: the relative one takes its error scale from the previous
+    # evaluation, which differs between the runs compared bit for bit
+    lib.gf_set_option(L.OPT_GRAVITY_REL, 0)
+    pos = G.T["pos"].clone()
+    res = {}
+    for mode, name in ((1, "cell_density"), (2, "learned")):
+        r = G.search_without_h(theta, pos, mode)
+        res[name] = {**r, "acc": G.acc.clone(), "dt": G.dt.clone()}
+    lib.gf_set_option(L.OPT_HGUESS, 0)
+    same = torch.equal(res["learned"]["acc"], res["cell_density"]["acc"]) and \
+        torch.equal(res["learned"]["dt"], res["cell_density"]["dt"])
+    out = {"workload": f"{G.n_gas:,} gas + {G.n - G.n_gas:,} DM, disk + 200 Plummer clumps (seed 3)",
+           "first_search": {k: {"iterations_per_gas": v["iterations_per_gas"], "knn_ms": v["knn_ms"]}
+                            for k, v in res.items()},
+           "converged_results_identical": bool(same),
+           "speedup_learned_vs_cell_density": res["cell_density"]["knn_ms"] / res["learned"]["knn_ms"]}
+    del G
+    torch.cuda.empty_cache()
+    return out
 
 
 def main():
