@@ -311,6 +311,13 @@ void ForceEngine::evaluate(const ForceArgs& a, cudaStream_t s) {
     // The gravity chain is queued first and without host synchronisation (a tree of this
     // particle set was built before: its node buffers bound the new one), so the GPU runs it
     // while the host drives the hydro chain, whose own synchronisations wait on its stream only.
+    if (!s3) {
+        int lowest = 0, greatest = 0;
+        GF_CUDA(cudaDeviceGetStreamPriorityRange(&lowest, &greatest));
+        GF_CUDA(cudaStreamCreateWithPriority(&s3, cudaStreamNonBlocking, greatest));
+        GF_CUDA(cudaEventCreateWithFlags(&ev_gathered, cudaEventDisableTiming));
+        GF_CUDA(cudaEventCreateWithFlags(&ev_moments, cudaEventDisableTiming));
+    }
     const bool fork = a.sph != 0;
     if (fork) {
         if (!s2) {
@@ -332,12 +339,16 @@ void ForceEngine::evaluate(const ForceArgs& a, cudaStream_t s) {
     const int gmax = gravity_quad ? walk_group : kGroupMax;  // the mixed form's groups are tunable
     const bool rel = gravity_quad && grav_rel > 0 && have_aold;
     const double theta = rel ? kRelFloorTheta : a.theta;
+    // a refit's moments run beside the preparation of the walk items (joined before the walk)
+    bool split_refit = false;
     if (a.nosync) {  // inside a captured graph: the tree of the last regular build, rebuilt or refitted
         if (!T.valid || T.n != n) throw Error(GF_ERR_ARG, "a synchronisation-free evaluation needs a built tree");
-        if (a.rebuild)
+        if (a.rebuild) {
             T.build(n, a.pos, a.mass, theta, s, true);
-        else
-            T.refit(a.pos, a.mass, s);
+        } else {
+            T.refit(a.pos, a.mass, s, s3, ev_gathered);
+            split_refit = true;
+        }
     } else if (a.rebuild || !T.valid || T.n != n || T.quad != (gravity_quad != 0) || T.group_max != gmax) {
         const bool same_set = T.valid && T.n == n && T.quad == (gravity_quad != 0) && T.group_max == gmax &&
                               !T.outgrowing();
@@ -350,11 +361,16 @@ void ForceEngine::evaluate(const ForceArgs& a, cudaStream_t s) {
             T.build(n, a.pos, a.mass, theta, s);
         }
     } else {
-        T.refit(a.pos, a.mass, s);
+        T.refit(a.pos, a.mass, s, s3, ev_gathered);
+        split_refit = true;
     }
     T.merge_cap = gravity_quad ? walk_merge : 0;
     T.prepare_walk(a.active, s, a.walk_chunk ? a.walk_chunk : walk_chunk, rel ? acc_grav.as<double>() : nullptr,
                    rel ? float(grav_rel) : 0.f, rel ? float(grav_rel_mono) : 0.f);
+    if (split_refit) {
+        GF_CUDA(cudaEventRecord(ev_moments, s3));
+        GF_CUDA(cudaStreamWaitEvent(s, ev_moments, 0));
+    }
     T.walk(a.eps, acc_grav.as<double>(), s, nullptr, a.walk_npl, a.walk_shape >= 0 ? a.walk_shape : walk_shape);
     if (!a.active) have_aold = true;  // every particle has a previous gravity now
 

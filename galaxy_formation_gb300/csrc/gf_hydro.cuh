@@ -85,6 +85,8 @@ struct ForceEngine {
     ScanScratch hscratch;    // scans of the hydro stream
     cudaStream_t s2 = nullptr;               // the hydro chain's stream
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaStream_t s3 = nullptr;               // a refit's moments, beside the walk items
+    cudaEvent_t ev_gathered = nullptr, ev_moments = nullptr;
     HydroScalars* scalars_h = nullptr;  // pinned copy, valid after the stream synchronises
 
     void evaluate(const ForceArgs& a, cudaStream_t s);

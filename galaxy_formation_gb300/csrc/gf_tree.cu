@@ -1184,7 +1184,8 @@ bool Octree::outgrowing() {
 
 // Node kernels cover node_cap and read the live node count on the device, so a refit stays
 // valid after a rebuild inside a captured graph (whose node count the host never sees).
-void Octree::refit(const double* pos, const double* mass, cudaStream_t s) {
+void Octree::refit(const double* pos, const double* mass, cudaStream_t s, cudaStream_t s_moments,
+                   cudaEvent_t gathered) {
     ProfScope ps(kStTreeRefit, s);
     const int grid = div_up(n, kThreads);
     const int span = std::max(node_cap, nn);
@@ -1195,6 +1196,11 @@ void Octree::refit(const double* pos, const double* mass, cudaStream_t s) {
     k_gather<<<grid, kThreads, 0, s>>>(n, perm.as<int>(), pos, mass, xbuild.as<double>(), pp, pd,
                                        want_knn ? plo.get<float4>(n) : nullptr, quad ? 1 : 0);
     GF_CHECK_LAUNCH();
+    if (s_moments) {  // the moments on their own stream, after the gather
+        GF_CUDA(cudaEventRecord(gathered, s));
+        GF_CUDA(cudaStreamWaitEvent(s_moments, gathered, 0));
+        s = s_moments;
+    }
     int* ctr = n_counter.as<int>();
     GF_CUDA(cudaMemsetAsync(ctr, 0, sizeof(int) * size_t(span), s));
     if (quad) {  // mixed form: straight into the walk layout

@@ -108,7 +108,11 @@ struct Octree {
     void reserve_graph_build();
     void deep_sort_attr();
     // Node kernels read the live node count on the device (valid after captured rebuilds).
-    void refit(const double* pos, const double* mass, cudaStream_t s);
+    // s_moments (with the event `gathered`): the moments run on that stream once the gathered
+    // positions are ready, and the caller joins it before reading them (the walk items, which
+    // need the positions only, can be prepared on s meanwhile).
+    void refit(const double* pos, const double* mass, cudaStream_t s, cudaStream_t s_moments = nullptr,
+               cudaEvent_t gathered = nullptr);
     // Work list of groups with at least one active particle (active may be null); chunk in
     // 1..kChunkMax cuts each group's active particles into items of <= chunk with their own
     // spheres; chunk in kChunkMax+1..kChunkCodeMax (active sets) merges runs of sibling groups
