@@ -13,7 +13,7 @@
 // (row group g, k group c) at byte offset (8 g + c) * 128, so the leading-dimension (K)
 // stride between core matrices is 128 bytes and the stride between row groups 1024 bytes.
 //
-// Every wait is bounded: a CTA whose MMA does not complete raises GF_ERR_CUDA in the status
+// Every wait is bounded: a CTA whose MMA does not complete raises GF_ERR_TIMEOUT in the status
 // word, waits once more (bounded) for the MMA in flight, frees its tensor memory and stops.
 #include <cuda_bf16.h>
 
@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_forward_tc(int n, const floa
         if (__syncthreads_or(!done)) {
             if (t == 0) {
                 S.fail = 1;
-                if (status) atomicOr(status, uint32_t(GF_ERR_CUDA));
+                if (status) atomicOr(status, uint32_t(GF_ERR_TIMEOUT));
             }
             mbar_wait_bounded(bar, phase);  // let an MMA in flight finish before the memory goes
             break;
