@@ -397,10 +397,23 @@ class Gpu:
             lib.gf_profile_stage(i, ctypes.byref(ms), ctypes.byref(cnt))
             if cnt.value:
                 stages[name] = {"ms_per_launch": ms.value / cnt.value, "launches": cnt.value}
+        # the gravity chain alone (no hydro stream beside it): what its stages cost without the
+        # contention of the neighbour search for the SMs (the step's stage times include it)
+        lib.gf_profile(1)
+        for _ in range(3):
+            self.step(theta, sph=0)
+            self.flush.zero_()
+        torch.cuda.synchronize()
+        alone = {}
+        for name in ("tree_build", "tree_sort", "tree_emit", "tree_moments", "group_prep", "walk"):
+            ms, cnt = ctypes.c_double(), ctypes.c_int()
+            lib.gf_profile_stage(L.STAGES.index(name), ctypes.byref(ms), ctypes.byref(cnt))
+            if cnt.value:
+                alone[name] = ms.value / cnt.value
         lib.gf_profile(0)
         st = np.zeros(9)
         lib.gf_force_stats(st, 9)
-        return {"theta": theta, "times_ms": times, "launches": launches, "stages": stages,
+        return {"theta": theta, "times_ms": times, "launches": launches, "stages": stages, "gravity_alone": alone,
                 "pairs": lib.gf_walk_pairs(), "qpairs": lib.gf_walk_quad_pairs(), "knn_iters": self.knn_iters(),
                 "nodes": int(st[8]), "autotune": tuned}
 
@@ -710,6 +723,10 @@ def run_gpu(args, world, rank, local):
                 "peak_source": "measured float32 FFMA throughput of this GPU (gf_fp32_peak)",
                 "work_per_launch": {"monopole_interactions": mono, "quadrupole_interactions": H["qpairs"],
                                     "flops_per_monopole": FLOPS_MONO, "flops_per_quadrupole": FLOPS_QUAD}}
+        t_alone = H["gravity_alone"].get("walk")
+        if t_alone:  # the same launch without the neighbour search beside it
+            roof["achieved_alone"] = flops / (t_alone * 1e-3) / 1e12
+            roof["frac_alone"] = roof["achieved_alone"] / fp32.value
     else:
         bytes_per_gas = {"knn": 24 + 48 * 4 + 8, "sph_density": 32 * 4 + 24 + 8 + 8 + 8,
                          "sph_force": 32 * 4 + 24 + 24 + 8 + 8 + 8 + 8 + 8 + 24 + 8 + 8,
@@ -790,6 +807,7 @@ def run_gpu(args, world, rank, local):
                            "previous h (learned MLP without one)"][hg],
                "grav_p99_rel_err_vs_f64_direct": r["p99"], "grav_median_rel_err": r["median"],
                "stages_ms": {k: round(v["ms_per_launch"], 4) for k, v in r["stages"].items()},
+               "gravity_chain_alone_ms": {k: round(v, 4) for k, v in r["gravity_alone"].items()},
                "knn_iterations_per_gas": r["knn_iters"], "walk_interactions": r["pairs"],
                "walk_quadrupole_interactions": r["qpairs"], "steps": len(r["times_ms"])}
         if r.get("autotune"):
