@@ -631,17 +631,6 @@ struct QuadSum {
         yz.add(3.f * m * dy * dz);
         tr.add(m * r2);
     }
-    // a child cell: its own moments (q, yt) plus the parallel-axis term of its mass m at d, added
-    // to each compensated sum as one term
-    __device__ __forceinline__ void cell(const float4 q, const float2 yt, float m, float dx, float dy, float dz) {
-        const float r2 = dx * dx + dy * dy + dz * dz;
-        xx.add(q.x + m * (3.f * dx * dx - r2));
-        yy.add(q.y + m * (3.f * dy * dy - r2));
-        xy.add(q.z + 3.f * m * dx * dy);
-        xz.add(q.w + 3.f * m * dx * dz);
-        yz.add(yt.x + 3.f * m * dy * dz);
-        tr.add(yt.y + m * r2);
-    }
 };
 
 // Mixed form: monopole and traceless quadrupole in one bottom-up pass, float32 with
@@ -669,119 +658,199 @@ struct RefitBfsArgs {
     const float* pdisp;  // null: no displacement (the build)
 };
 
-__device__ __forceinline__ float4 finalize_bfs(const RefitBfsArgs& A, int b, const KahanF& M, const KahanF& sx,
-                                               const KahanF& sy, const KahanF& sz, float dm) {
-    const float inv = M.s > 0.f ? 1.f / M.s : 0.f;
-    const float4 c = make_float4(sx.s * inv, sy.s * inv, sz.s * inv, M.s);
-    A.wa[b] = c;
-    const float4 g = A.wgeo[b];
-    const float ox = c.x - g.x, oy = c.y - g.y, oz = c.z - g.z;
+// Writes node b's monopole, opening radii and displacement bound (g: its cell, loaded early).
+__device__ __forceinline__ void finalize_bfs(const RefitBfsArgs& A, int b, const float4 g, float m, float cx,
+                                             float cy, float cz, float dm) {
+    A.wa[b] = make_float4(cx, cy, cz, m);
+    const float ox = cx - g.x, oy = cy - g.y, oz = cz - g.z;
     A.wb[b].x = 2.f * (g.w + dm) / A.theta + sqrtf(ox * ox + oy * oy + oz * oz);
-    const float2 rr = rel_radii(c.w, ox, oy, oz, g.w + dm);
+    const float2 rr = rel_radii(m, ox, oy, oz, g.w + dm);
     A.wb[b].w = rr.x;
     A.wrq[b] = rr.y;
     A.ndisp[b] = dm;
-    return c;
 }
 
-__global__ void k_refit_bfs_quad32(RefitBfsArgs A) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= live_nodes(A.span, A.nn_dev)) return;
-    const float4 wb = A.wb[b];
-    const int first = __float_as_int(wb.y), code = __float_as_int(wb.z);
-    if (code >= 0) return;  // internal: reached by the last of its children
-    const int cnt = -code;
-    if (cnt <= kLeafMax) {  // the leaf's particles loaded once, together (one memory latency)
-        float4 pp[kLeafMax];
-        float pd[kLeafMax];
+__device__ __forceinline__ float4 leaf_centre(const KahanF& M, const KahanF& sx, const KahanF& sy, const KahanF& sz) {
+    const float inv = M.s > 0.f ? 1.f / M.s : 0.f;
+    return make_float4(sx.s * inv, sy.s * inv, sz.s * inv, M.s);
+}
+
+// Compensated sum over the 8 lanes of an aligned lane group (all 32 lanes take part): Knuth's
+// two-sum at each of the three butterfly steps, the rounding errors carried in a second float.
+// Both lanes of a pair compute the same bits, so the 8 lanes end with identical values.
+__device__ __forceinline__ float group8_sum(float v) {
+    float s = v, e = 0.f;
 #pragma unroll
-        for (int t = 0; t < kLeafMax; ++t) {
-            pp[t] = t < cnt ? A.p4[first + t] : make_float4(0.f, 0.f, 0.f, 0.f);
-            pd[t] = t < cnt && A.pdisp ? A.pdisp[first + t] : 0.f;
-        }
-        KahanF M, sx, sy, sz;
-        float dm = 0.f;
-#pragma unroll
-        for (int t = 0; t < kLeafMax; ++t) {
-            if (t < cnt) {
-                M.add(pp[t].w);
-                sx.add(pp[t].w * pp[t].x);
-                sy.add(pp[t].w * pp[t].y);
-                sz.add(pp[t].w * pp[t].z);
-                dm = fmaxf(dm, pd[t]);
-            }
-        }
-        const float4 c = finalize_bfs(A, b, M, sx, sy, sz, dm);
-        QuadSum S;
-#pragma unroll
-        for (int t = 0; t < kLeafMax; ++t)
-            if (t < cnt) S.point(pp[t].w, pp[t].x - c.x, pp[t].y - c.y, pp[t].z - c.z);
-        A.wq[b] = make_float4(S.xx.s, S.yy.s, S.xy.s, S.xz.s);
-        A.wt[b] = make_float2(S.yz.s, S.tr.s);
-    } else {  // depth-48 leaves of coincident points
-        KahanF M, sx, sy, sz;
-        float dm = 0.f;
-        for (int i = first; i < first + cnt; ++i) {
-            const float4 p = A.p4[i];
-            M.add(p.w);
-            sx.add(p.w * p.x);
-            sy.add(p.w * p.y);
-            sz.add(p.w * p.z);
-            if (A.pdisp) dm = fmaxf(dm, A.pdisp[i]);
-        }
-        const float4 c = finalize_bfs(A, b, M, sx, sy, sz, dm);
-        QuadSum S;
-        for (int i = first; i < first + cnt; ++i) {
-            const float4 p = A.p4[i];
-            S.point(p.w, p.x - c.x, p.y - c.y, p.z - c.z);
-        }
-        A.wq[b] = make_float4(S.xx.s, S.yy.s, S.xy.s, S.xz.s);
-        A.wt[b] = make_float2(S.yz.s, S.tr.s);
+    for (int off = 4; off; off >>= 1) {
+        const float o = __shfl_xor_sync(0xffffffffu, s, off);
+        const float oe = __shfl_xor_sync(0xffffffffu, e, off);
+        const float t = s + o;
+        const float bp = t - s;
+        const float err = (s - (t - bp)) + (o - bp);
+        s = t;
+        e = (e + oe) + err;
     }
-    // Climb: the arrival counter is an acquire-release atomic (it publishes this node's records
-    // and, for the last child, makes its siblings' records visible), issued together with the
-    // loads of the parent's child range and of the next parent.
-    int p = A.wparent[b];
-    while (p >= 0) {
-        const int* pbi = reinterpret_cast<const int*>(A.wb) + 4 * size_t(p);
-        const int c0 = __ldg(pbi + 1), nc = __ldg(pbi + 2);  // structure fields: constant here
-        const int pnext = A.wparent[p];
-        const int arrived = atom_add_acq_rel(&A.counter[p], 1);
-        if (arrived != nc - 1) return;
-        float4 cm[8];
-        float dmc[8];
+    return s + e;
+}
+
+__device__ __forceinline__ float group8_max(float v) {
 #pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            if (c < nc) {
-                cm[c] = __ldcg(&A.wa[c0 + c]);
-                dmc[c] = __ldcg(&A.ndisp[c0 + c]);
-            }
+    for (int off = 4; off; off >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, off));
+    return v;
+}
+
+// The arrival of a finished node at its parent p (child range c0, nc: structure fields, loaded
+// before the atomic). The counter is an acquire-release atomic: it publishes this thread's
+// records of the node and, for the last child, makes its siblings' records visible. Returns
+// whether this arrival completed p.
+__device__ __forceinline__ bool arrive(const RefitBfsArgs& A, int p, int nc) {
+    return atom_add_acq_rel(&A.counter[p], 1) == nc - 1;
+}
+
+// Threads take the nodes from the end of the breadth-first layout (the deepest first), so the
+// deep subtrees are summed and climbed by the first blocks and the last blocks hold the shallow
+// nodes, whose climbs to the root are short. A leaf's thread sums its particles (sequential
+// Kahan sums); a parent is combined by a group of 8 lanes of the warp whose lane completed it,
+// lane c loading child c, so that all of a parent's records arrive with one memory latency and
+// the sums are pairwise with compensation. 64 registers: 4 blocks per SM.
+__global__ void __launch_bounds__(kThreads, 4) k_refit_bfs_quad32(RefitBfsArgs A) {
+    const int b = live_nodes(A.span, A.nn_dev) - 1 - int(blockIdx.x * blockDim.x + threadIdx.x);
+    const int lane = threadIdx.x & 31;
+    int p = -1, pc0 = 0, pnc = 0;  // a parent that this lane's arrival completed, its child range
+    const float4 wb = b >= 0 ? A.wb[b] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int first = __float_as_int(wb.y), code = __float_as_int(wb.z);
+    if (b >= 0 && code < 0) {  // a leaf (internal nodes are reached by the climb)
+        const int cnt = -code;
+        const float4 g = __ldg(&A.wgeo[b]);
+        const int par = __ldg(&A.wparent[b]);
+        int c0 = 0, nc = 0;
+        if (par >= 0) {
+            const int* pbi = reinterpret_cast<const int*>(A.wb) + 4 * size_t(par);
+            c0 = __ldg(pbi + 1);
+            nc = __ldg(pbi + 2);
         }
-        KahanF M, sx, sy, sz;
-        float dm = 0.f;
-#pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            if (c < nc) {
-                M.add(cm[c].w);
-                sx.add(cm[c].w * cm[c].x);
-                sy.add(cm[c].w * cm[c].y);
-                sz.add(cm[c].w * cm[c].z);
-                dm = fmaxf(dm, dmc[c]);
-            }
-        }
-        const float4 cp = finalize_bfs(A, p, M, sx, sy, sz, dm);
         QuadSum S;
+        if (cnt <= kLeafMax) {  // the leaf's particles loaded once, together (one memory latency)
+            float4 pp[kLeafMax];
+            float pd[kLeafMax];
 #pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            if (c < nc) {
-                const float4 qc = __ldcg(&A.wq[c0 + c]);
-                const float2 yt = __ldcg(&A.wt[c0 + c]);
-                S.cell(qc, yt, cm[c].w, cm[c].x - cp.x, cm[c].y - cp.y, cm[c].z - cp.z);
+            for (int t = 0; t < kLeafMax; ++t) {
+                pp[t] = t < cnt ? A.p4[first + t] : make_float4(0.f, 0.f, 0.f, 0.f);
+                pd[t] = t < cnt && A.pdisp ? A.pdisp[first + t] : 0.f;
+            }
+            KahanF M, sx, sy, sz;
+            float dm = 0.f;
+#pragma unroll
+            for (int t = 0; t < kLeafMax; ++t) {
+                if (t < cnt) {
+                    M.add(pp[t].w);
+                    sx.add(pp[t].w * pp[t].x);
+                    sy.add(pp[t].w * pp[t].y);
+                    sz.add(pp[t].w * pp[t].z);
+                    dm = fmaxf(dm, pd[t]);
+                }
+            }
+            const float4 c = leaf_centre(M, sx, sy, sz);
+            finalize_bfs(A, b, g, c.w, c.x, c.y, c.z, dm);
+#pragma unroll
+            for (int t = 0; t < kLeafMax; ++t)
+                if (t < cnt) S.point(pp[t].w, pp[t].x - c.x, pp[t].y - c.y, pp[t].z - c.z);
+        } else {  // depth-48 leaves of coincident points
+            KahanF M, sx, sy, sz;
+            float dm = 0.f;
+            for (int i = first; i < first + cnt; ++i) {
+                const float4 q = A.p4[i];
+                M.add(q.w);
+                sx.add(q.w * q.x);
+                sy.add(q.w * q.y);
+                sz.add(q.w * q.z);
+                if (A.pdisp) dm = fmaxf(dm, A.pdisp[i]);
+            }
+            const float4 c = leaf_centre(M, sx, sy, sz);
+            finalize_bfs(A, b, g, c.w, c.x, c.y, c.z, dm);
+            for (int i = first; i < first + cnt; ++i) {
+                const float4 q = A.p4[i];
+                S.point(q.w, q.x - c.x, q.y - c.y, q.z - c.z);
             }
         }
-        A.wq[p] = make_float4(S.xx.s, S.yy.s, S.xy.s, S.xz.s);
-        A.wt[p] = make_float2(S.yz.s, S.tr.s);
-        p = pnext;
+        A.wq[b] = make_float4(S.xx.s, S.yy.s, S.xy.s, S.xz.s);
+        A.wt[b] = make_float2(S.yz.s, S.tr.s);
+        if (par >= 0 && arrive(A, par, nc)) {
+            p = par;
+            pc0 = c0;
+            pnc = nc;
+        }
+    }
+    // Climb. Each round the four groups of 8 lanes take up to four of the warp's completed
+    // parents (group k the one held by the k-th lane holding one); the group's lane 0 writes
+    // the parent and arrives at the grandparent, and a completed grandparent goes back to the
+    // lane that held the parent. Each round serves at least one parent and a parent precedes
+    // its children in the layout, so the loop ends.
+    const int grp = lane >> 3, c = lane & 7;
+    for (;;) {
+        const unsigned pend = __ballot_sync(0xffffffffu, p >= 0);
+        if (pend == 0u) break;
+        unsigned rest = pend;  // the holders from the grp-th on (lowest lanes first)
+        for (int k = 0; k < grp; ++k) rest &= rest - 1u;
+        const int src = rest ? __ffs(int(rest)) - 1 : 0;
+        int q = __shfl_sync(0xffffffffu, p, src);
+        const int q0 = __shfl_sync(0xffffffffu, pc0, src);
+        const int qn = __shfl_sync(0xffffffffu, pnc, src);
+        if (!rest) q = -1;
+        __syncwarp();  // orders the holder's acquiring arrival before its group's loads
+        float4 cm = make_float4(0.f, 0.f, 0.f, 0.f), qc = cm, g = cm;
+        float2 yt = make_float2(0.f, 0.f);
+        float dmc = 0.f;
+        int gp = -1, gc0 = 0, gnc = 0;
+        if (q >= 0) {
+            if (c < qn) {
+                cm = __ldcg(&A.wa[q0 + c]);
+                dmc = __ldcg(&A.ndisp[q0 + c]);
+                qc = __ldcg(&A.wq[q0 + c]);
+                yt = __ldcg(&A.wt[q0 + c]);
+            }
+            if (c == 0) {
+                g = __ldg(&A.wgeo[q]);
+                gp = __ldg(&A.wparent[q]);
+                if (gp >= 0) {
+                    const int* pbi = reinterpret_cast<const int*>(A.wb) + 4 * size_t(gp);
+                    gc0 = __ldg(pbi + 1);
+                    gnc = __ldg(pbi + 2);
+                }
+            }
+        }
+        // children past qn (and groups without a parent) add zeros
+        const float M = group8_sum(cm.w);
+        const float sx = group8_sum(cm.w * cm.x), sy = group8_sum(cm.w * cm.y), sz = group8_sum(cm.w * cm.z);
+        const float dm = group8_max(dmc);
+        const float inv = M > 0.f ? 1.f / M : 0.f;
+        const float cx = sx * inv, cy = sy * inv, cz = sz * inv;
+        const float dx = cm.x - cx, dy = cm.y - cy, dz = cm.z - cz;
+        const float r2 = dx * dx + dy * dy + dz * dz, m = cm.w;
+        const float xx = group8_sum(qc.x + m * (3.f * dx * dx - r2));
+        const float yy = group8_sum(qc.y + m * (3.f * dy * dy - r2));
+        const float xy = group8_sum(qc.z + 3.f * m * dx * dy);
+        const float xz = group8_sum(qc.w + 3.f * m * dx * dz);
+        const float yz = group8_sum(yt.x + 3.f * m * dy * dz);
+        const float tr = group8_sum(yt.y + m * r2);
+        int np = -1;
+        if (q >= 0 && c == 0) {
+            finalize_bfs(A, q, g, M, cx, cy, cz, dm);
+            A.wq[q] = make_float4(xx, yy, xy, xz);
+            A.wt[q] = make_float2(yz, tr);
+            if (gp >= 0 && arrive(A, gp, gnc)) np = gp;
+        }
+        // back to the holders: the k-th holder (k < 4) was served by group k
+        const int rank = __popc(pend & lanemask_lt());
+        const int from = 8 * min(rank, 3);
+        const int np_ = __shfl_sync(0xffffffffu, np, from);
+        const int nc0_ = __shfl_sync(0xffffffffu, gc0, from);
+        const int nnc_ = __shfl_sync(0xffffffffu, gnc, from);
+        if (p >= 0 && rank < 4) {
+            p = np_;
+            pc0 = nc0_;
+            pnc = nnc_;
+        }
     }
 }
 
