@@ -186,23 +186,18 @@ __global__ void k_scatter_f(int ng, const int* __restrict__ gidx, const float* _
     if (subset_item(sub, i, ng, nullptr, i)) out[gidx[i]] = v[i];
 }
 
-// gas-local flags of the particles due, in the visiting order (order: position -> particle)
-__global__ void k_flag_in_order(int ng, const int* __restrict__ order, const uint8_t* __restrict__ gact,
-                                int* __restrict__ flag) {
+// gas-local flags of the particles due (active: per particle), in the visiting order (order:
+// position -> gas-local index)
+__global__ void k_flag_in_order(int ng, const int* __restrict__ order, const int* __restrict__ gidx,
+                                const uint8_t* __restrict__ active, int* __restrict__ flag) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < ng) flag[t] = gact[order ? order[t] : t] ? 1 : 0;
+    if (t < ng) flag[t] = active[gidx[order ? order[t] : t]] ? 1 : 0;
 }
 
 __global__ void k_compact(int ng, const int* __restrict__ order, const int* __restrict__ flag,
                           const int* __restrict__ scan, int* __restrict__ list) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < ng && flag[t]) list[scan[t]] = order ? order[t] : t;
-}
-
-__global__ void k_gas_active(int ng, const int* __restrict__ gidx, const uint8_t* __restrict__ active,
-                             uint8_t* __restrict__ gact) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < ng) gact[i] = active[gidx[i]];
 }
 
 __global__ void k_fill(int n, double* __restrict__ a, double v) {
@@ -483,14 +478,11 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
     // partial: the gas due, compacted in the visiting order of the last neighbour-search tree
     Subset sub;
     if (partial) {
-        uint8_t* ga = gact.get<uint8_t>(ng);
-        k_gas_active<<<ggrid, kThreads, 0, s>>>(ng, gi, a.sph_active, ga);
-        GF_CHECK_LAUNCH();
         const int* vorder = order_ng == ng ? knn_tree.perm.as<int>() : nullptr;
         int* fl2 = aflag.get<int>(ng);
         int* sc2 = ascan.get<int>(ng);
         int* lst = alist.get<int>(ng);
-        k_flag_in_order<<<ggrid, kThreads, 0, s>>>(ng, vorder, ga, fl2);
+        k_flag_in_order<<<ggrid, kThreads, 0, s>>>(ng, vorder, gi, a.sph_active, fl2);
         GF_CHECK_LAUNCH();
         exclusive_scan(fl2, sc2, ng, &sc->nact, s, &hscratch);
         k_compact<<<ggrid, kThreads, 0, s>>>(ng, vorder, fl2, sc2, lst);

@@ -81,7 +81,7 @@ struct ForceEngine {
     DevBuf acc_grav, acc_sph, dt_courant, h_prev, row, loc, cache, cgidx;
     DevBuf flag, scan, gidx, gpos, gvel, gmass, gu_, nb48, dsel, rguess, h, rho, gacc, dudt, dt_i;
     DevBuf scalars;
-    DevBuf divv_prev, gdivv, hX, hY, hrg, hdk, colX, colT, gact, aflag, ascan, alist;
+    DevBuf divv_prev, gdivv, hX, hY, hrg, hdk, colX, colT, aflag, ascan, alist;
     ScanScratch hscratch;    // scans of the hydro stream
     cudaStream_t s2 = nullptr;               // the hydro chain's stream
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -109,7 +109,6 @@ struct ForceEngine {
         grav.reserve_graph_build();
         reserve_scan_sort(n, &hscratch);
         if (ng > 0) {
-            gact.get<uint8_t>(ng);
             aflag.get<int>(ng);
             ascan.get<int>(ng);
             alist.get<int>(ng);

@@ -265,12 +265,38 @@ __global__ void k_kick_levels(int n, double* __restrict__ vel, const double* __r
     for (int c = 0; c < 3; ++c) vel[3 * size_t(i) + c] += h * acc[3 * size_t(i) + c];
 }
 
-__global__ void k_drift_bits(int n, double* __restrict__ pos, const double* __restrict__ vel,
-                             const unsigned long long* __restrict__ dbits) {
+// One pass between two sub-steps of a block: the kick of the particles due at sub-step s_kick
+// (k_kick_levels' mode 1; s_kick 0: none), the drift of everybody by the finest step with the
+// kicked velocities, and the flags of the particles due at sub-step s_next with their count
+// (act null: none). The same float64 operations, in the same order, as the three kernels.
+__global__ void k_kick_drift_active(int n, double* __restrict__ pos, double* __restrict__ vel,
+                                    const double* __restrict__ acc, const int8_t* __restrict__ level,
+                                    const unsigned long long* __restrict__ dbits, int s_kick, int s_next,
+                                    uint8_t* __restrict__ act, unsigned long long* __restrict__ count) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double dt = __longlong_as_double((long long)*dbits);
-    for (int c = 0; c < 3; ++c) pos[3 * size_t(i) + c] += dt * vel[3 * size_t(i) + c];
+    bool a = false;
+    if (i < n) {
+        const int j = level[i];
+        const double dt = __longlong_as_double((long long)*dbits);
+        double v[3];
+        for (int c = 0; c < 3; ++c) v[c] = vel[3 * size_t(i) + c];
+        if (s_kick > 0 && !(s_kick & ((1 << j) - 1))) {
+            const double step = dt * double(1 << j);
+            for (int c = 0; c < 3; ++c) {
+                v[c] += step * acc[3 * size_t(i) + c];
+                vel[3 * size_t(i) + c] = v[c];
+            }
+        }
+        for (int c = 0; c < 3; ++c) pos[3 * size_t(i) + c] += dt * v[c];
+        if (act) {
+            a = !(s_next & ((1 << j) - 1));
+            act[i] = a;
+        }
+    }
+    if (act) {
+        const unsigned m = __ballot_sync(0xffffffffu, a);
+        if ((threadIdx.x & 31) == 0 && m) atomicAdd(count, (unsigned long long)__popc(m));
+    }
 }
 
 __global__ void k_active_at(int n, const int8_t* __restrict__ level, int s, uint8_t* __restrict__ act,
@@ -377,19 +403,20 @@ struct BlockIntegrator {
         GF_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeGlobal));
         g_no_alloc = true;
         try {
+            // each sub-step opens with the kick of the previous one's particles due, the drift
+            // and the flags of its own particles due, in one pass
             for (int sub = 1; sub < nsub(); ++sub) {
-                k_drift_bits<<<div_up(S.n, 256), 256, 0, s>>>(S.n, S.pos.as<double>(), S.vel.as<double>(), d);
-                GF_CHECK_LAUNCH();
-                k_active_at<<<div_up(S.n, 256), 256, 0, s>>>(S.n, level.as<int8_t>(), sub, ac, d + 1);
+                k_kick_drift_active<<<div_up(S.n, 256), 256, 0, s>>>(S.n, S.pos.as<double>(), S.vel.as<double>(),
+                                                                     S.acc.as<double>(), level.as<int8_t>(), d,
+                                                                     sub - 1, sub, ac, d + 1);
                 GF_CHECK_LAUNCH();
                 const bool rb = tune.rebuild_every > 0 && sub % tune.rebuild_every == 0;
                 thermo_at(S, sub);
                 force(S, ac, true, rb, tune.chunk[bin_of(sub)], tune.npl[bin_of(sub)], tune.shape[bin_of(sub)]);
-                k_kick_levels<<<div_up(S.n, 256), 256, 0, s>>>(S.n, S.vel.as<double>(), S.acc.as<double>(),
-                                                               level.as<int8_t>(), d, 1, sub);
-                GF_CHECK_LAUNCH();
             }
-            k_drift_bits<<<div_up(S.n, 256), 256, 0, s>>>(S.n, S.pos.as<double>(), S.vel.as<double>(), d);
+            k_kick_drift_active<<<div_up(S.n, 256), 256, 0, s>>>(S.n, S.pos.as<double>(), S.vel.as<double>(),
+                                                                 S.acc.as<double>(), level.as<int8_t>(), d,
+                                                                 nsub() - 1, 0, nullptr, nullptr);
             GF_CHECK_LAUNCH();
         } catch (...) {
             g_no_alloc = false;

@@ -216,14 +216,13 @@ __global__ void k_item_flag(const int* __restrict__ groups, const int4* __restri
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const int ng = cnt->num_groups;
-    for (int g = wid; g < span; g += nw) {
-        int f = 0;
-        if (g < ng) {
-            int b, len;
-            f = cut_at(groups, n_i4, parent, gw, ng, merge, g, b, len) > 0 ? 1 : 0;
-        }
+    for (int g = wid; g < ng; g += nw) {
+        int b, len;
+        const int f = cut_at(groups, n_i4, parent, gw, ng, merge, g, b, len) > 0 ? 1 : 0;
         if (lane == 0) flag[g] = f;
     }
+    // past the live groups (the scan covers span): zeros, a thread per entry
+    for (int t = ng + blockIdx.x * blockDim.x + threadIdx.x; t < span; t += gridDim.x * blockDim.x) flag[t] = 0;
 }
 
 // The merged items in tree order: item of group g at slot[g] (the scan of the flags). An item
@@ -887,8 +886,13 @@ void Octree::prepare_walk(const uint8_t* active, cudaStream_t s, int chunk, cons
     walk_stride = 1;
     // The grid also fixes the order of this work list (each warp appends its groups' items as
     // it goes), which the walk follows; 4 blocks per SM was the best of 2 to 8 for the merged
-    // items before they were written in tree order.
-    k_group_prep<<<4 * C.sms, 256, 0, s>>>(groups.as<int>(), n_i4.as<int4>(), p4.as<float4>(),
+    // items before they were written in tree order. Items of an active set: as many blocks as
+    // fit on the SMs, so that the warps' passes over the groups (most without a particle due)
+    // are short.
+    static int prep_fit = 0;
+    if (!prep_fit) GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&prep_fit, k_group_prep, 256, 0));
+    const int prep_blocks = (active && chunk > 0 ? std::max(prep_fit, 4) : 4) * C.sms;
+    k_group_prep<<<prep_blocks, 256, 0, s>>>(groups.as<int>(), n_i4.as<int4>(), p4.as<float4>(),
                                           perm.as<int>(), active, cnt, work.get<int4>(cap),
                                           sphere.get<float4>(cap), active ? chunk : 0,
                                           quad && alpha > 0.f ? aold : nullptr, alpha, alpha_q,
