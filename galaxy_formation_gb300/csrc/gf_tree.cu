@@ -434,10 +434,13 @@ __global__ void k_leaf_sort(int span, const int* __restrict__ nn_dev, const int4
     }
 }
 
+// Positions (and masses) in tree order: p4 = float32 position and mass, plo = the float32
+// remainders. The build saves the float64 positions in tree order (xsave); a refit measures each
+// particle's displacement since the build against them (xbuild, tree order: coalesced reads).
 __global__ void k_gather(int n, const int* __restrict__ perm, const double* __restrict__ pos,
                          const double* __restrict__ mass, const double* __restrict__ xbuild,
                          float4* __restrict__ p4, float* __restrict__ pdisp, float4* __restrict__ plo,
-                         int disp32 = 0) {
+                         int disp32 = 0, double* __restrict__ xsave = nullptr) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int j = perm[i];
@@ -446,14 +449,19 @@ __global__ void k_gather(int n, const int* __restrict__ perm, const double* __re
     const float fx = float(x), fy = float(y), fz = float(z);
     p4[i] = make_float4(fx, fy, fz, float(m));
     if (plo) plo[i] = make_float4(float(x - double(fx)), float(y - double(fy)), float(z - double(fz)), 0.f);
+    if (xsave) {
+        xsave[3 * size_t(i)] = x;
+        xsave[3 * size_t(i) + 1] = y;
+        xsave[3 * size_t(i) + 2] = z;
+    }
     if (pdisp && disp32) {  // mixed form: float64 differences, float32 length
-        const float dx = float(x - xbuild[3 * size_t(j)]), dy = float(y - xbuild[3 * size_t(j) + 1]),
-                    dz = float(z - xbuild[3 * size_t(j) + 2]);
+        const float dx = float(x - xbuild[3 * size_t(i)]), dy = float(y - xbuild[3 * size_t(i) + 1]),
+                    dz = float(z - xbuild[3 * size_t(i) + 2]);
         pdisp[i] = m > 0 ? sqrtf(dx * dx + dy * dy + dz * dz) : 0.0f;
     } else if (pdisp) {  // refit: displacement since the build (cpp/nbody.cpp:273-275)
-        const double dx = __dsub_rn(x, xbuild[3 * size_t(j)]);
-        const double dy = __dsub_rn(y, xbuild[3 * size_t(j) + 1]);
-        const double dz = __dsub_rn(z, xbuild[3 * size_t(j) + 2]);
+        const double dx = __dsub_rn(x, xbuild[3 * size_t(i)]);
+        const double dy = __dsub_rn(y, xbuild[3 * size_t(i) + 1]);
+        const double dz = __dsub_rn(z, xbuild[3 * size_t(i) + 2]);
         pdisp[i] = m > 0 ? float(__dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
                                                       __dmul_rn(dz, dz))))
                          : 0.0f;
@@ -1157,11 +1165,10 @@ void Octree::build(int n_, const double* pos, const double* mass, double theta, 
     GF_CHECK_LAUNCH();
 
     float4* pp = p4.get<float4>(n);
-    k_gather<<<grid, kThreads, 0, s>>>(n, pm, pos, mass, nullptr, pp, nullptr,
-                                       want_knn ? plo.get<float4>(n) : nullptr);
-    GF_CHECK_LAUNCH();
     double* xb = xbuild.get<double>(3 * size_t(n));
-    GF_CUDA(cudaMemcpyAsync(xb, pos, sizeof(double) * 3 * size_t(n), cudaMemcpyDeviceToDevice, s));
+    k_gather<<<grid, kThreads, 0, s>>>(n, pm, pos, mass, nullptr, pp, nullptr,
+                                       want_knn ? plo.get<float4>(n) : nullptr, 0, xb);
+    GF_CHECK_LAUNCH();
 
     float4* mom = n_mom.get<float4>(cap);
     float* opr = n_open.get<float>(cap);
