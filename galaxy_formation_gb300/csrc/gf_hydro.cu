@@ -34,21 +34,31 @@ __global__ void k_gas_flag(int n, const int8_t* __restrict__ kind, int* __restri
     if (i < n) flag[i] = kind[i] == 0 ? 1 : 0;
 }
 
+// The gas in gas-local order; with ghi/glo also its positions as float32 hi + lo pairs
+// (x = float(x) + float(x - float(x))), for the float32 neighbour reselection.
 __global__ void k_gas_gather(int n, const int* __restrict__ flag, const int* __restrict__ scan,
                              const double* __restrict__ pos, const double* __restrict__ vel,
                              const double* __restrict__ mass, const double* __restrict__ u,
                              int* __restrict__ gidx, double* __restrict__ gpos, double* __restrict__ gvel,
-                             double* __restrict__ gmass, double* __restrict__ gu) {
+                             double* __restrict__ gmass, double* __restrict__ gu, float4* __restrict__ ghi,
+                             float4* __restrict__ glo) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || !flag[i]) return;
     const int g = scan[i];
     gidx[g] = i;
+    double x[3];
     for (int a = 0; a < 3; ++a) {
-        gpos[3 * size_t(g) + a] = pos[3 * size_t(i) + a];
+        x[a] = pos[3 * size_t(i) + a];
+        gpos[3 * size_t(g) + a] = x[a];
         gvel[3 * size_t(g) + a] = vel[3 * size_t(i) + a];
     }
     gmass[g] = mass[i];
     gu[g] = u[i];
+    if (ghi) {
+        const float fx = float(x[0]), fy = float(x[1]), fz = float(x[2]);
+        ghi[g] = make_float4(fx, fy, fz, 0.f);
+        glo[g] = make_float4(float(x[0] - double(fx)), float(x[1] - double(fy)), float(x[2] - double(fz)), 0.f);
+    }
 }
 
 // loc[global] = local gas index (loc preset to -1); fails when a gas particle has no cache row
@@ -129,6 +139,106 @@ __global__ void __launch_bounds__(kSelWarps * 32) k_verlet_select(
     }
 }
 
+// Float64 squared distance of gas particles i and j (gas-local), rounded as NumPy sums the three
+// squares: (dx^2 + dy^2) + dz^2.
+__device__ __forceinline__ double gas_d2(const double* __restrict__ gpos, int i, int j) {
+    const double dx = __dsub_rn(gpos[3 * size_t(i)], gpos[3 * size_t(j)]);
+    const double dy = __dsub_rn(gpos[3 * size_t(i) + 1], gpos[3 * size_t(j) + 1]);
+    const double dz = __dsub_rn(gpos[3 * size_t(i) + 2], gpos[3 * size_t(j) + 2]);
+    return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+}
+
+// The same reselection for the float32 SPH of the mixed form, in float32: the candidates'
+// squared distances from hi + lo positions (~1e-7 relative error), sorted as (float32 d^2,
+// slot) keys. Only the candidates within float32 rounding of the 32nd are measured in float64,
+// so the set of the 32 nearest is the float64 one; the neighbour that fixes h is returned in
+// sel (its float64 distance is taken by k_smoothing, a thread per particle, instead of
+// warp-uniformly here: the float64 pipe is narrow on this GPU). The 32 come out in float32
+// order (only float32 near-ties can swap with respect to the float64 order).
+__global__ void __launch_bounds__(kSelWarps * 32) k_verlet_select32(
+    int ng, const int* __restrict__ gidx, const int* __restrict__ row, const int* __restrict__ cache,
+    const int* __restrict__ cgidx, const int* __restrict__ loc, const float4* __restrict__ ghi,
+    const float4* __restrict__ glo, const double* __restrict__ gpos, int* __restrict__ nb, int* __restrict__ sel,
+    int* __restrict__ fail, Subset sub) {
+    __shared__ unsigned long long s_key[kSelWarps][64];  // (float32 d^2 bits << 32) | slot
+    __shared__ unsigned long long s_dd[kSelWarps][64];   // float64 d^2 bits of the boundary band
+    __shared__ int s_di[kSelWarps][64];
+    __shared__ int s_loc[kSelWarps][64];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int q = blockIdx.x * kSelWarps + w;; q += gridDim.x * kSelWarps) {
+        int i;
+        if (!subset_item(sub, q, ng, nullptr, i)) break;
+        const int r = row[gidx[i]];
+        if (r < 0) continue;  // handled by k_verlet_prep's flag
+        const float4 hi_i = ghi[i], lo_i = glo[i];
+        int valid = 0;
+        for (int jj = lane; jj < 64; jj += 32) {
+            unsigned long long key = ~0ull;
+            int j = -1;
+            if (jj < kCand) {
+                const int c = cache[size_t(r) * kCand + jj];
+                j = c < 0 ? -1 : loc ? loc[cgidx[c]] : c;
+                if (j >= 0) {
+                    const float4 hj = ghi[j], lj = glo[j];
+                    const float dx = (hi_i.x - hj.x) + (lo_i.x - lj.x);
+                    const float dy = (hi_i.y - hj.y) + (lo_i.y - lj.y);
+                    const float dz = (hi_i.z - hj.z) + (lo_i.z - lj.z);
+                    key = ((unsigned long long)__float_as_uint(dx * dx + dy * dy + dz * dz) << 32) | unsigned(jj);
+                    ++valid;
+                }
+            }
+            s_key[w][jj] = key;
+            s_loc[w][jj] = j;
+        }
+        valid = warp_sum(valid);
+        __syncwarp();
+        if (valid < kNgb) {
+            if (lane == 0) *fail = 1;
+            continue;
+        }
+        warp_sort_u64(s_key[w], 64);
+        // the boundary: entries within float32 rounding of the 32nd (the unused slots' keys
+        // read as NaN and fall in neither count)
+        constexpr int c = kNgb - 1;
+        const float dc = __uint_as_float(unsigned(s_key[w][c] >> 32));
+        const float blo = dc * (1.0f - 2e-5f), bhi = dc * (1.0f + 2e-5f);
+        int below = 0, inband = 0;
+        for (int t = lane; t < 64; t += 32) {
+            const float v = __uint_as_float(unsigned(s_key[w][t] >> 32));
+            below += v < blo;
+            inband += v >= blo && v <= bhi;
+        }
+        below = warp_sum(below);
+        inband = warp_sum(inband);
+        int selj;
+        if (inband == 1) {
+            selj = s_loc[w][unsigned(s_key[w][c]) & 63u];
+        } else {  // re-measure the band in float64; its entries take the float64 order
+            for (int t = lane; t < 64; t += 32) {
+                double v = INFINITY;
+                int tag = 0x7fffffff;
+                const float vf = __uint_as_float(unsigned(s_key[w][t] >> 32));
+                if (vf >= blo && vf <= bhi) {
+                    tag = int(unsigned(s_key[w][t]) & 63u);
+                    v = gas_d2(gpos, i, s_loc[w][tag]);
+                }
+                s_dd[w][t] = (unsigned long long)__double_as_longlong(v);
+                s_di[w][t] = tag;
+            }
+            __syncwarp();
+            warp_bitonic(s_dd[w], s_di[w], 64);
+            selj = s_loc[w][s_di[w][max(0, c - below)]];
+            if (below + inband <= 64)
+                for (int t = lane; t < inband; t += 32)
+                    s_key[w][below + t] = (s_key[w][below + t] & 0xffffffff00000000ull) | unsigned(s_di[w][t]);
+            __syncwarp();
+        }
+        nb[size_t(i) * kCand + lane] = s_loc[w][unsigned(s_key[w][lane]) & 63u];
+        if (lane == 0) sel[i] = selj;
+        __syncwarp();
+    }
+}
+
 // one thread per cache entry (coalesced rows of 48 local indices; cgidx keeps the local ->
 // global map of the caching call)
 // The full search wrote its candidates straight into the cache (kq columns of kCand); this
@@ -151,13 +261,23 @@ __global__ void k_guess(int ng, const int* __restrict__ gidx, const double* __re
     rg[i] = float(2.5 * hprev[gidx[i]]);
 }
 
-__global__ void k_smoothing(int ng, const double* __restrict__ d31, double eps, const int* __restrict__ gidx,
-                            double* __restrict__ h, double* __restrict__ hprev, Subset sub) {
+// h from the distance of the 32nd neighbour: d31, or (sel) measured here in float64 to the
+// neighbour sel[i] and stored into d31.
+__global__ void k_smoothing(int ng, double* __restrict__ d31, double eps, const int* __restrict__ gidx,
+                            double* __restrict__ h, double* __restrict__ hprev, Subset sub,
+                            const int* __restrict__ sel = nullptr, const double* __restrict__ gpos = nullptr) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (!subset_item(sub, i, ng, nullptr, i)) return;
-    const double v = fmax(0.5 * d31[i], 0.5 * eps);  // simulation.py:84
+    double d;
+    if (sel) {
+        d = __dsqrt_rn(gas_d2(gpos, i, sel[i]));
+        d31[i] = d;
+    } else {
+        d = d31[i];
+    }
+    const double v = fmax(0.5 * d, 0.5 * eps);  // simulation.py:84
     h[i] = v;
-    hprev[gidx[i]] = 0.5 * d31[i] > 0 ? 0.5 * d31[i] : v;
+    hprev[gidx[i]] = 0.5 * d > 0 ? 0.5 * d : v;
 }
 
 // Training pairs: the features and the log distance of the 48th nearest (the radius the
@@ -469,7 +589,11 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
     double* gm = gmass.get<double>(ng);
     double* gu = gu_.get<double>(ng);
     if (a.late_inputs) GF_CUDA(cudaStreamWaitEvent(s, a.late_inputs, 0));
-    k_gas_gather<<<grid, kThreads, 0, s>>>(n, fl, sc_, a.pos, a.vel, a.mass, a.u, gi, gp, gv, gm, gu);
+    // the mixed form reselects neighbours from float32 hi + lo positions
+    const bool sel32 = sph_float32 && !a.fresh_nb && cache_valid;
+    float4* ghi_ = sel32 ? ghi.get<float4>(ng) : nullptr;
+    float4* glo_ = sel32 ? glo.get<float4>(ng) : nullptr;
+    k_gas_gather<<<grid, kThreads, 0, s>>>(n, fl, sc_, a.pos, a.vel, a.mass, a.u, gi, gp, gv, gm, gu, ghi_, glo_);
     GF_CHECK_LAUNCH();
 
     const int ggrid = div_up(ng, kThreads);
@@ -490,6 +614,7 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
         sub = Subset{lst, &sc->nact};
     }
     bool have_nb = false;
+    int* vsel_ = nullptr;  // float32 reselection: the neighbour that fixes each h
     if (!a.fresh_nb && cache_valid) {
         // inside a captured block the gas set is the cached one: local index == cache row
         int* lc = a.nosync ? row.as<int>() : loc.as<int>();
@@ -501,8 +626,16 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
         }
         const int blocks = std::min(div_up(ng, kSelWarps), 16 * ctx().sms);
         ProfScope pv(kStVerlet, s);
-        k_verlet_select<<<blocks, kSelWarps * 32, 0, s>>>(ng, gi, row.as<int>(), cache.as<int>(), cgidx.as<int>(),
-                                                          a.nosync ? nullptr : lc, gp, nb, d31, &sc->fail, sub);
+        if (sel32) {
+            vsel_ = vsel.get<int>(ng);
+            k_verlet_select32<<<blocks, kSelWarps * 32, 0, s>>>(ng, gi, row.as<int>(), cache.as<int>(),
+                                                                cgidx.as<int>(), a.nosync ? nullptr : lc, ghi_,
+                                                                glo_, gp, nb, vsel_, &sc->fail, sub);
+        } else {
+            k_verlet_select<<<blocks, kSelWarps * 32, 0, s>>>(ng, gi, row.as<int>(), cache.as<int>(),
+                                                              cgidx.as<int>(), a.nosync ? nullptr : lc, gp, nb, d31,
+                                                              &sc->fail, sub);
+        }
         GF_CHECK_LAUNCH();
         if (a.nosync) {  // the gas set is the cached one: every particle keeps its candidates
             have_nb = true;
@@ -515,6 +648,7 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
     }
     if (!have_nb && a.nosync) throw Error(GF_ERR_ARG, "a synchronisation-free evaluation needs a neighbour cache");
     if (!have_nb) {  // full search, 48 candidates (sph.py:165-169), written into the cache
+        vsel_ = nullptr;  // the search measures d31 itself
         const int kq = std::min(kCand, ng);
         nb = cache.get<int>(size_t(ng) * kCand);
         float* rg = nullptr;
@@ -553,7 +687,7 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
     }
     last_nb = nb;
     double* hh = h.get<double>(ng);
-    k_smoothing<<<ggrid, kThreads, 0, s>>>(ng, d31, a.eps, gi, hh, h_prev.as<double>(), sub);
+    k_smoothing<<<ggrid, kThreads, 0, s>>>(ng, d31, a.eps, gi, hh, h_prev.as<double>(), sub, vsel_, gp);
     GF_CHECK_LAUNCH();
     have_hprev = true;
 

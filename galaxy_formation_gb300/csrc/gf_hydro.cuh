@@ -81,7 +81,7 @@ struct ForceEngine {
     DevBuf acc_grav, acc_sph, dt_courant, h_prev, row, loc, cache, cgidx;
     DevBuf flag, scan, gidx, gpos, gvel, gmass, gu_, nb48, dsel, rguess, h, rho, gacc, dudt, dt_i;
     DevBuf scalars;
-    DevBuf divv_prev, gdivv, hX, hY, hrg, hdk, colX, colT, aflag, ascan, alist;
+    DevBuf divv_prev, gdivv, hX, hY, hrg, hdk, colX, colT, ghi, glo, vsel, aflag, ascan, alist;
     ScanScratch hscratch;    // scans of the hydro stream
     cudaStream_t s2 = nullptr;               // the hydro chain's stream
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -110,6 +110,9 @@ struct ForceEngine {
         reserve_scan_sort(n, &hscratch);
         if (ng > 0) {
             aflag.get<int>(ng);
+            ghi.get<float4>(ng);
+            glo.get<float4>(ng);
+            vsel.get<int>(ng);
             ascan.get<int>(ng);
             alist.get<int>(ng);
         }

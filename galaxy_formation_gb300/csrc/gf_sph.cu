@@ -192,57 +192,6 @@ __global__ void k_sph_force(int n, int k, int ld, const double* __restrict__ pos
 
 // ------------------------------------------------------------------- warp bitonic sorts
 
-// In-place ascending bitonic sort of P (power of two <= 128) keys in shared memory by the
-// calling warp; ties broken by the integer tag. Non-negative float64 distances are sorted by
-// their bit patterns as unsigned 64-bit integers (the same order, including +inf): integer
-// compares avoid the float64 pipe, which is narrow on this GPU.
-template <class K>
-__device__ void warp_bitonic(K* key, int* tag, int P) {
-    const int lane = threadIdx.x & 31;
-    for (int size = 2; size <= P; size <<= 1) {
-        for (int stride = size >> 1; stride > 0; stride >>= 1) {
-            for (int t = lane; t < P / 2; t += 32) {
-                const int a = ((t & ~(stride - 1)) << 1) | (t & (stride - 1));
-                const int b = a + stride;
-                const bool up = (a & size) == 0;
-                const K ka = key[a], kb = key[b];
-                const int ta = tag[a], tb = tag[b];
-                const bool gt = ka > kb || (ka == kb && ta > tb);
-                if (gt == up) {
-                    key[a] = kb;
-                    key[b] = ka;
-                    tag[a] = tb;
-                    tag[b] = ta;
-                }
-            }
-            __syncwarp();
-        }
-    }
-}
-
-// Ascending bitonic sort of P (power of two <= 128) 64-bit keys in shared memory by the
-// calling warp (keys are unique when they carry an index in their low bits). (A register
-// version, keys exchanged by shuffles, removed the shared-memory bank conflicts but slowed the
-// neighbour search: more instructions and register spills in an issue-bound kernel.)
-__device__ void warp_sort_u64(unsigned long long* key, int P) {
-    const int lane = threadIdx.x & 31;
-    for (int size = 2; size <= P; size <<= 1) {
-        for (int stride = size >> 1; stride > 0; stride >>= 1) {
-            for (int t = lane; t < P / 2; t += 32) {
-                const int a = ((t & ~(stride - 1)) << 1) | (t & (stride - 1));
-                const int b = a + stride;
-                const bool up = (a & size) == 0;
-                const unsigned long long ka = key[a], kb = key[b];
-                if ((ka > kb) == up) {
-                    key[a] = kb;
-                    key[b] = ka;
-                }
-            }
-            __syncwarp();
-        }
-    }
-}
-
 // --------------------------------------------------------------- knn_from_candidates
 
 constexpr int kCandWarps = 8;
