@@ -270,7 +270,8 @@ __global__ void k_smoothing(int ng, double* __restrict__ d31, double eps, const 
     if (!subset_item(sub, i, ng, nullptr, i)) return;
     double d;
     if (sel) {
-        d = __dsqrt_rn(gas_d2(gpos, i, sel[i]));
+        const int j = sel[i];
+        d = j >= 0 ? __dsqrt_rn(gas_d2(gpos, i, j)) : INFINITY;
         d31[i] = d;
     } else {
         d = d31[i];
@@ -648,7 +649,7 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
     }
     if (!have_nb && a.nosync) throw Error(GF_ERR_ARG, "a synchronisation-free evaluation needs a neighbour cache");
     if (!have_nb) {  // full search, 48 candidates (sph.py:165-169), written into the cache
-        vsel_ = nullptr;  // the search measures d31 itself
+        vsel_ = vsel.get<int>(ng);  // the neighbour that fixes each h (k_smoothing measures it)
         const int kq = std::min(kCand, ng);
         nb = cache.get<int>(size_t(ng) * kCand);
         float* rg = nullptr;
@@ -667,7 +668,7 @@ void ForceEngine::hydro(const ForceArgs& a, cudaStream_t s) {
         GF_CUDA(cudaMemsetAsync(&sc->knn_iters, 0, sizeof(unsigned long long), s));
         // the gas of the last full search, moved (same count): rebuild without a host round trip
         knn_exact(knn_tree, ng, gp, kq, rg, nullptr, nullptr, &sc->knn_iters, s, nb, kCand, d31, kNgb - 1,
-                  features ? &hg : nullptr, order_ng == ng);
+                  features ? &hg : nullptr, order_ng == ng, vsel_);
         if (collect) {
             const long long take = std::min<long long>(ng, (collect_cap - collect_n) / 2);  // two rows each
             if (take > 0) {

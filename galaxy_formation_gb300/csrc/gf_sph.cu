@@ -285,6 +285,8 @@ struct KnnArgs {
     int ld32;
     double* dsel;           // distance of neighbour `dsel_col` (n,), or null
     int dsel_col;
+    int* dsel_idx;          // instead of dsel (float32 order): that neighbour's caller index, whose
+                            // float64 distance the caller measures a thread per query (-1: failed)
     float* dfar;            // distance of the k-th nearest in float32 (n,), or null
     uint32_t* status;
     unsigned long long* iters;
@@ -451,9 +453,11 @@ __device__ void knn_finish(const KnnArgs& A, unsigned long long* key, unsigned l
         }
         below = warp_sum(below);
         inband = warp_sum(inband);
-        double best;
+        double best = 0.0;
+        int selc = -1;  // caller index of the entry that fixes h
         if (inband == 1) {  // no float32 near-tie: entry c itself, measured in float64
-            best = d2_f64(A, pi, A.perm[key_idx(key[c])]);
+            selc = A.perm[key_idx(key[c])];
+            if (!A.dsel_idx) best = d2_f64(A, pi, selc);
         } else {
             const int rank_need = c - below;  // rank of the wanted entry among the ambiguous ones
             for (int t = lane; t < 64; t += 32) {
@@ -471,6 +475,7 @@ __device__ void knn_finish(const KnnArgs& A, unsigned long long* key, unsigned l
             __syncwarp();
             warp_bitonic(dd, di, 64);
             best = __longlong_as_double((long long)dd[max(0, rank_need)]);
+            selc = A.perm[di[max(0, rank_need)]];
             // the tied entries [below, below + inband) take the float64 order (ties by tree
             // position), so the first c + 1 entries are the exact set the smoothing length is
             // measured on; their float32 distance bits stay (all within the band)
@@ -484,7 +489,11 @@ __device__ void knn_finish(const KnnArgs& A, unsigned long long* key, unsigned l
             if (A.nb32) A.nb32[size_t(oq) * A.ld32 + t] = pj;
             if (A.nb) A.nb[size_t(oq) * k + t] = pj;
         }
-        if (A.dsel && lane == 0) A.dsel[oq] = __dsqrt_rn(best);
+        if (A.dsel_idx) {
+            if (lane == 0) A.dsel_idx[oq] = selc;
+        } else if (A.dsel && lane == 0) {
+            A.dsel[oq] = __dsqrt_rn(best);
+        }
         if (A.dfar && lane == 0) A.dfar[oq] = sqrtf(key_d2(key[k - 1]));
         __syncwarp();
         return;
@@ -528,6 +537,7 @@ __device__ void knn_fail_output(const KnnArgs& A, int q, bool stack) {
         if (A.nb32) A.nb32[size_t(oq) * A.ld32 + t] = -1;
     }
     if (A.dsel && lane == 0) A.dsel[oq] = INFINITY;
+    if (A.dsel_idx && lane == 0) A.dsel_idx[oq] = -1;
 }
 
 // Radius step of the count-to-k iteration: Newton on count ~ R^3 until the count is
@@ -692,7 +702,7 @@ __global__ void k_guess_from_logdk(int n, const float* __restrict__ Y, float* __
 
 void knn_exact(Octree& T, int n, const double* pos, int k, const float* r_guess, int64_t* nb,
                double* dist, unsigned long long* d_iters, cudaStream_t s, int* nb32, int ld32,
-               double* dsel, int dsel_col, const HGuess* hg, bool same_set) {
+               double* dsel, int dsel_col, const HGuess* hg, bool same_set, int* dsel_idx) {
     if (n <= 0) return;
     // same_set (the caller's point set drifted since the last search): the synchronisation-free
     // rebuild inside the node buffers of the last regular build (no host round trip in the middle
@@ -736,6 +746,7 @@ void knn_exact(Octree& T, int n, const double* pos, int k, const float* r_guess,
     A.ld32 = ld32;
     A.dsel = dsel;
     A.dsel_col = dsel_col;
+    A.dsel_idx = dsel_col >= 0 ? dsel_idx : nullptr;
     A.dfar = hg ? hg->dk : nullptr;
     A.exact_order = (nb != nullptr || dist != nullptr || dsel_col < 0) ? 1 : 0;
     A.status = ctx().d_status;

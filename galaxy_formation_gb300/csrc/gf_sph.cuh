@@ -60,12 +60,13 @@ void knn_from_candidates(int n, int m, const double* pos, const int64_t* cand, i
 // Exact float64 k nearest neighbours of every point (itself included), ascending; builds
 // the point octree in T. r_guess (caller order, optional): starting search radius.
 // Outputs either nb/dist (n,k) int64/float64, or nb32 (n, ld32) int32 plus the distance of
-// neighbour `dsel_col` in dsel (n,). same_set: the points are those of the last search on T,
-// moved (the tree is rebuilt without a host synchronisation).
+// neighbour `dsel_col` in dsel (n,) — or, with dsel_idx, that neighbour's index (the caller
+// measures its float64 distance; -1 for a failed query). same_set: the points are those of the
+// last search on T, moved (the tree is rebuilt without a host synchronisation).
 void knn_exact(Octree& T, int n, const double* pos, int k, const float* r_guess, int64_t* nb,
                double* dist, unsigned long long* d_iters, cudaStream_t s, int* nb32 = nullptr,
                int ld32 = 0, double* dsel = nullptr, int dsel_col = -1, const HGuess* hg = nullptr,
-               bool same_set = false);
+               bool same_set = false, int* dsel_idx = nullptr);
 
 void direct_sum(int n, const double* pos, const double* mass, int nt, const int64_t* targets,
                 double* acc, double eps, cudaStream_t s);
