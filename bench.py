@@ -88,6 +88,9 @@ def parse():
     ap.add_argument("--no-configs", dest="configs", action="store_false",
                     help="skip the shortened config 3 (clumped snapshot) and config 4 (4M drift) measurements")
     ap.add_argument("--drift-steps", type=int, default=10, help="long steps of the plain loop in the 4M drift run")
+    ap.add_argument("--block-config", default="",
+                    help="walk item code per bin and rebuild cadence of the batched form, e.g. "
+                         "'104,180,0,0,0,0:8', instead of the autotuner's choice (for profiles)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
@@ -543,9 +546,10 @@ class Gpu:
                 "note": "simulation.py:114-149 on the GPU: per sub-step the gravity of the fast particles on a "
                         "refitted tree and the SPH of all the gas"}
 
-    def batched(self, blocks, nlev=7, form="mixed_learned", plain_steps=10):
-        """Block time steps at the mixed + learned form: autotune, one warm block, then
-        `blocks` blocks timed with CUDA events on the library's stream."""
+    def batched(self, blocks, nlev=7, form="mixed_learned", plain_steps=10, config=""):
+        """Block time steps at the mixed + learned form: autotune (or the given configuration:
+        'codes:rebuild_every'), one warm block, then `blocks` blocks timed with CUDA events on
+        the library's stream."""
         torch, lib, L, p = self.torch, self.lib, self._lib, self.params
         theta = self.set_form(form)
         d = self.d
@@ -554,7 +558,13 @@ class Gpu:
         chunk = np.zeros(nlev - 1, np.int32)
         every, gms = ctypes.c_int(), ctypes.c_double()
         t0 = time.perf_counter()
-        L.check(lib.gf_sim_block_autotune(nlev, chunk.ctypes.data, ctypes.byref(every), ctypes.byref(gms)))
+        if config:
+            codes, _, reb = config.partition(":")
+            chunk[:] = [int(x) for x in codes.split(",")]
+            every.value = int(reb or 8)
+            L.check(lib.gf_sim_block_config(chunk.ctypes.data, len(chunk), every.value))
+        else:
+            L.check(lib.gf_sim_block_autotune(nlev, chunk.ctypes.data, ctypes.byref(every), ctypes.byref(gms)))
         tune_s = time.perf_counter() - t0
         upd = ctypes.c_double()
         L.check(lib.gf_sim_blocks(1, nlev, ctypes.byref(upd)))
@@ -595,7 +605,8 @@ class Gpu:
         return {"value": value, "unit": UNIT, "blocks": blocks, "substeps_per_block": 1 << (nlev - 1),
                 "levels": nlev, "level_fractions": [round(float(x), 5) for x in frac],
                 "updates": upd.value, "ms": ms, "ms_per_block": ms / blocks,
-                "autotune": {"chunk_per_bin": chunk.tolist(), "rebuild_every": every.value, "seconds": tune_s},
+                "autotune": {"chunk_per_bin": chunk.tolist(), "rebuild_every": every.value, "seconds": tune_s,
+                             "given": bool(config)},
                 "launches_outside_graphs": launches, "block_end_search": block_end, "form": form,
                 "simulated_time_per_wall_second": sim_rate,
                 "plain_step_loop": plain, "ratio_vs_plain_step_loop": value / plain["value"],
@@ -697,7 +708,7 @@ def run_gpu(args, world, rank, local):
     for f in forms:
         res[f]["p99"], res[f]["median"] = G.gravity_error(f, tgt, exact)
 
-    batched = G.batched(args.blocks) if args.blocks > 0 else None
+    batched = G.batched(args.blocks, config=args.block_config) if args.blocks > 0 else None
 
     H = res[head]
     # roofline of the dominant kernel of the headline form
