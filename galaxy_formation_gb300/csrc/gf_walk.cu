@@ -142,9 +142,11 @@ __device__ __forceinline__ void emit_item(int b, int e, const float4* __restrict
 // groups (the octree fan-out), so lanes 0..15 load groups g-8 .. g+7; the warp finds the run
 // around group g and replays the cut from the run's first group. Returns the weight of the item
 // that g starts (-1 if g starts none) and, in b and len, its first particle and particle count.
+// With status: a run longer than the fan-out (groups g-8 .. g all siblings, which the 8-child
+// node layout rules out) raises GF_ERR_CAPACITY instead of being cut silently.
 __device__ __forceinline__ int cut_at(const int* __restrict__ groups, const int4* __restrict__ n_i4,
                                       const int* __restrict__ parent, const int* __restrict__ gw, int ng,
-                                      int merge, int g, int& b, int& len) {
+                                      int merge, int g, int& b, int& len, uint32_t* status = nullptr) {
     const int lane = threadIdx.x & 31;
     const int idx = g - 8 + lane;
     int pg = -2, cg = 0, bg = 0, wg = 0;
@@ -159,6 +161,7 @@ __device__ __forceinline__ int cut_at(const int* __restrict__ groups, const int4
     const int par = __shfl_sync(0xffffffffu, pg, 8);
     b = __shfl_sync(0xffffffffu, bg, 8);
     const unsigned same = __ballot_sync(0xffffffffu, pg == par);
+    if (status && (same & 0xffu) == 0xffu && lane == 0) raise_status(status, GF_ERR_CAPACITY);
     const unsigned below = ~same & 0xffu;     // lanes 0..7 outside the run
     const unsigned above = ~same & 0xfe00u;   // lanes 9..15 outside the run
     const int first = below ? 32 - __clz(below) : 0;
@@ -211,14 +214,14 @@ __global__ void k_group_nact(const int* __restrict__ groups, const int4* __restr
 // group count)
 __global__ void k_item_flag(const int* __restrict__ groups, const int4* __restrict__ n_i4,
                             const int* __restrict__ parent, const int* __restrict__ gw, const TreeCounts* cnt,
-                            int merge, int span, int* __restrict__ flag) {
+                            int merge, int span, int* __restrict__ flag, uint32_t* status) {
     const int lane = threadIdx.x & 31;
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const int ng = cnt->num_groups;
     for (int g = wid; g < ng; g += nw) {
         int b, len;
-        const int f = cut_at(groups, n_i4, parent, gw, ng, merge, g, b, len) > 0 ? 1 : 0;
+        const int f = cut_at(groups, n_i4, parent, gw, ng, merge, g, b, len, status) > 0 ? 1 : 0;
         if (lane == 0) flag[g] = f;
     }
     // past the live groups (the scan covers span): zeros, a thread per entry
@@ -871,7 +874,7 @@ void Octree::prepare_walk(const uint8_t* active, cudaStream_t s, int chunk, cons
             GF_CHECK_LAUNCH();
         }
         k_item_flag<<<blocks, 256, 0, s>>>(groups.as<int>(), n_i4.as<int4>(), n_parent.as<int>(), gw, cnt, cap_w,
-                                           span, fl);
+                                           span, fl, C.d_status);
         GF_CHECK_LAUNCH();
         exclusive_scan(fl, sl, span, &cnt->num_work, s, &scratch);
         k_item_fill<<<blocks, 256, 0, s>>>(groups.as<int>(), n_i4.as<int4>(), n_parent.as<int>(), gw,
